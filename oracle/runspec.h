@@ -1,0 +1,281 @@
+// Run description shared by the two CPU oracles (test infrastructure only).
+//
+// A run spec is a small line-oriented text format written by the Python test
+// harness; it carries exactly what the reference's runmytrim JSON carries
+// (apps/runmytrim.C:103-285) plus the extensions the workloads need (tilted
+// incidence, CUT boundaries, generation cut, histogram binning, primary subsets).
+//
+//   seed <uint>                 master seed (runmytrim "options.seed")
+//   seeding compat|philox       compat: per-primary 16-bit mt19937 seeds drawn from
+//                               the master stream (runmytrim.C:288-302);
+//                               philox: counter-based streams keyed like the GPU
+//   ion <Z> <mass> <E_eV> <count> [<Ef_eV>]
+//   dir <x> <y> <z>             initial direction (runmytrim hard-codes 1 0 0)
+//   pos <x> <y> <z>             start position (default 0, w1/2, w2/2)
+//   size <wx> <wy> <wz>         sample box (runmytrim: total thickness, 100, 100)
+//   bc <b0> <b1> <b2>           0 = PBC, 1 = INF, 2 = CUT (sample.h:49-54)
+//   scale <l>                   length scale (simconf.C:75-80)
+//   layer <thickness> <rho>     appends a layer
+//   element <Z> <mass> <fraction> [<Edisp> <Elbind>]   appends to the last layer
+//   mode vaccount|range         vaccount: TrimVacCount; range: TrimRange (KP, gen cut)
+//   primaries_only 0|1          ThreadedTrimBase::_primaries_only
+//   hist_range <bin_A> <nbins>  histogram of primary stopping depth
+//   hist_vac <bin_A> <nbins>    histogram of vacancy depth (TrimVacCount bins are 1 A)
+//   subset <first> <count>      run primaries [first, first+count)
+//   records <n>                 emit per-primary records for the first n primaries
+#pragma once
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <sstream>
+#include <fstream>
+#include <iostream>
+
+namespace runspec
+{
+
+struct ElementSpec
+{
+  int Z;
+  double m, t, Edisp, Elbind;
+};
+
+struct LayerSpec
+{
+  double thickness, rho;
+  std::vector<ElementSpec> el;
+};
+
+struct Spec
+{
+  unsigned int seed = 1;
+  bool philox = false;
+  int Z = 29;
+  double m = 63.546, E = 1000.0, Ef = 3.0;
+  long long count = 1;
+  double dir[3] = {1.0, 0.0, 0.0};
+  bool have_pos = false;
+  double pos[3] = {0.0, 0.0, 0.0};
+  bool have_size = false;
+  double size[3] = {0.0, 100.0, 100.0};
+  int bc[3] = {0, 0, 0};
+  double scale = 1.0;
+  std::vector<LayerSpec> layers;
+  bool range_mode = false;
+  bool primaries_only = false;
+  double hist_range_bin = 10.0;
+  int hist_range_n = 0;
+  double hist_vac_bin = 1.0;
+  int hist_vac_n = 0;
+  long long first = 0, n = -1;
+  int records = 0;
+
+  double total_thickness() const
+  {
+    double t = 0.0;
+    for (auto & l : layers)
+      t += l.thickness;
+    return t;
+  }
+  void finalize()
+  {
+    if (!have_size)
+    {
+      size[0] = total_thickness();
+      size[1] = 100.0;
+      size[2] = 100.0;
+    }
+    if (!have_pos)
+    {
+      pos[0] = 0.0;
+      pos[1] = size[1] / 2.0;
+      pos[2] = size[2] / 2.0;
+    }
+    if (n < 0)
+      n = count - first;
+  }
+};
+
+inline bool
+parse(std::istream & in, Spec & s, std::string & err)
+{
+  std::string line;
+  int lineno = 0;
+  while (std::getline(in, line))
+  {
+    ++lineno;
+    auto hash = line.find('#');
+    if (hash != std::string::npos)
+      line.resize(hash);
+    std::istringstream ls(line);
+    std::string key;
+    if (!(ls >> key))
+      continue;
+    bool ok = true;
+    if (key == "seed")
+      ok = bool(ls >> s.seed);
+    else if (key == "seeding")
+    {
+      std::string v;
+      ok = bool(ls >> v);
+      s.philox = (v == "philox");
+    }
+    else if (key == "ion")
+    {
+      ok = bool(ls >> s.Z >> s.m >> s.E >> s.count);
+      double ef;
+      if (ok && (ls >> ef))
+        s.Ef = ef;
+    }
+    else if (key == "dir")
+      ok = bool(ls >> s.dir[0] >> s.dir[1] >> s.dir[2]);
+    else if (key == "pos")
+    {
+      ok = bool(ls >> s.pos[0] >> s.pos[1] >> s.pos[2]);
+      s.have_pos = true;
+    }
+    else if (key == "size")
+    {
+      ok = bool(ls >> s.size[0] >> s.size[1] >> s.size[2]);
+      s.have_size = true;
+    }
+    else if (key == "bc")
+      ok = bool(ls >> s.bc[0] >> s.bc[1] >> s.bc[2]);
+    else if (key == "scale")
+      ok = bool(ls >> s.scale);
+    else if (key == "layer")
+    {
+      LayerSpec l;
+      ok = bool(ls >> l.thickness >> l.rho);
+      s.layers.push_back(l);
+    }
+    else if (key == "element")
+    {
+      ElementSpec e;
+      e.Edisp = 25.0;
+      e.Elbind = 3.0;
+      ok = bool(ls >> e.Z >> e.m >> e.t) && !s.layers.empty();
+      double ed, eb;
+      if (ok && (ls >> ed >> eb))
+      {
+        e.Edisp = ed;
+        e.Elbind = eb;
+      }
+      if (ok)
+        s.layers.back().el.push_back(e);
+    }
+    else if (key == "mode")
+    {
+      std::string v;
+      ok = bool(ls >> v);
+      s.range_mode = (v == "range");
+    }
+    else if (key == "primaries_only")
+    {
+      int v;
+      ok = bool(ls >> v);
+      s.primaries_only = v != 0;
+    }
+    else if (key == "hist_range")
+      ok = bool(ls >> s.hist_range_bin >> s.hist_range_n);
+    else if (key == "hist_vac")
+      ok = bool(ls >> s.hist_vac_bin >> s.hist_vac_n);
+    else if (key == "subset")
+      ok = bool(ls >> s.first >> s.n);
+    else if (key == "records")
+      ok = bool(ls >> s.records);
+    else
+    {
+      err = "unknown key '" + key + "' on line " + std::to_string(lineno);
+      return false;
+    }
+    if (!ok)
+    {
+      err = "bad value for '" + key + "' on line " + std::to_string(lineno);
+      return false;
+    }
+  }
+  if (s.layers.empty())
+  {
+    err = "no layers";
+    return false;
+  }
+  for (auto & l : s.layers)
+    if (l.el.empty())
+    {
+      err = "layer without elements";
+      return false;
+    }
+  s.finalize();
+  return true;
+}
+
+// Tallies reported by both oracles (one line per key on stdout).
+struct Tally
+{
+  long long primaries = 0, members = 0, collisions = 0;
+  long long vacancies = 0, replacements = 0, interstitials = 0, substitutionals = 0,
+            lost = 0;
+  double Eel = 0.0, Enuc = 0.0, Elost = 0.0, Eunfollowed = 0.0;
+  // primary end points (generation 0, stopped inside the sample)
+  long long range_n = 0;
+  double sx = 0, sxx = 0, sy = 0, syy = 0, sz = 0, szz = 0;
+  // per-primary moments for Monte Carlo error bars
+  double vac_s2 = 0.0, eel_s2 = 0.0, enuc_s2 = 0.0, coll_s2 = 0.0;
+  std::vector<long long> hist_range, hist_vac, hist_repl;
+
+  void print(FILE * f) const
+  {
+    fprintf(f, "primaries %lld\nmembers %lld\ncollisions %lld\n", primaries, members, collisions);
+    fprintf(f, "vacancies %lld\nreplacements %lld\ninterstitials %lld\n", vacancies,
+            replacements, interstitials);
+    fprintf(f, "substitutionals %lld\nlost %lld\n", substitutionals, lost);
+    fprintf(f, "Eel %.17g\nEnuc %.17g\nElost %.17g\nEunfollowed %.17g\n", Eel, Enuc, Elost,
+            Eunfollowed);
+    fprintf(f, "range_n %lld\nsx %.17g\nsxx %.17g\nsy %.17g\nsyy %.17g\nsz %.17g\nszz %.17g\n",
+            range_n, sx, sxx, sy, syy, sz, szz);
+    fprintf(f, "vac_s2 %.17g\neel_s2 %.17g\nenuc_s2 %.17g\ncoll_s2 %.17g\n", vac_s2, eel_s2,
+            enuc_s2, coll_s2);
+    auto hist = [&](const char * name, const std::vector<long long> & h)
+    {
+      fprintf(f, "%s", name);
+      for (auto v : h)
+        fprintf(f, " %lld", v);
+      fprintf(f, "\n");
+    };
+    hist("hist_range", hist_range);
+    hist("hist_vac", hist_vac);
+    hist("hist_repl", hist_repl);
+  }
+};
+
+// Per-primary record (emitted for the first `records` primaries).
+struct Record
+{
+  long long index, members, collisions, vacancies;
+  double Eel, Enuc, x, y, z;
+  int state;
+};
+
+inline void
+print_record(FILE * f, const Record & r)
+{
+  fprintf(f, "rec %lld %lld %lld %lld %.17g %.17g %.17g %.17g %.17g %d\n", r.index, r.members,
+          r.collisions, r.vacancies, r.Eel, r.Enuc, r.x, r.y, r.z, r.state);
+}
+
+inline int
+bin_of(double x, double width, int n)
+{
+  // truncation toward zero like the reference's int(x) (TrimVacCount.C:36-39):
+  // depths in (-1 bin, 0) land in bin 0, smaller ones are dropped
+  double q = x / width;
+  if (n <= 0 || !(q > -1.0) || q >= double(n))
+    return -1;
+  return int(q);
+}
+
+} // namespace runspec
