@@ -1,0 +1,249 @@
+/*
+ * mytrim_gpu.h -- C ABI of the GB300 cascade engine (libmytrim_gpu.so).
+ *
+ * The engine runs MyTRIM's binary-collision cascade (TrimBase::trim, trim.C:36-425,
+ * driven by the FIFO loop of apps/runmytrim.C:71-93) on one GPU.  The ABI uses
+ * plain C types only: POD structs, pointers and sizes.  The caller owns every
+ * host buffer; a context owns the device memory it allocates.  All calls are
+ * synchronous unless named *_async.  A context is not thread-safe: use one per
+ * host thread, as the reference uses one SimconfType/TrimBase per thread
+ * (apps/runmytrim.C:59-67).  No call aborts the process; every call returns an
+ * mtg_status and mtg_last_error() describes the last failure.
+ *
+ * The reference has no foreign-function interface: each entry point below names
+ * the C++ interface of the reference it stands in for.
+ */
+#ifndef MYTRIM_GPU_H
+#define MYTRIM_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MTG_MAX_ELEMENTS 4
+#define MTG_MAX_LAYERS 8
+#define MTG_SCOEF_ROWS 92
+
+typedef enum
+{
+  MTG_OK = 0,
+  MTG_ERR_BAD_INPUT = 1,  /* invalid argument or unsupported sample */
+  MTG_ERR_DATA = 2,       /* stopping tables missing or unreadable */
+  MTG_ERR_OOM = 3,        /* device allocation failed */
+  MTG_ERR_QUEUE_FULL = 4, /* recoil overflow list exhausted; results incomplete */
+  MTG_ERR_TIMEOUT = 5,    /* a member exceeded the collision budget */
+  MTG_ERR_NUMERIC = 6,    /* NaN energy or degenerate geometry met */
+  MTG_ERR_CUDA = 7,       /* CUDA runtime error */
+  MTG_ERR_NO_DEVICE = 8,  /* no CUDA device */
+  MTG_ERR_STATE = 9       /* call out of order (e.g. run before tables) */
+} mtg_status;
+
+typedef enum
+{
+  MTG_PREC_FP64 = 0,          /* plain path: FP64 exact scattering (Newton + magic formula) */
+  MTG_PREC_FP32 = 1,          /* FP32 flight/stopping/scattering, compensated energy bookkeeping */
+  MTG_PREC_FP32_SURROGATE = 2 /* FP32 path with the learned scattering surrogate */
+} mtg_precision;
+
+typedef enum
+{
+  MTG_BC_PBC = 0, /* SampleBase::PBC (sample.h:49-54); positions are not wrapped, as in trim.C */
+  MTG_BC_INF = 1, /* SampleBase::INF */
+  MTG_BC_CUT = 2  /* SampleBase::CUT: a member leaving [0, w] is lost (trim.C:344-352) */
+} mtg_boundary;
+
+typedef enum
+{
+  MTG_TALLY_VACCOUNT = 0, /* TrimVacCount semantics (apps/src/TrimVacCount.C:32-54) */
+  MTG_TALLY_RANGE = 1     /* TrimRange semantics: no recoil followed, Kinchin-Pease
+                             vacancies (apps/src/TrimRange.C:32-47) */
+} mtg_tally_mode;
+
+/* One row of the stopping tables (SimconfType::ScoefLine, simconf.h:71-90). */
+typedef struct
+{
+  double mm1, m1, mnat, rho, atrho, vfermi, heat, lfctr;
+  double pcoef[8];
+} mtg_scoef_row;
+
+/* Element (element.h:29-41): _Z, _m, _t, _Edisp, _Elbind. */
+typedef struct
+{
+  int Z;
+  double m;
+  double t;
+  double Edisp;
+  double Elbind;
+} mtg_element;
+
+/* MaterialBase (material.h:34-75) before prepare(): density in g/cm^3. */
+typedef struct
+{
+  double rho;
+  int n_elements;
+  mtg_element elements[MTG_MAX_ELEMENTS];
+} mtg_material;
+
+/* SampleLayers (sample_layers.h:33-43) or SampleSolid (n_layers = 1): layers stacked
+ * along x from 0; x < 0 belongs to layer 0, the last layer extends to +infinity. */
+typedef struct
+{
+  int n_layers;
+  double thickness[MTG_MAX_LAYERS];
+  mtg_material material[MTG_MAX_LAYERS];
+  double w[3];
+  int bc[3];
+} mtg_sample;
+
+/* IonBase template of the primaries (ion.h:30-85, runmytrim.C:263-304). */
+typedef struct
+{
+  int Z;
+  double m;      /* mass [u]; 0 selects the SCOEF MAI mass for stopping */
+  double E;      /* energy [eV] */
+  double Ef;     /* final energy [eV] (IonBase::_Ef, default 3) */
+  double dir[3]; /* direction (normalised by the engine) */
+  double pos[3]; /* start position */
+} mtg_ion;
+
+/* One independent simulation. */
+typedef struct
+{
+  mtg_sample sample;
+  mtg_ion ion;
+  long long n_primaries;
+  long long first_primary; /* index of the first primary: the random streams of primary i
+                              depend only on (simulation, first_primary + i), so a run split
+                              into primary ranges reproduces the unsplit run exactly */
+  int tally_mode;         /* mtg_tally_mode */
+  int primaries_only;     /* ThreadedTrimBase::_primaries_only */
+  double hist_range_bin;  /* primary stopping-depth histogram: bin width [length unit] */
+  int hist_range_n;       /*   and number of bins (0 = none) */
+  double hist_vac_bin;    /* vacancy / replacement depth histograms (TrimVacCount uses 1) */
+  int hist_vac_n;
+} mtg_sim;
+
+/* Run-wide settings (SimconfType scalars, simconf.h:66). */
+typedef struct
+{
+  double tmin;           /* minimum energy transfer setting p_max [eV] (0.2 in runmytrim) */
+  double tau;            /* flight-path correction (0) */
+  double cw;             /* first-flight cap [Angstrom] (0.001) */
+  double length_scale;   /* SimconfType::setLengthScale */
+  int precision;         /* mtg_precision */
+  unsigned long long seed;
+  long long max_collisions_per_member; /* 0 = default (2^24) */
+  int stack_capacity;    /* recoil stack entries per warp, 0 = default */
+} mtg_config;
+
+/* Results of one simulation. */
+typedef struct
+{
+  long long primaries, members, collisions;
+  long long vacancies, replacements, interstitials, substitutionals, lost;
+  double Eel, Enuc, Elost, Eunfollowed;
+  long long range_n; /* primaries that came to rest (not lost) */
+  double sx, sxx, sy, syy, sz, szz;
+  double vac_s2, eel_s2, enuc_s2, coll_s2; /* sums of per-primary squares */
+  long long newton_iterations, rejection_passes, surrogate_fallbacks;
+} mtg_totals;
+
+/* Per-member trajectory summary (replay checks). */
+typedef struct
+{
+  unsigned long long key;
+  int sim, species, gen, state;
+  unsigned int ncoll, nvac;
+  double E, x, y, z, eel;
+} mtg_member_record;
+
+typedef struct
+{
+  double kernel_ms;        /* device time of the cascade launches of the last run */
+  double reduce_ms;        /* device time of the tally reduction of the last run */
+  int launches;            /* kernels launched by the last run */
+  int drains;              /* overflow drain passes of the last run */
+  int grid, block;         /* cascade launch shape */
+  int stack_capacity;
+  long long overflowed;    /* members spilled to the overflow list */
+  long long collisions;
+  size_t device_bytes;     /* device memory held by the context */
+} mtg_stats;
+
+typedef struct mtg_ctx mtg_ctx;
+
+/* Create a context on CUDA device `device`.
+ * Replaces: constructing SimconfType + TrimBase per thread (runmytrim.C:121-127). */
+mtg_status mtg_create(int device, mtg_ctx ** out);
+
+/* Release all device memory of the context. */
+mtg_status mtg_destroy(mtg_ctx * ctx);
+
+/* Text of the last error on this context (never NULL). */
+const char * mtg_last_error(const mtg_ctx * ctx);
+
+/* Stopping tables, 92 rows for Z = 1..92.
+ * Replaces: SimconfType::readDataFiles (simconf.C:82-137). */
+mtg_status mtg_set_tables(mtg_ctx * ctx, const mtg_scoef_row * rows, int n_rows);
+
+/* Read the tables from a stopping_tables.tsv file (mytrim_gb300/data).
+ * Replaces: SimconfType::readDataFiles with $MYTRIM_DATADIR (simconf.C:39, 82-137). */
+mtg_status mtg_load_tables(mtg_ctx * ctx, const char * path);
+
+/* Run-wide settings.  Replaces: SimconfType fields tmin/tau/cw and setLengthScale
+ * (simconf.C:44-49, 75-80). */
+mtg_status mtg_configure(mtg_ctx * ctx, const mtg_config * cfg);
+
+/* Run n_sims simulations to completion (full cascades), host in, host out.
+ * totals: n_sims entries.  hist: NULL or, per simulation in order, hist_range_n
+ * range bins, then hist_vac_n vacancy bins, then hist_vac_n replacement bins.
+ * Replaces: the cascade loop computeThread (runmytrim.C:71-93) over
+ * TrimBase::trim (trim.C:36-425) with the tally plugins (apps/src/Trim*.C). */
+mtg_status mtg_run(mtg_ctx * ctx, const mtg_sim * sims, int n_sims, mtg_totals * totals,
+                   long long * hist);
+
+/* Split form of mtg_run for callers that keep inputs resident: prepare uploads the
+ * tables of the simulations, launch runs the cascades on `stream` (a cudaStream_t,
+ * NULL = default stream) without host copies, collect waits and copies the results. */
+mtg_status mtg_prepare(mtg_ctx * ctx, const mtg_sim * sims, int n_sims);
+mtg_status mtg_launch_async(mtg_ctx * ctx, void * stream);
+mtg_status mtg_collect(mtg_ctx * ctx, mtg_totals * totals, long long * hist);
+
+/* Per-primary results of the last run, primaries [first, first + n) of the global
+ * index space (simulation after simulation).  Any pointer may be NULL.
+ * Replaces: the per-ion quantities the reference tallies through checkPKAState and
+ * vacancyCreation (trim.h:76-84). */
+mtg_status mtg_get_primaries(mtg_ctx * ctx, long long first, long long n, long long * vacancies,
+                             long long * collisions, double * eel, double * enuc, double * x,
+                             double * y, double * z, int * state);
+
+/* Record one summary per cascade member (up to `capacity`) in subsequent runs;
+ * 0 disables.  Replaces: the fullTraj trajectory dump (trim.C:370-371, 421-422). */
+mtg_status mtg_set_record_capacity(mtg_ctx * ctx, long long capacity);
+mtg_status mtg_get_records(mtg_ctx * ctx, mtg_member_record * out, long long capacity,
+                           long long * n_written);
+
+/* Electronic stopping [eV/Angstrom] of ion (Z1, m1) in `material` at n energies,
+ * evaluated on the GPU in FP64 (precision MTG_PREC_FP64) or through the FP32
+ * engine's stopping table (MTG_PREC_FP32).
+ * Replaces: MaterialBase::getrstop (material.C:114-121) as driven by runstopping
+ * (apps/runstopping.C:175-179). */
+mtg_status mtg_stopping(mtg_ctx * ctx, int Z1, double m1, const mtg_material * material,
+                        const double * E, long long n, int precision, double * out);
+
+/* Centre-of-mass scattering for n (reduced energy, reduced impact parameter) pairs:
+ * s2 = sin^2(theta/2).  precision selects the FP64 exact, FP32 exact or surrogate path.
+ * Replaces: the scattering block of TrimBase::trim (trim.C:172-271). */
+mtg_status mtg_scatter(mtg_ctx * ctx, const double * eps, const double * b, long long n,
+                       int precision, double * s2);
+
+/* Counters of the last run. */
+mtg_status mtg_get_stats(const mtg_ctx * ctx, mtg_stats * out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MYTRIM_GPU_H */

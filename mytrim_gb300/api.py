@@ -1,0 +1,132 @@
+"""Reference-shaped API: the classes of MyTRIM's C++ interface, backed by the GPU engine.
+
+A user of the reference builds a SimconfType, MaterialBase objects from Elements,
+a SampleSolid / SampleLayers, an IonBase template and a TrimBase subclass, then
+loops over primaries (apps/runmytrim.C:121-304).  The same objects exist here
+with the same field names; ``TrimGPU.runPrimaries`` replaces the per-primary
+FIFO loop of runmytrim.C:71-93 with one batched GPU run.  The C++ header
+mytrim_gb300/cpp/trim_gpu.h offers the same classes to C++ callers.
+"""
+from typing import List, Optional
+
+from . import _ffi as F
+from .engine import ElementSpec, Engine, LayerSpec, SimSpec, summarize
+
+
+class SimconfType:
+    """Run-wide settings (simconf.h:47-128): tmin, tau, cw, length scale, seed."""
+
+    def __init__(self, seed: int = 12345678):
+        self._seed = seed
+        self.tmin = 0.2  # runmytrim.C:126
+        self.tau = 0.0
+        self.cw = 0.001
+        self._length_scale = 1.0
+        self.EelTotal = 0.0
+        self.EnucTotal = 0.0
+        self.vacancies_created = 0
+
+    def seed(self, s: int):
+        self._seed = s
+
+    def setLengthScale(self, l: float):
+        self._length_scale = l
+
+    def lengthScale(self) -> float:
+        return self._length_scale
+
+
+class Element:
+    """Element (element.h:29-41)."""
+
+    def __init__(self, Z: int = 1, m: float = 1.0, t: float = 1.0, Edisp: float = 25.0, Elbind: float = 3.0):
+        self._Z, self._m, self._t, self._Edisp, self._Elbind = Z, m, t, Edisp, Elbind
+
+
+class MaterialBase:
+    """MaterialBase (material.h:34-75); rho in g/cm^3."""
+
+    def __init__(self, simconf: SimconfType, rho: float):
+        self._simconf = simconf
+        self._rho = rho
+        self._element: List[Element] = []
+
+    def prepare(self):
+        # normalisation happens in the engine's table setup (material.C:37-74)
+        if not self._element or sum(max(e._t, 0.0) for e in self._element) <= 0.0:
+            raise ValueError("Stoichiometry invalid, all elements zero.")
+
+    def _layer(self, thickness: float) -> LayerSpec:
+        return LayerSpec(thickness, self._rho,
+                         [ElementSpec(e._Z, e._m, e._t, e._Edisp, e._Elbind) for e in self._element])
+
+
+class SampleBase:
+    PBC, INF, CUT = F.BC_PBC, F.BC_INF, F.BC_CUT
+
+    def __init__(self, x: float = 10000.0, y: float = 10000.0, z: float = 10000.0):
+        self.w = [x, y, z]
+        self.bc = [self.PBC, self.PBC, self.PBC]  # sample.C:27-32
+        self.material: List[MaterialBase] = []
+
+
+class SampleSolid(SampleBase):
+    """One material everywhere (sample_solid.C:26-29)."""
+
+    def _layers(self):
+        return [self.material[0]._layer(self.w[0])]
+
+
+class SampleLayers(SampleBase):
+    """Layers along x; x < 0 is layer 0, the last layer extends to +inf (sample_layers.C:27-43)."""
+
+    def __init__(self, x: float, y: float, z: float):
+        super().__init__(x, y, z)
+        self.layerThickness: List[float] = []
+
+    def _layers(self):
+        return [m._layer(t) for m, t in zip(self.material, self.layerThickness)]
+
+
+class IonBase:
+    """Ion template (ion.h:30-85)."""
+
+    def __init__(self, Z: int = 1, m: float = 1.0, E: float = 0.0):
+        self._Z, self._m, self._E = Z, m, E
+        self._Ef = 3.0
+        self._gen = 0
+        self._dir = [1.0, 0.0, 0.0]
+        self._pos: Optional[List[float]] = None
+
+
+class TrimGPU:
+    """Drop-in for a runmytrim TrimBase subclass (TrimVacCount / TrimRange with
+    TrimPhononOut energy accounting), running every primary's full cascade on the GPU."""
+
+    UNIVERSAL = 0
+
+    def __init__(self, simconf: SimconfType, sample: SampleBase, precision: str = "fp64", device: int = 0,
+                 output: str = "vaccount", primaries_only: bool = False):
+        if not isinstance(sample, (SampleSolid, SampleLayers)):
+            raise TypeError("TrimGPU supports SampleSolid and SampleLayers")
+        self._simconf = simconf
+        self._sample = sample
+        self._potential = self.UNIVERSAL
+        self._output = output
+        self._primaries_only = primaries_only
+        self._engine = Engine(device=device, precision=precision, seed=simconf._seed, tmin=simconf.tmin,
+                              tau=simconf.tau, cw=simconf.cw, length_scale=simconf.lengthScale())
+
+    def runPrimaries(self, pka: IonBase, n: int, hist_range=(10.0, 0), hist_vac=(1.0, 0)) -> dict:
+        s = self._sample
+        spec = SimSpec(layers=s._layers(), Z=pka._Z, m=pka._m, E=pka._E, n_primaries=n, Ef=pka._Ef,
+                       dir=tuple(pka._dir), pos=tuple(pka._pos) if pka._pos else None, size=tuple(s.w),
+                       bc=tuple(s.bc), mode=self._output, primaries_only=self._primaries_only,
+                       hist_range_bin=hist_range[0], hist_range_n=hist_range[1], hist_vac_bin=hist_vac[0],
+                       hist_vac_n=hist_vac[1])
+        r = self._engine.run([spec])[0]
+        sc = self._simconf
+        sc.EelTotal += r["Eel"]
+        sc.EnucTotal += r["Enuc"]
+        sc.vacancies_created += r["vacancies"]
+        return summarize(r)

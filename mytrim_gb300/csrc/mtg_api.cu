@@ -1,0 +1,830 @@
+// C ABI of the cascade engine (include/mytrim_gpu.h): context, table upload,
+// launch sequence (cascade pass, overflow drains, tally reduction) and result
+// collection.  No CPU fallback exists: without a CUDA device every call that
+// needs one fails with MTG_ERR_NO_DEVICE.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mytrim_gpu.h"
+#include "mtg_engine.cuh"
+#include "mtg_kernels.h"
+#include "mtg_setup.h"
+
+using namespace mtg;
+
+namespace
+{
+
+struct DevBuf
+{
+  void * p = nullptr;
+  size_t bytes = 0;
+};
+
+cudaError_t
+ensure(DevBuf & b, size_t bytes)
+{
+  if (b.bytes >= bytes && b.p)
+    return cudaSuccess;
+  if (b.p)
+    cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+  if (bytes == 0)
+    return cudaSuccess;
+  cudaError_t e = cudaMalloc(&b.p, bytes);
+  if (e == cudaSuccess)
+    b.bytes = bytes;
+  return e;
+}
+
+template <class T>
+T *
+ptr(DevBuf & b)
+{
+  return reinterpret_cast<T *>(b.p);
+}
+
+// counters block layout (unsigned long long)
+enum Counter
+{
+  C_NEXT0 = 0, // work counters of up to MAX_PASSES passes
+  C_OVF0 = 64, // overflow counts of the two ping-pong lists
+  C_OVF1 = 65,
+  C_NREC = 66,
+  C_COUNT = 68
+};
+constexpr int MAX_PASSES = 64;
+
+} // namespace
+
+struct mtg_ctx
+{
+  int device = 0;
+  int n_sm = 0;
+  cudaStream_t stream = nullptr; // stream of the current launch
+  std::string err;
+  mtg_scoef_row rows[MTG_SCOEF_ROWS];
+  bool have_tables = false;
+  mtg_config cfg;
+  HostTables tables;
+  bool prepared = false;
+  bool launched = false;
+  // device buffers
+  DevBuf d_sims, d_prim_end, d_species, d_mats, d_row_species, d_stop;
+  DevBuf d_species32, d_mats32, d_sims32;
+  DevBuf p_vac, p_coll, p_eel, p_enuc, p_fx, p_fy, p_fz, p_state;
+  DevBuf d_totals, d_hist, d_err, d_counters, d_stacks, d_ovf0, d_ovf1, d_records;
+  DevBuf d_jobs, d_job_first, d_partials, d_out;
+  DevBuf d_tmp0, d_tmp1, d_tmp2, d_tmp3;
+  std::vector<ReduceJob> jobs;
+  std::vector<int> job_first;
+  int block = 128, grid = 0;
+  size_t smem = 0;
+  int stage = 0;
+  int stack_cap = 0;
+  long long ovf_cap = 0;
+  long long record_cap = 0;
+  int passes = 0; // cascade passes launched for the current run
+  int ovf_last = 0;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  mtg_stats stats;
+};
+
+namespace
+{
+
+mtg_status
+fail(mtg_ctx * ctx, mtg_status st, const std::string & msg)
+{
+  if (ctx)
+    ctx->err = msg;
+  return st;
+}
+
+#define CK(call)                                                                                   \
+  do                                                                                               \
+  {                                                                                                \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess)                                                                         \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? MTG_ERR_OOM : MTG_ERR_CUDA,             \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                           \
+  } while (0)
+
+mtg_config
+default_config()
+{
+  mtg_config c;
+  std::memset(&c, 0, sizeof c);
+  c.tmin = 0.2;
+  c.tau = 0.0;
+  c.cw = 0.001;
+  c.length_scale = 1.0;
+  c.precision = MTG_PREC_FP64;
+  c.seed = 1;
+  c.max_collisions_per_member = 1 << 24;
+  c.stack_capacity = 0;
+  return c;
+}
+
+size_t
+record_size(int precision)
+{
+  return precision == MTG_PREC_FP64 ? record_size64() : record_size32();
+}
+
+mtg_status
+setup_launch_shape(mtg_ctx * ctx)
+{
+  const int prec = ctx->cfg.precision;
+  const HostTables & t = ctx->tables;
+  // stage species and material tables in shared memory for single-simulation runs
+  size_t tab = 0;
+  ctx->stage = 0;
+  if (t.sims.size() == 1)
+  {
+    if (prec == MTG_PREC_FP64)
+      tab = sizeof(SpeciesConst) * t.species.size() + sizeof(MatConst) * t.mats.size();
+    else
+      tab = sizeof(Species32) * t.species.size() + sizeof(Mat32) * t.mats.size() +
+            sizeof(float) * STOP_N * t.mats.size();
+    if (tab <= 160 * 1024)
+      ctx->stage = 1;
+    else
+      tab = 0;
+  }
+  ctx->smem = ctx->stage ? tab : 0;
+  int bps = 0;
+  cudaError_t e = prec == MTG_PREC_FP64 ? occupancy64(ctx->block, ctx->smem, &bps)
+                                        : occupancy32(ctx->block, ctx->smem, &bps, prec == MTG_PREC_FP32_SURROGATE);
+  if (e != cudaSuccess)
+    return fail(ctx, MTG_ERR_CUDA, std::string("occupancy query: ") + cudaGetErrorString(e));
+  if (bps < 1)
+    return fail(ctx, MTG_ERR_CUDA, "cascade kernel cannot be resident with this launch shape");
+  ctx->grid = ctx->n_sm * bps;
+  const long long warps = (long long)ctx->grid * (ctx->block / 32);
+  const size_t rec = record_size(prec);
+  int cap = ctx->cfg.stack_capacity;
+  if (cap <= 0)
+    cap = prec == MTG_PREC_FP64 ? 4096 : 8192;
+  ctx->stack_cap = cap;
+  ctx->ovf_cap = std::max<long long>(1 << 20, warps * 64);
+  mtg_status st = MTG_OK;
+  auto chk = [&](cudaError_t ce, const char * what) {
+    if (ce != cudaSuccess && st == MTG_OK)
+      st = fail(ctx, ce == cudaErrorMemoryAllocation ? MTG_ERR_OOM : MTG_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(ce));
+  };
+  chk(ensure(ctx->d_stacks, size_t(warps) * cap * rec), "stack allocation");
+  chk(ensure(ctx->d_ovf0, size_t(ctx->ovf_cap) * rec), "overflow allocation");
+  chk(ensure(ctx->d_ovf1, size_t(ctx->ovf_cap) * rec), "overflow allocation");
+  return st;
+}
+
+void
+fill_params(mtg_ctx * ctx, EngineParams & prm)
+{
+  const HostTables & t = ctx->tables;
+  std::memset(&prm, 0, sizeof prm);
+  prm.sims = ptr<SimDesc>(ctx->d_sims);
+  prm.n_sims = int(t.sims.size());
+  prm.sim_prim_end = ptr<long long>(ctx->d_prim_end);
+  if (ctx->cfg.precision == MTG_PREC_FP64)
+  {
+    prm.species = ptr<SpeciesConst>(ctx->d_species);
+    prm.mats = ptr<MatConst>(ctx->d_mats);
+  }
+  else
+  {
+    // the FP32 engine reads the single-precision copies through the same pointers
+    prm.species = reinterpret_cast<const SpeciesConst *>(ctx->d_species32.p);
+    prm.mats = reinterpret_cast<const MatConst *>(ctx->d_mats32.p);
+  }
+  prm.stage_tables = ctx->stage;
+  prm.n_stage_species = int(t.species.size());
+  prm.n_stage_mats = int(t.mats.size());
+  prm.total_primaries = t.total_primaries;
+  prm.stacks = ctx->d_stacks.p;
+  prm.stack_cap = ctx->stack_cap;
+  prm.overflow_cap = ctx->ovf_cap;
+  prm.prim.vac = ptr<unsigned long long>(ctx->p_vac);
+  prm.prim.coll = ptr<unsigned long long>(ctx->p_coll);
+  prm.prim.eel = ptr<double>(ctx->p_eel);
+  prm.prim.enuc = ptr<double>(ctx->p_enuc);
+  prm.prim.fx = ptr<double>(ctx->p_fx);
+  prm.prim.fy = ptr<double>(ctx->p_fy);
+  prm.prim.fz = ptr<double>(ctx->p_fz);
+  prm.prim.fstate = ptr<int>(ctx->p_state);
+  prm.totals = ptr<SimTotals>(ctx->d_totals);
+  prm.hist = ptr<unsigned long long>(ctx->d_hist);
+  prm.error_flags = ptr<unsigned int>(ctx->d_err);
+  prm.k0 = t.k0;
+  prm.k1 = t.k1;
+  long long mc = ctx->cfg.max_collisions_per_member;
+  prm.max_collisions = (unsigned int)(mc <= 0 ? (1 << 24) : std::min<long long>(mc, 0xffffffffLL));
+  if (ctx->record_cap > 0)
+  {
+    prm.records = ptr<MemberRecord>(ctx->d_records);
+    prm.n_records = ptr<unsigned long long>(ctx->d_counters) + C_NREC;
+    prm.records_cap = ctx->record_cap;
+  }
+}
+
+// Launch cascade pass `pass` (0 = fresh primaries, >0 = drain of the previous
+// pass's overflow list).
+mtg_status
+launch_pass(mtg_ctx * ctx, int pass)
+{
+  EngineParams prm;
+  fill_params(ctx, prm);
+  unsigned long long * cnt = ptr<unsigned long long>(ctx->d_counters);
+  prm.next_primary = cnt + C_NEXT0 + (pass % MAX_PASSES);
+  CK(cudaMemsetAsync(prm.next_primary, 0, sizeof(unsigned long long), ctx->stream));
+  const int out_list = pass & 1;
+  prm.overflow = out_list ? ctx->d_ovf1.p : ctx->d_ovf0.p;
+  prm.overflow_count = cnt + (out_list ? C_OVF1 : C_OVF0);
+  CK(cudaMemsetAsync(prm.overflow_count, 0, sizeof(unsigned long long), ctx->stream));
+  if (pass > 0)
+  {
+    prm.in_records = out_list ? ctx->d_ovf0.p : ctx->d_ovf1.p;
+    prm.in_count = cnt + (out_list ? C_OVF0 : C_OVF1);
+    prm.in_cap = ctx->ovf_cap;
+  }
+  cudaError_t e;
+  const int prec = ctx->cfg.precision;
+  if (prec == MTG_PREC_FP64)
+    e = launch_cascade64(prm, ctx->grid, ctx->block, ctx->smem, ctx->stream);
+  else
+  {
+    Fp32Tables ft;
+    ft.stop = ptr<float>(ctx->d_stop);
+    ft.lnE_min = float(std::log(STOP_EMIN));
+    ft.inv_dlnE = float(1.0 / ((std::log(ctx->tables.emax * 1.05) - std::log(STOP_EMIN)) / (STOP_N - 1)));
+    ft.mlp = nullptr;
+    ft.sims32 = ctx->d_sims32.p;
+    e = launch_cascade32(prm, ft, ctx->grid, ctx->block, ctx->smem, ctx->stream,
+                         prec == MTG_PREC_FP32_SURROGATE);
+  }
+  if (e != cudaSuccess)
+    return fail(ctx, MTG_ERR_CUDA, std::string("cascade launch: ") + cudaGetErrorString(e));
+  ctx->passes = pass + 1;
+  ctx->ovf_last = out_list;
+  ctx->stats.launches += 1;
+  return MTG_OK;
+}
+
+mtg_status
+launch_reduction(mtg_ctx * ctx)
+{
+  PrimaryTallies pt;
+  pt.vac = ptr<unsigned long long>(ctx->p_vac);
+  pt.coll = ptr<unsigned long long>(ctx->p_coll);
+  pt.eel = ptr<double>(ctx->p_eel);
+  pt.enuc = ptr<double>(ctx->p_enuc);
+  pt.fx = ptr<double>(ctx->p_fx);
+  pt.fy = ptr<double>(ctx->p_fy);
+  pt.fz = ptr<double>(ctx->p_fz);
+  pt.fstate = ptr<int>(ctx->p_state);
+  cudaError_t e = launch_reduce(ptr<ReduceJob>(ctx->d_jobs), int(ctx->jobs.size()), pt, ptr<double>(ctx->d_partials),
+                                ptr<int>(ctx->d_job_first), int(ctx->tables.sims.size()), ptr<double>(ctx->d_out),
+                                ctx->stream);
+  if (e != cudaSuccess)
+    return fail(ctx, MTG_ERR_CUDA, std::string("reduction launch: ") + cudaGetErrorString(e));
+  ctx->stats.launches += (ctx->jobs.empty() ? 1 : 2);
+  return MTG_OK;
+}
+
+mtg_status
+require_device(mtg_ctx * ctx)
+{
+  if (!ctx)
+    return MTG_ERR_BAD_INPUT;
+  CK(cudaSetDevice(ctx->device));
+  return MTG_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+mtg_status
+mtg_create(int device, mtg_ctx ** out)
+{
+  if (!out)
+    return MTG_ERR_BAD_INPUT;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0)
+    return MTG_ERR_NO_DEVICE;
+  if (device < 0 || device >= n)
+    return MTG_ERR_BAD_INPUT;
+  if (cudaSetDevice(device) != cudaSuccess)
+    return MTG_ERR_CUDA;
+  mtg_ctx * ctx = new mtg_ctx();
+  ctx->device = device;
+  ctx->cfg = default_config();
+  std::memset(&ctx->stats, 0, sizeof ctx->stats);
+  cudaDeviceGetAttribute(&ctx->n_sm, cudaDevAttrMultiProcessorCount, device);
+  for (auto & e : ctx->ev)
+    if (cudaEventCreate(&e) != cudaSuccess)
+    {
+      delete ctx;
+      return MTG_ERR_CUDA;
+    }
+  *out = ctx;
+  return MTG_OK;
+}
+
+mtg_status
+mtg_destroy(mtg_ctx * ctx)
+{
+  if (!ctx)
+    return MTG_OK;
+  cudaSetDevice(ctx->device);
+  DevBuf * bufs[] = {&ctx->d_sims,   &ctx->d_prim_end, &ctx->d_species, &ctx->d_mats,    &ctx->d_row_species,
+                     &ctx->d_stop,   &ctx->p_vac,      &ctx->p_coll,    &ctx->p_eel,     &ctx->p_enuc,
+                     &ctx->p_fx,     &ctx->p_fy,       &ctx->p_fz,      &ctx->p_state,   &ctx->d_totals,
+                     &ctx->d_hist,   &ctx->d_err,      &ctx->d_counters, &ctx->d_stacks, &ctx->d_ovf0,
+                     &ctx->d_ovf1,   &ctx->d_records,  &ctx->d_jobs,    &ctx->d_job_first, &ctx->d_partials,
+                     &ctx->d_out,    &ctx->d_tmp0,     &ctx->d_tmp1,    &ctx->d_tmp2,    &ctx->d_tmp3,
+                     &ctx->d_species32, &ctx->d_mats32, &ctx->d_sims32};
+  for (DevBuf * b : bufs)
+    if (b->p)
+      cudaFree(b->p);
+  for (auto & e : ctx->ev)
+    if (e)
+      cudaEventDestroy(e);
+  delete ctx;
+  return MTG_OK;
+}
+
+const char *
+mtg_last_error(const mtg_ctx * ctx)
+{
+  return ctx ? ctx->err.c_str() : "no context";
+}
+
+mtg_status
+mtg_set_tables(mtg_ctx * ctx, const mtg_scoef_row * rows, int n_rows)
+{
+  if (!ctx)
+    return MTG_ERR_BAD_INPUT;
+  if (!rows || n_rows != MTG_SCOEF_ROWS)
+    return fail(ctx, MTG_ERR_DATA, "stopping tables must hold 92 rows");
+  std::memcpy(ctx->rows, rows, sizeof(mtg_scoef_row) * MTG_SCOEF_ROWS);
+  ctx->have_tables = true;
+  ctx->prepared = false;
+  return MTG_OK;
+}
+
+mtg_status
+mtg_load_tables(mtg_ctx * ctx, const char * path)
+{
+  if (!ctx)
+    return MTG_ERR_BAD_INPUT;
+  if (!path)
+    return fail(ctx, MTG_ERR_DATA, "no table path");
+  std::string err;
+  mtg_scoef_row rows[MTG_SCOEF_ROWS];
+  if (!read_table_file(path, rows, err))
+    return fail(ctx, MTG_ERR_DATA, err);
+  return mtg_set_tables(ctx, rows, MTG_SCOEF_ROWS);
+}
+
+mtg_status
+mtg_configure(mtg_ctx * ctx, const mtg_config * cfg)
+{
+  if (!ctx || !cfg)
+    return MTG_ERR_BAD_INPUT;
+  if (cfg->precision < MTG_PREC_FP64 || cfg->precision > MTG_PREC_FP32_SURROGATE)
+    return fail(ctx, MTG_ERR_BAD_INPUT, "unknown precision");
+  if (!(cfg->length_scale > 0.0) || !(cfg->tmin > 0.0) || !(cfg->cw > 0.0) || cfg->stack_capacity < 0)
+    return fail(ctx, MTG_ERR_BAD_INPUT, "length_scale, tmin and cw must be positive");
+  ctx->cfg = *cfg;
+  ctx->prepared = false;
+  return MTG_OK;
+}
+
+mtg_status
+mtg_prepare(mtg_ctx * ctx, const mtg_sim * sims, int n_sims)
+{
+  mtg_status st = require_device(ctx);
+  if (st != MTG_OK)
+    return st;
+  if (!ctx->have_tables)
+    return fail(ctx, MTG_ERR_STATE, "stopping tables not loaded");
+  std::string err;
+  int rc = build_tables(ctx->rows, ctx->cfg, sims, n_sims, ctx->tables, err);
+  if (rc != MTG_OK)
+    return fail(ctx, mtg_status(rc), err);
+  const HostTables & t = ctx->tables;
+  const size_t ns = t.sims.size();
+  const size_t np = size_t(std::max<long long>(t.total_primaries, 1));
+  CK(ensure(ctx->d_sims, sizeof(SimDesc) * ns));
+  CK(ensure(ctx->d_prim_end, sizeof(long long) * ns));
+  CK(ensure(ctx->d_species, sizeof(SpeciesConst) * t.species.size()));
+  CK(ensure(ctx->d_mats, sizeof(MatConst) * t.mats.size()));
+  CK(ensure(ctx->p_vac, 8 * np));
+  CK(ensure(ctx->p_coll, 8 * np));
+  CK(ensure(ctx->p_eel, 8 * np));
+  CK(ensure(ctx->p_enuc, 8 * np));
+  CK(ensure(ctx->p_fx, 8 * np));
+  CK(ensure(ctx->p_fy, 8 * np));
+  CK(ensure(ctx->p_fz, 8 * np));
+  CK(ensure(ctx->p_state, 4 * np));
+  CK(ensure(ctx->d_totals, sizeof(SimTotals) * ns));
+  CK(ensure(ctx->d_hist, 8 * size_t(std::max<long long>(t.hist_total, 1))));
+  CK(ensure(ctx->d_err, 16));
+  CK(ensure(ctx->d_counters, 8 * C_COUNT));
+  CK(cudaMemcpy(ctx->d_sims.p, t.sims.data(), sizeof(SimDesc) * ns, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_prim_end.p, t.prim_end.data(), sizeof(long long) * ns, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_species.p, t.species.data(), sizeof(SpeciesConst) * t.species.size(),
+                cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_mats.p, t.mats.data(), sizeof(MatConst) * t.mats.size(), cudaMemcpyHostToDevice));
+
+  // reduction jobs: contiguous chunks of at most 65536 primaries per simulation
+  ctx->jobs.clear();
+  ctx->job_first.assign(1, 0);
+  for (size_t s = 0; s < ns; ++s)
+  {
+    const long long b = t.sims[s].prim_begin, n = t.sims[s].n_primaries;
+    const long long chunk = 65536;
+    for (long long o = 0; o < n; o += chunk)
+      ctx->jobs.push_back(ReduceJob{int(s), b + o, b + std::min(n, o + chunk)});
+    ctx->job_first.push_back(int(ctx->jobs.size()));
+  }
+  CK(ensure(ctx->d_jobs, sizeof(ReduceJob) * std::max<size_t>(ctx->jobs.size(), 1)));
+  CK(ensure(ctx->d_job_first, sizeof(int) * ctx->job_first.size()));
+  CK(ensure(ctx->d_partials, sizeof(double) * NQ * std::max<size_t>(ctx->jobs.size(), 1)));
+  CK(ensure(ctx->d_out, sizeof(double) * NQ * ns));
+  if (!ctx->jobs.empty())
+    CK(cudaMemcpy(ctx->d_jobs.p, ctx->jobs.data(), sizeof(ReduceJob) * ctx->jobs.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_job_first.p, ctx->job_first.data(), sizeof(int) * ctx->job_first.size(),
+                cudaMemcpyHostToDevice));
+
+  if (ctx->cfg.precision != MTG_PREC_FP64)
+  {
+    // FP32 path: stopping tables evaluated on the device in FP64
+    std::vector<int> row_species(t.mats.size());
+    for (size_t s = 0; s < ns; ++s)
+      for (int sp = 0; sp < t.sims[s].n_species; ++sp)
+        for (int k = 0; k < t.sims[s].n_mat; ++k)
+          row_species[t.sims[s].mat_base + sp * t.sims[s].n_mat + k] = t.sims[s].species_base + sp;
+    CK(ensure(ctx->d_row_species, sizeof(int) * row_species.size()));
+    CK(ensure(ctx->d_stop, sizeof(float) * STOP_N * t.mats.size()));
+    CK(cudaMemcpy(ctx->d_row_species.p, row_species.data(), sizeof(int) * row_species.size(),
+                  cudaMemcpyHostToDevice));
+    const double lo = std::log(STOP_EMIN), hi = std::log(t.emax * 1.05);
+    CK(launch_build_stop_tables(ptr<SpeciesConst>(ctx->d_species), ptr<MatConst>(ctx->d_mats), nullptr, 0,
+                                int(t.mats.size()), ptr<int>(ctx->d_row_species), ptr<float>(ctx->d_stop), lo,
+                                (hi - lo) / (STOP_N - 1), nullptr));
+    CK(cudaDeviceSynchronize());
+    std::vector<Species32> sp32;
+    std::vector<Mat32> mc32;
+    std::vector<Sim32> sm32;
+    build_fp32_tables(t, sp32, mc32, sm32);
+    CK(ensure(ctx->d_species32, sizeof(Species32) * sp32.size()));
+    CK(ensure(ctx->d_mats32, sizeof(Mat32) * mc32.size()));
+    CK(ensure(ctx->d_sims32, sizeof(Sim32) * sm32.size()));
+    CK(cudaMemcpy(ctx->d_species32.p, sp32.data(), sizeof(Species32) * sp32.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_mats32.p, mc32.data(), sizeof(Mat32) * mc32.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_sims32.p, sm32.data(), sizeof(Sim32) * sm32.size(), cudaMemcpyHostToDevice));
+  }
+  if (ctx->record_cap > 0)
+    CK(ensure(ctx->d_records, sizeof(MemberRecord) * size_t(ctx->record_cap)));
+  st = setup_launch_shape(ctx);
+  if (st != MTG_OK)
+    return st;
+  ctx->prepared = true;
+  ctx->launched = false;
+  return MTG_OK;
+}
+
+mtg_status
+mtg_launch_async(mtg_ctx * ctx, void * stream)
+{
+  mtg_status st = require_device(ctx);
+  if (st != MTG_OK)
+    return st;
+  if (!ctx->prepared)
+    return fail(ctx, MTG_ERR_STATE, "mtg_prepare must come first");
+  ctx->stream = reinterpret_cast<cudaStream_t>(stream);
+  const HostTables & t = ctx->tables;
+  const size_t np = size_t(std::max<long long>(t.total_primaries, 1));
+  ctx->stats.launches = 0;
+  ctx->stats.drains = 0;
+  cudaStream_t s = ctx->stream;
+  CK(cudaMemsetAsync(ctx->p_vac.p, 0, 8 * np, s));
+  CK(cudaMemsetAsync(ctx->p_coll.p, 0, 8 * np, s));
+  CK(cudaMemsetAsync(ctx->p_eel.p, 0, 8 * np, s));
+  CK(cudaMemsetAsync(ctx->p_enuc.p, 0, 8 * np, s));
+  CK(cudaMemsetAsync(ctx->p_state.p, 0, 4 * np, s));
+  CK(cudaMemsetAsync(ctx->d_totals.p, 0, sizeof(SimTotals) * t.sims.size(), s));
+  CK(cudaMemsetAsync(ctx->d_hist.p, 0, 8 * size_t(std::max<long long>(t.hist_total, 1)), s));
+  CK(cudaMemsetAsync(ctx->d_err.p, 0, 16, s));
+  CK(cudaMemsetAsync(ctx->d_counters.p, 0, 8 * C_COUNT, s));
+  CK(cudaEventRecord(ctx->ev[0], s));
+  st = launch_pass(ctx, 0);
+  if (st != MTG_OK)
+    return st;
+  st = launch_pass(ctx, 1); // drains whatever the first pass spilled (usually nothing)
+  if (st != MTG_OK)
+    return st;
+  CK(cudaEventRecord(ctx->ev[1], s));
+  st = launch_reduction(ctx);
+  if (st != MTG_OK)
+    return st;
+  CK(cudaEventRecord(ctx->ev[2], s));
+  ctx->launched = true;
+  return MTG_OK;
+}
+
+mtg_status
+mtg_collect(mtg_ctx * ctx, mtg_totals * totals, long long * hist)
+{
+  mtg_status st = require_device(ctx);
+  if (st != MTG_OK)
+    return st;
+  if (!ctx->launched)
+    return fail(ctx, MTG_ERR_STATE, "nothing launched");
+  CK(cudaStreamSynchronize(ctx->stream));
+  const HostTables & t = ctx->tables;
+  unsigned long long cnt[C_COUNT];
+  CK(cudaMemcpy(cnt, ctx->d_counters.p, sizeof cnt, cudaMemcpyDeviceToHost));
+  // further drain passes while the last pass spilled members
+  long long overflowed = (long long)cnt[C_OVF0];
+  int extra = 0;
+  while (cnt[ctx->ovf_last ? C_OVF1 : C_OVF0] > 0 && ctx->passes < MAX_PASSES)
+  {
+    overflowed += (long long)cnt[ctx->ovf_last ? C_OVF1 : C_OVF0];
+    st = launch_pass(ctx, ctx->passes);
+    if (st != MTG_OK)
+      return st;
+    ++extra;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(cnt, ctx->d_counters.p, sizeof cnt, cudaMemcpyDeviceToHost));
+  }
+  const bool unfinished = cnt[ctx->ovf_last ? C_OVF1 : C_OVF0] > 0;
+  if (extra)
+  {
+    st = launch_reduction(ctx);
+    if (st != MTG_OK)
+      return st;
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  float ms = 0.0f;
+  if (!extra)
+  {
+    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+    ctx->stats.kernel_ms = ms;
+    cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
+    ctx->stats.reduce_ms = ms;
+  }
+  ctx->stats.drains = ctx->passes - 1;
+  ctx->stats.grid = ctx->grid;
+  ctx->stats.block = ctx->block;
+  ctx->stats.stack_capacity = ctx->stack_cap;
+  ctx->stats.overflowed = overflowed;
+
+  unsigned int errf = 0;
+  CK(cudaMemcpy(&errf, ctx->d_err.p, sizeof errf, cudaMemcpyDeviceToHost));
+  const size_t ns = t.sims.size();
+  std::vector<double> out(NQ * ns);
+  std::vector<SimTotals> tot(ns);
+  CK(cudaMemcpy(out.data(), ctx->d_out.p, sizeof(double) * NQ * ns, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(tot.data(), ctx->d_totals.p, sizeof(SimTotals) * ns, cudaMemcpyDeviceToHost));
+  long long coll_all = 0;
+  if (totals)
+    for (size_t s = 0; s < ns; ++s)
+    {
+      mtg_totals & o = totals[s];
+      std::memset(&o, 0, sizeof o);
+      const double * q = &out[NQ * s];
+      o.primaries = t.sims[s].n_primaries;
+      o.members = (long long)tot[s].members;
+      o.collisions = (long long)llround(q[2]);
+      o.vacancies = (long long)llround(q[0]);
+      o.replacements = (long long)tot[s].replacements;
+      o.interstitials = (long long)tot[s].interstitials;
+      o.substitutionals = (long long)tot[s].substitutionals;
+      o.lost = (long long)tot[s].lost;
+      o.Eel = q[4];
+      o.Enuc = q[6];
+      o.Elost = tot[s].Elost;
+      o.Eunfollowed = tot[s].Eunfollowed;
+      o.range_n = (long long)llround(q[8]);
+      o.sx = q[9];
+      o.sxx = q[10];
+      o.sy = q[11];
+      o.syy = q[12];
+      o.sz = q[13];
+      o.szz = q[14];
+      o.vac_s2 = q[1];
+      o.eel_s2 = q[5];
+      o.enuc_s2 = q[7];
+      o.coll_s2 = q[3];
+      o.newton_iterations = (long long)tot[s].newton_iters;
+      o.rejection_passes = (long long)tot[s].rejection_passes;
+      o.surrogate_fallbacks = (long long)tot[s].fallbacks;
+      coll_all += o.collisions;
+    }
+  ctx->stats.collisions = coll_all;
+  if (hist && t.hist_total > 0)
+  {
+    std::vector<unsigned long long> h(t.hist_total);
+    CK(cudaMemcpy(h.data(), ctx->d_hist.p, 8 * h.size(), cudaMemcpyDeviceToHost));
+    for (long long i = 0; i < t.hist_total; ++i)
+      hist[i] = (long long)h[i];
+  }
+  size_t bytes = 0;
+  DevBuf * bufs[] = {&ctx->d_sims,   &ctx->d_prim_end, &ctx->d_species, &ctx->d_mats,    &ctx->d_row_species,
+                     &ctx->d_stop,   &ctx->p_vac,      &ctx->p_coll,    &ctx->p_eel,     &ctx->p_enuc,
+                     &ctx->p_fx,     &ctx->p_fy,       &ctx->p_fz,      &ctx->p_state,   &ctx->d_totals,
+                     &ctx->d_hist,   &ctx->d_err,      &ctx->d_counters, &ctx->d_stacks, &ctx->d_ovf0,
+                     &ctx->d_ovf1,   &ctx->d_records,  &ctx->d_jobs,    &ctx->d_job_first, &ctx->d_partials,
+                     &ctx->d_out,    &ctx->d_species32, &ctx->d_mats32, &ctx->d_sims32};
+  for (DevBuf * b : bufs)
+    bytes += b->bytes;
+  ctx->stats.device_bytes = bytes;
+
+  if (unfinished || (errf & ERRB_QUEUE_FULL))
+    return fail(ctx, MTG_ERR_QUEUE_FULL, "recoil overflow list exhausted; results incomplete");
+  if (errf & ERRB_BUDGET)
+    return fail(ctx, MTG_ERR_TIMEOUT, "a cascade member exceeded the collision budget");
+  if (errf & ERRB_NUMERIC)
+    return fail(ctx, MTG_ERR_NUMERIC, "non-finite energy or degenerate direction met");
+  return MTG_OK;
+}
+
+mtg_status
+mtg_run(mtg_ctx * ctx, const mtg_sim * sims, int n_sims, mtg_totals * totals, long long * hist)
+{
+  mtg_status st = mtg_prepare(ctx, sims, n_sims);
+  if (st != MTG_OK)
+    return st;
+  st = mtg_launch_async(ctx, nullptr);
+  if (st != MTG_OK)
+    return st;
+  return mtg_collect(ctx, totals, hist);
+}
+
+mtg_status
+mtg_get_primaries(mtg_ctx * ctx, long long first, long long n, long long * vacancies, long long * collisions,
+                  double * eel, double * enuc, double * x, double * y, double * z, int * state)
+{
+  mtg_status st = require_device(ctx);
+  if (st != MTG_OK)
+    return st;
+  if (!ctx->launched)
+    return fail(ctx, MTG_ERR_STATE, "no run to read");
+  if (first < 0 || n < 0 || first + n > ctx->tables.total_primaries)
+    return fail(ctx, MTG_ERR_BAD_INPUT, "primary range out of bounds");
+  if (n == 0)
+    return MTG_OK;
+  auto get_u64 = [&](DevBuf & b, long long * dst) -> cudaError_t {
+    if (!dst)
+      return cudaSuccess;
+    return cudaMemcpy(dst, ptr<unsigned long long>(b) + first, 8 * n, cudaMemcpyDeviceToHost);
+  };
+  auto get_f64 = [&](DevBuf & b, double * dst) -> cudaError_t {
+    if (!dst)
+      return cudaSuccess;
+    return cudaMemcpy(dst, ptr<double>(b) + first, 8 * n, cudaMemcpyDeviceToHost);
+  };
+  CK(get_u64(ctx->p_vac, vacancies));
+  CK(get_u64(ctx->p_coll, collisions));
+  CK(get_f64(ctx->p_eel, eel));
+  CK(get_f64(ctx->p_enuc, enuc));
+  CK(get_f64(ctx->p_fx, x));
+  CK(get_f64(ctx->p_fy, y));
+  CK(get_f64(ctx->p_fz, z));
+  if (state)
+    CK(cudaMemcpy(state, ptr<int>(ctx->p_state) + first, 4 * n, cudaMemcpyDeviceToHost));
+  return MTG_OK;
+}
+
+mtg_status
+mtg_set_record_capacity(mtg_ctx * ctx, long long capacity)
+{
+  if (!ctx || capacity < 0)
+    return MTG_ERR_BAD_INPUT;
+  ctx->record_cap = capacity;
+  ctx->prepared = false;
+  return MTG_OK;
+}
+
+mtg_status
+mtg_get_records(mtg_ctx * ctx, mtg_member_record * out, long long capacity, long long * n_written)
+{
+  mtg_status st = require_device(ctx);
+  if (st != MTG_OK)
+    return st;
+  if (!out || !n_written || capacity < 0)
+    return fail(ctx, MTG_ERR_BAD_INPUT, "bad record buffer");
+  *n_written = 0;
+  if (ctx->record_cap <= 0 || !ctx->launched)
+    return MTG_OK;
+  unsigned long long n = 0;
+  CK(cudaMemcpy(&n, ptr<unsigned long long>(ctx->d_counters) + C_NREC, 8, cudaMemcpyDeviceToHost));
+  long long m = std::min<long long>((long long)n, std::min(capacity, ctx->record_cap));
+  static_assert(sizeof(mtg_member_record) == sizeof(MemberRecord), "record layout");
+  if (m > 0)
+    CK(cudaMemcpy(out, ctx->d_records.p, sizeof(MemberRecord) * m, cudaMemcpyDeviceToHost));
+  *n_written = m;
+  if ((long long)n > ctx->record_cap)
+    return fail(ctx, MTG_ERR_QUEUE_FULL, "record buffer too small; records truncated");
+  return MTG_OK;
+}
+
+mtg_status
+mtg_stopping(mtg_ctx * ctx, int Z1, double m1, const mtg_material * material, const double * E, long long n,
+             int precision, double * out)
+{
+  mtg_status st = require_device(ctx);
+  if (st != MTG_OK)
+    return st;
+  if (!ctx->have_tables)
+    return fail(ctx, MTG_ERR_STATE, "stopping tables not loaded");
+  if (!material || (n > 0 && (!E || !out)) || n < 0 || Z1 < 1 || Z1 > MTG_SCOEF_ROWS)
+    return fail(ctx, MTG_ERR_BAD_INPUT, "bad stopping request");
+  if (precision != MTG_PREC_FP64 && precision != MTG_PREC_FP32)
+    return fail(ctx, MTG_ERR_BAD_INPUT, "stopping precision must be FP64 or FP32");
+  std::string err;
+  SpeciesConst sc = make_species(ctx->rows, Z1, m1);
+  MatConst mc;
+  int rc = make_material(ctx->rows, sc, *material, ctx->cfg.tmin, mc, err);
+  if (rc != MTG_OK)
+    return fail(ctx, mtg_status(rc), err);
+  if (n == 0)
+    return MTG_OK;
+  CK(ensure(ctx->d_tmp0, sizeof sc + sizeof mc));
+  CK(ensure(ctx->d_tmp1, 8 * size_t(n)));
+  CK(ensure(ctx->d_tmp2, 8 * size_t(n)));
+  SpeciesConst * d_sc = ptr<SpeciesConst>(ctx->d_tmp0);
+  MatConst * d_mc = reinterpret_cast<MatConst *>(reinterpret_cast<char *>(ctx->d_tmp0.p) + sizeof sc);
+  CK(cudaMemcpy(d_sc, &sc, sizeof sc, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_mc, &mc, sizeof mc, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_tmp1.p, E, 8 * n, cudaMemcpyHostToDevice));
+  if (precision == MTG_PREC_FP64)
+    CK(launch_stopping64(d_sc, d_mc, ptr<double>(ctx->d_tmp1), n, ptr<double>(ctx->d_tmp2), nullptr));
+  else
+  {
+    // one stopping-table row, exactly as the FP32 engine builds it
+    double emax = 0.0;
+    for (long long i = 0; i < n; ++i)
+      emax = std::max(emax, E[i]);
+    const double lo = std::log(STOP_EMIN), hi = std::log(std::max(emax, 1.0) * 1.05);
+    const double dl = (hi - lo) / (STOP_N - 1);
+    CK(ensure(ctx->d_tmp3, sizeof(float) * STOP_N + sizeof(int)));
+    int zero = 0;
+    int * d_rs = reinterpret_cast<int *>(reinterpret_cast<char *>(ctx->d_tmp3.p) + sizeof(float) * STOP_N);
+    CK(cudaMemcpy(d_rs, &zero, sizeof zero, cudaMemcpyHostToDevice));
+    CK(launch_build_stop_tables(d_sc, d_mc, nullptr, 0, 1, d_rs, ptr<float>(ctx->d_tmp3), lo, dl, nullptr));
+    CK(launch_stopping32(ptr<float>(ctx->d_tmp3), float(lo), float(1.0 / dl), ptr<double>(ctx->d_tmp1), n,
+                         ptr<double>(ctx->d_tmp2), nullptr));
+  }
+  CK(cudaMemcpy(out, ctx->d_tmp2.p, 8 * n, cudaMemcpyDeviceToHost));
+  return MTG_OK;
+}
+
+mtg_status
+mtg_scatter(mtg_ctx * ctx, const double * eps, const double * b, long long n, int precision, double * s2)
+{
+  mtg_status st = require_device(ctx);
+  if (st != MTG_OK)
+    return st;
+  if (n < 0 || (n > 0 && (!eps || !b || !s2)))
+    return fail(ctx, MTG_ERR_BAD_INPUT, "bad scatter request");
+  if (n == 0)
+    return MTG_OK;
+  CK(ensure(ctx->d_tmp1, 8 * size_t(n)));
+  CK(ensure(ctx->d_tmp2, 8 * size_t(n)));
+  CK(ensure(ctx->d_tmp3, 8 * size_t(n)));
+  CK(cudaMemcpy(ctx->d_tmp1.p, eps, 8 * n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_tmp2.p, b, 8 * n, cudaMemcpyHostToDevice));
+  if (precision == MTG_PREC_FP64)
+    CK(launch_scatter64(ptr<double>(ctx->d_tmp1), ptr<double>(ctx->d_tmp2), n, ptr<double>(ctx->d_tmp3), nullptr));
+  else if (precision == MTG_PREC_FP32)
+    CK(launch_scatter32(ptr<double>(ctx->d_tmp1), ptr<double>(ctx->d_tmp2), n, ptr<double>(ctx->d_tmp3), nullptr,
+                        0, nullptr));
+  else
+    return fail(ctx, MTG_ERR_STATE, "no trained surrogate loaded");
+  CK(cudaMemcpy(s2, ctx->d_tmp3.p, 8 * n, cudaMemcpyDeviceToHost));
+  return MTG_OK;
+}
+
+mtg_status
+mtg_get_stats(const mtg_ctx * ctx, mtg_stats * out)
+{
+  if (!ctx || !out)
+    return MTG_ERR_BAD_INPUT;
+  *out = ctx->stats;
+  return MTG_OK;
+}
+
+} // extern "C"

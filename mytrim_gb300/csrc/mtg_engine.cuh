@@ -1,0 +1,508 @@
+// Persistent, warp-cooperative cascade kernel.
+//
+// The reference follows one cascade with a host FIFO: pop a member, run
+// TrimBase::trim on it until it stops, push every recoil it displaces
+// (apps/runmytrim.C:71-93, trim.C:369).  Here every lane of a warp holds one
+// cascade member in registers and the 32 lanes advance one collision per loop
+// iteration.  Each warp owns a LIFO recoil stack in HBM:
+//   * a lane whose member came to rest pops the next recoil from its warp's
+//     stack (warp-synchronous ballot + prefix count, no atomics);
+//   * with the stack empty, idle lanes take fresh primaries from one global
+//     counter (one atomicAdd per warp refill);
+//   * recoils are pushed with a ballot + prefix count; a full stack spills into
+//     a global overflow list that a follow-up launch drains.
+// No warp ever waits on another, so the kernel needs no spin loops; every loop
+// is bounded (collisions per member, Newton iterations, rejection passes).
+//
+// Random numbers are keyed by the member's path key and collision index, so the
+// result does not depend on which lane or warp ran which member.
+//
+// Tallies: per-lane accumulators flushed to per-primary arrays when a lane
+// switches primary (vacancies, collisions, electronic and nuclear energy), the
+// primary's stopping point written once, depth histograms through warp-aggregated
+// atomics (__match_any_sync), per-simulation counters flushed once per lane.
+#pragma once
+
+#include "mtg_tables.h"
+#include "mtg_common.cuh"
+
+namespace mtg
+{
+
+struct PrimaryTallies
+{
+  unsigned long long * vac;  // vacancies (KP count in range mode)
+  unsigned long long * coll; // collisions
+  double * eel;              // electronic loss [eV]
+  double * enuc;             // nuclear (phonon) deposit [eV]
+  double * fx;               // stopping point of the primary (generation 0)
+  double * fy;
+  double * fz;
+  int * fstate;              // final state of the primary, 0 if lost / not stopped
+};
+
+struct MemberRecord
+{
+  uint64_t key;
+  int sim, species, gen, state;
+  unsigned int ncoll, nvac;
+  double E, x, y, z, eel;
+};
+
+struct EngineParams
+{
+  const SimDesc * sims;
+  int n_sims;
+  const long long * sim_prim_end; // exclusive prefix end of each simulation's primaries
+  const SpeciesConst * species;
+  const MatConst * mats;
+  int stage_tables;               // stage species+mats of simulation 0 into shared memory
+  int n_stage_species, n_stage_mats;
+  long long total_primaries;
+  unsigned long long * next_primary;
+  // drain mode: members read from `in_records` (count in device memory) instead
+  // of fresh primaries
+  const void * in_records;
+  const unsigned long long * in_count;
+  long long in_cap;
+  // per-warp stacks and overflow list
+  void * stacks;
+  int stack_cap;
+  void * overflow;
+  unsigned long long * overflow_count;
+  long long overflow_cap;
+  // tallies
+  PrimaryTallies prim;
+  SimTotals * totals;
+  unsigned long long * hist; // all histograms, per-simulation bases in SimDesc
+  unsigned int * error_flags;
+  uint32_t k0, k1;
+  unsigned int max_collisions; // per member
+  // optional per-member records (replay checks)
+  MemberRecord * records;
+  unsigned long long * n_records;
+  long long records_cap;
+};
+
+__device__ __forceinline__ unsigned int
+lanemask_lt()
+{
+  unsigned int m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+__device__ __forceinline__ int
+find_sim(const long long * ends, int n, long long g)
+{
+  int lo = 0, hi = n - 1;
+  while (lo < hi)
+  {
+    const int mid = (lo + hi) >> 1;
+    if (g < ends[mid])
+      hi = mid;
+    else
+      lo = mid + 1;
+  }
+  return lo;
+}
+
+// Plain FP64 accumulator (FP64 engine)
+struct AccF64
+{
+  double s;
+  __device__ void reset() { s = 0.0; }
+  __device__ void add(double x) { s += x; }
+  __device__ double value() const { return s; }
+  __device__ bool nonzero() const { return s != 0.0; }
+};
+
+// Kahan-compensated FP32 accumulator (FP32 engine): keeps FP64 work out of the
+// per-collision path while the sum stays accurate to ~1e-14 relative
+struct AccKahan32
+{
+  float s, c;
+  __device__ void reset() { s = c = 0.0f; }
+  __device__ void add(float x)
+  {
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ double value() const { return double(s) - double(c); }
+  __device__ bool nonzero() const { return s != 0.0f; }
+};
+
+// Device tally sink for one lane.
+template <class Pol>
+struct LaneSink
+{
+  using Acc = typename Pol::Acc;
+  using Real = typename Pol::Real;
+  const EngineParams * prm;
+  const SimDesc * sim;
+  long long gprim;     // global primary index of the current member
+  int range_mode;
+  // per-primary accumulators
+  unsigned long long a_vac, a_coll;
+  Acc a_eel, a_enuc;
+  // per-simulation accumulators
+  unsigned long long n_repl, n_inter, n_subst, n_lost, n_members, n_newton, n_passes, n_fallbacks;
+  double e_lost, e_unf;
+  // events of the current collision, aggregated per warp after it
+  int vac_bin, repl_bin;
+  // current member record
+  unsigned int m_vac;
+  int m_state;
+  Acc m_eel;
+
+  __device__ void reset_sim()
+  {
+    n_repl = n_inter = n_subst = n_lost = n_members = n_newton = n_passes = n_fallbacks = 0;
+    e_lost = e_unf = 0.0;
+  }
+  __device__ void reset_prim()
+  {
+    a_vac = a_coll = 0;
+    a_eel.reset();
+    a_enuc.reset();
+  }
+
+  // ---- events raised by the collision code (the reference's hooks, trim.h:72-84)
+  __device__ void eel(Real d)
+  {
+    a_eel.add(d);
+    m_eel.add(d);
+  }
+  __device__ void newton(int n) { n_newton += (unsigned long long)n; }
+  __device__ void passes(int n) { n_passes += (unsigned long long)n; }
+  __device__ void fallback() { ++n_fallbacks; }
+  __device__ void numeric() { atomicOr(prm->error_flags, ERRB_NUMERIC); }
+  __device__ void enuc(Real e) { a_enuc.add(e); }
+  __device__ void unfollowed(Real e) { e_unf += double(e); }
+  __device__ void lost(Real e)
+  {
+    ++n_lost;
+    e_lost += double(e);
+    m_state = ST_LOST;
+  }
+
+  template <class R, class E>
+  __device__ void vacancy(const R & rec, const E & el)
+  {
+    if (range_mode)
+    {
+      // TrimRange::vacancyCreation (apps/src/TrimRange.C:32-47): Kinchin-Pease
+      // count of the displaced recoil, each increment truncated like the
+      // reference's int accumulator
+      const double Z = double(el.Z2), m = el.m2, Er = double(rec.E);
+      const double Ed = el.Edisp;
+      const double ed = 0.0115 * pow64(Z, -7.0 / 3.0) * Er;
+      const double kd = 0.1337 * pow64(Z, 2.0 / 3.0) / sqrt(m);
+      const double g = 3.4008 * pow64(ed, 1.0 / 6.0) + 0.40244 * pow64(ed, 3.0 / 4.0) + ed;
+      const double Ev = Er / (1.0 + kd * g);
+      unsigned long long add = 0;
+      if (Ev < Ed)
+        add = 0;
+      else if (Ev >= Ed / 0.4)
+        add = (unsigned long long)(Ev * 0.4 / Ed);
+      else
+        add = 1;
+      a_vac += add;
+      m_vac += (unsigned int)add;
+      return;
+    }
+    ++a_vac;
+    ++m_vac;
+    vac_bin = depth_bin(double(rec.x), sim->inv_hist_vac_bin, sim->hist_vac_n);
+    if (vac_bin >= 0)
+      vac_bin += int(sim->hist_vac_base);
+  }
+  __device__ void replacement(double x)
+  {
+    ++n_repl;
+    repl_bin = depth_bin(x, sim->inv_hist_vac_bin, sim->hist_vac_n);
+    if (repl_bin >= 0)
+      repl_bin += int(sim->hist_vac_base + sim->hist_vac_n);
+  }
+  template <class P>
+  __device__ void stop(int state, const P & p)
+  {
+    m_state = state;
+    a_enuc.add(Real(p.E));
+    if (state == ST_INTERSTITIAL)
+      ++n_inter;
+    else if (state == ST_SUBSTITUTIONAL)
+      ++n_subst;
+    if (p.gen == 0)
+    {
+      prm->prim.fx[gprim] = double(p.x);
+      prm->prim.fy[gprim] = double(p.y);
+      prm->prim.fz[gprim] = double(p.z);
+      prm->prim.fstate[gprim] = state;
+      const int b = depth_bin(double(p.x), sim->inv_hist_range_bin, sim->hist_range_n);
+      if (b >= 0)
+        atomicAdd(prm->hist + sim->hist_range_base + b, 1ull);
+    }
+  }
+
+  // truncation toward zero like int(x) in the reference (TrimVacCount.C:36-39)
+  static __device__ int depth_bin(double x, double inv_bin, int n)
+  {
+    const double q = x * inv_bin;
+    if (n <= 0 || !(q > -1.0) || q >= double(n))
+      return -1;
+    return int(q);
+  }
+
+  __device__ void flush_prim()
+  {
+    if (gprim < 0)
+      return;
+    if (a_vac)
+      atomicAdd(prm->prim.vac + gprim, a_vac);
+    if (a_coll)
+      atomicAdd(prm->prim.coll + gprim, a_coll);
+    if (a_eel.nonzero())
+      atomicAdd(prm->prim.eel + gprim, a_eel.value());
+    if (a_enuc.nonzero())
+      atomicAdd(prm->prim.enuc + gprim, a_enuc.value());
+    reset_prim();
+  }
+  __device__ void flush_sim(int s)
+  {
+    if (s < 0)
+      return;
+    SimTotals * t = prm->totals + s;
+    if (n_members)
+      atomicAdd(&t->members, n_members);
+    if (n_repl)
+      atomicAdd(&t->replacements, n_repl);
+    if (n_inter)
+      atomicAdd(&t->interstitials, n_inter);
+    if (n_subst)
+      atomicAdd(&t->substitutionals, n_subst);
+    if (n_lost)
+      atomicAdd(&t->lost, n_lost);
+    if (n_newton)
+      atomicAdd(&t->newton_iters, n_newton);
+    if (n_passes)
+      atomicAdd(&t->rejection_passes, n_passes);
+    if (n_fallbacks)
+      atomicAdd(&t->fallbacks, n_fallbacks);
+    if (e_lost != 0.0)
+      atomicAdd(&t->Elost, e_lost);
+    if (e_unf != 0.0)
+      atomicAdd(&t->Eunfollowed, e_unf);
+    reset_sim();
+  }
+};
+
+// warp-aggregated histogram increment: lanes with the same bin add once
+__device__ __forceinline__ void
+warp_hist_add(unsigned long long * hist, int bin)
+{
+  const unsigned int active = __ballot_sync(0xffffffffu, bin >= 0);
+  if (bin >= 0)
+  {
+    const unsigned int peers = __match_any_sync(active, bin);
+    const int leader = __ffs(peers) - 1;
+    if ((threadIdx.x & 31) == leader)
+      atomicAdd(hist + bin, (unsigned long long)__popc(peers));
+  }
+}
+
+template <class Pol>
+__global__ void
+cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
+{
+  using Particle = typename Pol::Particle;
+  extern __shared__ __align__(16) unsigned char smem[];
+
+  // stage the tables of a single-simulation run in shared memory
+  const typename Pol::Tables tab = Pol::stage(prm, tabs, smem);
+
+  const unsigned int FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned int lt = lanemask_lt();
+  const long long warp_id = (long long)(blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  Particle * stack = reinterpret_cast<Particle *>(prm.stacks) + warp_id * prm.stack_cap;
+  Particle * overflow = reinterpret_cast<Particle *>(prm.overflow);
+  const Particle * in_records = reinterpret_cast<const Particle *>(prm.in_records);
+  long long n_work = prm.total_primaries;
+  if (prm.in_records)
+  {
+    const long long c = (long long)*prm.in_count;
+    n_work = c < prm.in_cap ? c : prm.in_cap;
+  }
+
+  int top = 0;
+  bool work_done = false; // no more primaries / input records for this warp
+  bool live = false;
+  Particle p;
+  uint32_t ic = 0;
+  double r1 = 0.0;
+  int cur_sim = -1;
+  const SimDesc * sim = nullptr;
+  typename Pol::MemberCtx mctx;
+
+  LaneSink<Pol> sink;
+  sink.prm = &prm;
+  sink.sim = nullptr;
+  sink.gprim = -1;
+  sink.range_mode = 0;
+  sink.reset_prim();
+  sink.reset_sim();
+  sink.m_vac = 0;
+  sink.m_state = 0;
+  sink.m_eel.reset();
+
+  auto start_member = [&](const Particle & q) {
+    p = q;
+    ic = 0;
+    if (p.sim != cur_sim)
+    {
+      sink.flush_prim();
+      sink.flush_sim(cur_sim);
+      cur_sim = p.sim;
+      sim = prm.sims + cur_sim;
+      sink.sim = sim;
+      sink.range_mode = sim->range_mode;
+      sink.gprim = -1;
+    }
+    if ((long long)p.prim != sink.gprim)
+    {
+      sink.flush_prim();
+      sink.gprim = (long long)p.prim;
+    }
+    Pol::begin_member(mctx, prm, tab, *sim, p);
+    r1 = Pol::first_draw(p.key, prm.k0, prm.k1);
+    sink.m_vac = 0;
+    sink.m_state = 0;
+    sink.m_eel.reset();
+    ++sink.n_members;
+  };
+
+  while (true)
+  {
+    // ---- refill idle lanes: recoils from the warp stack first, then new work
+    const unsigned int idle = __ballot_sync(FULL, !live);
+    if (idle)
+    {
+      const int nidle = __popc(idle);
+      const int rank = __popc(idle & lt);
+      const int npop = nidle < top ? nidle : top;
+      if (!live && rank < npop)
+      {
+        start_member(stack[top - 1 - rank]);
+        live = true;
+      }
+      top -= npop;
+      const int need = nidle - npop;
+      if (need > 0 && !work_done)
+      {
+        unsigned long long base = 0;
+        const int leader = __ffs(idle) - 1;
+        if (lane == leader)
+          base = atomicAdd(prm.next_primary, (unsigned long long)need);
+        base = __shfl_sync(FULL, base, leader);
+        const long long avail = n_work - (long long)base;
+        if (avail <= need)
+          work_done = true;
+        const int r = rank - npop;
+        if (!live && r >= 0 && r < avail)
+        {
+          const long long g = (long long)base + r;
+          if (prm.in_records)
+            start_member(in_records[g]);
+          else
+          {
+            const int s = prm.n_sims > 1 ? find_sim(prm.sim_prim_end, prm.n_sims, g) : 0;
+            start_member(Pol::make_primary(prm.sims[s], s, g));
+          }
+          live = true;
+        }
+      }
+    }
+    if (__ballot_sync(FULL, live) == 0)
+      break;
+
+    // ---- one collision per live lane
+    Particle rec;
+    int flags = 0;
+    sink.vac_bin = -1;
+    sink.repl_bin = -1;
+    if (live)
+    {
+      ++ic;
+      ++sink.a_coll;
+      flags = Pol::collide(p, ic, r1, mctx, prm.k0, prm.k1, rec, sink);
+      if (!(flags & CF_DONE) && ic >= prm.max_collisions)
+      {
+        atomicOr(prm.error_flags, ERRB_BUDGET);
+        flags |= CF_DONE;
+      }
+      if (flags & CF_DONE)
+      {
+        live = false;
+        if (prm.records)
+        {
+          const unsigned long long slot = atomicAdd(prm.n_records, 1ull);
+          if ((long long)slot < prm.records_cap)
+          {
+            MemberRecord m;
+            m.key = p.key;
+            m.sim = p.sim;
+            m.species = p.species;
+            m.gen = p.gen;
+            m.state = sink.m_state;
+            m.ncoll = ic;
+            m.nvac = sink.m_vac;
+            m.E = double(p.E);
+            m.x = double(p.x);
+            m.y = double(p.y);
+            m.z = double(p.z);
+            m.eel = sink.m_eel.value();
+            prm.records[slot] = m;
+          }
+        }
+      }
+      if (flags & CF_PUSH)
+      {
+        rec.sim = p.sim;
+        rec.prim = p.prim;
+      }
+    }
+    warp_hist_add(prm.hist, sink.vac_bin);
+    warp_hist_add(prm.hist, sink.repl_bin);
+
+    // ---- push displaced recoils onto the warp stack
+    const bool push = (flags & CF_PUSH) != 0;
+    const unsigned int pm = __ballot_sync(FULL, push);
+    if (pm)
+    {
+      if (push)
+      {
+        const int slot = top + __popc(pm & lt);
+        if (slot < prm.stack_cap)
+          stack[slot] = rec;
+        else
+        {
+          const unsigned long long o = atomicAdd(prm.overflow_count, 1ull);
+          if ((long long)o < prm.overflow_cap)
+            overflow[o] = rec;
+          else
+            atomicOr(prm.error_flags, ERRB_QUEUE_FULL);
+        }
+      }
+      top += __popc(pm);
+      if (top > prm.stack_cap)
+        top = prm.stack_cap;
+    }
+  }
+  sink.flush_prim();
+  sink.flush_sim(cur_sim);
+}
+
+} // namespace mtg

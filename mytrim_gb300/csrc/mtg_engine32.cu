@@ -1,0 +1,501 @@
+// FP32 cascade path: the same collision loop as the FP64 plain path
+// (TrimBase::trim, trim.C:74-424) in single precision, with three changes of
+// evaluation that keep FP32 accurate and fast:
+//   * electronic stopping is read from a per-(species, material) table of
+//     S(E), uniform in ln E with 2048 points and filled by the FP64 stopping code,
+//     instead of re-evaluating ~11 transcendentals per element per collision;
+//   * the Newton solve for the distance of closest approach iterates on
+//     d = r - b (the same Newton steps as trim.C:192-233 written in a variable
+//     that does not cancel), and sin^2(theta/2) is formed as (1 - co)(1 + co)
+//     with 1 - co = d (1 - A F / (F + 1)) / (r + roc), algebraically equal to
+//     1 - co^2 of trim.C:266-269 without its cancellation at small angles;
+//   * the random azimuth is drawn directly (uniform angle around the flight
+//     direction) instead of by unit-ball rejection; the two give the same
+//     distribution, and the direct draw has no data-dependent loop.
+// Energies are kept as a float pair (value + rounding remainder) so that
+// the small per-collision losses are not rounded away, and the lane tallies use
+// Kahan-compensated sums; FP64 instructions stay out of the collision loop.
+#include "mtg_common.cuh"
+#include "mtg_collide64.cuh"
+#include "mtg_engine.cuh"
+#include "mtg_kernels.h"
+#include "mtg_surrogate.cuh"
+
+namespace mtg
+{
+
+struct P32
+{
+  float x, y, z;
+  float dx, dy, dz;
+  float E, El;   // energy as value + remainder
+  uint64_t key;
+  int species;
+  int gen;
+  int sim;
+  uint32_t prim;
+};
+
+struct Tables32
+{
+  const Species32 * species;
+  const Mat32 * mats;
+  const Sim32 * sims;
+  const float * stop;
+  float lnE_min, inv_dlnE;
+  const SurrogateNet * net;
+};
+
+// E -= d, keeping the rounding remainder (TwoSum followed by FastTwoSum)
+__device__ __forceinline__ void
+ff_sub(float & hi, float & lo, float d)
+{
+  const float s = hi - d;
+  const float bb = s - hi;
+  const float err = (hi - (s - bb)) + (-d - bb);
+  const float l = lo + err;
+  const float h = s + l;
+  lo = l - (h - s);
+  hi = h;
+}
+
+__device__ __forceinline__ float
+stop_lookup(const float * row, float lnE_min, float inv_d, float E)
+{
+  const float u = (__logf(E) - lnE_min) * inv_d;
+  if (!(u > 0.0f))
+    return row[0] * sqrtf(E * float(1.0 / STOP_EMIN));
+  const int i = min(int(u), STOP_N - 2);
+  const float f = u - float(i);
+  const float a = row[i], b = row[i + 1];
+  return fmaf(f, b - a, a);
+}
+
+// Universal-potential scattering in FP32.  Returns s2 = sin^2(theta/2) and
+// c2 = cos^2(theta/2).
+__device__ __forceinline__ void
+scatter32(float eps, float b, float & s2, float & c2, int & niter)
+{
+  niter = 0;
+  if (eps > 10.0f)
+  {
+    const float w = 2.0f * eps * b;
+    s2 = 1.0f / (1.0f + (1.0f + b * (1.0f + b)) * (w * w));
+    c2 = 1.0f - s2;
+    return;
+  }
+  // first guess at the distance of closest approach (trim.C:183-190)
+  float r = b;
+  float rr = -2.7f * __logf(eps * b);
+  if (rr >= b)
+  {
+    rr = -2.7f * __logf(eps * rr);
+    if (rr >= b)
+      r = rr;
+  }
+  float d = r - b;
+  const float inv_eps = 1.0f / eps;
+  float v, v1, q;
+  do
+  {
+    r = b + d;
+    const float ex1 = 0.18175f * __expf(-3.1998f * r);
+    const float ex2 = 0.50986f * __expf(-0.94229f * r);
+    const float ex3 = 0.28022f * __expf(-0.4029f * r);
+    const float ex4 = 0.028171f * __expf(-0.20162f * r);
+    const float phi = ex1 + ex2 + ex3 + ex4;
+    const float tk = 3.1998f * ex1 + 0.94229f * ex2 + 0.4029f * ex3 + 0.20162f * ex4;
+    const float ir = 1.0f / r;
+    v = phi * ir;
+    v1 = -(v + tk) * ir;
+    // f(r) = b^2/r + v r/eps - r and f'(r), written in d = r - b
+    const float fr = -d * (2.0f * b + d) * ir + phi * inv_eps;
+    const float br = b * ir;
+    const float fr1 = -br * br - tk * inv_eps - 1.0f;
+    q = fr / fr1;
+    d -= q;
+    ++niter;
+  } while (fabsf(q) > 0.001f * fabsf(b + d) && niter < 100);
+  r = b + d;
+  const float roc = -2.0f * (eps - v) / v1;
+  const float sqe = sqrtf(eps);
+  const float cc = (0.011615f + sqe) / (0.0071222f + sqe);
+  const float aa = 2.0f * eps * (1.0f + (0.99229f / sqe)) * __expf(cc * __logf(b));
+  const float ff = (1.0f / (sqrtf(aa * aa + 1.0f) + aa)) * ((9.3066f + eps) / (14.813f + eps));
+  const float omc = d * (1.0f - aa * ff / (ff + 1.0f)) / (r + roc);
+  s2 = omc * (2.0f - omc);
+  c2 = 1.0f - s2;
+}
+
+template <bool SURROGATE>
+struct Fp32Policy
+{
+  using Particle = P32;
+  using Real = float;
+  using Acc = AccKahan32;
+  using Tables = Tables32;
+
+  struct MemberCtx
+  {
+    const Sim32 * sim;
+    const Species32 * sc;
+    const Mat32 * mrow;
+    const float * stop;
+    float lnE_min, inv_dlnE;
+    float E; // unused
+    const SurrogateNet * net;
+  };
+
+  static __device__ Tables stage(const EngineParams & prm, const Tables & g, unsigned char * smem)
+  {
+    if (!prm.stage_tables)
+      return g;
+    Tables t = g;
+    unsigned char * q = smem;
+    const int ns = prm.n_stage_species, nm = prm.n_stage_mats;
+    Species32 * s_sp = reinterpret_cast<Species32 *>(q);
+    q += sizeof(Species32) * ns;
+    Mat32 * s_mc = reinterpret_cast<Mat32 *>(q);
+    q += sizeof(Mat32) * nm;
+    float * s_st = reinterpret_cast<float *>(q);
+    const int n1 = int(sizeof(Species32) / 4) * ns;
+    const int n2 = int(sizeof(Mat32) / 4) * nm;
+    const int n3 = STOP_N * nm;
+    for (int i = threadIdx.x; i < n1; i += blockDim.x)
+      reinterpret_cast<float *>(s_sp)[i] = reinterpret_cast<const float *>(g.species)[i];
+    for (int i = threadIdx.x; i < n2; i += blockDim.x)
+      reinterpret_cast<float *>(s_mc)[i] = reinterpret_cast<const float *>(g.mats)[i];
+    for (int i = threadIdx.x; i < n3; i += blockDim.x)
+      s_st[i] = g.stop[i];
+    __syncthreads();
+    t.species = s_sp;
+    t.mats = s_mc;
+    t.stop = s_st;
+    return t;
+  }
+
+  static __device__ __forceinline__ void begin_member(MemberCtx & m, const EngineParams & prm, const Tables & t,
+                                                      const SimDesc & /*sim*/, const P32 & p)
+  {
+    const Sim32 * s = t.sims + p.sim;
+    const int sbase = prm.stage_tables ? 0 : s->species_base;
+    const int mbase = prm.stage_tables ? 0 : s->mat_base;
+    m.sim = s;
+    m.sc = t.species + sbase + p.species;
+    m.mrow = t.mats + mbase + p.species * s->n_mat;
+    m.stop = t.stop + (long long)(mbase + p.species * s->n_mat) * STOP_N;
+    m.lnE_min = t.lnE_min;
+    m.inv_dlnE = t.inv_dlnE;
+    m.net = t.net;
+  }
+
+  static __device__ __forceinline__ double first_draw(uint64_t key, uint32_t k0, uint32_t k1)
+  {
+    const U4 d = draw_block(key, 0u, 0u, k0, k1);
+    return double(u24f(d.x));
+  }
+
+  static __device__ __forceinline__ P32 make_primary(const SimDesc & s, int si, long long g)
+  {
+    P32 p;
+    p.x = float(s.pos[0]);
+    p.y = float(s.pos[1]);
+    p.z = float(s.pos[2]);
+    p.dx = float(s.dir[0]);
+    p.dy = float(s.dir[1]);
+    p.dz = float(s.dir[2]);
+    p.E = float(s.E0);
+    p.El = float(s.E0 - double(p.E));
+    p.key = root_key(s.sim_key, uint64_t(g - s.prim_begin + s.key_offset));
+    p.species = 0;
+    p.gen = 0;
+    p.sim = si;
+    p.prim = uint32_t(g);
+    return p;
+  }
+
+  template <class Sink>
+  static __device__ __forceinline__ int collide(P32 & p, uint32_t ic, double r1d, const MemberCtx & m, uint32_t k0,
+                                                uint32_t k1, P32 & rec, Sink & sink)
+  {
+    const Sim32 & sim = *m.sim;
+    // material lookup (sample_layers.C:27-43)
+    int layer = 0;
+    while (layer < sim.n_layers - 1 && !(p.x < sim.layer_end[layer]))
+      ++layer;
+    const int k = sim.layer_mat[layer];
+    const Mat32 & mc = m.mrow[k];
+
+    // normalise direction
+    {
+      const float s = rsqrtf(p.dx * p.dx + p.dy * p.dy + p.dz * p.dz);
+      p.dx *= s;
+      p.dy *= s;
+      p.dz *= s;
+    }
+    const float E = p.E;
+
+    // maximum impact parameter and free flight (trim.C:88-94)
+    const float eps0 = E * mc.f;
+    const float eeg = sqrtf(eps0 * mc.epsdg);
+    const float pmax = mc.a / (eeg + sqrtf(eeg) + 0.125f * __expf(0.1f * __logf(eeg)));
+    float ls = mc.inv_pi_arho / (pmax * pmax);
+    if (ic == 1)
+      ls = float(r1d) * fminf(ls, sim.cw);
+
+    // impact parameter, target atom and azimuth: one Philox block per collision
+    const U4 dr = draw_block(p.key, ic, 0u, k0, k1);
+    const float r2 = u24f(dr.x);
+    float hh = u24f(dr.y);
+    const float pimp = pmax * sqrtf(r2);
+    int nn = 0;
+    for (; nn < mc.nel - 1; ++nn)
+    {
+      hh -= mc.el[nn].t;
+      if (hh <= 0.0f)
+        break;
+    }
+    const Elem32 & el = mc.el[nn];
+    const float eps = el.fi * E;
+    const float b = pimp * el.inv_ai;
+
+    // electronic loss from the stopping table (material.C:114-121)
+    float dee = ls * stop_lookup(m.stop + (long long)k * STOP_N, m.lnE_min, m.inv_dlnE, E);
+
+    float s2, c2;
+    int niter = 0;
+    if (SURROGATE && surrogate_in_domain(eps, b))
+      surrogate_s2(m.net, eps, b, s2, c2);
+    else
+    {
+      if (SURROGATE)
+        sink.fallback();
+      scatter32(eps, b, s2, c2, niter);
+    }
+    sink.newton(niter);
+
+    // energy transfer, electronic loss, momenta (trim.C:275-296)
+    float den = el.ec * s2 * E;
+    if (dee >= E)
+    {
+      dee = E + p.El;
+      p.E = 0.0f;
+      p.El = 0.0f;
+    }
+    else
+      ff_sub(p.E, p.El, dee);
+    sink.eel(dee);
+    const float p1 = sqrtf(m.sc->two_m1 * p.E);
+    if (den >= p.E)
+    {
+      den = p.E + p.El;
+      p.E = 0.0f;
+      p.El = 0.0f;
+    }
+    else
+      ff_sub(p.E, p.El, den);
+    const float p2 = sqrtf(m.sc->two_m1 * p.E);
+
+    // recoil at the pre-flight position (trim.C:306-318)
+    rec.x = p.x;
+    rec.y = p.y;
+    rec.z = p.z;
+    rec.gen = p.gen + 1;
+    const float fl = (ls - sim.tau) * sim.flscale;
+    p.x = fmaf(p.dx, fl, p.x);
+    p.y = fmaf(p.dy, fl, p.y);
+    p.z = fmaf(p.dz, fl, p.z);
+    rec.dx = p.dx * p1;
+    rec.dy = p.dy * p1;
+    rec.dz = p.dz * p1;
+    const float recE = den - el.Elbind;
+    rec.E = recE;
+    rec.El = 0.0f;
+    rec.species = el.rspecies;
+
+    // azimuth around the flight direction: orthonormal basis by Duff et al.,
+    // "Building an Orthonormal Basis, Revisited" (JCGT 2017)
+    const float sgn = copysignf(1.0f, p.dz);
+    const float ia = -1.0f / (sgn + p.dz);
+    const float bxy = p.dx * p.dy * ia;
+    const float ux = 1.0f + sgn * p.dx * p.dx * ia, uy = sgn * bxy, uz = -sgn * p.dx;
+    const float vx = bxy, vy = sgn + p.dy * p.dy * ia, vz = -p.dy;
+    float sphi, cphi;
+    __sincosf(6.283185307179586f * u24f(dr.z), &sphi, &cphi);
+    const float px = cphi * ux + sphi * vx;
+    const float py = cphi * uy + sphi * vy;
+    const float pz = cphi * uz + sphi * vz;
+
+    // new direction: cos(psi), sin(psi) of psi = atan2(st, ct + my) (trim.C:336-341)
+    const float ct = c2 - s2;
+    const float st = 2.0f * sqrtf(s2 * c2);
+    const float cy = ct + el.my;
+    const float ih = rsqrtf(st * st + cy * cy);
+    const float cpsi = cy * ih, spsi = st * ih;
+    p.dx = p.dx * cpsi + px * spsi;
+    p.dy = p.dy * cpsi + py * spsi;
+    p.dz = p.dz * cpsi + pz * spsi;
+    rec.dx -= p.dx * p2;
+    rec.dy -= p.dy * p2;
+    rec.dz -= p.dz * p2;
+
+    // CUT boundaries (trim.C:344-352)
+    if (sim.any_cut)
+    {
+      const float pos[3] = {p.x, p.y, p.z};
+      for (int i = 0; i < 3; ++i)
+        if (sim.bc[i] == 2 && (pos[i] > sim.w[i] || pos[i] < 0.0f))
+        {
+          sink.lost(p.E + p.El + den);
+          return CF_DONE;
+        }
+    }
+
+    // fate of recoil and projectile (trim.C:357-411)
+    int flags = 0;
+    int state = ST_MOVING;
+    if (recE > el.disp_thresh)
+    {
+      sink.enuc(el.Elbind);
+      const bool follow = sim.range_mode ? (rec.gen < 1) : !sim.primaries_only;
+      if (follow)
+      {
+        const float s = rsqrtf(rec.dx * rec.dx + rec.dy * rec.dy + rec.dz * rec.dz);
+        rec.dx *= s;
+        rec.dy *= s;
+        rec.dz *= s;
+        rec.key = child_key(p.key, ic);
+        flags |= CF_PUSH;
+      }
+      else
+        sink.unfollowed(recE);
+      if (p.E > el.Edisp)
+        sink.vacancy(rec, el);
+      else
+      {
+        sink.replacement(double(rec.x));
+        state = (m.sc->Z1 == el.Z2) ? ST_REPLACEMENT : ST_SUBSTITUTIONAL;
+      }
+    }
+    else
+    {
+      sink.enuc(den);
+      if (p.E < sim.Ef)
+        state = ST_INTERSTITIAL;
+    }
+    if (state != ST_MOVING)
+    {
+      p.E += p.El;
+      p.El = 0.0f;
+      sink.stop(state, p);
+      flags |= CF_DONE;
+    }
+    else if (!(p.E == p.E))
+    {
+      sink.numeric();
+      flags |= CF_DONE;
+    }
+    return flags;
+  }
+};
+
+cudaError_t
+launch_cascade32(const EngineParams & prm, const Fp32Tables & t, int grid, int block, size_t smem, cudaStream_t st,
+                 int surrogate)
+{
+  Tables32 tabs;
+  tabs.species = reinterpret_cast<const Species32 *>(prm.species);
+  tabs.mats = reinterpret_cast<const Mat32 *>(prm.mats);
+  tabs.sims = reinterpret_cast<const Sim32 *>(t.sims32);
+  tabs.stop = t.stop;
+  tabs.lnE_min = t.lnE_min;
+  tabs.inv_dlnE = t.inv_dlnE;
+  tabs.net = reinterpret_cast<const SurrogateNet *>(t.mlp);
+  if (surrogate)
+    cascade_kernel<Fp32Policy<true>><<<grid, block, smem, st>>>(prm, tabs);
+  else
+    cascade_kernel<Fp32Policy<false>><<<grid, block, smem, st>>>(prm, tabs);
+  return cudaGetLastError();
+}
+
+cudaError_t
+occupancy32(int block, size_t smem, int * blocks_per_sm, int surrogate)
+{
+  if (surrogate)
+  {
+    if (smem > 48 * 1024)
+    {
+      cudaError_t e = cudaFuncSetAttribute(cascade_kernel<Fp32Policy<true>>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+      if (e != cudaSuccess)
+        return e;
+    }
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, cascade_kernel<Fp32Policy<true>>, block,
+                                                         smem);
+  }
+  if (smem > 48 * 1024)
+  {
+    cudaError_t e = cudaFuncSetAttribute(cascade_kernel<Fp32Policy<false>>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess)
+      return e;
+  }
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, cascade_kernel<Fp32Policy<false>>, block,
+                                                       smem);
+}
+
+size_t
+record_size32()
+{
+  return sizeof(P32);
+}
+
+// ---- scattering service (FP32 exact and surrogate)
+__global__ void
+scatter32_kernel(const double * eps, const double * b, long long n, double * s2, const SurrogateNet * net,
+                 int surrogate)
+{
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  const float e = float(eps[i]), bb = float(b[i]);
+  float s, c;
+  int it;
+  if (surrogate && surrogate_in_domain(e, bb))
+    surrogate_s2(net, e, bb, s, c);
+  else
+    scatter32(e, bb, s, c, it);
+  s2[i] = double(s);
+}
+
+cudaError_t
+launch_scatter32(const double * eps, const double * b, long long n, double * s2, const void * net, int surrogate,
+                 cudaStream_t st)
+{
+  const int block = 256;
+  if (n > 0)
+    scatter32_kernel<<<(unsigned int)((n + block - 1) / block), block, 0, st>>>(
+        eps, b, n, s2, reinterpret_cast<const SurrogateNet *>(net), surrogate);
+  return cudaGetLastError();
+}
+
+// ---- stopping through the FP32 table (one (species, material) row)
+__global__ void
+stopping32_kernel(const float * row, float lnE_min, float inv_d, const double * E, long long n, double * out)
+{
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+    out[i] = double(stop_lookup(row, lnE_min, inv_d, float(E[i])));
+}
+
+cudaError_t
+launch_stopping32(const float * row, float lnE_min, float inv_d, const double * E, long long n, double * out,
+                  cudaStream_t st)
+{
+  const int block = 256;
+  if (n > 0)
+    stopping32_kernel<<<(unsigned int)((n + block - 1) / block), block, 0, st>>>(row, lnE_min, inv_d, E, n, out);
+  return cudaGetLastError();
+}
+
+} // namespace mtg

@@ -1,0 +1,195 @@
+// FP64 ("plain", exact scattering) instantiation of the cascade kernel, plus the
+// FP64 stopping and scattering service kernels.  Compiled with -fmad=false so
+// that every multiply and add is rounded separately, exactly as in the host
+// replay build of the same code.
+#include "mtg_collide64.cuh"
+#include "mtg_engine.cuh"
+#include "mtg_kernels.h"
+
+namespace mtg
+{
+
+struct Fp64Policy
+{
+  using Particle = P64;
+  using Real = double;
+  using Acc = AccF64;
+
+  struct Tables
+  {
+    const SpeciesConst * species;
+    const MatConst * mats;
+  };
+
+  struct MemberCtx
+  {
+    const SimDesc * sim;
+    const SpeciesConst * sc;
+    const MatConst * mrow;
+  };
+
+  // copy the species and material rows of a single-simulation run to shared memory
+  static __device__ Tables stage(const EngineParams & prm, const Tables & g, unsigned char * smem)
+  {
+    if (!prm.stage_tables)
+      return g;
+    SpeciesConst * s_sp = reinterpret_cast<SpeciesConst *>(smem);
+    MatConst * s_mc = reinterpret_cast<MatConst *>(smem + sizeof(SpeciesConst) * prm.n_stage_species);
+    const int n1 = int(sizeof(SpeciesConst) / 8) * prm.n_stage_species;
+    const int n2 = int(sizeof(MatConst) / 8) * prm.n_stage_mats;
+    for (int i = threadIdx.x; i < n1; i += blockDim.x)
+      reinterpret_cast<double *>(s_sp)[i] = reinterpret_cast<const double *>(g.species)[i];
+    for (int i = threadIdx.x; i < n2; i += blockDim.x)
+      reinterpret_cast<double *>(s_mc)[i] = reinterpret_cast<const double *>(g.mats)[i];
+    __syncthreads();
+    return Tables{s_sp, s_mc};
+  }
+
+  static __device__ __forceinline__ void begin_member(MemberCtx & m, const EngineParams & prm, const Tables & t,
+                                                      const SimDesc & sim, const P64 & p)
+  {
+    const int sbase = prm.stage_tables ? 0 : sim.species_base;
+    const int mbase = prm.stage_tables ? 0 : sim.mat_base;
+    m.sim = &sim;
+    m.sc = t.species + sbase + p.species;
+    m.mrow = t.mats + mbase + p.species * sim.n_mat;
+  }
+
+  static __device__ __forceinline__ double first_draw(uint64_t key, uint32_t k0, uint32_t k1)
+  {
+    const U4 d = draw_block(key, 0u, 0u, k0, k1);
+    return u53(d.x, d.y);
+  }
+
+  static __device__ __forceinline__ P64 make_primary(const SimDesc & s, int si, long long g)
+  {
+    P64 p;
+    p.x = s.pos[0];
+    p.y = s.pos[1];
+    p.z = s.pos[2];
+    p.dx = s.dir[0];
+    p.dy = s.dir[1];
+    p.dz = s.dir[2];
+    p.E = s.E0;
+    p.key = root_key(s.sim_key, uint64_t(g - s.prim_begin + s.key_offset));
+    p.species = 0;
+    p.gen = 0;
+    p.sim = si;
+    p.prim = uint32_t(g);
+    return p;
+  }
+
+  template <class Sink>
+  static __device__ __forceinline__ int collide(P64 & p, uint32_t ic, double r1, const MemberCtx & m, uint32_t k0,
+                                                uint32_t k1, P64 & rec, Sink & sink)
+  {
+    return collide64(p, ic, r1, *m.sim, *m.sc, m.mrow, k0, k1, rec, sink);
+  }
+};
+
+cudaError_t
+launch_cascade64(const EngineParams & prm, int grid, int block, size_t smem, cudaStream_t st)
+{
+  cascade_kernel<Fp64Policy><<<grid, block, smem, st>>>(prm, Fp64Policy::Tables{prm.species, prm.mats});
+  return cudaGetLastError();
+}
+
+cudaError_t
+occupancy64(int block, size_t smem, int * blocks_per_sm)
+{
+  if (smem > 48 * 1024)
+  {
+    cudaError_t e = cudaFuncSetAttribute(cascade_kernel<Fp64Policy>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess)
+      return e;
+  }
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, cascade_kernel<Fp64Policy>,
+                                                       block, smem);
+}
+
+size_t
+record_size64()
+{
+  return sizeof(P64);
+}
+
+// ---- service kernels
+
+__global__ void
+stopping64_kernel(const SpeciesConst * sc, const MatConst * mc, const double * E, long long n,
+                  double * out)
+{
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+    out[i] = material_stop64(*sc, *mc, E[i]);
+}
+
+cudaError_t
+launch_stopping64(const SpeciesConst * sc, const MatConst * mc, const double * E, long long n,
+                  double * out, cudaStream_t st)
+{
+  const int block = 256;
+  const long long grid = (n + block - 1) / block;
+  if (grid > 0)
+    stopping64_kernel<<<(unsigned int)grid, block, 0, st>>>(sc, mc, E, n, out);
+  return cudaGetLastError();
+}
+
+__global__ void
+scatter64_kernel(const double * eps, const double * b, long long n, double * s2)
+{
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+  {
+    double ct, st, s;
+    int it;
+    scatter64(eps[i], b[i], s, ct, st, it);
+    s2[i] = s;
+  }
+}
+
+cudaError_t
+launch_scatter64(const double * eps, const double * b, long long n, double * s2, cudaStream_t st)
+{
+  const int block = 256;
+  const long long grid = (n + block - 1) / block;
+  if (grid > 0)
+    scatter64_kernel<<<(unsigned int)grid, block, 0, st>>>(eps, b, n, s2);
+  return cudaGetLastError();
+}
+
+} // namespace mtg
+
+namespace mtg
+{
+
+// FP32-path stopping tables: S(E) of every (species, material) row on a grid
+// uniform in ln E, evaluated with the FP64 stopping above.
+__global__ void
+build_stop_tables_kernel(const SpeciesConst * species, const MatConst * mats, int n_rows,
+                         const int * row_species, float * out, double lnE_min, double dlnE)
+{
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)n_rows * STOP_N)
+    return;
+  const int row = int(i / STOP_N);
+  const int j = int(i % STOP_N);
+  const double E = exp64(lnE_min + dlnE * double(j));
+  out[i] = float(material_stop64(species[row_species[row]], mats[row], E));
+}
+
+cudaError_t
+launch_build_stop_tables(const SpeciesConst * species, const MatConst * mats, const SimDesc * /*sims*/,
+                         int /*n_sims*/, int n_rows, const int * row_species, float * out, double lnE_min,
+                         double dlnE, cudaStream_t st)
+{
+  const long long n = (long long)n_rows * STOP_N;
+  const int block = 256;
+  if (n > 0)
+    build_stop_tables_kernel<<<(unsigned int)((n + block - 1) / block), block, 0, st>>>(
+        species, mats, n_rows, row_species, out, lnE_min, dlnE);
+  return cudaGetLastError();
+}
+
+} // namespace mtg

@@ -1,0 +1,409 @@
+// Host-side table construction for the cascade engine (see mtg_setup.h).
+#include "mtg_setup.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+
+namespace mtg
+{
+
+void
+seed_key(unsigned long long seed, uint32_t & k0, uint32_t & k1)
+{
+  k0 = uint32_t(seed);
+  k1 = uint32_t(seed >> 32) ^ 0x4D795452u;
+}
+
+bool
+read_table_file(const char * path, mtg_scoef_row * rows, std::string & err)
+{
+  std::ifstream in(path);
+  if (!in)
+  {
+    err = std::string("cannot open stopping table file ") + path;
+    return false;
+  }
+  std::string line;
+  bool seen[MTG_SCOEF_ROWS] = {false};
+  int n = 0;
+  while (std::getline(in, line))
+  {
+    if (line.empty() || line[0] == '#')
+      continue;
+    std::istringstream ls(line);
+    int Z;
+    std::string sym;
+    mtg_scoef_row r;
+    ls >> Z >> sym >> r.mm1 >> r.m1 >> r.mnat >> r.rho >> r.atrho >> r.vfermi >> r.heat >> r.lfctr;
+    for (int j = 0; j < 8; ++j)
+      ls >> r.pcoef[j];
+    if (!ls || Z < 1 || Z > MTG_SCOEF_ROWS || seen[Z - 1])
+    {
+      err = std::string("malformed stopping table row: ") + line;
+      return false;
+    }
+    rows[Z - 1] = r;
+    seen[Z - 1] = true;
+    ++n;
+  }
+  if (n != MTG_SCOEF_ROWS)
+  {
+    err = "stopping table file must hold 92 rows";
+    return false;
+  }
+  return true;
+}
+
+// proton stopping with libm (material.C:134-158), used for the constant
+// low-velocity matching value
+static double
+proton_stop_host(const mtg_scoef_row & r, int z2p, double e)
+{
+  const double pe0 = 25.0;
+  const double pe = std::max(pe0, e);
+  const double sl = (r.pcoef[0] * std::pow(pe, r.pcoef[1])) + (r.pcoef[2] * std::pow(pe, r.pcoef[3]));
+  const double sh = r.pcoef[4] / std::pow(pe, r.pcoef[5]) * std::log(r.pcoef[6] / pe + r.pcoef[7] * pe);
+  double sp = sl * sh / (sl + sh);
+  if (e <= pe0)
+    sp *= std::pow(e / pe0, z2p <= 6 ? 0.25 : 0.45);
+  return sp;
+}
+
+SpeciesConst
+make_species(const mtg_scoef_row * rows, int Z1, double m1)
+{
+  SpeciesConst s;
+  std::memset(&s, 0, sizeof s);
+  s.Z1 = Z1;
+  s.branch = Z1 == 1 ? STOP_H : (Z1 == 2 ? STOP_HE : STOP_HEAVY);
+  s.m1 = m1;
+  const double mstop = (m1 == 0.0) ? rows[Z1 - 1].mm1 : m1;
+  s.inv_m1k = 0.001 / mstop;
+  s.fz1 = double(Z1);
+  s.cb = std::cbrt(s.fz1);
+  s.cb2 = s.cb * s.cb;
+  s.lfctr = rows[Z1 - 1].lfctr;
+  s.bq = (std::min(0.43, std::max(0.32, 0.12 + 0.025 * s.fz1))) / s.cb;
+  s.l0a = std::min(1.2, 0.6 + s.fz1 / 30.0);
+  s.qlo = std::max(0.0, 0.9 - 0.025 * s.fz1);
+  s.qden = std::abs(s.qlo - 0.2000001);
+  s.qhi = std::max(0.0, 1.0 - 0.025 * std::min(16.0, s.fz1));
+  s.qden2 = 0.025 * std::min(16.0, s.fz1);
+  s.inv_z1sq = 1.0 / (s.fz1 * s.fz1);
+  return s;
+}
+
+StopPair
+make_stop_pair(const mtg_scoef_row * rows, const SpeciesConst & sc, int Z2)
+{
+  StopPair p;
+  std::memset(&p, 0, sizeof p);
+  const mtg_scoef_row & r = rows[Z2 - 1];
+  for (int j = 0; j < 8; ++j)
+    p.pcoef[j] = r.pcoef[j];
+  p.vfermi = r.vfermi;
+  p.inv2vf2 = 1.0 / (2.0 * r.vfermi * r.vfermi);
+  p.velpwr = Z2 <= 6 ? 0.25 : 0.45;
+  // heavy-ion low-velocity branch (material.C:251-268)
+  const double yrmin = 0.13, vrmin0 = 1.0;
+  p.yrcut = std::max(yrmin, vrmin0 / sc.cb2);
+  const double vrmin = std::max(vrmin0, yrmin * sc.cb2);
+  const double vmin = 0.5 * (vrmin + std::sqrt(std::max(0.0, vrmin * vrmin - 0.8 * r.vfermi * r.vfermi)));
+  p.eee = 25.0 * vmin * vmin;
+  p.sp_eee = proton_stop_host(r, Z2, p.eee);
+  p.power = (Z2 == 6 || ((Z2 == 14 || Z2 == 32) && sc.Z1 <= 19)) ? 0.375 : 0.5;
+  p.zc = 0.18 + 0.0015 * double(Z2);
+  p.hez = 0.007 + 0.00005 * double(Z2);
+  p.Z2 = Z2;
+  return p;
+}
+
+int
+make_material(const mtg_scoef_row * rows, const SpeciesConst & sc, const mtg_material & m,
+              double tmin, MatConst & mc, std::string & err)
+{
+  std::memset(&mc, 0, sizeof mc);
+  if (m.n_elements < 1 || m.n_elements > MAX_EL)
+  {
+    err = "a material needs 1 to 4 elements";
+    return MTG_ERR_BAD_INPUT;
+  }
+  if (!(m.rho > 0.0))
+  {
+    err = "material density must be positive";
+    return MTG_ERR_BAD_INPUT;
+  }
+  // MaterialBase::prepare (material.C:37-74)
+  double t[MAX_EL];
+  double tt = 0.0;
+  for (int i = 0; i < m.n_elements; ++i)
+  {
+    const mtg_element & e = m.elements[i];
+    if (e.Z < 1 || e.Z > MTG_SCOEF_ROWS || !(e.m > 0.0))
+    {
+      err = "element Z must be 1..92 and its mass positive";
+      return MTG_ERR_BAD_INPUT;
+    }
+    t[i] = e.t < 0.0 ? 0.0 : e.t;
+    tt += t[i];
+  }
+  if (!(tt > 0.0))
+  {
+    err = "stoichiometry invalid, all elements zero";
+    return MTG_ERR_BAD_INPUT;
+  }
+  for (int i = 0; i < m.n_elements; ++i)
+    t[i] /= tt;
+  double am = 0.0, az = 0.0;
+  for (int i = 0; i < m.n_elements; ++i)
+  {
+    am += m.elements[i].m * t[i];
+    az += double(m.elements[i].Z) * t[i];
+  }
+  mc.am = am;
+  mc.az = az;
+  mc.arho = m.rho * 0.6022 / am;
+  mc.nel = m.n_elements;
+
+  // MaterialBase::average (material.C:78-110)
+  const double m1 = sc.m1;
+  const double mu = m1 / am;
+  const double fZ = sc.fz1;
+  const double fZ023 = std::pow(fZ, 0.23);
+  mc.a = .5292 * .8853 / (fZ023 + std::pow(az, 0.23));
+  mc.f = mc.a * am / (az * fZ * 14.4 * (m1 + am));
+  mc.epsdg = tmin * mc.f * ((1.0 + mu) * (1.0 + mu)) / (4.0 * mu);
+  for (int i = 0; i < m.n_elements; ++i)
+  {
+    const mtg_element & e = m.elements[i];
+    ElemConst & ec = mc.el[i];
+    ec.t = t[i];
+    ec.my = m1 / e.m;
+    ec.ec = 4.0 * ec.my / ((1.0 + ec.my) * (1.0 + ec.my));
+    ec.ai = .5292 * .8853 / (fZ023 + std::pow(e.Z, 0.23));
+    ec.fi = ec.ai * e.m / (fZ * double(e.Z) * 14.4 * (m1 + e.m));
+    ec.Edisp = e.Edisp;
+    ec.Elbind = e.Elbind;
+    ec.m2 = e.m;
+    ec.Z2 = e.Z;
+    ec.rspecies = -1;
+    mc.sp[i] = make_stop_pair(rows, sc, e.Z);
+  }
+  return MTG_OK;
+}
+
+void
+build_fp32_tables(const HostTables & t, std::vector<Species32> & species, std::vector<Mat32> & mats,
+                  std::vector<Sim32> & sims)
+{
+  species.resize(t.species.size());
+  for (size_t i = 0; i < t.species.size(); ++i)
+  {
+    std::memset(&species[i], 0, sizeof(Species32));
+    species[i].m1 = float(t.species[i].m1);
+    species[i].two_m1 = float(2.0 * t.species[i].m1);
+    species[i].Z1 = t.species[i].Z1;
+  }
+  mats.resize(t.mats.size());
+  for (size_t i = 0; i < t.mats.size(); ++i)
+  {
+    const MatConst & m = t.mats[i];
+    Mat32 & o = mats[i];
+    std::memset(&o, 0, sizeof o);
+    o.a = float(m.a);
+    o.f = float(m.f);
+    o.epsdg = float(m.epsdg);
+    o.inv_pi_arho = float(1.0 / (3.14159265358979323846 * m.arho));
+    o.nel = m.nel;
+    o.row = int(i);
+    for (int j = 0; j < m.nel; ++j)
+    {
+      const ElemConst & e = m.el[j];
+      Elem32 & f = o.el[j];
+      f.t = float(e.t);
+      f.my = float(e.my);
+      f.ec = float(e.ec);
+      f.inv_ai = float(1.0 / e.ai);
+      f.fi = float(e.fi);
+      f.Edisp = float(e.Edisp);
+      f.Elbind = float(e.Elbind);
+      f.m2 = float(e.m2);
+      f.disp_thresh = float(e.Edisp - e.Elbind);
+      f.Z2 = e.Z2;
+      f.rspecies = e.rspecies;
+    }
+  }
+  sims.resize(t.sims.size());
+  for (size_t i = 0; i < t.sims.size(); ++i)
+  {
+    const SimDesc & d = t.sims[i];
+    Sim32 & o = sims[i];
+    std::memset(&o, 0, sizeof o);
+    for (int k = 0; k < MAX_LAYERS; ++k)
+    {
+      o.layer_end[k] = float(d.layer_end[k]);
+      o.layer_mat[k] = d.layer_mat[k];
+    }
+    for (int k = 0; k < 3; ++k)
+    {
+      o.w[k] = float(d.w[k]);
+      o.bc[k] = d.bc[k];
+      o.any_cut |= d.bc[k] == 2;
+    }
+    o.n_layers = d.n_layers;
+    o.n_mat = d.n_mat;
+    o.mat_base = d.mat_base;
+    o.species_base = d.species_base;
+    o.Ef = float(d.Ef);
+    o.flscale = float(d.invscale);
+    o.tau = float(d.tau);
+    o.cw = float(d.cw);
+    o.range_mode = d.range_mode;
+    o.primaries_only = d.primaries_only;
+  }
+}
+
+int
+build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim * sims, int n_sims,
+             HostTables & out, std::string & err)
+{
+  out = HostTables();
+  if (n_sims < 1 || !sims)
+  {
+    err = "need at least one simulation";
+    return MTG_ERR_BAD_INPUT;
+  }
+  if (!(cfg.length_scale > 0.0) || !(cfg.tmin > 0.0) || !(cfg.cw > 0.0))
+  {
+    err = "length_scale, tmin and cw must be positive";
+    return MTG_ERR_BAD_INPUT;
+  }
+  seed_key(cfg.seed, out.k0, out.k1);
+  long long prim = 0, hist = 0;
+  for (int si = 0; si < n_sims; ++si)
+  {
+    const mtg_sim & s = sims[si];
+    const mtg_sample & smp = s.sample;
+    if (smp.n_layers < 1 || smp.n_layers > MAX_LAYERS)
+    {
+      err = "a sample needs 1 to 8 layers";
+      return MTG_ERR_BAD_INPUT;
+    }
+    if (s.ion.Z < 1 || s.ion.Z > MTG_SCOEF_ROWS || !(s.ion.m > 0.0) || !(s.ion.E > 0.0))
+    {
+      err = "ion Z must be 1..92 with positive mass and energy";
+      return MTG_ERR_BAD_INPUT;
+    }
+    if (s.n_primaries < 0 || s.first_primary < 0 || s.hist_range_n < 0 || s.hist_vac_n < 0 ||
+        (s.hist_range_n > 0 && !(s.hist_range_bin > 0.0)) ||
+        (s.hist_vac_n > 0 && !(s.hist_vac_bin > 0.0)))
+    {
+      err = "invalid primary count or histogram binning";
+      return MTG_ERR_BAD_INPUT;
+    }
+    for (int i = 0; i < 3; ++i)
+      if (smp.bc[i] < 0 || smp.bc[i] > 2)
+      {
+        err = "boundary conditions must be 0 (PBC), 1 (INF) or 2 (CUT)";
+        return MTG_ERR_BAD_INPUT;
+      }
+    const double dn = std::sqrt(s.ion.dir[0] * s.ion.dir[0] + s.ion.dir[1] * s.ion.dir[1] +
+                                s.ion.dir[2] * s.ion.dir[2]);
+    if (!(dn > 0.0))
+    {
+      err = "ion direction must be non-zero";
+      return MTG_ERR_BAD_INPUT;
+    }
+
+    // species: the ion, then every distinct (Z, m) of the target elements
+    std::vector<std::pair<int, double>> spc;
+    spc.push_back({s.ion.Z, s.ion.m});
+    auto species_of = [&](int Z, double m) {
+      for (size_t i = 0; i < spc.size(); ++i)
+        if (spc[i].first == Z && spc[i].second == m)
+          return int(i);
+      spc.push_back({Z, m});
+      return int(spc.size() - 1);
+    };
+    for (int k = 0; k < smp.n_layers; ++k)
+      for (int j = 0; j < smp.material[k].n_elements && j < MAX_EL; ++j)
+        species_of(smp.material[k].elements[j].Z, smp.material[k].elements[j].m);
+
+    SimDesc d;
+    std::memset(&d, 0, sizeof d);
+    d.species_base = int(out.species.size());
+    d.n_species = int(spc.size());
+    d.mat_base = int(out.mats.size());
+    d.n_mat = smp.n_layers;
+    for (auto & sp : spc)
+      out.species.push_back(make_species(rows, sp.first, sp.second));
+    for (int sidx = 0; sidx < d.n_species; ++sidx)
+      for (int k = 0; k < smp.n_layers; ++k)
+      {
+        MatConst mc;
+        int rc = make_material(rows, out.species[d.species_base + sidx], smp.material[k], cfg.tmin, mc, err);
+        if (rc != MTG_OK)
+          return rc;
+        for (int j = 0; j < mc.nel; ++j)
+          mc.el[j].rspecies = species_of(mc.el[j].Z2, mc.el[j].m2);
+        out.mats.push_back(mc);
+      }
+    // SampleLayers: cumulative layer ends, summed like lookupLayer does
+    d.n_layers = smp.n_layers;
+    double dsum = 0.0;
+    for (int k = 0; k < smp.n_layers; ++k)
+    {
+      if (smp.n_layers > 1 && !(smp.thickness[k] >= 0.0))
+      {
+        err = "layer thickness must be non-negative";
+        return MTG_ERR_BAD_INPUT;
+      }
+      dsum += smp.n_layers > 1 ? smp.thickness[k] : 0.0;
+      d.layer_end[k] = dsum;
+      d.layer_mat[k] = k;
+    }
+    for (int i = 0; i < 3; ++i)
+    {
+      d.bc[i] = smp.bc[i];
+      d.w[i] = smp.w[i];
+      d.dir[i] = s.ion.dir[i];
+      d.pos[i] = s.ion.pos[i];
+    }
+    d.E0 = s.ion.E;
+    d.Ef = s.ion.Ef;
+    d.scale = cfg.length_scale;
+    d.invscale = 1.0 / cfg.length_scale;
+    d.tau = cfg.tau;
+    d.cw = cfg.cw;
+    d.range_mode = s.tally_mode == MTG_TALLY_RANGE;
+    d.primaries_only = s.primaries_only != 0;
+    d.prim_begin = prim;
+    d.n_primaries = s.n_primaries;
+    d.sim_key = uint64_t(si);
+    d.key_offset = s.first_primary;
+    d.hist_range_n = s.hist_range_n;
+    d.hist_vac_n = s.hist_vac_n;
+    d.hist_range_base = hist;
+    d.hist_vac_base = hist + s.hist_range_n;
+    d.inv_hist_range_bin = s.hist_range_n > 0 ? 1.0 / s.hist_range_bin : 0.0;
+    d.inv_hist_vac_bin = s.hist_vac_n > 0 ? 1.0 / s.hist_vac_bin : 0.0;
+    hist += s.hist_range_n + 2LL * s.hist_vac_n;
+    prim += s.n_primaries;
+    out.prim_end.push_back(prim);
+    out.sims.push_back(d);
+    out.emax = std::max(out.emax, s.ion.E);
+  }
+  if (prim > 0xffffffffLL)
+  {
+    err = "at most 2^32 - 1 primaries per run";
+    return MTG_ERR_BAD_INPUT;
+  }
+  out.total_primaries = prim;
+  out.hist_total = hist;
+  return MTG_OK;
+}
+
+} // namespace mtg

@@ -1,0 +1,50 @@
+// Host-side table construction: turns the reference-style inputs (stopping rows,
+// materials, layers, ion template) into the POD tables of mtg_tables.h.
+// Plain C++ (no CUDA), so the host replay check builds exactly the same tables.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "mytrim_gpu.h"
+#include "mtg_tables.h"
+
+namespace mtg
+{
+
+struct HostTables
+{
+  std::vector<SimDesc> sims;
+  std::vector<long long> prim_end;        // exclusive end of each simulation's primaries
+  std::vector<SpeciesConst> species;
+  std::vector<MatConst> mats;
+  long long total_primaries = 0;
+  long long hist_total = 0;               // entries of the concatenated histograms
+  uint32_t k0 = 0, k1 = 0;                // Philox key
+  double emax = 0.0;                      // largest primary energy
+};
+
+// Build the tables; returns MTG_OK or MTG_ERR_BAD_INPUT with `err` set.
+int build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim * sims,
+                 int n_sims, HostTables & out, std::string & err);
+
+// Species constants of projectile (Z1, m1) and its stopping constants in Z2.
+SpeciesConst make_species(const mtg_scoef_row * rows, int Z1, double m1);
+StopPair make_stop_pair(const mtg_scoef_row * rows, const SpeciesConst & sc, int Z2);
+
+// One material as seen by species sc (MaterialBase::prepare + average,
+// material.C:37-110); rspecies is filled by the caller.
+int make_material(const mtg_scoef_row * rows, const SpeciesConst & sc, const mtg_material & m,
+                  double tmin, MatConst & out, std::string & err);
+
+// Single-precision copies of the tables for the FP32 engine.
+void build_fp32_tables(const HostTables & t, std::vector<Species32> & species, std::vector<Mat32> & mats,
+                       std::vector<Sim32> & sims);
+
+// Philox key of a run seed
+void seed_key(unsigned long long seed, uint32_t & k0, uint32_t & k1);
+
+// Parse stopping_tables.tsv (92 rows); returns false on a malformed file.
+bool read_table_file(const char * path, mtg_scoef_row * rows, std::string & err);
+
+} // namespace mtg

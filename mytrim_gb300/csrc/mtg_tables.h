@@ -1,0 +1,179 @@
+// Plain-old-data tables the cascade kernels read.  Built on the host from the
+// reference-style inputs (stopping coefficients, materials, layers, ion template)
+// by mtg_setup.cpp and copied to the device once per run.
+//
+// Everything that depends only on the projectile species and the material is
+// precomputed here in FP64 on the host, exactly as the reference computes it once
+// per cascade member (MaterialBase::average, material.C:78-110), and the
+// velocity-independent parts of the electronic stopping (material.C:161-281).
+#pragma once
+
+#include <stdint.h>
+
+namespace mtg
+{
+
+constexpr int MAX_EL = 4;      // elements per material
+constexpr int MAX_LAYERS = 8;  // layers per sample (the last extends to +inf)
+
+// stopping branch of the projectile (material.C:187, 192, 213)
+enum StopBranch : int
+{
+  STOP_H = 1,
+  STOP_HE = 2,
+  STOP_HEAVY = 3
+};
+
+// Constants of projectile species s that the stopping and scattering use.
+struct SpeciesConst
+{
+  int Z1;
+  int branch;
+  double m1;        // mass [u] used for momenta and reduced energies
+  double inv_m1k;   // 0.001 / m_stop, m_stop = m1 or SCOEF mm1 if m1 == 0 (material.C:178-185)
+  double fz1;
+  double cb, cb2;   // cbrt(Z1), cbrt(Z1)^2
+  double lfctr;     // SLFCTR screening factor
+  double bq;        // min(.43, max(.32, .12 + .025 Z1)) / cbrt(Z1)
+  double l0a;       // min(1.2, 0.6 + Z1 / 30)
+  double qlo, qden; // max(0, .9 - .025 Z1), |qlo - .2000001|
+  double qhi, qden2;// max(0, 1 - .025 min(16, Z1)), .025 min(16, Z1)
+  double inv_z1sq;  // 1 / Z1^2
+};
+
+// Electronic-stopping constants of species s in target element Z2.
+struct StopPair
+{
+  double pcoef[8];  // SCOEF.95A proton coefficients of Z2
+  double vfermi;    // Fermi velocity of Z2
+  double inv2vf2;   // 1 / (2 vfermi^2)
+  double velpwr;    // 0.25 for Z2 <= 6, else 0.45 (material.C:148-152)
+  double yrcut;     // max(yrmin, vrmin / cbrt(Z1)^2)
+  double eee;       // low-velocity matching energy (material.C:259-261)
+  double sp_eee;    // proton stopping at eee
+  double power;     // low-velocity exponent (material.C:264-267)
+  double zc;        // 0.18 + 0.0015 Z2
+  double hez;       // 0.007 + 0.00005 Z2 (helium)
+  int Z2;
+  int pad;
+};
+
+// One target element as seen by species s.
+struct ElemConst
+{
+  double t;         // normalised stoichiometric fraction (material.C:52-55)
+  double my;        // m1 / m2
+  double ec;        // 4 my / (1 + my)^2
+  double ai;        // screening length with Z1
+  double fi;        // reduced-energy factor with Z1
+  double Edisp, Elbind, m2;
+  int Z2;
+  int rspecies;     // species index (within the simulation) of a recoil of this element
+};
+
+// Material k as seen by species s.
+struct MatConst
+{
+  double a, f, epsdg, arho;
+  double am, az;
+  int nel;
+  int pad;
+  ElemConst el[MAX_EL];
+  StopPair sp[MAX_EL];
+};
+
+// One simulation: sample, ion template, run parameters, tally layout.
+struct SimDesc
+{
+  // species and material tables: MatConst index = mat_base + s * n_mat + k
+  int species_base, n_species;
+  int mat_base, n_mat;
+  // SampleLayers: x < layer_end[i] selects layer i, the last extends to +inf
+  int n_layers;
+  int layer_mat[MAX_LAYERS];
+  double layer_end[MAX_LAYERS];
+  int bc[3];        // 0 PBC, 1 INF, 2 CUT (sample.h:49-54)
+  double w[3];
+  // primary template (IonBase as built by runmytrim.C:290-304)
+  double E0, Ef;
+  double dir[3], pos[3];
+  // run control
+  double scale, invscale, tau, cw;
+  int range_mode;       // TrimRange semantics: no recoil followed, KP vacancies
+  int primaries_only;   // ThreadedTrimBase::_primaries_only
+  long long prim_begin; // first global primary index of this simulation
+  long long n_primaries;
+  uint64_t sim_key;     // simulation number used in the member keys
+  long long key_offset; // primary index offset of the member keys (sharded runs)
+  // tallies
+  int hist_range_n, hist_vac_n;
+  long long hist_range_base, hist_vac_base;
+  double inv_hist_range_bin, inv_hist_vac_bin;
+};
+
+// Totals per simulation (device accumulators, reduced on the host).
+struct SimTotals
+{
+  unsigned long long members, replacements, interstitials, substitutionals, lost;
+  unsigned long long newton_iters, rejection_passes, fallbacks;
+  double Elost, Eunfollowed;
+};
+
+// ---- single-precision copies used by the FP32 engine (built from the tables above)
+struct Elem32
+{
+  float t, my, ec, inv_ai, fi, Edisp, Elbind, m2;
+  float disp_thresh; // Edisp - Elbind (trim.C:359)
+  int Z2, rspecies, pad;
+};
+
+struct Mat32
+{
+  float a, f, epsdg, inv_pi_arho; // 1 / (pi * atomic density)
+  int nel, row, pad0, pad1;       // row: stopping-table row of this (species, material)
+  Elem32 el[MAX_EL];
+};
+
+struct Species32
+{
+  float m1, two_m1;
+  int Z1, pad;
+};
+
+struct Sim32
+{
+  float layer_end[MAX_LAYERS];
+  int layer_mat[MAX_LAYERS];
+  float w[3];
+  int bc[3];
+  int n_layers, n_mat, mat_base, species_base;
+  float Ef, flscale, tau, cw; // flscale = 1 / length scale
+  int range_mode, primaries_only, any_cut, pad;
+};
+
+// final state of a cascade member (IonBase::StateType, ion.h:75-84)
+enum MemberState : int
+{
+  ST_MOVING = 0,
+  ST_REPLACEMENT = 1,
+  ST_SUBSTITUTIONAL = 2,
+  ST_INTERSTITIAL = 3,
+  ST_LOST = 4
+};
+
+// outcome flags of one collision
+enum CollideFlags : int
+{
+  CF_PUSH = 1, // the collision displaced a recoil to follow
+  CF_DONE = 2  // the member came to rest or left the sample
+};
+
+enum ErrorBits : unsigned int
+{
+  ERRB_QUEUE_FULL = 1u,
+  ERRB_NUMERIC = 2u,
+  ERRB_BUDGET = 4u,
+  ERRB_BAD_INDEX = 8u
+};
+
+} // namespace mtg

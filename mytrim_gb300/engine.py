@@ -1,0 +1,275 @@
+"""Python front of the GB300 cascade engine (ctypes over include/mytrim_gpu.h).
+
+``Engine`` owns one mtg_ctx.  ``SimSpec`` describes one simulation in the terms
+of the reference's runmytrim input (layers of elements, an ion template, a
+primary count and the tally options of apps/runmytrim.C:103-285).
+"""
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+from pathlib import Path
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _ffi as F
+
+DATA_DIR = Path(__file__).resolve().parent / "data"
+TABLES = DATA_DIR / "stopping_tables.tsv"
+
+PRECISIONS = {"fp64": F.PREC_FP64, "fp32": F.PREC_FP32, "surrogate": F.PREC_FP32_SURROGATE}
+
+
+@dataclass
+class ElementSpec:
+    Z: int
+    m: float
+    t: float = 1.0
+    Edisp: float = 25.0  # Element defaults (element.C:25)
+    Elbind: float = 3.0
+
+
+@dataclass
+class LayerSpec:
+    thickness: float
+    rho: float
+    elements: List[ElementSpec]
+
+
+@dataclass
+class SimSpec:
+    """One simulation: sample, ion template, primaries and tallies."""
+    layers: List[LayerSpec]
+    Z: int
+    m: float
+    E: float
+    n_primaries: int
+    Ef: float = 3.0                      # IonBase::_Ef default (ion.C:26)
+    first_primary: int = 0               # primary index offset (sharded runs)
+    dir: Tuple[float, float, float] = (1.0, 0.0, 0.0)
+    pos: Optional[Tuple[float, float, float]] = None  # default (0, w1/2, w2/2) as runmytrim.C:298
+    size: Optional[Tuple[float, float, float]] = None  # default (total thickness, 100, 100)
+    bc: Tuple[int, int, int] = (F.BC_PBC, F.BC_PBC, F.BC_PBC)
+    mode: str = "vaccount"               # or "range"
+    primaries_only: bool = False
+    hist_range_bin: float = 10.0
+    hist_range_n: int = 0
+    hist_vac_bin: float = 1.0
+    hist_vac_n: int = 0
+
+    def box(self):
+        if self.size is not None:
+            return tuple(self.size)
+        return (sum(l.thickness for l in self.layers), 100.0, 100.0)
+
+    def start(self):
+        if self.pos is not None:
+            return tuple(self.pos)
+        w = self.box()
+        return (0.0, w[1] / 2.0, w[2] / 2.0)
+
+    def hist_sizes(self):
+        return self.hist_range_n, self.hist_vac_n, self.hist_vac_n
+
+    def to_c(self) -> F.Sim:
+        if not 1 <= len(self.layers) <= F.MAX_LAYERS:
+            raise ValueError("1 to 8 layers")
+        s = F.Sim()
+        s.sample.n_layers = len(self.layers)
+        for i, l in enumerate(self.layers):
+            if not 1 <= len(l.elements) <= F.MAX_ELEMENTS:
+                raise ValueError("1 to 4 elements per layer")
+            s.sample.thickness[i] = l.thickness
+            mat = s.sample.material[i]
+            mat.rho = l.rho
+            mat.n_elements = len(l.elements)
+            for j, e in enumerate(l.elements):
+                mat.elements[j].Z = e.Z
+                mat.elements[j].m = e.m
+                mat.elements[j].t = e.t
+                mat.elements[j].Edisp = e.Edisp
+                mat.elements[j].Elbind = e.Elbind
+        w = self.box()
+        for i in range(3):
+            s.sample.w[i] = w[i]
+            s.sample.bc[i] = self.bc[i]
+        s.ion.Z = self.Z
+        s.ion.m = self.m
+        s.ion.E = self.E
+        s.ion.Ef = self.Ef
+        p = self.start()
+        for i in range(3):
+            s.ion.dir[i] = self.dir[i]
+            s.ion.pos[i] = p[i]
+        s.n_primaries = self.n_primaries
+        s.first_primary = self.first_primary
+        s.tally_mode = F.TALLY_RANGE if self.mode == "range" else F.TALLY_VACCOUNT
+        s.primaries_only = int(self.primaries_only)
+        s.hist_range_bin = self.hist_range_bin
+        s.hist_range_n = self.hist_range_n
+        s.hist_vac_bin = self.hist_vac_bin
+        s.hist_vac_n = self.hist_vac_n
+        return s
+
+
+def summarize(t: dict) -> dict:
+    """Per-ion statistics with standard errors from the per-primary moments."""
+    n = max(t["primaries"], 1)
+    out = dict(t)
+
+    def mean_err(s1, s2, count):
+        if count <= 0:
+            return float("nan"), float("nan")
+        m = s1 / count
+        var = max(s2 / count - m * m, 0.0)
+        return m, math.sqrt(var / max(count - 1, 1))
+
+    out["vac_per_ion"], out["vac_per_ion_err"] = mean_err(t["vacancies"], t["vac_s2"], n)
+    out["eel_per_ion"], out["eel_per_ion_err"] = mean_err(t["Eel"], t["eel_s2"], n)
+    out["enuc_per_ion"], out["enuc_per_ion_err"] = mean_err(t["Enuc"], t["enuc_s2"], n)
+    out["coll_per_ion"], out["coll_per_ion_err"] = mean_err(t["collisions"], t["coll_s2"], n)
+    rn = t["range_n"]
+    if rn > 1:
+        mx = t["sx"] / rn
+        vx = max(t["sxx"] / rn - mx * mx, 0.0)
+        my, mz = t["sy"] / rn, t["sz"] / rn
+        vy = max(t["syy"] / rn - my * my, 0.0)
+        vz = max(t["szz"] / rn - mz * mz, 0.0)
+        out["range_mean"] = mx
+        out["range_mean_err"] = math.sqrt(vx / (rn - 1))
+        out["straggle"] = math.sqrt(vx)
+        # standard error of a standard deviation (normal approximation)
+        out["straggle_err"] = math.sqrt(vx) / math.sqrt(2.0 * (rn - 1))
+        out["lateral"] = math.sqrt(vy + vz)
+        out["lateral_err"] = math.sqrt(vy + vz) / math.sqrt(2.0 * (rn - 1))
+    return out
+
+
+class Engine:
+    """One engine context on one GPU."""
+
+    def __init__(self, device: int = 0, precision: str = "fp64", seed: int = 1, tmin: float = 0.2,
+                 tau: float = 0.0, cw: float = 0.001, length_scale: float = 1.0, max_collisions: int = 0,
+                 stack_capacity: int = 0, tables: Optional[str] = None):
+        self.lib = F.load()
+        self.ctx = C.c_void_p()
+        st = self.lib.mtg_create(device, C.byref(self.ctx))
+        if st != F.OK:
+            raise F.EngineError(st, "mtg_create failed")
+        self._check(self.lib.mtg_load_tables(self.ctx, str(tables or TABLES).encode()))
+        self.cfg = F.Config()
+        self.configure(precision=precision, seed=seed, tmin=tmin, tau=tau, cw=cw, length_scale=length_scale,
+                       max_collisions=max_collisions, stack_capacity=stack_capacity)
+        self._sims: List[SimSpec] = []
+
+    def _check(self, st):
+        if st != F.OK:
+            msg = self.lib.mtg_last_error(self.ctx)
+            raise F.EngineError(st, msg.decode() if msg else "")
+        return st
+
+    def configure(self, precision="fp64", seed=1, tmin=0.2, tau=0.0, cw=0.001, length_scale=1.0,
+                  max_collisions=0, stack_capacity=0):
+        c = self.cfg
+        c.tmin, c.tau, c.cw, c.length_scale = tmin, tau, cw, length_scale
+        c.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        c.seed = seed
+        c.max_collisions_per_member = max_collisions
+        c.stack_capacity = stack_capacity
+        self._check(self.lib.mtg_configure(self.ctx, C.byref(c)))
+
+    def close(self):
+        if self.ctx:
+            self.lib.mtg_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- runs
+    def prepare(self, sims: Sequence[SimSpec]):
+        arr = (F.Sim * len(sims))(*[s.to_c() for s in sims])
+        self._sims = list(sims)
+        self._check(self.lib.mtg_prepare(self.ctx, arr, len(sims)))
+
+    def launch(self, stream: Optional[int] = None):
+        self._check(self.lib.mtg_launch_async(self.ctx, C.c_void_p(stream or 0)))
+
+    def collect(self, check=True):
+        n = len(self._sims)
+        tot = (F.Totals * n)()
+        nh = sum(sum(s.hist_sizes()) for s in self._sims)
+        hist = (C.c_longlong * max(nh, 1))()
+        st = self.lib.mtg_collect(self.ctx, tot, hist)
+        if check:
+            self._check(st)
+        out = []
+        off = 0
+        for i, s in enumerate(self._sims):
+            d = tot[i].as_dict()
+            hr, hv, hp = s.hist_sizes()
+            h = np.frombuffer(hist, dtype=np.int64, count=max(nh, 1))
+            d["hist_range"] = h[off:off + hr].copy()
+            d["hist_vac"] = h[off + hr:off + hr + hv].copy()
+            d["hist_repl"] = h[off + hr + hv:off + hr + hv + hp].copy()
+            off += hr + hv + hp
+            d["status"] = st
+            out.append(d)
+        return out
+
+    def run(self, sims: Sequence[SimSpec], check=True):
+        self.prepare(sims)
+        self.launch()
+        return self.collect(check=check)
+
+    def primaries(self, first: int, n: int) -> dict:
+        out = {k: np.zeros(n, dtype=np.int64) for k in ("vacancies", "collisions")}
+        out.update({k: np.zeros(n, dtype=np.float64) for k in ("eel", "enuc", "x", "y", "z")})
+        out["state"] = np.zeros(n, dtype=np.int32)
+        p = lambda a, t: a.ctypes.data_as(C.POINTER(t))
+        self._check(self.lib.mtg_get_primaries(
+            self.ctx, first, n, p(out["vacancies"], C.c_longlong), p(out["collisions"], C.c_longlong),
+            p(out["eel"], C.c_double), p(out["enuc"], C.c_double), p(out["x"], C.c_double),
+            p(out["y"], C.c_double), p(out["z"], C.c_double), p(out["state"], C.c_int)))
+        return out
+
+    def set_record_capacity(self, cap: int):
+        self._check(self.lib.mtg_set_record_capacity(self.ctx, cap))
+        self._record_cap = cap
+
+    def records(self) -> np.ndarray:
+        cap = getattr(self, "_record_cap", 0)
+        buf = (F.MemberRecord * max(cap, 1))()
+        n = C.c_longlong(0)
+        self._check(self.lib.mtg_get_records(self.ctx, buf, cap, C.byref(n)))
+        dt = np.dtype([("key", "<u8"), ("sim", "<i4"), ("species", "<i4"), ("gen", "<i4"), ("state", "<i4"),
+                       ("ncoll", "<u4"), ("nvac", "<u4"), ("E", "<f8"), ("x", "<f8"), ("y", "<f8"),
+                       ("z", "<f8"), ("eel", "<f8")])
+        assert dt.itemsize == C.sizeof(F.MemberRecord)
+        return np.frombuffer(bytes(buf)[: n.value * dt.itemsize], dtype=dt).copy()
+
+    def stopping(self, Z1, m1, layer: LayerSpec, energies, precision="fp64") -> np.ndarray:
+        e = np.ascontiguousarray(energies, dtype=np.float64)
+        out = np.zeros_like(e)
+        mat = SimSpec([layer], Z1, m1, 1.0, 0).to_c().sample.material[0]
+        prec = PRECISIONS[precision] if isinstance(precision, str) else precision
+        self._check(self.lib.mtg_stopping(self.ctx, Z1, m1, C.byref(mat), e.ctypes.data_as(C.POINTER(C.c_double)),
+                                          len(e), prec, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def scatter(self, eps, b, precision="fp64") -> np.ndarray:
+        e = np.ascontiguousarray(eps, dtype=np.float64)
+        bb = np.ascontiguousarray(b, dtype=np.float64)
+        out = np.zeros_like(e)
+        prec = PRECISIONS[precision] if isinstance(precision, str) else precision
+        pd = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        self._check(self.lib.mtg_scatter(self.ctx, pd(e), pd(bb), len(e), prec, pd(out)))
+        return out
+
+    def stats(self) -> dict:
+        s = F.Stats()
+        self._check(self.lib.mtg_get_stats(self.ctx, C.byref(s)))
+        return {n: getattr(s, n) for n, _ in s._fields_}

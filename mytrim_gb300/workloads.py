@@ -1,0 +1,98 @@
+"""The benchmark workloads: simulations described by their physical parameters.
+
+Masses are the SRIM "MAI weight" column of the stopping tables for the ions and
+the natural weights for targets; densities are the ones the workload names.
+"""
+import math
+
+import numpy as np
+
+from . import _ffi as F
+from .engine import ElementSpec, LayerSpec, SimSpec
+
+CU = 63.546
+SI = 28.086
+O = 15.999
+
+
+def cu_self_ion(n_primaries=10_000, E=100e3):
+    """Cu 100 keV normal incidence into bulk Cu (8.96 g/cm3, Edisp 25, Ebind 3, Ef 5 eV),
+    full cascade, 1 nm range histogram to 200 nm."""
+    return SimSpec(layers=[LayerSpec(1e7, 8.96, [ElementSpec(29, CU, 1.0, 25.0, 3.0)])],
+                   Z=29, m=CU, E=E, Ef=5.0, n_primaries=n_primaries,
+                   hist_range_bin=10.0, hist_range_n=200, hist_vac_bin=10.0, hist_vac_n=200)
+
+
+def sio2_on_si(Z, m, E, n_primaries, tilt_deg=7.0):
+    """Ion at `tilt_deg` into 10 nm SiO2 (2.2 g/cm3; Edisp Si 15, O 28) on bulk Si (2.33,
+    Edisp 15); backscattered ions leave through the surface (CUT at x < 0);
+    0.5 nm depth histogram to 300 nm."""
+    t = math.radians(tilt_deg)
+    layers = [LayerSpec(100.0, 2.2, [ElementSpec(14, SI, 1.0, 15.0, 3.0), ElementSpec(8, O, 2.0, 28.0, 3.0)]),
+              LayerSpec(1e7, 2.33, [ElementSpec(14, SI, 1.0, 15.0, 3.0)])]
+    return SimSpec(layers=layers, Z=Z, m=m, E=E, n_primaries=n_primaries, dir=(math.cos(t), math.sin(t), 0.0),
+                   pos=(0.0, 0.0, 0.0), size=(1e9, 1e9, 1e9), bc=(F.BC_CUT, F.BC_INF, F.BC_INF),
+                   hist_range_bin=5.0, hist_range_n=600, hist_vac_bin=5.0, hist_vac_n=600)
+
+
+def boron_implant(n_primaries=1_000_000):
+    return sio2_on_si(5, 11.009, 10e3, n_primaries)
+
+
+def arsenic_implant(n_primaries=1_000_000):
+    return sio2_on_si(33, 74.922, 50e3, n_primaries)
+
+
+def silver_into_silicon(n_primaries=10_000_000):
+    """Ag 200 keV into bulk Si (2.33 g/cm3, Edisp 15, Ebind 3): the surrogate workload."""
+    return SimSpec(layers=[LayerSpec(1e7, 2.33, [ElementSpec(14, SI, 1.0, 15.0, 3.0)])],
+                   Z=47, m=106.905, E=200e3, n_primaries=n_primaries,
+                   hist_range_bin=10.0, hist_range_n=300, hist_vac_bin=10.0, hist_vac_n=300)
+
+
+def gold_deposition(n_primaries=100_000_000):
+    """Au 1 MeV into 50 nm Ag / 200 nm Cu / bulk Si with surface loss (CUT at x < 0)."""
+    layers = [LayerSpec(500.0, 10.49, [ElementSpec(47, 107.868, 1.0)]),
+              LayerSpec(2000.0, 8.96, [ElementSpec(29, CU, 1.0)]),
+              LayerSpec(1e7, 2.33, [ElementSpec(14, SI, 1.0, 15.0, 3.0)])]
+    return SimSpec(layers=layers, Z=79, m=196.967, E=1e6, n_primaries=n_primaries, pos=(0.0, 0.0, 0.0),
+                   size=(1e9, 1e9, 1e9), bc=(F.BC_CUT, F.BC_INF, F.BC_INF),
+                   hist_range_bin=10.0, hist_range_n=300, hist_vac_bin=10.0, hist_vac_n=300)
+
+
+# targets of the batched workload: (name, rho, [(Z, mass, fraction, Edisp)])
+TARGETS = [
+    ("Si", 2.33, [(14, SI, 1.0, 15.0)]),
+    ("Cu", 8.96, [(29, CU, 1.0, 25.0)]),
+    ("Ag", 10.49, [(47, 107.868, 1.0, 25.0)]),
+    ("Au", 19.32, [(79, 196.967, 1.0, 25.0)]),
+    ("SiO2", 2.2, [(14, SI, 1.0, 15.0), (8, O, 2.0, 28.0)]),
+    ("Al2O3", 3.95, [(13, 26.982, 2.0, 25.0), (8, O, 3.0, 28.0)]),
+]
+
+
+def batched_uneven(n_sims=4096, seed=1, scale_primaries=1.0, ion_masses=None):
+    """4096 independent simulations drawn from `seed`: Z1 uniform 1..83 with the SRIM
+    mass, E0 log-uniform 1 keV - 1 MeV, incidence angle uniform 0-60 deg, 1-4 layers
+    from TARGETS with thickness log-uniform 5-500 nm over bulk Si, primaries
+    log-uniform 1e2 - 1e5 (times `scale_primaries`)."""
+    rng = np.random.default_rng(seed)
+    sims = []
+    for _ in range(n_sims):
+        Z = int(rng.integers(1, 84))
+        m = ion_masses[Z - 1] if ion_masses is not None else 2.0 * Z
+        E = float(10 ** rng.uniform(3, 6))
+        ang = math.radians(float(rng.uniform(0, 60)))
+        nl = int(rng.integers(1, 5))
+        layers = []
+        for _ in range(nl):
+            name, rho, els = TARGETS[int(rng.integers(0, len(TARGETS)))]
+            th = float(10 ** rng.uniform(math.log10(50.0), math.log10(5000.0)))
+            layers.append(LayerSpec(th, rho, [ElementSpec(z, mm, f, ed, 3.0) for z, mm, f, ed in els]))
+        layers.append(LayerSpec(1e7, 2.33, [ElementSpec(14, SI, 1.0, 15.0, 3.0)]))
+        n = max(1, int(round(10 ** rng.uniform(2, 5) * scale_primaries)))
+        sims.append(SimSpec(layers=layers, Z=Z, m=m, E=E, n_primaries=n,
+                            dir=(math.cos(ang), math.sin(ang), 0.0), pos=(0.0, 0.0, 0.0),
+                            size=(1e9, 1e9, 1e9), bc=(F.BC_CUT, F.BC_INF, F.BC_INF),
+                            hist_range_bin=10.0, hist_range_n=100))
+    return sims

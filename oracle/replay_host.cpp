@@ -1,0 +1,189 @@
+// Host replay build of the GPU engine's FP64 collision code (test infrastructure).
+//
+// Compiles the product's shared physics (mytrim_gb300/csrc/mtg_collide64.cuh,
+// mtg_common.cuh) and table setup (mtg_setup.cpp) for the CPU with every multiply
+// and add rounded separately (-ffp-contract=off), the same rounding the FP64 GPU
+// engine is compiled with (-fmad=false).  It follows every cascade member of a
+// run spec to rest and prints one record per member; the GPU engine's member
+// records (mtg_get_records) must match these bit for bit, whatever order the GPU
+// ran the members in, because every random number is keyed by the member's path
+// and collision index.
+//
+// Usage: replay_host <stopping_tables.tsv> < spec     (spec format: runspec.h)
+
+#include "runspec.h"
+
+#include "mtg_collide64.cuh"
+#include "mtg_setup.h"
+
+#include <algorithm>
+#include <cinttypes>
+#include <vector>
+
+using namespace mtg;
+
+struct HostSink
+{
+  const SimDesc * sim;
+  unsigned int m_vac = 0;
+  int m_state = 0;
+  double m_eel = 0.0;
+  int range_mode = 0;
+
+  void eel(double d) { m_eel += d; }
+  void newton(int) {}
+  void passes(int) {}
+  void fallback() {}
+  void numeric() {}
+  void enuc(double) {}
+  void unfollowed(double) {}
+  void lost(double) { m_state = ST_LOST; }
+  template <class R, class E>
+  void vacancy(const R & rec, const E & el)
+  {
+    if (range_mode)
+    {
+      const double Z = double(el.Z2), m = el.m2, Er = double(rec.E);
+      const double Ed = el.Edisp;
+      const double ed = 0.0115 * pow64(Z, -7.0 / 3.0) * Er;
+      const double kd = 0.1337 * pow64(Z, 2.0 / 3.0) / sqrt(m);
+      const double g = 3.4008 * pow64(ed, 1.0 / 6.0) + 0.40244 * pow64(ed, 3.0 / 4.0) + ed;
+      const double Ev = Er / (1.0 + kd * g);
+      unsigned long long add = 0;
+      if (Ev < Ed)
+        add = 0;
+      else if (Ev >= Ed / 0.4)
+        add = (unsigned long long)(Ev * 0.4 / Ed);
+      else
+        add = 1;
+      m_vac += (unsigned int)add;
+      return;
+    }
+    ++m_vac;
+  }
+  void replacement(double) {}
+  template <class P>
+  void stop(int state, const P &)
+  {
+    m_state = state;
+  }
+};
+
+int
+main(int argc, char ** argv)
+{
+  if (argc < 2)
+  {
+    fprintf(stderr, "usage: replay_host <stopping_tables.tsv> < spec\n");
+    return 2;
+  }
+  std::string err;
+  mtg_scoef_row rows[MTG_SCOEF_ROWS];
+  if (!read_table_file(argv[1], rows, err))
+  {
+    fprintf(stderr, "replay_host: %s\n", err.c_str());
+    return 2;
+  }
+  runspec::Spec spec;
+  if (!runspec::parse(std::cin, spec, err))
+  {
+    fprintf(stderr, "replay_host: %s\n", err.c_str());
+    return 2;
+  }
+  if (spec.layers.size() > MTG_MAX_LAYERS)
+  {
+    fprintf(stderr, "replay_host: too many layers\n");
+    return 2;
+  }
+  mtg_sim sim;
+  memset(&sim, 0, sizeof sim);
+  sim.sample.n_layers = int(spec.layers.size());
+  for (size_t k = 0; k < spec.layers.size(); ++k)
+  {
+    sim.sample.thickness[k] = spec.layers[k].thickness;
+    mtg_material & m = sim.sample.material[k];
+    m.rho = spec.layers[k].rho;
+    m.n_elements = int(spec.layers[k].el.size());
+    for (int j = 0; j < m.n_elements && j < MTG_MAX_ELEMENTS; ++j)
+    {
+      const auto & e = spec.layers[k].el[j];
+      m.elements[j] = mtg_element{e.Z, e.m, e.t, e.Edisp, e.Elbind};
+    }
+  }
+  for (int i = 0; i < 3; ++i)
+  {
+    sim.sample.w[i] = spec.size[i];
+    sim.sample.bc[i] = spec.bc[i];
+    sim.ion.dir[i] = spec.dir[i];
+    sim.ion.pos[i] = spec.pos[i];
+  }
+  sim.ion.Z = spec.Z;
+  sim.ion.m = spec.m;
+  sim.ion.E = spec.E;
+  sim.ion.Ef = spec.Ef;
+  sim.n_primaries = spec.count;
+  sim.first_primary = 0;
+  sim.tally_mode = spec.range_mode ? MTG_TALLY_RANGE : MTG_TALLY_VACCOUNT;
+  sim.primaries_only = spec.primaries_only;
+  mtg_config cfg;
+  memset(&cfg, 0, sizeof cfg);
+  cfg.tmin = 0.2;
+  cfg.tau = 0.0;
+  cfg.cw = 0.001;
+  cfg.length_scale = spec.scale;
+  cfg.seed = spec.seed;
+  HostTables t;
+  if (build_tables(rows, cfg, &sim, 1, t, err) != MTG_OK)
+  {
+    fprintf(stderr, "replay_host: %s\n", err.c_str());
+    return 2;
+  }
+  const SimDesc & sd = t.sims[0];
+  std::vector<P64> stack;
+  for (long long n = spec.first; n < spec.first + spec.n; ++n)
+  {
+    P64 p;
+    p.x = sd.pos[0];
+    p.y = sd.pos[1];
+    p.z = sd.pos[2];
+    p.dx = sd.dir[0];
+    p.dy = sd.dir[1];
+    p.dz = sd.dir[2];
+    p.E = sd.E0;
+    p.key = root_key(sd.sim_key, uint64_t(n));
+    p.species = 0;
+    p.gen = 0;
+    p.sim = 0;
+    p.prim = uint32_t(n);
+    stack.push_back(p);
+    while (!stack.empty())
+    {
+      P64 m = stack.back();
+      stack.pop_back();
+      const SpeciesConst & sc = t.species[sd.species_base + m.species];
+      const MatConst * mrow = &t.mats[sd.mat_base + m.species * sd.n_mat];
+      const U4 d = draw_block(m.key, 0u, 0u, t.k0, t.k1);
+      const double r1 = u53(d.x, d.y);
+      HostSink sink;
+      sink.sim = &sd;
+      sink.range_mode = sd.range_mode;
+      uint32_t ic = 0;
+      int flags = 0;
+      do
+      {
+        ++ic;
+        P64 rec;
+        flags = collide64(m, ic, r1, sd, sc, mrow, t.k0, t.k1, rec, sink);
+        if (flags & CF_PUSH)
+        {
+          rec.sim = m.sim;
+          rec.prim = m.prim;
+          stack.push_back(rec);
+        }
+      } while (!(flags & CF_DONE) && ic < (1u << 24));
+      printf("%" PRIu64 " %d %d %d %u %u %a %a %a %a %a\n", m.key, m.species, m.gen, sink.m_state, ic,
+             sink.m_vac, m.E, m.x, m.y, m.z, sink.m_eel);
+    }
+  }
+  return 0;
+}

@@ -1,0 +1,39 @@
+import os
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "oracle"))
+
+REFERENCE = Path(os.environ.get("MYTRIM_REFERENCE", "/root/reference"))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (run on the GB300)")
+
+
+@pytest.fixture(scope="session")
+def oracle_built():
+    import oracle_io
+    oracle_io.build(REFERENCE if (REFERENCE / "trim.C").exists() else None)
+    return oracle_io
+
+
+@pytest.fixture(scope="session")
+def engine_lib():
+    from mytrim_gb300 import build
+    return build.build()
+
+
+@pytest.fixture(scope="session")
+def gpu_engine(engine_lib):
+    import torch
+    if not torch.cuda.is_available():
+        pytest.fail("GPU test without a CUDA device")
+    from mytrim_gb300 import Engine
+    e = Engine(precision="fp64")
+    yield e
+    e.close()

@@ -1,0 +1,222 @@
+"""GPU parity of the cascade engine, through the C ABI (libmytrim_gpu.so).
+
+* stopping: the FP64 device stopping equals the oracle's getrstop to 1e-12;
+  the FP32 table to 2e-4;
+* trajectories: the FP64 engine's per-member records equal, bit for bit, the host
+  build of the same code (oracle/_build/replay_host) on the same Philox streams;
+* statistics: FP64 discrete totals equal the oracle on the same Philox streams;
+  against the reference's own mt19937 streams, vacancies/ion, range, straggle,
+  electronic loss agree within 3 sigma of the combined Monte Carlo error; FP32
+  agrees with FP64 within 3 sigma and 1 %;
+* properties at full size: energy conservation, sharding invariance, overflow
+  drains, error returns instead of hangs.
+"""
+import math
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+sys.path.insert(0, str(ROOT / "tests" / "golden"))
+
+from golden_cases import CASES  # noqa: E402
+from mytrim_gb300 import Engine, summarize  # noqa: E402
+from mytrim_gb300 import _ffi as F  # noqa: E402
+from mytrim_gb300.engine import ElementSpec, LayerSpec, SimSpec  # noqa: E402
+from mytrim_gb300 import workloads as W  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+TARGETS = {
+    "Si": LayerSpec(1.0, 2.33, [ElementSpec(14, 28.086, 1.0)]),
+    "Fe": LayerSpec(1.0, 7.8658, [ElementSpec(26, 55.847, 1.0)]),
+    "W": LayerSpec(1.0, 19.35, [ElementSpec(74, 183.85, 1.0)]),
+    "SiO2": LayerSpec(1.0, 2.2, [ElementSpec(14, 28.086, 1.0), ElementSpec(8, 15.999, 2.0)]),
+    "C": LayerSpec(1.0, 2.253, [ElementSpec(6, 12.01, 1.0)]),
+}
+IONS = [(1, 1.008), (2, 4.003), (5, 11.009), (14, 27.977), (29, 63.546), (47, 106.905), (79, 196.967), (92, 238.05)]
+
+
+@pytest.mark.parametrize("target", sorted(TARGETS))
+def test_stopping_fp64_matches_oracle(gpu_engine, oracle_built, target):
+    E = np.logspace(0, 7.2, 97)
+    layer = TARGETS[target]
+    for Z1, m1 in IONS:
+        want = np.array(oracle_built.stopping(Z1, m1, layer, E))
+        got = gpu_engine.stopping(Z1, m1, layer, E, precision="fp64")
+        rel = np.abs(got - want) / np.abs(want)
+        assert rel.max() < 1e-12, (target, Z1, rel.max())
+
+
+@pytest.mark.parametrize("target", ["Si", "SiO2", "W"])
+def test_stopping_fp32_table(gpu_engine, oracle_built, target):
+    E = np.logspace(0.5, 6.3, 301)
+    layer = TARGETS[target]
+    for Z1, m1 in IONS:
+        want = np.array(oracle_built.stopping(Z1, m1, layer, E))
+        got = gpu_engine.stopping(Z1, m1, layer, E, precision="fp32")
+        rel = np.abs(got - want) / np.abs(want)
+        assert rel.max() < 2e-4, (target, Z1, rel.max())
+
+
+def _replay(oracle_built, sim, seed):
+    txt = oracle_built.spec_text(sim, seed=seed, philox=True)
+    exe = ROOT / "oracle" / "_build" / "replay_host"
+    r = subprocess.run([str(exe), str(oracle_built.TABLES)], input=txt, capture_output=True, text=True,
+                       check=True)
+    rows = []
+    for line in r.stdout.splitlines():
+        p = line.split()
+        rows.append((int(p[0]), int(p[1]), int(p[2]), int(p[3]), int(p[4]), int(p[5]),
+                     *(float.fromhex(v) for v in p[6:11])))
+    return sorted(rows)
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_fp64_trajectories_bitwise_vs_host_build(oracle_built, engine_lib, case):
+    sim, seed, _ = CASES[case]
+    e = Engine(precision="fp64", seed=seed)
+    e.set_record_capacity(200_000)
+    e.run([sim])
+    rec = e.records()
+    e.close()
+    got = sorted((int(r["key"]), int(r["species"]), int(r["gen"]), int(r["state"]), int(r["ncoll"]),
+                  int(r["nvac"]), float(r["E"]), float(r["x"]), float(r["y"]), float(r["z"]), float(r["eel"]))
+                 for r in rec)
+    want = _replay(oracle_built, sim, seed)
+    assert len(got) == len(want)
+    assert got == want
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_fp64_totals_equal_oracle_on_same_streams(oracle_built, engine_lib, case):
+    sim, seed, _ = CASES[case]
+    e = Engine(precision="fp64", seed=seed)
+    g = e.run([sim])[0]
+    e.close()
+    o = oracle_built.run(sim, seed=seed, philox=True)
+    for k in ("members", "collisions", "vacancies", "replacements", "interstitials", "substitutionals", "lost",
+              "range_n"):
+        assert g[k] == o[k], (case, k, g[k], o[k])
+    for k in ("Eel", "Enuc", "sx", "sxx"):
+        assert math.isclose(g[k], o[k], rel_tol=1e-9, abs_tol=1e-6), (case, k, g[k], o[k])
+    assert list(g["hist_range"]) == o["hist_range"]
+
+
+def _z(a, b, key):
+    ea, eb = a[key + "_err"], b[key + "_err"]
+    return abs(a[key] - b[key]) / math.sqrt(ea * ea + eb * eb)
+
+
+def test_fp64_statistics_vs_reference_streams(oracle_built, engine_lib):
+    """GPU (Philox) against the oracle on the reference's own mt19937 streams."""
+    sim = SimSpec(layers=[LayerSpec(1e5, 8.92, [ElementSpec(29, 63.546, 1.0)])], Z=29, m=63.546, E=10e3,
+                  n_primaries=4000)
+    e = Engine(precision="fp64", seed=2344)
+    g = summarize(e.run([sim])[0])
+    e.close()
+    o = summarize(oracle_built.run_parallel(sim, seed=2344, philox=False, procs=8))
+    for key in ("vac_per_ion", "eel_per_ion", "range_mean", "straggle", "lateral", "coll_per_ion"):
+        assert _z(g, o, key) < 3.5, (key, g[key], o[key])
+
+
+@pytest.mark.parametrize("name", ["cu", "as_layered"])
+def test_fp32_matches_fp64(engine_lib, name):
+    if name == "cu":
+        sim = W.cu_self_ion(n_primaries=3000, E=20e3)
+    else:
+        sim = W.arsenic_implant(n_primaries=3000)
+        sim.E = 20e3
+    r = {}
+    for prec in ("fp64", "fp32"):
+        e = Engine(precision=prec, seed=5)
+        r[prec] = summarize(e.run([sim])[0])
+        e.close()
+    for key in ("vac_per_ion", "eel_per_ion", "range_mean", "straggle", "lateral"):
+        a, b = r["fp32"], r["fp64"]
+        rel = abs(a[key] - b[key]) / abs(b[key])
+        assert _z(a, b, key) < 3.5 or rel < 0.01, (name, key, a[key], b[key])
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_energy_conservation(engine_lib, prec):
+    sim = W.arsenic_implant(n_primaries=2000)
+    e = Engine(precision=prec, seed=3)
+    t = e.run([sim])[0]
+    e.close()
+    total = t["Eel"] + t["Enuc"] + t["Elost"] + t["Eunfollowed"]
+    tol = 1e-12 if prec == "fp64" else 2e-6
+    assert abs(total - sim.E * sim.n_primaries) <= tol * sim.E * sim.n_primaries
+
+
+def test_sharded_runs_reproduce_the_whole(engine_lib):
+    """Primary ranges run separately sum to the unsplit run (integer tallies exactly)."""
+    sim = W.cu_self_ion(n_primaries=1500, E=5e3)
+    e = Engine(precision="fp64", seed=9)
+    whole = e.run([sim])[0]
+    parts = []
+    for first, n in ((0, 700), (700, 800)):
+        s = SimSpec(**{**sim.__dict__, "n_primaries": n, "first_primary": first})
+        parts.append(e.run([s])[0])
+    e.close()
+    for k in ("members", "collisions", "vacancies", "replacements", "interstitials", "range_n"):
+        assert whole[k] == sum(p[k] for p in parts), k
+    assert list(whole["hist_range"]) == list(parts[0]["hist_range"] + parts[1]["hist_range"])
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_overflow_drain_gives_identical_results(engine_lib, prec):
+    """A recoil stack of 4 entries per warp forces spills to the overflow list and
+    drain passes; the integer tallies are unchanged."""
+    sim = W.cu_self_ion(n_primaries=300, E=20e3)
+    e = Engine(precision=prec, seed=4)
+    ref = e.run([sim])[0]
+    e.configure(precision=prec, seed=4, stack_capacity=4)
+    small = e.run([sim])[0]
+    st = e.stats()
+    e.close()
+    assert st["overflowed"] > 0
+    for k in ("members", "collisions", "vacancies", "replacements", "interstitials"):
+        assert ref[k] == small[k], k
+
+
+def test_collision_budget_returns_timeout(engine_lib):
+    """A per-member collision budget that is too small ends the run with an
+    error status (no hang, context stays usable)."""
+    sim = W.cu_self_ion(n_primaries=50, E=20e3)
+    e = Engine(precision="fp64", seed=1, max_collisions=3)
+    with pytest.raises(F.EngineError) as ei:
+        e.run([sim])
+    assert ei.value.status == 5
+    e.configure(precision="fp64", seed=1)
+    t = e.run([sim])[0]
+    e.close()
+    assert t["members"] > 50
+
+
+def test_bad_input_is_rejected(engine_lib):
+    e = Engine(precision="fp64")
+    bad = SimSpec(layers=[LayerSpec(1.0, -1.0, [ElementSpec(29, 63.5, 1.0)])], Z=29, m=63.5, E=1e3, n_primaries=1)
+    with pytest.raises(F.EngineError) as ei:
+        e.run([bad])
+    assert ei.value.status == 1
+    e.close()
+
+
+def test_multi_simulation_run(engine_lib):
+    """Simulation 0 of a batch replays its standalone run exactly; the others are
+    independent and statistically consistent."""
+    a = W.cu_self_ion(n_primaries=400, E=5e3)
+    b = W.boron_implant(n_primaries=400)
+    e = Engine(precision="fp64", seed=2)
+    alone = e.run([a])[0]
+    both = e.run([a, b, b])
+    e.close()
+    for k in ("members", "collisions", "vacancies"):
+        assert both[0][k] == alone[k]
+    s1, s2 = summarize(both[1]), summarize(both[2])
+    assert both[1]["vacancies"] != both[2]["vacancies"]
+    assert _z(s1, s2, "vac_per_ion") < 4.0
