@@ -1,0 +1,322 @@
+#!/usr/bin/env python
+"""Benchmark: primary ions per second, full cascade, on one GB300.
+
+Workload: Ag 200 keV into bulk Si (2.33 g/cm3, Edisp 15 eV, Ebind 3 eV), full
+recoil cascade -- the surrogate workload of the benchmark suite.  One step is
+one batch of fresh primaries through the whole cascade on the fast path
+(FP32, with the learned scattering surrogate when a trained network is present).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Printed JSON line (rank 0):
+  value        primaries/s over the K timed steps, device-timed with CUDA events on
+               the launching stream, inputs resident in HBM, L2 flushed (256 MiB
+               write) before every timed step
+  e2e          the same metric through the public call (host structs in, host
+               totals out, uploads and read-back inside the timed region)
+  fp64         the plain FP64 exact-scattering path on the same workload, and the
+               relative difference of mean projected range fast vs FP64
+  roofline     the cascade kernel against the FP32 issue rate
+  cpu_baseline the CPU oracle (reference algorithm and RNG) on the host cores
+--impl reference times the reference's CPU implementation of the path (the
+reference library itself where it was built from source, else the oracle port
+pinned bit-identical to it) on every host core.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "primary ions/sec full cascade on 1 GB300: surrogate vs exact FP64, range err <1%"
+UNIT = "primary ions/s"
+WORKLOAD = "Ag 200 keV into bulk Si (2.33 g/cm3, Edisp 15 eV, Ebind 3 eV), full cascade"
+W_COLL = 300 + 91 * 1  # algorithmic ops per collision (one-element target)
+L2_FLUSH_BYTES = 256 << 20
+
+
+def args_parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--batch", type=int, default=1 << 17, help="primaries per step")
+    p.add_argument("--precision", default="auto", choices=["auto", "fp32", "surrogate", "fp64"])
+    p.add_argument("--fp64-batch", type=int, default=8192)
+    p.add_argument("--cpu-per-core", type=int, default=0, help="primaries per core in the CPU sample")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-fp64", action="store_true")
+    return p.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        self.f.flush()
+        rows = [l.split(", ") for l in Path(self.f.name).read_text().splitlines() if l.strip()]
+        rows = [r for r in rows if len(r) >= 9]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.strip() == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_sample(sim, per_core, seed, reference):
+    """Time the CPU oracle on nproc independent processes of `per_core` primaries."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle_io
+    cores = os.cpu_count() or 1
+    s = type(sim)(**{**sim.__dict__, "n_primaries": per_core * cores})
+    t0 = time.time()
+    r = oracle_io.run_parallel(s, seed=seed, philox=False, procs=cores, reference=reference)
+    wall = time.time() - t0
+    return r, wall, cores
+
+
+def have_reference_build():
+    ref = ROOT / "oracle" / "_ref" / "ref_driver"
+    if not ref.exists():
+        return False
+    try:
+        subprocess.run([str(ref)], input="ion 1 1.0 1.0 0\nlayer 1 1\nelement 1 1 1\n", capture_output=True,
+                       timeout=30, check=True)
+        return True
+    except Exception:
+        return False
+
+
+def run_reference(a):
+    """The reference arm: the reference's CPU implementation on all host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle_io
+    from mytrim_gb300 import workloads as W
+    oracle_io.build(None)
+    reference = have_reference_build()
+    per_core = a.cpu_per_core or 48
+    sim = W.silver_into_silicon(n_primaries=1)
+    rates = []
+    cores = os.cpu_count() or 1
+    for i in range(a.warmup + a.steps):
+        r, wall, cores = cpu_sample(sim, per_core, seed=1000 + i, reference=reference)
+        if i >= a.warmup:
+            rates.append(r["primaries"] / wall)
+    value = sum(rates) / len(rates)
+    kind = "reference" if reference else "port"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": 1e3 * per_core * cores / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "primaries_per_step": per_core * cores, "path": "CPU, FP64, mt19937"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                         "sample": f"{per_core} primaries per core x {cores} independent processes per step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def dist_setup(a):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        return dist, world, rank, local
+    return None, 1, 0, local
+
+
+def main():
+    a = args_parse()
+    if a.impl == "reference":
+        run_reference(a)
+        return
+    import torch
+    from mytrim_gb300 import build
+    build.build()
+    from mytrim_gb300 import Engine, summarize
+    from mytrim_gb300 import workloads as W
+
+    dist, world, rank, local = dist_setup(a)
+    torch.cuda.set_device(local)
+    prec = a.precision
+    if prec == "auto":
+        prec = "fp32"
+    eng = Engine(device=local, precision=prec, seed=20261203)
+    stream = torch.cuda.Stream(device=local)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def sim_for(step):
+        s = W.silver_into_silicon(n_primaries=a.batch)
+        s.first_primary = (step * world + rank) * a.batch
+        return s
+
+    # warm-up steps (untimed)
+    for i in range(a.warmup):
+        eng.prepare([sim_for(i)])
+        eng.launch(stream.cuda_stream)
+        eng.collect()
+
+    # timed steps: inputs resident, L2 flushed before each step, CUDA events on the
+    # launching stream
+    times, colls, launches, kernel_ms = [], 0, 0, []
+    results = []
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for k in range(a.steps):
+            eng.prepare([sim_for(a.warmup + k)])
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            eng.launch(stream.cuda_stream)
+            e1.record(stream)
+            r = eng.collect()[0]
+            times.append(e0.elapsed_time(e1) / 1e3)
+            st = eng.stats()
+            kernel_ms.append(st["kernel_ms"])
+            launches += st["launches"]
+            colls += r["collisions"]
+            results.append(r)
+    torch.cuda.synchronize()
+    clocks = clk.summary()
+    total = sum(times)
+    if dist:
+        t = torch.tensor([total], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total = float(t.item())
+        dist.barrier()
+    value = world * a.batch * a.steps / total
+    coll_rate = colls * world / total
+
+    # end to end through the public call: host structs in, host totals out
+    e2e_times = []
+    h2d = d2h = 0
+    for k in range(2):
+        s = sim_for(a.warmup + a.steps + k)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        eng.run([s])
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+        st = eng.stats()
+        h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
+    e2e = a.batch / statistics.mean(e2e_times) * world
+
+    if rank != 0:
+        return
+    agg = {k: sum(r[k] for r in results) for k in ("primaries", "collisions", "vacancies", "Eel", "Enuc",
+                                                    "range_n", "sx", "sxx", "sy", "syy", "sz", "szz",
+                                                    "vac_s2", "eel_s2", "enuc_s2", "coll_s2")}
+    fast = summarize(agg)
+
+    fp64 = None
+    if not a.no_fp64 and prec != "fp64":
+        e64 = Engine(device=local, precision="fp64", seed=20261203)
+        s = W.silver_into_silicon(n_primaries=a.fp64_batch)
+        r64 = summarize(e64.run([s])[0])
+        ms64 = e64.stats()["kernel_ms"]
+        e64.close()
+        d = fast["range_mean"] - r64["range_mean"]
+        err = math.sqrt(fast["range_mean_err"] ** 2 + r64["range_mean_err"] ** 2)
+        fp64 = {"value": a.fp64_batch / (ms64 / 1e3), "unit": UNIT, "primaries": a.fp64_batch,
+                "collisions_per_s": r64["collisions"] / (ms64 / 1e3),
+                "range_mean_A": r64["range_mean"], "fast_range_mean_A": fast["range_mean"],
+                "range_rel_err": d / r64["range_mean"], "range_rel_err_sigma": err / r64["range_mean"],
+                "straggle_rel_err": (fast["straggle"] - r64["straggle"]) / r64["straggle"],
+                "vac_rel_err": (fast["vac_per_ion"] - r64["vac_per_ion"]) / r64["vac_per_ion"],
+                "speedup_fast_over_fp64": value / (a.fp64_batch / (ms64 / 1e3))}
+
+    # roofline of the cascade kernel: algorithmic ops / kernel time against the FP32
+    # issue rate (SMs x 128 lanes x SM clock, one op per lane per cycle)
+    props = torch.cuda.get_device_properties(local)
+    sm_mhz = clocks.get("sm_mhz") or 1920.0
+    peak = props.multi_processor_count * 128 * sm_mhz * 1e6 / 1e12
+    per_launch_coll = colls / a.steps
+    kms = statistics.mean(kernel_ms)
+    achieved = per_launch_coll * W_COLL / (kms / 1e3) / 1e12
+    traffic = None
+    prof = ROOT / "profiles" / "cascade_fp32_agsi.md"
+    if prof.exists():
+        for line in prof.read_text().splitlines():
+            if line.startswith("dram_bytes_per_collision:"):
+                traffic = float(line.split(":")[1]) * per_launch_coll
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": 1e3 * total / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if prec != "fp64" else "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "primaries_per_step": a.batch * world, "path": prec,
+                   "l2": "flushed before each timed step (256 MiB write)", "seeded": True},
+        "collisions_per_s": coll_rate,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "physics": {"vac_per_ion": fast["vac_per_ion"], "range_mean_A": fast["range_mean"],
+                    "straggle_A": fast["straggle"], "lateral_A": fast["lateral"],
+                    "collisions_per_ion": fast["coll_per_ion"]},
+        "fp64": fp64,
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": f"derived: {props.multi_processor_count} SMs x 128 FP32 lanes x "
+                                    f"{sm_mhz:.0f} MHz measured (MEASURED_PEAKS.json has no FP32 figure)",
+                     "work": f"{W_COLL} ops per collision x {per_launch_coll:.4g} collisions per launch",
+                     "kernel_ms": kms},
+    }
+    if not a.no_cpu and world == 1:
+        cores = os.cpu_count() or 1
+        per_core = a.cpu_per_core or 100
+        reference = have_reference_build()
+        r, wall, cores = cpu_sample(W.silver_into_silicon(n_primaries=1), per_core, seed=7, reference=reference)
+        line["cpu_baseline"] = {"value": r["primaries"] / wall, "unit": UNIT, "cores": cores,
+                                "kind": "reference" if reference else "port",
+                                "sample": f"{per_core} primaries per core x {cores} independent processes "
+                                          f"({r['primaries']} primaries, {wall:.1f} s)"}
+    print(json.dumps(line), flush=True)
+    eng.close()
+
+
+if __name__ == "__main__":
+    main()

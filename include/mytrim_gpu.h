@@ -170,6 +170,8 @@ typedef struct
   long long overflowed;    /* members spilled to the overflow list */
   long long collisions;
   size_t device_bytes;     /* device memory held by the context */
+  long long h2d_bytes;     /* host-to-device bytes of the last prepare */
+  long long d2h_bytes;     /* device-to-host bytes of the last collect */
 } mtg_stats;
 
 typedef struct mtg_ctx mtg_ctx;

@@ -47,7 +47,9 @@ def lib_path():
 def _compile(unit, flags, nvcc, verbose):
     src = CSRC / unit
     obj = OBJ_DIR / (unit + ".o")
-    cmd = [nvcc, *ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
+    # host code: no FMA contraction, so the tables built on the host are the same bits
+    # on x86 and on Arm (where g++ contracts a*b+c by default) and in the host replay
+    cmd = [nvcc, *ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
            f"-I{INCLUDE}", f"-I{CSRC}", *flags, "-c", str(src), "-o", str(obj)]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")

@@ -299,6 +299,13 @@ launch_reduction(mtg_ctx * ctx)
   return MTG_OK;
 }
 
+cudaError_t
+h2d(mtg_ctx * ctx, void * dst, const void * src, size_t bytes)
+{
+  ctx->stats.h2d_bytes += (long long)bytes;
+  return cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+}
+
 mtg_status
 require_device(mtg_ctx * ctx)
 {
@@ -416,6 +423,7 @@ mtg_prepare(mtg_ctx * ctx, const mtg_sim * sims, int n_sims)
   mtg_status st = require_device(ctx);
   if (st != MTG_OK)
     return st;
+  ctx->stats.h2d_bytes = 0;
   if (!ctx->have_tables)
     return fail(ctx, MTG_ERR_STATE, "stopping tables not loaded");
   std::string err;
@@ -441,11 +449,10 @@ mtg_prepare(mtg_ctx * ctx, const mtg_sim * sims, int n_sims)
   CK(ensure(ctx->d_hist, 8 * size_t(std::max<long long>(t.hist_total, 1))));
   CK(ensure(ctx->d_err, 16));
   CK(ensure(ctx->d_counters, 8 * C_COUNT));
-  CK(cudaMemcpy(ctx->d_sims.p, t.sims.data(), sizeof(SimDesc) * ns, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(ctx->d_prim_end.p, t.prim_end.data(), sizeof(long long) * ns, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(ctx->d_species.p, t.species.data(), sizeof(SpeciesConst) * t.species.size(),
-                cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(ctx->d_mats.p, t.mats.data(), sizeof(MatConst) * t.mats.size(), cudaMemcpyHostToDevice));
+  CK(h2d(ctx, ctx->d_sims.p, t.sims.data(), sizeof(SimDesc) * ns));
+  CK(h2d(ctx, ctx->d_prim_end.p, t.prim_end.data(), sizeof(long long) * ns));
+  CK(h2d(ctx, ctx->d_species.p, t.species.data(), sizeof(SpeciesConst) * t.species.size()));
+  CK(h2d(ctx, ctx->d_mats.p, t.mats.data(), sizeof(MatConst) * t.mats.size()));
 
   // reduction jobs: contiguous chunks of at most 65536 primaries per simulation
   ctx->jobs.clear();
@@ -463,9 +470,8 @@ mtg_prepare(mtg_ctx * ctx, const mtg_sim * sims, int n_sims)
   CK(ensure(ctx->d_partials, sizeof(double) * NQ * std::max<size_t>(ctx->jobs.size(), 1)));
   CK(ensure(ctx->d_out, sizeof(double) * NQ * ns));
   if (!ctx->jobs.empty())
-    CK(cudaMemcpy(ctx->d_jobs.p, ctx->jobs.data(), sizeof(ReduceJob) * ctx->jobs.size(), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(ctx->d_job_first.p, ctx->job_first.data(), sizeof(int) * ctx->job_first.size(),
-                cudaMemcpyHostToDevice));
+    CK(h2d(ctx, ctx->d_jobs.p, ctx->jobs.data(), sizeof(ReduceJob) * ctx->jobs.size()));
+  CK(h2d(ctx, ctx->d_job_first.p, ctx->job_first.data(), sizeof(int) * ctx->job_first.size()));
 
   if (ctx->cfg.precision != MTG_PREC_FP64)
   {
@@ -477,8 +483,7 @@ mtg_prepare(mtg_ctx * ctx, const mtg_sim * sims, int n_sims)
           row_species[t.sims[s].mat_base + sp * t.sims[s].n_mat + k] = t.sims[s].species_base + sp;
     CK(ensure(ctx->d_row_species, sizeof(int) * row_species.size()));
     CK(ensure(ctx->d_stop, sizeof(float) * STOP_N * t.mats.size()));
-    CK(cudaMemcpy(ctx->d_row_species.p, row_species.data(), sizeof(int) * row_species.size(),
-                  cudaMemcpyHostToDevice));
+    CK(h2d(ctx, ctx->d_row_species.p, row_species.data(), sizeof(int) * row_species.size()));
     const double lo = std::log(STOP_EMIN), hi = std::log(t.emax * 1.05);
     CK(launch_build_stop_tables(ptr<SpeciesConst>(ctx->d_species), ptr<MatConst>(ctx->d_mats), nullptr, 0,
                                 int(t.mats.size()), ptr<int>(ctx->d_row_species), ptr<float>(ctx->d_stop), lo,
@@ -491,9 +496,9 @@ mtg_prepare(mtg_ctx * ctx, const mtg_sim * sims, int n_sims)
     CK(ensure(ctx->d_species32, sizeof(Species32) * sp32.size()));
     CK(ensure(ctx->d_mats32, sizeof(Mat32) * mc32.size()));
     CK(ensure(ctx->d_sims32, sizeof(Sim32) * sm32.size()));
-    CK(cudaMemcpy(ctx->d_species32.p, sp32.data(), sizeof(Species32) * sp32.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(ctx->d_mats32.p, mc32.data(), sizeof(Mat32) * mc32.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(ctx->d_sims32.p, sm32.data(), sizeof(Sim32) * sm32.size(), cudaMemcpyHostToDevice));
+    CK(h2d(ctx, ctx->d_species32.p, sp32.data(), sizeof(Species32) * sp32.size()));
+    CK(h2d(ctx, ctx->d_mats32.p, mc32.data(), sizeof(Mat32) * mc32.size()));
+    CK(h2d(ctx, ctx->d_sims32.p, sm32.data(), sizeof(Sim32) * sm32.size()));
   }
   if (ctx->record_cap > 0)
     CK(ensure(ctx->d_records, sizeof(MemberRecord) * size_t(ctx->record_cap)));
@@ -555,6 +560,8 @@ mtg_collect(mtg_ctx * ctx, mtg_totals * totals, long long * hist)
   CK(cudaStreamSynchronize(ctx->stream));
   const HostTables & t = ctx->tables;
   unsigned long long cnt[C_COUNT];
+  ctx->stats.d2h_bytes = sizeof cnt + sizeof(unsigned int) + (long long)(sizeof(double) * NQ + sizeof(SimTotals)) *
+                         (long long)t.sims.size() + (hist ? 8LL * t.hist_total : 0LL);
   CK(cudaMemcpy(cnt, ctx->d_counters.p, sizeof cnt, cudaMemcpyDeviceToHost));
   // further drain passes while the last pass spilled members
   long long overflowed = (long long)cnt[C_OVF0];

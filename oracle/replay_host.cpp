@@ -84,6 +84,47 @@ main(int argc, char ** argv)
     fprintf(stderr, "replay_host: %s\n", err.c_str());
     return 2;
   }
+  if (argc >= 3 && std::string(argv[2]) == "--stopping")
+  {
+    // line 1: Z1 m1 rho n Z m t [Z m t ...]; then one energy per line
+    int Z1, n;
+    double m1, rho;
+    std::cin >> Z1 >> m1 >> rho >> n;
+    mtg_material mat;
+    memset(&mat, 0, sizeof mat);
+    mat.rho = rho;
+    mat.n_elements = n;
+    for (int j = 0; j < n && j < MTG_MAX_ELEMENTS; ++j)
+    {
+      std::cin >> mat.elements[j].Z >> mat.elements[j].m >> mat.elements[j].t;
+      mat.elements[j].Edisp = 25.0;
+      mat.elements[j].Elbind = 3.0;
+    }
+    SpeciesConst sc = make_species(rows, Z1, m1);
+    MatConst mc;
+    if (make_material(rows, sc, mat, 0.2, mc, err) != MTG_OK)
+    {
+      fprintf(stderr, "replay_host: %s\n", err.c_str());
+      return 2;
+    }
+    double E;
+    while (std::cin >> E)
+      printf("%a\n", material_stop64(sc, mc, E));
+    return 0;
+  }
+  if (argc >= 3 && std::string(argv[2]) == "--scatter")
+  {
+    // lines "eps b" -> s2
+    double eps, b;
+    while (std::cin >> eps >> b)
+    {
+      double s2, ct, st;
+      int it;
+      scatter64(eps, b, s2, ct, st, it);
+      printf("%a\n", s2);
+    }
+    return 0;
+  }
   runspec::Spec spec;
   if (!runspec::parse(std::cin, spec, err))
   {

