@@ -89,7 +89,7 @@ def test_scatter_fp64_bitwise_vs_host_build(gpu_engine):
     rng = np.random.default_rng(3)
     eps = 10 ** rng.uniform(-5, 1.5, 20000)
     b = rng.uniform(0, 1, 20000) ** 0.5 * 40 + 1e-6
-    want = _host(["--scatter"], "\n".join(f"{x!r} {y!r}" for x, y in zip(eps, b)) + "\n")
+    want = _host(["--scatter"], "\n".join(f"{float(x)!r} {float(y)!r}" for x, y in zip(eps, b)) + "\n")
     got = gpu_engine.scatter(eps, b, precision="fp64")
     bad = np.nonzero(got != want)[0]
     assert bad.size == 0, (eps[bad[:5]], b[bad[:5]], got[bad[:5]], want[bad[:5]])
