@@ -42,6 +42,19 @@ WORKLOAD = "Ag 200 keV into bulk Si (2.33 g/cm3, Edisp 15 eV, Ebind 3 eV), full 
 W_COLL = 300 + 91 * 1  # algorithmic ops per collision (one-element target)
 L2_FLUSH_BYTES = 256 << 20
 
+# name -> (description, builder(n_primaries)); builders from mytrim_gb300.workloads
+WORKLOADS = {
+    "ag200k_si": (WORKLOAD, "silver_into_silicon"),
+    "cu100k_cu": ("Cu 100 keV into bulk Cu (8.96 g/cm3), full cascade", "cu_self_ion"),
+    "b10k_sio2_si": ("B 10 keV at 7 deg into 10 nm SiO2 on Si, full cascade", "boron_implant"),
+    "as50k_sio2_si": ("As 50 keV at 7 deg into 10 nm SiO2 on Si, full cascade", "arsenic_implant"),
+}
+
+
+def make_sim(name, n):
+    from mytrim_gb300 import workloads as W
+    return getattr(W, WORKLOADS[name][1])(n_primaries=n)
+
 
 def args_parse():
     p = argparse.ArgumentParser()
@@ -55,6 +68,8 @@ def args_parse():
     p.add_argument("--cpu-per-core", type=int, default=0, help="primaries per core in the CPU sample")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--workload", default="ag200k_si", choices=sorted(WORKLOADS),
+                   help="ag200k_si is the benchmark; the others are for profiling and checks")
     return p.parse_args()
 
 
@@ -187,7 +202,7 @@ def main():
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
 
     def sim_for(step):
-        s = W.silver_into_silicon(n_primaries=a.batch)
+        s = make_sim(a.workload, a.batch)
         s.first_primary = (step * world + rank) * a.batch
         return s
 
@@ -256,7 +271,7 @@ def main():
     fp64 = None
     if not a.no_fp64 and prec != "fp64":
         e64 = Engine(device=local, precision="fp64", seed=20261203)
-        s = W.silver_into_silicon(n_primaries=a.fp64_batch)
+        s = make_sim(a.workload, a.fp64_batch)
         r64 = summarize(e64.run([s])[0])
         ms64 = e64.stats()["kernel_ms"]
         e64.close()
@@ -288,7 +303,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": 1e3 * total / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if prec != "fp64" else "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "primaries_per_step": a.batch * world, "path": prec,
+        "config": {"workload": WORKLOADS[a.workload][0], "primaries_per_step": a.batch * world, "path": prec,
                    "l2": "flushed before each timed step (256 MiB write)", "seeded": True},
         "collisions_per_s": coll_rate,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -309,7 +324,7 @@ def main():
         cores = os.cpu_count() or 1
         per_core = a.cpu_per_core or 100
         reference = have_reference_build()
-        r, wall, cores = cpu_sample(W.silver_into_silicon(n_primaries=1), per_core, seed=7, reference=reference)
+        r, wall, cores = cpu_sample(make_sim(a.workload, 1), per_core, seed=7, reference=reference)
         line["cpu_baseline"] = {"value": r["primaries"] / wall, "unit": UNIT, "cores": cores,
                                 "kind": "reference" if reference else "port",
                                 "sample": f"{per_core} primaries per core x {cores} independent processes "
