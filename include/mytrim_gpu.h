@@ -244,6 +244,32 @@ mtg_status mtg_scatter(mtg_ctx * ctx, const double * eps, const double * b, long
 /* Counters of the last run. */
 mtg_status mtg_get_stats(const mtg_ctx * ctx, mtg_stats * out);
 
+/* Allocation-free reduction of per-primary tallies held in caller-owned device
+ * buffers (n entries each, layout of mtg_get_primaries: vacancies, collisions,
+ * electronic and nuclear energy, stopping point x/y/z, final state) into 15
+ * doubles at device pointer `out`: sum and sum of squares of vacancies, of
+ * collisions, of electronic energy and of nuclear energy; then the number of
+ * primaries that came to rest and the sums and sums of squares of their x, y, z.
+ * The same bits as the totals mtg_collect reports for a single simulation.
+ *
+ * For hosts that cannot let the library call cudaMalloc (for instance because
+ * their own pool allocator owns all device memory): this call allocates nothing.
+ * Its scratch is a fixed 120 KiB array in the library's device memory, so n is
+ * limited to 67,108,864 primaries; larger n fails with MTG_ERR_BAD_INPUT and a
+ * message in errbuf (may be NULL).  It works on the current device and queues its
+ * kernels on `stream` (a cudaStream_t, NULL = default stream) without waiting.
+ * The first call on each device looks up the scratch array's device address,
+ * so make that first call before any stream capture.  All calls on a device
+ * share the scratch array: calls whose kernels could overlap on the GPU race,
+ * so order them (one stream, or synchronise between them).
+ * This entry point has no counterpart in the reference. */
+mtg_status mtg_reduce_primaries_noalloc(const unsigned long long * vacancies,
+                                        const unsigned long long * collisions, const double * eel,
+                                        const double * enuc, const double * x, const double * y,
+                                        const double * z, const int * state, long long n,
+                                        double * out, void * stream, char * errbuf,
+                                        size_t errbuf_len);
+
 #ifdef __cplusplus
 }
 #endif

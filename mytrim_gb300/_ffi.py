@@ -111,6 +111,8 @@ SIGNATURES = {
     "mtg_scatter": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_longlong, C.c_int,
                               C.POINTER(C.c_double)]),
     "mtg_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
+    "mtg_reduce_primaries_noalloc": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, C.c_longlong, _P, _P,
+                                               C.c_char_p, C.c_size_t]),
 }
 
 _lib = None

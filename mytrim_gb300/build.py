@@ -29,6 +29,7 @@ UNITS = [
     ("mtg_surrogate.cu", ["--use_fast_math"]),
     ("mtg_reduce.cu", []),
     ("mtg_api.cu", []),
+    ("mtg_noalloc.cu", []),
     ("mtg_setup.cpp", []),
 ]
 

@@ -1,0 +1,211 @@
+// Allocation-free variant of the per-primary tally reduction.
+//
+// Some programs that embed this engine cannot let it call cudaMalloc: a host code
+// that has already handed all device memory to its own pool allocator (as large
+// multiphysics applications coupling a cascade code often do), or one that forbids
+// libraries to allocate once its time loop runs.  Such a caller keeps the
+// per-primary tallies in device buffers it owns and still needs the run totals.
+// mtg_reduce_primaries_noalloc gives it those totals with no allocation at all:
+// its scratch space (the per-chunk partial sums) is a fixed array in this
+// library's own device memory, NOALLOC_MAX_CHUNKS * NQ doubles (120 KiB), which
+// every GPU that loads the library holds until the process exits.
+//
+// The arithmetic is the one mtg_collect uses (mtg_reduce.cu): chunks of 65536
+// primaries reduced with Neumaier-compensated FP64 sums in a fixed order, then
+// the chunks in index order, so the totals are the same bits as the ones
+// mtg_collect reports for a single simulation.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "mytrim_gpu.h"
+#include "mtg_kernels.h"
+
+namespace
+{
+
+constexpr int NOALLOC_BLOCK = 256;
+constexpr long long NOALLOC_CHUNK = 65536; // primaries per block, as in mtg_collect
+constexpr int NOALLOC_MAX_CHUNKS = 1024;   // at most 67,108,864 primaries per call
+constexpr int NQ = mtg::NQ;
+
+// The scratch array shared by every call on a device.  Each call writes every
+// slot it later reads (one row of NQ partial sums per chunk), so nothing has to
+// be cleared between calls; two calls whose kernels overlap on the GPU would
+// overwrite each other's partial sums, so calls must be ordered (one stream, or
+// synchronised).
+static __device__ __align__(256) double g_noalloc_partials[NOALLOC_MAX_CHUNKS * NQ];
+
+struct Comp
+{
+  double s, c;
+};
+
+__device__ __forceinline__ void
+comp_add(Comp & a, double x)
+{
+  const double t = a.s + x;
+  if (fabs(a.s) >= fabs(x))
+    a.c += (a.s - t) + x;
+  else
+    a.c += (x - t) + a.s;
+  a.s = t;
+}
+
+__device__ __forceinline__ void
+comp_merge(Comp & a, const Comp & b)
+{
+  comp_add(a, b.s);
+  a.c += b.c;
+}
+
+__global__ void __launch_bounds__(NOALLOC_BLOCK)
+noalloc_chunk_kernel(const unsigned long long * vac, const unsigned long long * coll, const double * eel,
+                     const double * enuc, const double * fx, const double * fy, const double * fz,
+                     const int * fstate, long long n, double * partials)
+{
+  const long long begin = (long long)blockIdx.x * NOALLOC_CHUNK;
+  const long long end = begin + NOALLOC_CHUNK < n ? begin + NOALLOC_CHUNK : n;
+  Comp q[NQ];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k)
+    q[k] = Comp{0.0, 0.0};
+  for (long long i = begin + threadIdx.x; i < end; i += NOALLOC_BLOCK)
+  {
+    const double v = double(vac[i]);
+    const double c = double(coll[i]);
+    const double e = eel[i];
+    const double u = enuc[i];
+    comp_add(q[0], v);
+    comp_add(q[1], v * v);
+    comp_add(q[2], c);
+    comp_add(q[3], c * c);
+    comp_add(q[4], e);
+    comp_add(q[5], e * e);
+    comp_add(q[6], u);
+    comp_add(q[7], u * u);
+    const int st = fstate[i];
+    if (st >= 1 && st <= 3)
+    {
+      const double x = fx[i], y = fy[i], z = fz[i];
+      comp_add(q[8], 1.0);
+      comp_add(q[9], x);
+      comp_add(q[10], x * x);
+      comp_add(q[11], y);
+      comp_add(q[12], y * y);
+      comp_add(q[13], z);
+      comp_add(q[14], z * z);
+    }
+  }
+  __shared__ Comp red[NOALLOC_BLOCK];
+  for (int k = 0; k < NQ; ++k)
+  {
+    red[threadIdx.x] = q[k];
+    __syncthreads();
+    for (int w = NOALLOC_BLOCK / 2; w > 0; w >>= 1)
+    {
+      if (threadIdx.x < w)
+        comp_merge(red[threadIdx.x], red[threadIdx.x + w]);
+      __syncthreads();
+    }
+    if (threadIdx.x == 0)
+      partials[(long long)blockIdx.x * NQ + k] = red[0].s + red[0].c;
+    __syncthreads();
+  }
+}
+
+__global__ void
+noalloc_finish_kernel(const double * partials, int nchunks, double * out)
+{
+  const int k = threadIdx.x;
+  if (k >= NQ)
+    return;
+  Comp a{0.0, 0.0};
+  for (int j = 0; j < nchunks; ++j)
+    comp_add(a, partials[(long long)j * NQ + k]);
+  out[k] = a.s + a.c;
+}
+
+constexpr int MAX_DEVICES = 64;
+std::mutex g_setup_mutex;
+double * g_scratch_addr[MAX_DEVICES] = {nullptr};
+
+void
+set_error(char * buf, size_t len, const char * msg)
+{
+  if (buf && len > 0)
+  {
+    std::strncpy(buf, msg, len - 1);
+    buf[len - 1] = '\0';
+  }
+}
+
+} // namespace
+
+extern "C" mtg_status
+mtg_reduce_primaries_noalloc(const unsigned long long * vacancies, const unsigned long long * collisions,
+                             const double * eel, const double * enuc, const double * x, const double * y,
+                             const double * z, const int * state, long long n, double * out, void * stream,
+                             char * errbuf, size_t errbuf_len)
+{
+  if (n < 0 || !out || (n > 0 && (!vacancies || !collisions || !eel || !enuc || !x || !y || !z || !state)))
+  {
+    set_error(errbuf, errbuf_len, "mtg_reduce_primaries_noalloc: null buffer or negative count");
+    return MTG_ERR_BAD_INPUT;
+  }
+  if (n > NOALLOC_CHUNK * NOALLOC_MAX_CHUNKS)
+  {
+    char msg[160];
+    std::snprintf(msg, sizeof msg,
+                  "mtg_reduce_primaries_noalloc: %lld primaries exceed the fixed scratch limit of %lld",
+                  n, NOALLOC_CHUNK * NOALLOC_MAX_CHUNKS);
+    set_error(errbuf, errbuf_len, msg);
+    return MTG_ERR_BAD_INPUT;
+  }
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess)
+  {
+    set_error(errbuf, errbuf_len, cudaGetErrorString(e));
+    return e == cudaErrorNoDevice ? MTG_ERR_NO_DEVICE : MTG_ERR_CUDA;
+  }
+  if (dev < 0 || dev >= MAX_DEVICES)
+  {
+    set_error(errbuf, errbuf_len, "mtg_reduce_primaries_noalloc: device index out of range");
+    return MTG_ERR_BAD_INPUT;
+  }
+  double * scratch = nullptr;
+  {
+    // once per device, with that device current: the device address of the
+    // scratch array (its host-side name is only a stand-in, not an address)
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    if (!g_scratch_addr[dev])
+    {
+      void * p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+      if (e != cudaSuccess || !p)
+      {
+        set_error(errbuf, errbuf_len, e != cudaSuccess ? cudaGetErrorString(e) : "null symbol address");
+        return MTG_ERR_CUDA;
+      }
+      g_scratch_addr[dev] = static_cast<double *>(p);
+    }
+    scratch = g_scratch_addr[dev];
+  }
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const int nchunks = int((n + NOALLOC_CHUNK - 1) / NOALLOC_CHUNK);
+  if (nchunks > 0)
+    noalloc_chunk_kernel<<<nchunks, NOALLOC_BLOCK, 0, st>>>(vacancies, collisions, eel, enuc, x, y, z, state, n,
+                                                            scratch);
+  noalloc_finish_kernel<<<1, 32, 0, st>>>(scratch, nchunks, out);
+  e = cudaGetLastError();
+  if (e != cudaSuccess)
+  {
+    set_error(errbuf, errbuf_len, cudaGetErrorString(e));
+    return MTG_ERR_CUDA;
+  }
+  return MTG_OK;
+}
