@@ -145,11 +145,11 @@ struct LaneSink
   long long gprim;     // global primary index of the current member
   int range_mode;
   // per-primary accumulators
-  unsigned long long a_vac, a_coll;
+  unsigned int a_vac, a_coll;
   Acc a_eel, a_enuc;
-  // per-simulation accumulators
-  unsigned long long n_repl, n_inter, n_subst, n_lost, n_members, n_newton, n_passes, n_fallbacks;
-  double e_lost, e_unf;
+  // per-simulation accumulators (32-bit per lane; flushed long before they can wrap)
+  unsigned int n_repl, n_inter, n_subst, n_lost, n_members, n_newton, n_passes, n_fallbacks;
+  Acc e_lost, e_unf;
   // events of the current collision, aggregated per warp after it
   int vac_bin, repl_bin;
   // current member record
@@ -160,7 +160,8 @@ struct LaneSink
   __device__ void reset_sim()
   {
     n_repl = n_inter = n_subst = n_lost = n_members = n_newton = n_passes = n_fallbacks = 0;
-    e_lost = e_unf = 0.0;
+    e_lost.reset();
+    e_unf.reset();
   }
   __device__ void reset_prim()
   {
@@ -175,16 +176,16 @@ struct LaneSink
     a_eel.add(d);
     m_eel.add(d);
   }
-  __device__ void newton(int n) { n_newton += (unsigned long long)n; }
-  __device__ void passes(int n) { n_passes += (unsigned long long)n; }
+  __device__ void newton(int n) { n_newton += (unsigned int)n; }
+  __device__ void passes(int n) { n_passes += (unsigned int)n; }
   __device__ void fallback() { ++n_fallbacks; }
   __device__ void numeric() { atomicOr(prm->error_flags, ERRB_NUMERIC); }
   __device__ void enuc(Real e) { a_enuc.add(e); }
-  __device__ void unfollowed(Real e) { e_unf += double(e); }
+  __device__ void unfollowed(Real e) { e_unf.add(e); }
   __device__ void lost(Real e)
   {
     ++n_lost;
-    e_lost += double(e);
+    e_lost.add(e);
     m_state = ST_LOST;
   }
 
@@ -196,33 +197,33 @@ struct LaneSink
       // TrimRange::vacancyCreation (apps/src/TrimRange.C:32-47): Kinchin-Pease
       // count of the displaced recoil, each increment truncated like the
       // reference's int accumulator
-      const double Z = double(el.Z2), m = el.m2, Er = double(rec.E);
-      const double Ed = el.Edisp;
-      const double ed = 0.0115 * pow64(Z, -7.0 / 3.0) * Er;
-      const double kd = 0.1337 * pow64(Z, 2.0 / 3.0) / sqrt(m);
-      const double g = 3.4008 * pow64(ed, 1.0 / 6.0) + 0.40244 * pow64(ed, 3.0 / 4.0) + ed;
-      const double Ev = Er / (1.0 + kd * g);
-      unsigned long long add = 0;
+      const Real Z = Real(el.Z2), m = Real(el.m2), Er = Real(rec.E);
+      const Real Ed = Real(el.Edisp);
+      const Real ed = Real(0.0115) * powr(Z, Real(-7.0 / 3.0)) * Er;
+      const Real kd = Real(0.1337) * powr(Z, Real(2.0 / 3.0)) / sqrt(m);
+      const Real g = Real(3.4008) * powr(ed, Real(1.0 / 6.0)) + Real(0.40244) * powr(ed, Real(3.0 / 4.0)) + ed;
+      const Real Ev = Er / (Real(1) + kd * g);
+      unsigned int add = 0;
       if (Ev < Ed)
         add = 0;
-      else if (Ev >= Ed / 0.4)
-        add = (unsigned long long)(Ev * 0.4 / Ed);
+      else if (Ev >= Ed / Real(0.4))
+        add = (unsigned int)(Ev * Real(0.4) / Ed);
       else
         add = 1;
       a_vac += add;
-      m_vac += (unsigned int)add;
+      m_vac += add;
       return;
     }
     ++a_vac;
     ++m_vac;
-    vac_bin = depth_bin(double(rec.x), sim->inv_hist_vac_bin, sim->hist_vac_n);
+    vac_bin = depth_bin(Real(rec.x), inv_vac_bin(), sim->hist_vac_n);
     if (vac_bin >= 0)
       vac_bin += int(sim->hist_vac_base);
   }
-  __device__ void replacement(double x)
+  __device__ void replacement(Real x)
   {
     ++n_repl;
-    repl_bin = depth_bin(x, sim->inv_hist_vac_bin, sim->hist_vac_n);
+    repl_bin = depth_bin(x, inv_vac_bin(), sim->hist_vac_n);
     if (repl_bin >= 0)
       repl_bin += int(sim->hist_vac_base + sim->hist_vac_n);
   }
@@ -241,19 +242,41 @@ struct LaneSink
       prm->prim.fy[gprim] = double(p.y);
       prm->prim.fz[gprim] = double(p.z);
       prm->prim.fstate[gprim] = state;
-      const int b = depth_bin(double(p.x), sim->inv_hist_range_bin, sim->hist_range_n);
+      const int b = depth_bin(Real(p.x), inv_range_bin(), sim->hist_range_n);
       if (b >= 0)
         atomicAdd(prm->hist + sim->hist_range_base + b, 1ull);
     }
   }
 
-  // truncation toward zero like int(x) in the reference (TrimVacCount.C:36-39)
-  static __device__ int depth_bin(double x, double inv_bin, int n)
+  // truncation toward zero like int(x) in the reference (TrimVacCount.C:36-39),
+  // in the engine's own precision
+  static __device__ int depth_bin(Real x, Real inv_bin, int n)
   {
-    const double q = x * inv_bin;
-    if (n <= 0 || !(q > -1.0) || q >= double(n))
+    const Real q = x * inv_bin;
+    if (n <= 0 || !(q > Real(-1)) || q >= Real(n))
       return -1;
     return int(q);
+  }
+  __device__ Real inv_vac_bin() const
+  {
+    if constexpr (sizeof(Real) == sizeof(float))
+      return sim->inv_hist_vac_bin_f;
+    else
+      return sim->inv_hist_vac_bin;
+  }
+  __device__ Real inv_range_bin() const
+  {
+    if constexpr (sizeof(Real) == sizeof(float))
+      return sim->inv_hist_range_bin_f;
+    else
+      return sim->inv_hist_range_bin;
+  }
+  static __device__ Real powr(Real x, Real y)
+  {
+    if constexpr (sizeof(Real) == sizeof(float))
+      return __powf(x, y);
+    else
+      return pow64(x, y);
   }
 
   __device__ void flush_prim()
@@ -261,9 +284,9 @@ struct LaneSink
     if (gprim < 0)
       return;
     if (a_vac)
-      atomicAdd(prm->prim.vac + gprim, a_vac);
+      atomicAdd(prm->prim.vac + gprim, (unsigned long long)a_vac);
     if (a_coll)
-      atomicAdd(prm->prim.coll + gprim, a_coll);
+      atomicAdd(prm->prim.coll + gprim, (unsigned long long)a_coll);
     if (a_eel.nonzero())
       atomicAdd(prm->prim.eel + gprim, a_eel.value());
     if (a_enuc.nonzero())
@@ -275,26 +298,27 @@ struct LaneSink
     if (s < 0)
       return;
     SimTotals * t = prm->totals + s;
+    using ull = unsigned long long;
     if (n_members)
-      atomicAdd(&t->members, n_members);
+      atomicAdd(&t->members, ull(n_members));
     if (n_repl)
-      atomicAdd(&t->replacements, n_repl);
+      atomicAdd(&t->replacements, ull(n_repl));
     if (n_inter)
-      atomicAdd(&t->interstitials, n_inter);
+      atomicAdd(&t->interstitials, ull(n_inter));
     if (n_subst)
-      atomicAdd(&t->substitutionals, n_subst);
+      atomicAdd(&t->substitutionals, ull(n_subst));
     if (n_lost)
-      atomicAdd(&t->lost, n_lost);
+      atomicAdd(&t->lost, ull(n_lost));
     if (n_newton)
-      atomicAdd(&t->newton_iters, n_newton);
+      atomicAdd(&t->newton_iters, ull(n_newton));
     if (n_passes)
-      atomicAdd(&t->rejection_passes, n_passes);
+      atomicAdd(&t->rejection_passes, ull(n_passes));
     if (n_fallbacks)
-      atomicAdd(&t->fallbacks, n_fallbacks);
-    if (e_lost != 0.0)
-      atomicAdd(&t->Elost, e_lost);
-    if (e_unf != 0.0)
-      atomicAdd(&t->Eunfollowed, e_unf);
+      atomicAdd(&t->fallbacks, ull(n_fallbacks));
+    if (e_lost.nonzero())
+      atomicAdd(&t->Elost, e_lost.value());
+    if (e_unf.nonzero())
+      atomicAdd(&t->Eunfollowed, e_unf.value());
     reset_sim();
   }
 };
@@ -314,7 +338,7 @@ warp_hist_add(unsigned long long * hist, int bin)
 }
 
 template <class Pol>
-__global__ void
+__global__ void __launch_bounds__(128, Pol::MIN_BLOCKS)
 cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
 {
   using Particle = typename Pol::Particle;
@@ -342,7 +366,7 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
   bool live = false;
   Particle p;
   uint32_t ic = 0;
-  double r1 = 0.0;
+  typename Pol::Real r1 = 0;
   int cur_sim = -1;
   const SimDesc * sim = nullptr;
   typename Pol::MemberCtx mctx;
@@ -375,6 +399,8 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
     {
       sink.flush_prim();
       sink.gprim = (long long)p.prim;
+      if (sink.n_newton > 0x40000000u || sink.n_passes > 0x40000000u)
+        sink.flush_sim(cur_sim);
     }
     Pol::begin_member(mctx, prm, tab, *sim, p);
     r1 = Pol::first_draw(p.key, prm.k0, prm.k1);

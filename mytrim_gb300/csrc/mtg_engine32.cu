@@ -21,6 +21,10 @@
 #include "mtg_kernels.h"
 #include "mtg_surrogate.cuh"
 
+#ifndef MTG_FP32_MIN_BLOCKS
+#define MTG_FP32_MIN_BLOCKS 6
+#endif
+
 namespace mtg
 {
 
@@ -134,6 +138,8 @@ struct Fp32Policy
   using Real = float;
   using Acc = AccKahan32;
   using Tables = Tables32;
+  // resident 128-thread blocks per SM the register budget is cut for
+  static constexpr int MIN_BLOCKS = MTG_FP32_MIN_BLOCKS;
 
   struct MemberCtx
   {
@@ -189,10 +195,10 @@ struct Fp32Policy
     m.net = t.net;
   }
 
-  static __device__ __forceinline__ double first_draw(uint64_t key, uint32_t k0, uint32_t k1)
+  static __device__ __forceinline__ float first_draw(uint64_t key, uint32_t k0, uint32_t k1)
   {
     const U4 d = draw_block(key, 0u, 0u, k0, k1);
-    return double(u24f(d.x));
+    return u24f(d.x);
   }
 
   static __device__ __forceinline__ P32 make_primary(const SimDesc & s, int si, long long g)
@@ -215,7 +221,7 @@ struct Fp32Policy
   }
 
   template <class Sink>
-  static __device__ __forceinline__ int collide(P32 & p, uint32_t ic, double r1d, const MemberCtx & m, uint32_t k0,
+  static __device__ __forceinline__ int collide(P32 & p, uint32_t ic, float r1, const MemberCtx & m, uint32_t k0,
                                                 uint32_t k1, P32 & rec, Sink & sink)
   {
     const Sim32 & sim = *m.sim;
@@ -241,7 +247,7 @@ struct Fp32Policy
     const float pmax = mc.a / (eeg + sqrtf(eeg) + 0.125f * __expf(0.1f * __logf(eeg)));
     float ls = mc.inv_pi_arho / (pmax * pmax);
     if (ic == 1)
-      ls = float(r1d) * fminf(ls, sim.cw);
+      ls = r1 * fminf(ls, sim.cw);
 
     // impact parameter, target atom and azimuth: one Philox block per collision
     const U4 dr = draw_block(p.key, ic, 0u, k0, k1);
@@ -373,7 +379,7 @@ struct Fp32Policy
         sink.vacancy(rec, el);
       else
       {
-        sink.replacement(double(rec.x));
+        sink.replacement(rec.x);
         state = (m.sc->Z1 == el.Z2) ? ST_REPLACEMENT : ST_SUBSTITUTIONAL;
       }
     }

@@ -14,6 +14,7 @@ struct Fp64Policy
   using Particle = P64;
   using Real = double;
   using Acc = AccF64;
+  static constexpr int MIN_BLOCKS = 3; // <= 170 registers: 12 warps per SM
 
   struct Tables
   {

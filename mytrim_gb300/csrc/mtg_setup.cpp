@@ -390,6 +390,8 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
     d.hist_vac_base = hist + s.hist_range_n;
     d.inv_hist_range_bin = s.hist_range_n > 0 ? 1.0 / s.hist_range_bin : 0.0;
     d.inv_hist_vac_bin = s.hist_vac_n > 0 ? 1.0 / s.hist_vac_bin : 0.0;
+    d.inv_hist_range_bin_f = float(d.inv_hist_range_bin);
+    d.inv_hist_vac_bin_f = float(d.inv_hist_vac_bin);
     hist += s.hist_range_n + 2LL * s.hist_vac_n;
     prim += s.n_primaries;
     out.prim_end.push_back(prim);

@@ -109,6 +109,7 @@ struct SimDesc
   int hist_range_n, hist_vac_n;
   long long hist_range_base, hist_vac_base;
   double inv_hist_range_bin, inv_hist_vac_bin;
+  float inv_hist_range_bin_f, inv_hist_vac_bin_f; // single-precision copies (FP32 engine)
 };
 
 // Totals per simulation (device accumulators, reduced on the host).
