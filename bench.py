@@ -197,7 +197,12 @@ def main():
     prec = a.precision
     if prec == "auto":
         prec = "fp32"
-    eng = Engine(device=local, precision=prec, seed=20261203)
+    eng = Engine(device=local, precision="fp32" if prec == "surrogate" else prec, seed=20261203)
+    if prec == "surrogate":
+        import numpy as np
+        from mytrim_gb300.train_surrogate import PARAMS
+        eng.set_surrogate_params(np.load(PARAMS))
+        eng.configure(precision="surrogate", seed=20261203)
     stream = torch.cuda.Stream(device=local)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
 

@@ -244,6 +244,50 @@ mtg_status mtg_scatter(mtg_ctx * ctx, const double * eps, const double * b, long
 /* Counters of the last run. */
 mtg_status mtg_get_stats(const mtg_ctx * ctx, mtg_stats * out);
 
+/* ---- learned scattering surrogate (MTG_PREC_FP32_SURROGATE) ----
+ * An MLP 2 -> 64 -> 64 -> 64 -> 2 (SiLU) from (log10 reduced energy, reduced impact
+ * parameter) to sin^2(theta/2) and the reduced time integral, trained on FP64
+ * quadrature of the universal-potential scattering integral.  No counterpart in the
+ * reference, which evaluates the magic formula (trim.C:235-271) every collision; the
+ * exact path stays the fallback outside log10(eps) in [-4, 4], b in [0, 12]. */
+#define MTG_SURROGATE_NPARAM 8642
+
+typedef struct
+{
+  long long n_train;       /* quadrature samples generated on the GPU (e.g. 2e7) */
+  int batch;               /* mini-batch size */
+  int epochs;              /* passes over the samples */
+  int qat_epochs;          /* last epochs with BF16-rounded hidden layers in the forward pass */
+  float lr;                /* Adam learning rate (cosine decay to 2 %) */
+  unsigned long long seed;
+  float w_tau;             /* loss weight of the time-integral output */
+} mtg_surrogate_config;
+
+typedef struct
+{
+  double final_loss;       /* mean loss of the last mini-batch */
+  double train_seconds;    /* device time of data generation + training */
+  long long steps;
+} mtg_surrogate_report;
+
+/* Train the network on the GPU with the project's own kernels; the context keeps it. */
+mtg_status mtg_surrogate_train(mtg_ctx * ctx, const mtg_surrogate_config * cfg, mtg_surrogate_report * rep);
+
+/* Flat FP32 parameter vector (MTG_SURROGATE_NPARAM floats: W1[64][2] b1 W2[64][64] b2
+ * W3[64][64] b3 W4[2][64] b4) of the context's network, or load one into it. */
+mtg_status mtg_surrogate_get_params(mtg_ctx * ctx, float * params, long long n);
+mtg_status mtg_surrogate_set_params(mtg_ctx * ctx, const float * params, long long n);
+
+/* Loss and gradient of the training loss for a batch (x: n x 2 normalised inputs, y:
+ * n x 2 targets) at `params`, computed by the training kernels (gradient check). */
+mtg_status mtg_surrogate_gradients(mtg_ctx * ctx, const float * params, const float * x, const float * y,
+                                   long long n, float w_tau, float * loss, float * grads);
+
+/* FP64 Gauss-Mehler quadrature of the scattering integral (the training target):
+ * s2 = sin^2(theta/2) and the reduced time integral (tau may be NULL). */
+mtg_status mtg_surrogate_quadrature(mtg_ctx * ctx, const double * eps, const double * b, long long n,
+                                    double * s2, double * tau);
+
 /* Allocation-free reduction of per-primary tallies held in caller-owned device
  * buffers (n entries each, layout of mtg_get_primaries: vacancies, collisions,
  * electronic and nuclear energy, stopping point x/y/z, final state) into 15

@@ -80,6 +80,18 @@ class MemberRecord(C.Structure):
                 ("x", C.c_double), ("y", C.c_double), ("z", C.c_double), ("eel", C.c_double)]
 
 
+class SurrogateConfig(C.Structure):
+    _fields_ = [("n_train", C.c_longlong), ("batch", C.c_int), ("epochs", C.c_int), ("qat_epochs", C.c_int),
+                ("lr", C.c_float), ("seed", C.c_ulonglong), ("w_tau", C.c_float)]
+
+
+class SurrogateReport(C.Structure):
+    _fields_ = [("final_loss", C.c_double), ("train_seconds", C.c_double), ("steps", C.c_longlong)]
+
+
+SURROGATE_NPARAM = 8642
+
+
 class Stats(C.Structure):
     _fields_ = [("kernel_ms", C.c_double), ("reduce_ms", C.c_double), ("launches", C.c_int),
                 ("drains", C.c_int), ("grid", C.c_int), ("block", C.c_int), ("stack_capacity", C.c_int),
@@ -111,6 +123,13 @@ SIGNATURES = {
     "mtg_scatter": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_longlong, C.c_int,
                               C.POINTER(C.c_double)]),
     "mtg_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
+    "mtg_surrogate_train": (C.c_int, [_P, C.POINTER(SurrogateConfig), C.POINTER(SurrogateReport)]),
+    "mtg_surrogate_get_params": (C.c_int, [_P, C.POINTER(C.c_float), C.c_longlong]),
+    "mtg_surrogate_set_params": (C.c_int, [_P, C.POINTER(C.c_float), C.c_longlong]),
+    "mtg_surrogate_gradients": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                          C.c_longlong, C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "mtg_surrogate_quadrature": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_longlong,
+                                           C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "mtg_reduce_primaries_noalloc": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, C.c_longlong, _P, _P,
                                                C.c_char_p, C.c_size_t]),
 }

@@ -78,6 +78,8 @@ struct mtg_ctx
   // device buffers
   DevBuf d_sims, d_prim_end, d_species, d_mats, d_row_species, d_stop;
   DevBuf d_species32, d_mats32, d_sims32;
+  DevBuf d_sg_params, d_sg_net; // surrogate network
+  bool sg_ready = false;
   DevBuf p_vac, p_coll, p_eel, p_enuc, p_fx, p_fy, p_fz, p_state;
   DevBuf d_totals, d_hist, d_err, d_counters, d_stacks, d_ovf0, d_ovf1, d_records;
   DevBuf d_jobs, d_job_first, d_partials, d_out;
@@ -153,12 +155,16 @@ setup_launch_shape(mtg_ctx * ctx)
     else
       tab = sizeof(Species32) * t.species.size() + sizeof(Mat32) * t.mats.size() +
             sizeof(float) * STOP_N * t.mats.size();
+    if (prec == MTG_PREC_FP32_SURROGATE)
+      tab += surrogate_net_bytes();
     if (tab <= 160 * 1024)
       ctx->stage = 1;
     else
       tab = 0;
   }
   ctx->smem = ctx->stage ? tab : 0;
+  if (!ctx->stage && prec == MTG_PREC_FP32_SURROGATE)
+    ctx->smem = surrogate_net_bytes();
   int bps = 0;
   cudaError_t e = prec == MTG_PREC_FP64 ? occupancy64(ctx->block, ctx->smem, &bps)
                                         : occupancy32(ctx->block, ctx->smem, &bps, prec == MTG_PREC_FP32_SURROGATE);
@@ -265,7 +271,7 @@ launch_pass(mtg_ctx * ctx, int pass)
     ft.stop = ptr<float>(ctx->d_stop);
     ft.lnE_min = float(std::log(STOP_EMIN));
     ft.inv_dlnE = float(1.0 / ((std::log(ctx->tables.emax * 1.05) - std::log(STOP_EMIN)) / (STOP_N - 1)));
-    ft.mlp = nullptr;
+    ft.mlp = ctx->sg_ready ? ctx->d_sg_net.p : nullptr;
     ft.sims32 = ctx->d_sims32.p;
     e = launch_cascade32(prm, ft, ctx->grid, ctx->block, ctx->smem, ctx->stream,
                          prec == MTG_PREC_FP32_SURROGATE);
@@ -359,7 +365,7 @@ mtg_destroy(mtg_ctx * ctx)
                      &ctx->d_hist,   &ctx->d_err,      &ctx->d_counters, &ctx->d_stacks, &ctx->d_ovf0,
                      &ctx->d_ovf1,   &ctx->d_records,  &ctx->d_jobs,    &ctx->d_job_first, &ctx->d_partials,
                      &ctx->d_out,    &ctx->d_tmp0,     &ctx->d_tmp1,    &ctx->d_tmp2,    &ctx->d_tmp3,
-                     &ctx->d_species32, &ctx->d_mats32, &ctx->d_sims32};
+                     &ctx->d_species32, &ctx->d_mats32, &ctx->d_sims32, &ctx->d_sg_params, &ctx->d_sg_net};
   for (DevBuf * b : bufs)
     if (b->p)
       cudaFree(b->p);
@@ -426,6 +432,8 @@ mtg_prepare(mtg_ctx * ctx, const mtg_sim * sims, int n_sims)
   ctx->stats.h2d_bytes = 0;
   if (!ctx->have_tables)
     return fail(ctx, MTG_ERR_STATE, "stopping tables not loaded");
+  if (ctx->cfg.precision == MTG_PREC_FP32_SURROGATE && !ctx->sg_ready)
+    return fail(ctx, MTG_ERR_STATE, "no trained surrogate: call mtg_surrogate_train or mtg_surrogate_set_params");
   std::string err;
   int rc = build_tables(ctx->rows, ctx->cfg, sims, n_sims, ctx->tables, err);
   if (rc != MTG_OK)
@@ -820,8 +828,112 @@ mtg_scatter(mtg_ctx * ctx, const double * eps, const double * b, long long n, in
     CK(launch_scatter32(ptr<double>(ctx->d_tmp1), ptr<double>(ctx->d_tmp2), n, ptr<double>(ctx->d_tmp3), nullptr,
                         0, nullptr));
   else
-    return fail(ctx, MTG_ERR_STATE, "no trained surrogate loaded");
+  {
+    if (!ctx->sg_ready)
+      return fail(ctx, MTG_ERR_STATE, "no trained surrogate loaded");
+    CK(launch_surrogate_eval(ctx->d_sg_net.p, ptr<double>(ctx->d_tmp1), ptr<double>(ctx->d_tmp2), n,
+                             ptr<double>(ctx->d_tmp3), nullptr));
+  }
   CK(cudaMemcpy(s2, ctx->d_tmp3.p, 8 * n, cudaMemcpyDeviceToHost));
+  return MTG_OK;
+}
+
+mtg_status
+mtg_surrogate_train(mtg_ctx * ctx, const mtg_surrogate_config * cfg, mtg_surrogate_report * rep)
+{
+  mtg_status st = require_device(ctx);
+  if (st != MTG_OK)
+    return st;
+  if (!cfg || cfg->n_train < 1024 || cfg->batch < 32 || cfg->batch > cfg->n_train || cfg->epochs < 1 ||
+      cfg->qat_epochs < 0 || cfg->qat_epochs > cfg->epochs || !(cfg->lr > 0.0f))
+    return fail(ctx, MTG_ERR_BAD_INPUT, "bad surrogate training configuration");
+  CK(ensure(ctx->d_sg_params, 4 * MTG_SURROGATE_NPARAM));
+  CK(ensure(ctx->d_sg_net, surrogate_net_bytes()));
+  double loss = 0.0, secs = 0.0;
+  CK(surrogate_train(cfg->n_train, cfg->batch, cfg->epochs, cfg->qat_epochs, cfg->lr, cfg->seed, cfg->w_tau,
+                     ptr<float>(ctx->d_sg_params), ctx->d_sg_net.p, &loss, &secs));
+  ctx->sg_ready = true;
+  if (rep)
+  {
+    rep->final_loss = loss;
+    rep->train_seconds = secs;
+    rep->steps = (long long)cfg->epochs * std::max<long long>(1, cfg->n_train / cfg->batch);
+  }
+  return MTG_OK;
+}
+
+mtg_status
+mtg_surrogate_get_params(mtg_ctx * ctx, float * params, long long n)
+{
+  mtg_status st = require_device(ctx);
+  if (st != MTG_OK)
+    return st;
+  if (!params || n != MTG_SURROGATE_NPARAM)
+    return fail(ctx, MTG_ERR_BAD_INPUT, "parameter vector must hold MTG_SURROGATE_NPARAM floats");
+  if (!ctx->sg_ready)
+    return fail(ctx, MTG_ERR_STATE, "no trained surrogate");
+  CK(cudaMemcpy(params, ctx->d_sg_params.p, 4 * n, cudaMemcpyDeviceToHost));
+  return MTG_OK;
+}
+
+mtg_status
+mtg_surrogate_set_params(mtg_ctx * ctx, const float * params, long long n)
+{
+  mtg_status st = require_device(ctx);
+  if (st != MTG_OK)
+    return st;
+  if (!params || n != MTG_SURROGATE_NPARAM)
+    return fail(ctx, MTG_ERR_BAD_INPUT, "parameter vector must hold MTG_SURROGATE_NPARAM floats");
+  for (long long i = 0; i < n; ++i)
+    if (!std::isfinite(params[i]))
+      return fail(ctx, MTG_ERR_BAD_INPUT, "non-finite surrogate parameter");
+  CK(ensure(ctx->d_sg_params, 4 * MTG_SURROGATE_NPARAM));
+  CK(ensure(ctx->d_sg_net, surrogate_net_bytes()));
+  CK(cudaMemcpy(ctx->d_sg_params.p, params, 4 * n, cudaMemcpyHostToDevice));
+  CK(launch_pack_net(ptr<float>(ctx->d_sg_params), ctx->d_sg_net.p, nullptr));
+  CK(cudaDeviceSynchronize());
+  ctx->sg_ready = true;
+  return MTG_OK;
+}
+
+mtg_status
+mtg_surrogate_gradients(mtg_ctx * ctx, const float * params, const float * x, const float * y, long long n,
+                        float w_tau, float * loss, float * grads)
+{
+  mtg_status st = require_device(ctx);
+  if (st != MTG_OK)
+    return st;
+  if (!params || !x || !y || !loss || !grads || n < 1 || n > (1 << 22))
+    return fail(ctx, MTG_ERR_BAD_INPUT, "bad gradient request");
+  CK(surrogate_gradients(params, x, y, n, w_tau, loss, grads));
+  return MTG_OK;
+}
+
+mtg_status
+mtg_surrogate_quadrature(mtg_ctx * ctx, const double * eps, const double * b, long long n, double * s2,
+                         double * tau)
+{
+  mtg_status st = require_device(ctx);
+  if (st != MTG_OK)
+    return st;
+  if (n < 0 || (n > 0 && (!eps || !b || !s2)))
+    return fail(ctx, MTG_ERR_BAD_INPUT, "bad quadrature request");
+  if (n == 0)
+    return MTG_OK;
+  for (long long i = 0; i < n; ++i)
+    if (!(eps[i] > 0.0) || !(b[i] >= 0.0))
+      return fail(ctx, MTG_ERR_BAD_INPUT, "quadrature needs eps > 0 and b >= 0");
+  CK(ensure(ctx->d_tmp0, 8 * size_t(n)));
+  CK(ensure(ctx->d_tmp1, 8 * size_t(n)));
+  CK(ensure(ctx->d_tmp2, 8 * size_t(n)));
+  CK(ensure(ctx->d_tmp3, 8 * size_t(n)));
+  CK(cudaMemcpy(ctx->d_tmp0.p, eps, 8 * n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_tmp1.p, b, 8 * n, cudaMemcpyHostToDevice));
+  CK(launch_quadrature(ptr<double>(ctx->d_tmp0), ptr<double>(ctx->d_tmp1), n, ptr<double>(ctx->d_tmp2),
+                       ptr<double>(ctx->d_tmp3), nullptr));
+  CK(cudaMemcpy(s2, ctx->d_tmp2.p, 8 * n, cudaMemcpyDeviceToHost));
+  if (tau)
+    CK(cudaMemcpy(tau, ctx->d_tmp3.p, 8 * n, cudaMemcpyDeviceToHost));
   return MTG_OK;
 }
 

@@ -463,7 +463,12 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
     {
       ++ic;
       ++sink.a_coll;
-      flags = Pol::collide(p, ic, r1, mctx, prm.k0, prm.k1, rec, sink);
+    }
+    // every lane takes part (a policy may evaluate warp-collective code); lanes
+    // without a member do no work and get no flags
+    flags = Pol::collide(live, p, ic, r1, mctx, prm.k0, prm.k1, rec, sink);
+    if (live)
+    {
       if (!(flags & CF_DONE) && ic >= prm.max_collisions)
       {
         atomicOr(prm.error_flags, ERRB_BUDGET);

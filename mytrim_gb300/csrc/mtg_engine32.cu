@@ -19,6 +19,7 @@
 #include "mtg_collide64.cuh"
 #include "mtg_engine.cuh"
 #include "mtg_kernels.h"
+#include "mtg_scatter32.cuh"
 #include "mtg_surrogate.cuh"
 
 #ifndef MTG_FP32_MIN_BLOCKS
@@ -75,62 +76,6 @@ stop_lookup(const float * row, float lnE_min, float inv_d, float E)
   return fmaf(f, b - a, a);
 }
 
-// Universal-potential scattering in FP32.  Returns s2 = sin^2(theta/2) and
-// c2 = cos^2(theta/2).
-__device__ __forceinline__ void
-scatter32(float eps, float b, float & s2, float & c2, int & niter)
-{
-  niter = 0;
-  if (eps > 10.0f)
-  {
-    const float w = 2.0f * eps * b;
-    s2 = 1.0f / (1.0f + (1.0f + b * (1.0f + b)) * (w * w));
-    c2 = 1.0f - s2;
-    return;
-  }
-  // first guess at the distance of closest approach (trim.C:183-190)
-  float r = b;
-  float rr = -2.7f * __logf(eps * b);
-  if (rr >= b)
-  {
-    rr = -2.7f * __logf(eps * rr);
-    if (rr >= b)
-      r = rr;
-  }
-  float d = r - b;
-  const float inv_eps = 1.0f / eps;
-  float v, v1, q;
-  do
-  {
-    r = b + d;
-    const float ex1 = 0.18175f * __expf(-3.1998f * r);
-    const float ex2 = 0.50986f * __expf(-0.94229f * r);
-    const float ex3 = 0.28022f * __expf(-0.4029f * r);
-    const float ex4 = 0.028171f * __expf(-0.20162f * r);
-    const float phi = ex1 + ex2 + ex3 + ex4;
-    const float tk = 3.1998f * ex1 + 0.94229f * ex2 + 0.4029f * ex3 + 0.20162f * ex4;
-    const float ir = 1.0f / r;
-    v = phi * ir;
-    v1 = -(v + tk) * ir;
-    // f(r) = b^2/r + v r/eps - r and f'(r), written in d = r - b
-    const float fr = -d * (2.0f * b + d) * ir + phi * inv_eps;
-    const float br = b * ir;
-    const float fr1 = -br * br - tk * inv_eps - 1.0f;
-    q = fr / fr1;
-    d -= q;
-    ++niter;
-  } while (fabsf(q) > 0.001f * fabsf(b + d) && niter < 100);
-  r = b + d;
-  const float roc = -2.0f * (eps - v) / v1;
-  const float sqe = sqrtf(eps);
-  const float cc = (0.011615f + sqe) / (0.0071222f + sqe);
-  const float aa = 2.0f * eps * (1.0f + (0.99229f / sqe)) * __expf(cc * __logf(b));
-  const float ff = (1.0f / (sqrtf(aa * aa + 1.0f) + aa)) * ((9.3066f + eps) / (14.813f + eps));
-  const float omc = d * (1.0f - aa * ff / (ff + 1.0f)) / (r + roc);
-  s2 = omc * (2.0f - omc);
-  c2 = 1.0f - s2;
-}
-
 template <bool SURROGATE>
 struct Fp32Policy
 {
@@ -138,8 +83,9 @@ struct Fp32Policy
   using Real = float;
   using Acc = AccKahan32;
   using Tables = Tables32;
-  // resident 128-thread blocks per SM the register budget is cut for
-  static constexpr int MIN_BLOCKS = MTG_FP32_MIN_BLOCKS;
+  // resident 128-thread blocks per SM the register budget is cut for (the
+  // surrogate's tensor-core fragments need more registers)
+  static constexpr int MIN_BLOCKS = SURROGATE ? 4 : MTG_FP32_MIN_BLOCKS;
 
   struct MemberCtx
   {
@@ -155,7 +101,18 @@ struct Fp32Policy
   static __device__ Tables stage(const EngineParams & prm, const Tables & g, unsigned char * smem)
   {
     if (!prm.stage_tables)
-      return g;
+    {
+      if constexpr (!SURROGATE)
+        return g;
+      // the network always lives in shared memory
+      Tables t = g;
+      SurrogateNet * s_net = reinterpret_cast<SurrogateNet *>(smem);
+      for (int i = threadIdx.x; i < int(sizeof(SurrogateNet) / 4); i += blockDim.x)
+        reinterpret_cast<float *>(s_net)[i] = reinterpret_cast<const float *>(g.net)[i];
+      __syncthreads();
+      t.net = s_net;
+      return t;
+    }
     Tables t = g;
     unsigned char * q = smem;
     const int ns = prm.n_stage_species, nm = prm.n_stage_mats;
@@ -173,6 +130,13 @@ struct Fp32Policy
       reinterpret_cast<float *>(s_mc)[i] = reinterpret_cast<const float *>(g.mats)[i];
     for (int i = threadIdx.x; i < n3; i += blockDim.x)
       s_st[i] = g.stop[i];
+    if (SURROGATE)
+    {
+      SurrogateNet * s_net = reinterpret_cast<SurrogateNet *>(s_st + n3);
+      for (int i = threadIdx.x; i < int(sizeof(SurrogateNet) / 4); i += blockDim.x)
+        reinterpret_cast<float *>(s_net)[i] = reinterpret_cast<const float *>(g.net)[i];
+      t.net = s_net;
+    }
     __syncthreads();
     t.species = s_sp;
     t.mats = s_mc;
@@ -220,9 +184,19 @@ struct Fp32Policy
     return p;
   }
 
-  template <class Sink>
-  static __device__ __forceinline__ int collide(P32 & p, uint32_t ic, float r1, const MemberCtx & m, uint32_t k0,
-                                                uint32_t k1, P32 & rec, Sink & sink)
+  // what the first half of a collision hands to the scattering and the second half
+  struct PhaseA
+  {
+    const Mat32 * mc;
+    int nn;        // target element
+    float eps, b;  // reduced energy and impact parameter
+    float ls, dee; // flight length and electronic loss
+    uint32_t azimuth;
+  };
+
+  // flight, target atom and electronic loss (trim.C:80-170)
+  static __device__ __forceinline__ PhaseA phase_a(P32 & p, uint32_t ic, float r1, const MemberCtx & m, uint32_t k0,
+                                                   uint32_t k1)
   {
     const Sim32 & sim = *m.sim;
     // material lookup (sample_layers.C:27-43)
@@ -230,7 +204,9 @@ struct Fp32Policy
     while (layer < sim.n_layers - 1 && !(p.x < sim.layer_end[layer]))
       ++layer;
     const int k = sim.layer_mat[layer];
-    const Mat32 & mc = m.mrow[k];
+    PhaseA a;
+    a.mc = m.mrow + k;
+    const Mat32 & mc = *a.mc;
 
     // normalise direction
     {
@@ -248,11 +224,13 @@ struct Fp32Policy
     float ls = mc.inv_pi_arho / (pmax * pmax);
     if (ic == 1)
       ls = r1 * fminf(ls, sim.cw);
+    a.ls = ls;
 
     // impact parameter, target atom and azimuth: one Philox block per collision
     const U4 dr = draw_block(p.key, ic, 0u, k0, k1);
     const float r2 = u24f(dr.x);
     float hh = u24f(dr.y);
+    a.azimuth = dr.z;
     const float pimp = pmax * sqrtf(r2);
     int nn = 0;
     for (; nn < mc.nel - 1; ++nn)
@@ -261,24 +239,56 @@ struct Fp32Policy
       if (hh <= 0.0f)
         break;
     }
-    const Elem32 & el = mc.el[nn];
-    const float eps = el.fi * E;
-    const float b = pimp * el.inv_ai;
+    a.nn = nn;
+    a.eps = mc.el[nn].fi * E;
+    a.b = pimp * mc.el[nn].inv_ai;
 
     // electronic loss from the stopping table (material.C:114-121)
-    float dee = ls * stop_lookup(m.stop + (long long)k * STOP_N, m.lnE_min, m.inv_dlnE, E);
+    a.dee = ls * stop_lookup(m.stop + (long long)k * STOP_N, m.lnE_min, m.inv_dlnE, E);
+    return a;
+  }
 
+  template <class Sink>
+  static __device__ __forceinline__ int collide(bool live, P32 & p, uint32_t ic, float r1, const MemberCtx & m,
+                                                uint32_t k0, uint32_t k1, P32 & rec, Sink & sink)
+  {
+    PhaseA a;
     float s2, c2;
     int niter = 0;
-    if (SURROGATE && surrogate_in_domain(eps, b))
-      surrogate_s2(m.net, eps, b, s2, c2);
+    if constexpr (SURROGATE)
+    {
+      bool nn = false;
+      if (live)
+      {
+        a = phase_a(p, ic, r1, m, k0, k1);
+        nn = surrogate_in_domain(a.eps, a.b);
+      }
+      // every lane of the warp, with or without a member, evaluates the network
+      const float o0 = surrogate_eval_warp(m.net, nn ? surrogate_x1(a.eps) : 0.0f, nn ? surrogate_x2(a.b) : 0.0f);
+      if (!live)
+        return 0;
+      if (nn)
+        surrogate_s2_from(a.eps, a.b, o0, s2, c2);
+      else
+      {
+        sink.fallback();
+        scatter32(a.eps, a.b, s2, c2, niter);
+      }
+    }
     else
     {
-      if (SURROGATE)
-        sink.fallback();
-      scatter32(eps, b, s2, c2, niter);
+      if (!live)
+        return 0;
+      a = phase_a(p, ic, r1, m, k0, k1);
+      scatter32(a.eps, a.b, s2, c2, niter);
     }
     sink.newton(niter);
+    const Sim32 & sim = *m.sim;
+    const Mat32 & mc = *a.mc;
+    const Elem32 & el = mc.el[a.nn];
+    const float E = p.E;
+    const float ls = a.ls;
+    float dee = a.dee;
 
     // energy transfer, electronic loss, momenta (trim.C:275-296)
     float den = el.ec * s2 * E;
@@ -327,7 +337,7 @@ struct Fp32Policy
     const float ux = 1.0f + sgn * p.dx * p.dx * ia, uy = sgn * bxy, uz = -sgn * p.dx;
     const float vx = bxy, vy = sgn + p.dy * p.dy * ia, vz = -p.dy;
     float sphi, cphi;
-    __sincosf(6.283185307179586f * u24f(dr.z), &sphi, &cphi);
+    __sincosf(6.283185307179586f * u24f(a.azimuth), &sphi, &cphi);
     const float px = cphi * ux + sphi * vx;
     const float py = cphi * uy + sphi * vy;
     const float pz = cphi * uz + sphi * vz;
@@ -467,10 +477,7 @@ scatter32_kernel(const double * eps, const double * b, long long n, double * s2,
   const float e = float(eps[i]), bb = float(b[i]);
   float s, c;
   int it;
-  if (surrogate && surrogate_in_domain(e, bb))
-    surrogate_s2(net, e, bb, s, c);
-  else
-    scatter32(e, bb, s, c, it);
+  scatter32(e, bb, s, c, it);
   s2[i] = double(s);
 }
 

@@ -81,9 +81,11 @@ struct Fp64Policy
   }
 
   template <class Sink>
-  static __device__ __forceinline__ int collide(P64 & p, uint32_t ic, double r1, const MemberCtx & m, uint32_t k0,
-                                                uint32_t k1, P64 & rec, Sink & sink)
+  static __device__ __forceinline__ int collide(bool live, P64 & p, uint32_t ic, double r1, const MemberCtx & m,
+                                                uint32_t k0, uint32_t k1, P64 & rec, Sink & sink)
   {
+    if (!live)
+      return 0;
     return collide64(p, ic, r1, *m.sim, *m.sc, m.mrow, k0, k1, rec, sink);
   }
 };

@@ -42,6 +42,19 @@ cudaError_t launch_scatter32(const double * eps, const double * b, long long n, 
 cudaError_t launch_stopping32(const float * row, float lnE_min, float inv_d, const double * E, long long n,
                               double * out, cudaStream_t st);
 
+// Surrogate (mtg_surrogate.cu)
+cudaError_t launch_quadrature(const double * eps, const double * b, long long n, double * s2, double * tau,
+                              cudaStream_t st);
+cudaError_t launch_surrogate_eval(const void * net, const double * eps, const double * b, long long n, double * s2,
+                                  cudaStream_t st);
+cudaError_t launch_pack_net(const float * params, void * net, cudaStream_t st);
+size_t surrogate_net_bytes();
+cudaError_t surrogate_gradients(const float * params_h, const float * x_h, const float * y_h, long long n,
+                                float w_tau, float * loss_h, float * grads_h);
+cudaError_t surrogate_train(long long n_train, int batch, int epochs, int qat_epochs, float lr,
+                            unsigned long long seed, float w_tau, float * params_dev, void * net_dev,
+                            double * final_loss, double * train_seconds);
+
 // Tally reduction (mtg_reduce.cu)
 constexpr int NQ = 15; // reduced quantities per simulation
 struct ReduceJob

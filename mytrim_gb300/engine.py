@@ -269,6 +269,43 @@ class Engine:
         self._check(self.lib.mtg_scatter(self.ctx, pd(e), pd(bb), len(e), prec, pd(out)))
         return out
 
+    # ---- learned scattering surrogate
+    def surrogate_train(self, n_train=20_000_000, batch=16384, epochs=12, qat_epochs=2, lr=2e-3, seed=1,
+                        w_tau=0.1) -> dict:
+        cfg = F.SurrogateConfig(n_train, batch, epochs, qat_epochs, lr, seed, w_tau)
+        rep = F.SurrogateReport()
+        self._check(self.lib.mtg_surrogate_train(self.ctx, C.byref(cfg), C.byref(rep)))
+        return {"final_loss": rep.final_loss, "train_seconds": rep.train_seconds, "steps": rep.steps}
+
+    def surrogate_params(self) -> np.ndarray:
+        out = np.zeros(F.SURROGATE_NPARAM, dtype=np.float32)
+        self._check(self.lib.mtg_surrogate_get_params(self.ctx, out.ctypes.data_as(C.POINTER(C.c_float)), len(out)))
+        return out
+
+    def set_surrogate_params(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        self._check(self.lib.mtg_surrogate_set_params(self.ctx, p.ctypes.data_as(C.POINTER(C.c_float)), len(p)))
+
+    def surrogate_gradients(self, params, x, y, w_tau=0.1):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        xx = np.ascontiguousarray(x, dtype=np.float32)
+        yy = np.ascontiguousarray(y, dtype=np.float32)
+        g = np.zeros(F.SURROGATE_NPARAM, dtype=np.float32)
+        loss = C.c_float(0.0)
+        pf = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        self._check(self.lib.mtg_surrogate_gradients(self.ctx, pf(p), pf(xx), pf(yy), len(xx), w_tau, C.byref(loss),
+                                                     pf(g)))
+        return loss.value, g
+
+    def quadrature(self, eps, b):
+        e = np.ascontiguousarray(eps, dtype=np.float64)
+        bb = np.ascontiguousarray(b, dtype=np.float64)
+        s2 = np.zeros_like(e)
+        tau = np.zeros_like(e)
+        pd = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        self._check(self.lib.mtg_surrogate_quadrature(self.ctx, pd(e), pd(bb), len(e), pd(s2), pd(tau)))
+        return s2, tau
+
     def stats(self) -> dict:
         s = F.Stats()
         self._check(self.lib.mtg_get_stats(self.ctx, C.byref(s)))

@@ -1,0 +1,183 @@
+"""The learned scattering surrogate: training target, training kernels, network,
+and the engine path that uses it (GB300).
+
+* the FP64 Gauss-Mehler quadrature (training target) agrees with an independent
+  adaptive integration of the scattering integral (scipy, CPU) to 1e-7;
+* the magic formula of the exact path (trim.C:235-271) against the quadrature: the
+  gap the surrogate is trained to close, measured;
+* loss and all 8642 gradients of the project's training kernels equal a numpy
+  forward/backward of the same network (float64 on the CPU) to 1e-4;
+* a trained network reproduces the quadrature, and improves on the magic formula;
+* the FP32 engine with the surrogate matches the FP64 exact path statistically.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from mytrim_gb300 import Engine, summarize
+from mytrim_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+PHI_C = np.array([0.18175, 0.50986, 0.28022, 0.028171])
+PHI_D = np.array([3.1998, 0.94229, 0.4029, 0.20162])
+
+
+def phi(r):
+    return np.sum(PHI_C * np.exp(-PHI_D * np.asarray(r)[..., None]), axis=-1)
+
+
+def theta_scipy(eps, b):
+    """theta = pi - 2 b Int_{r0}^inf dr / (r^2 sqrt(1 - Phi(r)/(r eps) - b^2/r^2)), adaptive (CPU)."""
+    from scipy import integrate, optimize
+    f = lambda r: 1.0 - phi(r) / (r * eps) - b * b / (r * r)
+    hi = 0.5 * (1 / eps + math.sqrt(1 / eps ** 2 + 4 * b * b)) * 1.0000001 + 1e-12
+    lo = b if b > 0 else hi * 1e-9
+    r0 = optimize.brentq(f, lo, hi, xtol=1e-15, rtol=1e-15)
+    beta = b / r0
+    # u = r0 / r, then u = sin(w) removes the inverse square-root end point
+    def integrand(w):
+        u = math.sin(w)
+        g2 = 1.0 - phi(r0 / u) * u / (r0 * eps) - beta * beta * u * u
+        return math.cos(w) / math.sqrt(g2) if g2 > 0 else 0.0
+    I, _ = integrate.quad(integrand, 0.0, math.pi / 2, epsabs=1e-13, epsrel=1e-12, limit=400)
+    return math.pi - 2.0 * beta * I
+
+
+def test_quadrature_matches_adaptive_integration(gpu_engine):
+    pytest.importorskip("scipy")
+    pts = [(1e-3, 0.5), (1e-2, 2.0), (0.1, 1.0), (0.5, 0.3), (1.0, 3.0), (5.0, 0.7), (100.0, 0.05), (1e-4, 0.0),
+           (3e-3, 8.0), (2.0, 11.0)]
+    eps = np.array([p[0] for p in pts])
+    b = np.array([p[1] for p in pts])
+    s2, _ = gpu_engine.quadrature(eps, b)
+    for (e, bb), s in zip(pts, s2):
+        th = theta_scipy(e, bb)
+        want = math.sin(th / 2) ** 2
+        assert abs(s - want) <= 1e-7 * max(want, 1e-12) + 1e-14, (e, bb, s, want)
+
+
+def _grid(n=4000, seed=0):
+    rng = np.random.default_rng(seed)
+    eps = 10 ** rng.uniform(-4, 1, n)  # the exact path uses the magic formula for eps <= 10
+    b = 12 * np.sqrt(rng.uniform(0, 1, n))
+    return eps, b
+
+
+def test_magic_formula_gap(gpu_engine):
+    """Measure how far the magic formula is from the true scattering integral."""
+    eps, b = _grid()
+    s2q, _ = gpu_engine.quadrature(eps, b)
+    s2m = gpu_engine.scatter(eps, b, precision="fp64")
+    rel = np.abs(s2m - s2q) / s2q
+    big = s2q > 1e-3
+    # Biersack-Haggmark quote a few percent for the magic formula
+    assert np.median(rel[big]) < 0.02
+    assert np.quantile(rel[big], 0.95) < 0.08
+
+
+def _np_forward_backward(params, x, y, w_tau):
+    """float64 reference of the network, loss and gradients."""
+    p = params.astype(np.float64)
+    o = [0, 128, 192, 4288, 4352, 8448, 8512, 8640]
+    W1 = p[o[0]:o[1]].reshape(64, 2)
+    b1 = p[o[1]:o[2]]
+    W2 = p[o[2]:o[3]].reshape(64, 64)
+    b2 = p[o[3]:o[4]]
+    W3 = p[o[4]:o[5]].reshape(64, 64)
+    b3 = p[o[5]:o[6]]
+    W4 = p[o[6]:o[7]].reshape(2, 64)
+    b4 = p[o[7]:]
+    silu = lambda z: z / (1 + np.exp(-z))
+    dsilu = lambda z: (1 / (1 + np.exp(-z))) * (1 + z * (1 - 1 / (1 + np.exp(-z))))
+    X = x.astype(np.float64)
+    Y = y.astype(np.float64)
+    z1 = X @ W1.T + b1
+    h1 = silu(z1)
+    z2 = h1 @ W2.T + b2
+    h2 = silu(z2)
+    z3 = h2 @ W3.T + b3
+    h3 = silu(z3)
+    out = h3 @ W4.T + b4
+    B = len(X)
+    wc = np.array([1.0, w_tau])
+    loss = np.sum(wc * (out - Y) ** 2) / B
+    dO = 2 * wc * (out - Y) / B
+    gW4 = dO.T @ h3
+    gb4 = dO.sum(0)
+    d3 = (dO @ W4) * dsilu(z3)
+    gW3 = d3.T @ h2
+    gb3 = d3.sum(0)
+    d2 = (d3 @ W3) * dsilu(z2)
+    gW2 = d2.T @ h1
+    gb2 = d2.sum(0)
+    d1 = (d2 @ W2) * dsilu(z1)
+    gW1 = d1.T @ X
+    gb1 = d1.sum(0)
+    g = np.concatenate([gW1.ravel(), gb1, gW2.ravel(), gb2, gW3.ravel(), gb3, gW4.ravel(), gb4])
+    return loss, g
+
+
+def test_training_gradients_match_cpu(gpu_engine):
+    rng = np.random.default_rng(7)
+    params = np.concatenate([rng.normal(0, 0.6, 128), rng.normal(0, 0.1, 64), rng.normal(0, 0.15, 4096),
+                             rng.normal(0, 0.1, 64), rng.normal(0, 0.15, 4096), rng.normal(0, 0.1, 64),
+                             rng.normal(0, 0.2, 128), rng.normal(0, 0.1, 2)]).astype(np.float32)
+    x = rng.uniform(-1, 1, (777, 2)).astype(np.float32)
+    y = rng.normal(0, 0.5, (777, 2)).astype(np.float32)
+    loss, g = gpu_engine.surrogate_gradients(params, x, y, w_tau=0.3)
+    lref, gref = _np_forward_backward(params, x, y, 0.3)
+    assert abs(loss - lref) <= 1e-4 * abs(lref)
+    scale = np.abs(gref).max()
+    err = np.abs(g - gref)
+    assert err.max() <= 1e-4 * scale, (err.max(), scale, int(err.argmax()))
+    # relative agreement of the larger components
+    big = np.abs(gref) > 1e-3 * scale
+    assert np.quantile(err[big] / np.abs(gref[big]), 0.99) < 1e-3
+
+
+@pytest.fixture(scope="module")
+def trained():
+    e = Engine(precision="fp32", seed=3)
+    rep = e.surrogate_train(n_train=2_000_000, batch=8192, epochs=6, qat_epochs=1, lr=3e-3, seed=11)
+    yield e, rep
+    e.close()
+
+
+def test_trained_network_reproduces_the_quadrature(trained):
+    e, rep = trained
+    assert rep["final_loss"] < 1e-3
+    rng = np.random.default_rng(99)
+    eps = 10 ** rng.uniform(-4, 4, 20000)
+    b = 12 * np.sqrt(rng.uniform(0, 1, 20000))
+    s2q, _ = e.quadrature(eps, b)
+    s2n = e.scatter(eps, b, precision="surrogate")
+    big = s2q > 1e-4
+    rel = np.abs(s2n - s2q) / s2q
+    assert np.median(rel[big]) < 0.03, np.median(rel[big])
+    assert np.quantile(rel[big], 0.95) < 0.15, np.quantile(rel[big], 0.95)
+
+
+def test_params_roundtrip(trained):
+    e, _ = trained
+    p = e.surrogate_params()
+    f = Engine(precision="fp32", seed=3)
+    f.set_surrogate_params(p)
+    eps, b = _grid(2000, 5)
+    assert np.array_equal(f.scatter(eps, b, precision="surrogate"), e.scatter(eps, b, precision="surrogate"))
+    f.close()
+
+
+def test_surrogate_engine_matches_fp64(trained):
+    e, _ = trained
+    sim = W.cu_self_ion(n_primaries=2000, E=20e3)
+    e.configure(precision="surrogate", seed=8)
+    g = summarize(e.run([sim])[0])
+    e.configure(precision="fp32", seed=8)
+    f = summarize(e.run([sim])[0])
+    assert g["surrogate_fallbacks"] > 0
+    for key in ("vac_per_ion", "range_mean", "eel_per_ion"):
+        rel = abs(g[key] - f[key]) / abs(f[key])
+        z = abs(g[key] - f[key]) / math.hypot(g[key + "_err"], f[key + "_err"])
+        assert z < 5 or rel < 0.05, (key, g[key], f[key])
