@@ -48,12 +48,28 @@ WORKLOADS = {
     "cu100k_cu": ("Cu 100 keV into bulk Cu (8.96 g/cm3), full cascade", "cu_self_ion"),
     "b10k_sio2_si": ("B 10 keV at 7 deg into 10 nm SiO2 on Si, full cascade", "boron_implant"),
     "as50k_sio2_si": ("As 50 keV at 7 deg into 10 nm SiO2 on Si, full cascade", "arsenic_implant"),
+    "batched4096": ("4096 independent simulations in one launch (Z1 1-83, E0 1 keV-1 MeV log-uniform, 0-60 deg, "
+                    "1-4 layers of Si/Cu/Ag/Au/SiO2/Al2O3 5-500 nm over Si); primaries per simulation "
+                    "log-uniform 1e2-1e5 scaled so that one step holds about the batch size", "batched_uneven"),
 }
 
 
-def make_sim(name, n):
+def make_sims(name, n, first=0):
+    """the simulations of one step: n primaries (the batched workload: about n, over 4096 simulations)"""
     from mytrim_gb300 import workloads as W
-    return getattr(W, WORKLOADS[name][1])(n_primaries=n)
+    if name == "batched4096":
+        sims = W.batched_uneven(n_sims=4096, seed=1, scale_primaries=n / 5.9e7)
+        step = first // max(n, 1)  # fresh primaries of every simulation at each step
+        for s in sims:
+            s.first_primary = step * s.n_primaries
+        return sims
+    s = getattr(W, WORKLOADS[name][1])(n_primaries=n)
+    s.first_primary = first
+    return [s]
+
+
+def make_sim(name, n):
+    return make_sims(name, n)[0]
 
 
 def args_parse():
@@ -206,27 +222,25 @@ def main():
     stream = torch.cuda.Stream(device=local)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
 
-    def sim_for(step):
-        s = make_sim(a.workload, a.batch)
-        s.first_primary = (step * world + rank) * a.batch
-        return s
+    def sims_for(step):
+        return make_sims(a.workload, a.batch, (step * world + rank) * a.batch)
 
     # warm-up steps (untimed)
     for i in range(a.warmup):
-        eng.prepare([sim_for(i)])
+        eng.prepare(sims_for(i))
         eng.launch(stream.cuda_stream)
         eng.collect()
 
     # timed steps: inputs resident, L2 flushed before each step, CUDA events on the
     # launching stream
-    times, colls, launches, kernel_ms = [], 0, 0, []
+    times, colls, launches, kernel_ms, prims = [], 0, 0, [], 0
     results = []
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         for k in range(a.steps):
-            eng.prepare([sim_for(a.warmup + k)])
+            eng.prepare(sims_for(a.warmup + k))
             with torch.cuda.stream(stream):
                 flush.zero_()
             e0 = torch.cuda.Event(enable_timing=True)
@@ -234,12 +248,14 @@ def main():
             e0.record(stream)
             eng.launch(stream.cuda_stream)
             e1.record(stream)
-            r = eng.collect()[0]
+            rr = eng.collect()
+            r = {kk: sum(x[kk] for x in rr) for kk in rr[0] if not kk.startswith("hist") and kk != "status"}
             times.append(e0.elapsed_time(e1) / 1e3)
             st = eng.stats()
             kernel_ms.append(st["kernel_ms"])
             launches += st["launches"]
             colls += r["collisions"]
+            prims += r["primaries"]
             results.append(r)
     torch.cuda.synchronize()
     clocks = clk.summary()
@@ -249,22 +265,24 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total = float(t.item())
         dist.barrier()
-    value = world * a.batch * a.steps / total
+    value = world * prims / total
     coll_rate = colls * world / total
 
     # end to end through the public call: host structs in, host totals out
     e2e_times = []
     h2d = d2h = 0
+    n_step = 0
     for k in range(2):
-        s = sim_for(a.warmup + a.steps + k)
+        ss = sims_for(a.warmup + a.steps + k)
+        n_step = sum(x.n_primaries for x in ss)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        eng.run([s])
+        eng.run(ss)
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t0)
         st = eng.stats()
         h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
-    e2e = a.batch / statistics.mean(e2e_times) * world
+    e2e = n_step / statistics.mean(e2e_times) * world
 
     if rank != 0:
         return
@@ -273,6 +291,41 @@ def main():
                                                     "vac_s2", "eel_s2", "enuc_s2", "coll_s2")}
     fast = summarize(agg)
 
+    def time_path(path, steps, base):
+        """device-timed steps of another path on fresh primaries (same workload)"""
+        e2 = Engine(device=local, precision="fp32", seed=20261203)
+        if path == "surrogate":
+            import numpy as np
+            from mytrim_gb300.train_surrogate import PARAMS
+            e2.set_surrogate_params(np.load(PARAMS))
+        e2.configure(precision=path, seed=20261203)
+        rs, ts = [], []
+        for k in range(steps + 1):
+            e2.prepare(sims_for(base + k))
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            e2.launch(stream.cuda_stream)
+            e1.record(stream)
+            rr = e2.collect()
+            r = {kk: sum(x[kk] for x in rr) for kk in rr[0] if not kk.startswith("hist") and kk != "status"}
+            if k > 0:  # first one is a warm-up
+                rs.append(r)
+                ts.append(e0.elapsed_time(e1) / 1e3)
+        e2.close()
+        agg2 = {kk: sum(r[kk] for r in rs) for kk in agg}
+        agg2["surrogate_fallbacks"] = sum(r["surrogate_fallbacks"] for r in rs)
+        return summarize(agg2), agg2["primaries"] / sum(ts), agg2
+
+    paths = {prec: {"value": value, "unit": UNIT, "collisions_per_s": coll_rate}}
+    if prec != "surrogate" and not a.no_fp64:
+        from mytrim_gb300.train_surrogate import PARAMS
+        if PARAMS.exists():
+            sg, sg_rate, sg_agg = time_path("surrogate", 2, 1000)
+            paths["surrogate"] = {"value": sg_rate, "unit": UNIT, "summary": sg,
+                                  "fallback_fraction": sg_agg["surrogate_fallbacks"] / max(sg_agg["collisions"], 1)}
     fp64 = None
     if not a.no_fp64 and prec != "fp64":
         e64 = Engine(device=local, precision="fp64", seed=20261203)
@@ -280,15 +333,30 @@ def main():
         r64 = summarize(e64.run([s])[0])
         ms64 = e64.stats()["kernel_ms"]
         e64.close()
-        d = fast["range_mean"] - r64["range_mean"]
-        err = math.sqrt(fast["range_mean_err"] ** 2 + r64["range_mean_err"] ** 2)
         fp64 = {"value": a.fp64_batch / (ms64 / 1e3), "unit": UNIT, "primaries": a.fp64_batch,
-                "collisions_per_s": r64["collisions"] / (ms64 / 1e3),
-                "range_mean_A": r64["range_mean"], "fast_range_mean_A": fast["range_mean"],
-                "range_rel_err": d / r64["range_mean"], "range_rel_err_sigma": err / r64["range_mean"],
-                "straggle_rel_err": (fast["straggle"] - r64["straggle"]) / r64["straggle"],
-                "vac_rel_err": (fast["vac_per_ion"] - r64["vac_per_ion"]) / r64["vac_per_ion"],
-                "speedup_fast_over_fp64": value / (a.fp64_batch / (ms64 / 1e3))}
+                "collisions_per_s": r64["collisions"] / (ms64 / 1e3), "range_mean_A": r64["range_mean"],
+                "straggle_A": r64["straggle"], "vac_per_ion": r64["vac_per_ion"]}
+
+        def rel_errors(f):
+            d = f["range_mean"] - r64["range_mean"]
+            return {"range_mean_A": f["range_mean"],
+                    "range_rel_err": d / r64["range_mean"],
+                    "range_rel_err_sigma": math.hypot(f["range_mean_err"], r64["range_mean_err"]) / r64["range_mean"],
+                    "straggle_rel_err": (f["straggle"] - r64["straggle"]) / r64["straggle"],
+                    "straggle_rel_err_sigma": math.hypot(f["straggle_err"], r64["straggle_err"]) / r64["straggle"],
+                    "vac_rel_err": (f["vac_per_ion"] - r64["vac_per_ion"]) / r64["vac_per_ion"],
+                    "vac_rel_err_sigma": math.hypot(f["vac_per_ion_err"], r64["vac_per_ion_err"]) / r64["vac_per_ion"],
+                    "speedup_over_fp64": None}
+
+        paths[prec].update(rel_errors(fast))
+        paths[prec]["speedup_over_fp64"] = value / fp64["value"]
+        if "surrogate" in paths:
+            sgp = paths["surrogate"]
+            sgp.update(rel_errors(sgp.pop("summary")))
+            sgp["speedup_over_fp64"] = sgp["value"] / fp64["value"]
+        paths["fp64"] = fp64
+    for v in paths.values():
+        v.pop("summary", None)
 
     # roofline of the cascade kernel: algorithmic ops / kernel time against the FP32
     # issue rate (SMs x 128 lanes x SM clock, one op per lane per cycle)
@@ -317,7 +385,7 @@ def main():
         "physics": {"vac_per_ion": fast["vac_per_ion"], "range_mean_A": fast["range_mean"],
                     "straggle_A": fast["straggle"], "lateral_A": fast["lateral"],
                     "collisions_per_ion": fast["coll_per_ion"]},
-        "fp64": fp64,
+        "paths": paths,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": f"derived: {props.multi_processor_count} SMs x 128 FP32 lanes x "

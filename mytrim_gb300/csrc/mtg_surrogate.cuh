@@ -72,10 +72,15 @@ lds_f32(const void * p)
   return __uint_as_float(lds_u32(p));
 }
 
+// SiLU for inference: x sigmoid(x) = x (1 + tanh(x/2)) / 2 with the hardware tanh
+// (one special-function operation instead of an exponential and a reciprocal)
 __device__ __forceinline__ float
 silu(float x)
 {
-  return x / (1.0f + __expf(-x));
+  const float h = 0.5f * x;
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(h));
+  return fmaf(h, t, h);
 }
 
 __device__ __forceinline__ uint32_t

@@ -71,16 +71,29 @@ TARGETS = [
 ]
 
 
+def srim_masses():
+    """MAI weight (SCOEF.95A "m1" column) of Z = 1..92, the mass the batched workload gives each ion."""
+    from .engine import TABLES
+    out = []
+    for line in TABLES.read_text().splitlines():
+        if line.startswith("#") or not line.strip():
+            continue
+        out.append(float(line.split()[3]))
+    return out
+
+
 def batched_uneven(n_sims=4096, seed=1, scale_primaries=1.0, ion_masses=None):
     """4096 independent simulations drawn from `seed`: Z1 uniform 1..83 with the SRIM
     mass, E0 log-uniform 1 keV - 1 MeV, incidence angle uniform 0-60 deg, 1-4 layers
     from TARGETS with thickness log-uniform 5-500 nm over bulk Si, primaries
     log-uniform 1e2 - 1e5 (times `scale_primaries`)."""
     rng = np.random.default_rng(seed)
+    if ion_masses is None:
+        ion_masses = srim_masses()
     sims = []
     for _ in range(n_sims):
         Z = int(rng.integers(1, 84))
-        m = ion_masses[Z - 1] if ion_masses is not None else 2.0 * Z
+        m = ion_masses[Z - 1]
         E = float(10 ** rng.uniform(3, 6))
         ang = math.radians(float(rng.uniform(0, 60)))
         nl = int(rng.integers(1, 5))

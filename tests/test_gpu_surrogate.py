@@ -145,18 +145,46 @@ def trained():
     e.close()
 
 
-def test_trained_network_reproduces_the_quadrature(trained):
-    e, rep = trained
-    assert rep["final_loss"] < 1e-3
-    rng = np.random.default_rng(99)
-    eps = 10 ** rng.uniform(-4, 4, 20000)
-    b = 12 * np.sqrt(rng.uniform(0, 1, 20000))
+def _network_errors(e, n=40000, seed=99):
+    rng = np.random.default_rng(seed)
+    eps = 10 ** rng.uniform(-4, 4, n)
+    b = 12 * np.sqrt(rng.uniform(0, 1, n))
     s2q, _ = e.quadrature(eps, b)
     s2n = e.scatter(eps, b, precision="surrogate")
+    s2m = e.scatter(eps, b, precision="fp64")
     big = s2q > 1e-4
-    rel = np.abs(s2n - s2q) / s2q
-    assert np.median(rel[big]) < 0.03, np.median(rel[big])
-    assert np.quantile(rel[big], 0.95) < 0.15, np.quantile(rel[big], 0.95)
+    low = big & (eps <= 10)  # where the exact path uses the magic formula
+    rn = np.abs(s2n - s2q) / s2q
+    rm = np.abs(s2m - s2q) / s2q
+    return rn, rm, big, low
+
+
+def test_short_training_learns(trained):
+    """A short training run (2e6 samples, 6 epochs) already fits the quadrature to a
+    few percent; its loss falls below 1e-3."""
+    e, rep = trained
+    assert rep["final_loss"] < 1e-3
+    rn, _, big, _ = _network_errors(e)
+    assert np.median(rn[big]) < 0.10
+
+
+@pytest.fixture(scope="module")
+def committed():
+    from mytrim_gb300.train_surrogate import PARAMS
+    e = Engine(precision="fp32", seed=3)
+    e.set_surrogate_params(np.load(PARAMS))
+    yield e
+    e.close()
+
+
+def test_committed_network_reproduces_the_quadrature(committed):
+    """The network trained on 2e7 quadrature samples (mytrim_gb300/data) reproduces the
+    true scattering integral, and closer than the magic formula it replaces: that is
+    what the learned part gains over the method without it."""
+    rn, rm, big, low = _network_errors(committed)
+    assert np.median(rn[big]) < 0.01, np.median(rn[big])
+    assert np.quantile(rn[big], 0.95) < 0.03, np.quantile(rn[big], 0.95)
+    assert np.median(rn[low]) < 0.5 * np.median(rm[low]), (np.median(rn[low]), np.median(rm[low]))
 
 
 def test_params_roundtrip(trained):
@@ -169,8 +197,8 @@ def test_params_roundtrip(trained):
     f.close()
 
 
-def test_surrogate_engine_matches_fp64(trained):
-    e, _ = trained
+def test_surrogate_engine_matches_fp64(committed):
+    e = committed
     sim = W.cu_self_ion(n_primaries=2000, E=20e3)
     e.configure(precision="surrogate", seed=8)
     g = summarize(e.run([sim])[0])
