@@ -48,6 +48,8 @@ WORKLOADS = {
     "cu100k_cu": ("Cu 100 keV into bulk Cu (8.96 g/cm3), full cascade", "cu_self_ion"),
     "b10k_sio2_si": ("B 10 keV at 7 deg into 10 nm SiO2 on Si, full cascade", "boron_implant"),
     "as50k_sio2_si": ("As 50 keV at 7 deg into 10 nm SiO2 on Si, full cascade", "arsenic_implant"),
+    "au1m_agcusi": ("Au 1 MeV into 50 nm Ag / 200 nm Cu / Si, full cascade, sputter counting (E_surf 3 eV), "
+                    "256^3 energy-deposition voxels over 300 x 100 x 100 nm", "gold_deposition"),
     "batched4096": ("4096 independent simulations in one launch (Z1 1-83, E0 1 keV-1 MeV log-uniform, 0-60 deg, "
                     "1-4 layers of Si/Cu/Ag/Au/SiO2/Al2O3 5-500 nm over Si); primaries per simulation "
                     "log-uniform 1e2-1e5 scaled so that one step holds about the batch size", "batched_uneven"),

@@ -123,6 +123,12 @@ typedef struct
   int hist_range_n;       /*   and number of bins (0 = none) */
   double hist_vac_bin;    /* vacancy / replacement depth histograms (TrimVacCount uses 1) */
   int hist_vac_n;
+  /* extensions with no counterpart in the reference (0 disables them): */
+  double surface_binding; /* E_surf [eV]: a recoil leaving through x < 0 with
+                             E cos^2(angle to the surface normal) > E_surf counts as sputtered */
+  int voxel_n[3];         /* energy-deposition voxel tally: cells per axis (all > 0 to enable) */
+  double voxel_origin[3]; /* corner of the voxel box [length unit] */
+  double voxel_size[3];   /* edge lengths of the voxel box [length unit] */
 } mtg_sim;
 
 /* Run-wide settings (SimconfType scalars, simconf.h:66). */
@@ -148,6 +154,9 @@ typedef struct
   double sx, sxx, sy, syy, sz, szz;
   double vac_s2, eel_s2, enuc_s2, coll_s2; /* sums of per-primary squares */
   long long newton_iterations, rejection_passes, surrogate_fallbacks;
+  long long sputtered, backscattered; /* recoils / primaries lost through x < 0 */
+  double Esputtered;                  /* kinetic energy carried out by sputtered atoms */
+  double Evoxel;                      /* energy deposited inside the voxel box */
 } mtg_totals;
 
 /* Per-member trajectory summary (replay checks). */
@@ -220,6 +229,12 @@ mtg_status mtg_collect(mtg_ctx * ctx, mtg_totals * totals, long long * hist);
 mtg_status mtg_get_primaries(mtg_ctx * ctx, long long first, long long n, long long * vacancies,
                              long long * collisions, double * eel, double * enuc, double * x,
                              double * y, double * z, int * state);
+
+/* Energy-deposition voxels of simulation `sim` of the last run (voxel_n[0] * voxel_n[1] *
+ * voxel_n[2] floats, x fastest): electronic loss at the start of each flight path,
+ * nuclear deposits (binding energy, sub-threshold recoils, stopped members) where
+ * they happen, in eV.  No counterpart in the reference. */
+mtg_status mtg_get_voxels(mtg_ctx * ctx, int sim, float * out, long long n);
 
 /* Record one summary per cascade member (up to `capacity`) in subsequent runs;
  * 0 disables.  Replaces: the fullTraj trajectory dump (trim.C:370-371, 421-422). */

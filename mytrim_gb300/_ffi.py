@@ -52,7 +52,8 @@ class Sim(C.Structure):
     _fields_ = [("sample", Sample), ("ion", Ion), ("n_primaries", C.c_longlong),
                 ("first_primary", C.c_longlong), ("tally_mode", C.c_int),
                 ("primaries_only", C.c_int), ("hist_range_bin", C.c_double), ("hist_range_n", C.c_int),
-                ("hist_vac_bin", C.c_double), ("hist_vac_n", C.c_int)]
+                ("hist_vac_bin", C.c_double), ("hist_vac_n", C.c_int), ("surface_binding", C.c_double),
+                ("voxel_n", C.c_int * 3), ("voxel_origin", C.c_double * 3), ("voxel_size", C.c_double * 3)]
 
 
 class Config(C.Structure):
@@ -68,7 +69,9 @@ class Totals(C.Structure):
                [("range_n", C.c_longlong)] + \
                [(n, C.c_double) for n in ("sx", "sxx", "sy", "syy", "sz", "szz",
                                           "vac_s2", "eel_s2", "enuc_s2", "coll_s2")] + \
-               [(n, C.c_longlong) for n in ("newton_iterations", "rejection_passes", "surrogate_fallbacks")]
+               [(n, C.c_longlong) for n in ("newton_iterations", "rejection_passes", "surrogate_fallbacks",
+                                            "sputtered", "backscattered")] + \
+               [(n, C.c_double) for n in ("Esputtered", "Evoxel")]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -116,6 +119,7 @@ SIGNATURES = {
                                     C.POINTER(C.c_longlong), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                     C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                     C.POINTER(C.c_int)]),
+    "mtg_get_voxels": (C.c_int, [_P, C.c_int, C.POINTER(C.c_float), C.c_longlong]),
     "mtg_set_record_capacity": (C.c_int, [_P, C.c_longlong]),
     "mtg_get_records": (C.c_int, [_P, C.POINTER(MemberRecord), C.c_longlong, C.POINTER(C.c_longlong)]),
     "mtg_stopping": (C.c_int, [_P, C.c_int, C.c_double, C.POINTER(Material), C.POINTER(C.c_double),

@@ -79,6 +79,7 @@ struct mtg_ctx
   DevBuf d_sims, d_prim_end, d_species, d_mats, d_row_species, d_stop;
   DevBuf d_species32, d_mats32, d_sims32;
   DevBuf d_sg_params, d_sg_net; // surrogate network
+  DevBuf d_vox, d_vox_range, d_vox_sum; // energy-deposition voxels
   bool sg_ready = false;
   DevBuf p_vac, p_coll, p_eel, p_enuc, p_fx, p_fy, p_fz, p_state;
   DevBuf d_totals, d_hist, d_err, d_counters, d_stacks, d_ovf0, d_ovf1, d_records;
@@ -228,6 +229,7 @@ fill_params(mtg_ctx * ctx, EngineParams & prm)
   prm.prim.fstate = ptr<int>(ctx->p_state);
   prm.totals = ptr<SimTotals>(ctx->d_totals);
   prm.hist = ptr<unsigned long long>(ctx->d_hist);
+  prm.voxels = t.voxel_total > 0 ? ptr<float>(ctx->d_vox) : nullptr;
   prm.error_flags = ptr<unsigned int>(ctx->d_err);
   prm.k0 = t.k0;
   prm.k1 = t.k1;
@@ -365,7 +367,8 @@ mtg_destroy(mtg_ctx * ctx)
                      &ctx->d_hist,   &ctx->d_err,      &ctx->d_counters, &ctx->d_stacks, &ctx->d_ovf0,
                      &ctx->d_ovf1,   &ctx->d_records,  &ctx->d_jobs,    &ctx->d_job_first, &ctx->d_partials,
                      &ctx->d_out,    &ctx->d_tmp0,     &ctx->d_tmp1,    &ctx->d_tmp2,    &ctx->d_tmp3,
-                     &ctx->d_species32, &ctx->d_mats32, &ctx->d_sims32, &ctx->d_sg_params, &ctx->d_sg_net};
+                     &ctx->d_species32, &ctx->d_mats32, &ctx->d_sims32, &ctx->d_sg_params, &ctx->d_sg_net,
+                     &ctx->d_vox,    &ctx->d_vox_range, &ctx->d_vox_sum};
   for (DevBuf * b : bufs)
     if (b->p)
       cudaFree(b->p);
@@ -457,6 +460,20 @@ mtg_prepare(mtg_ctx * ctx, const mtg_sim * sims, int n_sims)
   CK(ensure(ctx->d_hist, 8 * size_t(std::max<long long>(t.hist_total, 1))));
   CK(ensure(ctx->d_err, 16));
   CK(ensure(ctx->d_counters, 8 * C_COUNT));
+  if (t.voxel_total > 0)
+  {
+    std::vector<long long> vr(2 * ns);
+    for (size_t s = 0; s < ns; ++s)
+    {
+      const SimDesc & d = t.sims[s];
+      vr[2 * s] = d.voxel_base;
+      vr[2 * s + 1] = d.voxel_n[0] > 0 ? (long long)d.voxel_n[0] * d.voxel_n[1] * d.voxel_n[2] : 0;
+    }
+    CK(ensure(ctx->d_vox, sizeof(float) * size_t(t.voxel_total)));
+    CK(ensure(ctx->d_vox_range, sizeof(long long) * vr.size()));
+    CK(ensure(ctx->d_vox_sum, sizeof(double) * ns));
+    CK(h2d(ctx, ctx->d_vox_range.p, vr.data(), sizeof(long long) * vr.size()));
+  }
   CK(h2d(ctx, ctx->d_sims.p, t.sims.data(), sizeof(SimDesc) * ns));
   CK(h2d(ctx, ctx->d_prim_end.p, t.prim_end.data(), sizeof(long long) * ns));
   CK(h2d(ctx, ctx->d_species.p, t.species.data(), sizeof(SpeciesConst) * t.species.size()));
@@ -540,6 +557,8 @@ mtg_launch_async(mtg_ctx * ctx, void * stream)
   CK(cudaMemsetAsync(ctx->d_totals.p, 0, sizeof(SimTotals) * t.sims.size(), s));
   CK(cudaMemsetAsync(ctx->d_hist.p, 0, 8 * size_t(std::max<long long>(t.hist_total, 1)), s));
   CK(cudaMemsetAsync(ctx->d_err.p, 0, 16, s));
+  if (t.voxel_total > 0)
+    CK(cudaMemsetAsync(ctx->d_vox.p, 0, sizeof(float) * size_t(t.voxel_total), s));
   CK(cudaMemsetAsync(ctx->d_counters.p, 0, 8 * C_COUNT, s));
   CK(cudaEventRecord(ctx->ev[0], s));
   st = launch_pass(ctx, 0);
@@ -549,6 +568,12 @@ mtg_launch_async(mtg_ctx * ctx, void * stream)
   if (st != MTG_OK)
     return st;
   CK(cudaEventRecord(ctx->ev[1], s));
+  if (t.voxel_total > 0)
+  {
+    CK(launch_voxel_sum(ptr<float>(ctx->d_vox), ptr<long long>(ctx->d_vox_range), int(t.sims.size()),
+                        ptr<double>(ctx->d_vox_sum), s));
+    ctx->stats.launches += 1;
+  }
   st = launch_reduction(ctx);
   if (st != MTG_OK)
     return st;
@@ -613,6 +638,17 @@ mtg_collect(mtg_ctx * ctx, mtg_totals * totals, long long * hist)
   std::vector<SimTotals> tot(ns);
   CK(cudaMemcpy(out.data(), ctx->d_out.p, sizeof(double) * NQ * ns, cudaMemcpyDeviceToHost));
   CK(cudaMemcpy(tot.data(), ctx->d_totals.p, sizeof(SimTotals) * ns, cudaMemcpyDeviceToHost));
+  std::vector<double> vsum(ns, 0.0);
+  if (t.voxel_total > 0)
+  {
+    if (extra)
+    {
+      CK(launch_voxel_sum(ptr<float>(ctx->d_vox), ptr<long long>(ctx->d_vox_range), int(ns),
+                          ptr<double>(ctx->d_vox_sum), ctx->stream));
+      CK(cudaStreamSynchronize(ctx->stream));
+    }
+    CK(cudaMemcpy(vsum.data(), ctx->d_vox_sum.p, sizeof(double) * ns, cudaMemcpyDeviceToHost));
+  }
   long long coll_all = 0;
   if (totals)
     for (size_t s = 0; s < ns; ++s)
@@ -646,6 +682,10 @@ mtg_collect(mtg_ctx * ctx, mtg_totals * totals, long long * hist)
       o.newton_iterations = (long long)tot[s].newton_iters;
       o.rejection_passes = (long long)tot[s].rejection_passes;
       o.surrogate_fallbacks = (long long)tot[s].fallbacks;
+      o.sputtered = (long long)tot[s].sputtered;
+      o.backscattered = (long long)tot[s].backscattered;
+      o.Esputtered = tot[s].Esputtered;
+      o.Evoxel = vsum[s];
       coll_all += o.collisions;
     }
   ctx->stats.collisions = coll_all;
@@ -662,7 +702,7 @@ mtg_collect(mtg_ctx * ctx, mtg_totals * totals, long long * hist)
                      &ctx->p_fx,     &ctx->p_fy,       &ctx->p_fz,      &ctx->p_state,   &ctx->d_totals,
                      &ctx->d_hist,   &ctx->d_err,      &ctx->d_counters, &ctx->d_stacks, &ctx->d_ovf0,
                      &ctx->d_ovf1,   &ctx->d_records,  &ctx->d_jobs,    &ctx->d_job_first, &ctx->d_partials,
-                     &ctx->d_out,    &ctx->d_species32, &ctx->d_mats32, &ctx->d_sims32};
+                     &ctx->d_out,    &ctx->d_species32, &ctx->d_mats32, &ctx->d_sims32, &ctx->d_vox};
   for (DevBuf * b : bufs)
     bytes += b->bytes;
   ctx->stats.device_bytes = bytes;
@@ -720,6 +760,25 @@ mtg_get_primaries(mtg_ctx * ctx, long long first, long long n, long long * vacan
   CK(get_f64(ctx->p_fz, z));
   if (state)
     CK(cudaMemcpy(state, ptr<int>(ctx->p_state) + first, 4 * n, cudaMemcpyDeviceToHost));
+  return MTG_OK;
+}
+
+mtg_status
+mtg_get_voxels(mtg_ctx * ctx, int sim, float * out, long long n)
+{
+  mtg_status st = require_device(ctx);
+  if (st != MTG_OK)
+    return st;
+  if (!ctx->launched)
+    return fail(ctx, MTG_ERR_STATE, "no run to read");
+  if (sim < 0 || sim >= int(ctx->tables.sims.size()) || !out)
+    return fail(ctx, MTG_ERR_BAD_INPUT, "bad simulation index or buffer");
+  const SimDesc & d = ctx->tables.sims[sim];
+  const long long cells = d.voxel_n[0] > 0 ? (long long)d.voxel_n[0] * d.voxel_n[1] * d.voxel_n[2] : 0;
+  if (n != cells)
+    return fail(ctx, MTG_ERR_BAD_INPUT, "buffer size must equal the simulation's voxel count");
+  if (cells > 0)
+    CK(cudaMemcpy(out, ptr<float>(ctx->d_vox) + d.voxel_base, sizeof(float) * cells, cudaMemcpyDeviceToHost));
   return MTG_OK;
 }
 

@@ -241,7 +241,7 @@ collide64(P64 & p, uint32_t ic, double r1, const SimDesc & sim, const SpeciesCon
   if (dee > p.E)
     dee = p.E;
   p.E -= dee;
-  sink.eel(dee);
+  sink.eel(dee, p.x, p.y, p.z);
   const double p1 = sqrt(2.0 * sc.m1 * p.E);
   if (den > p.E)
     den = p.E;
@@ -311,7 +311,7 @@ collide64(P64 & p, uint32_t ic, double r1, const SimDesc & sim, const SpeciesCon
   for (int i = 0; i < 3; ++i)
     if (sim.bc[i] == 2 && (pos[i] > sim.w[i] || pos[i] < 0.0))
     {
-      sink.lost(p.E + den);
+      sink.lost(p.E + den, p);
       return CF_DONE;
     }
 
@@ -320,7 +320,7 @@ collide64(P64 & p, uint32_t ic, double r1, const SimDesc & sim, const SpeciesCon
   int state = ST_MOVING;
   if (rec.E > el.Edisp - el.Elbind)
   {
-    sink.enuc(el.Elbind);
+    sink.enuc(el.Elbind, rec.x, rec.y, rec.z);
     const bool follow = sim.range_mode ? (rec.gen < 1) : !sim.primaries_only;
     if (follow)
     {
@@ -343,7 +343,7 @@ collide64(P64 & p, uint32_t ic, double r1, const SimDesc & sim, const SpeciesCon
   }
   else
   {
-    sink.enuc(rec.E + el.Elbind);
+    sink.enuc(rec.E + el.Elbind, rec.x, rec.y, rec.z);
     if (p.E < sim.Ef)
       state = ST_INTERSTITIAL;
   }

@@ -75,6 +75,7 @@ struct EngineParams
   PrimaryTallies prim;
   SimTotals * totals;
   unsigned long long * hist; // all histograms, per-simulation bases in SimDesc
+  float * voxels;            // energy-deposition voxels of all simulations (may be NULL)
   unsigned int * error_flags;
   uint32_t k0, k1;
   unsigned int max_collisions; // per member
@@ -149,7 +150,9 @@ struct LaneSink
   Acc a_eel, a_enuc;
   // per-simulation accumulators (32-bit per lane; flushed long before they can wrap)
   unsigned int n_repl, n_inter, n_subst, n_lost, n_members, n_newton, n_passes, n_fallbacks;
-  Acc e_lost, e_unf;
+  unsigned int n_sput, n_back;
+  Acc e_lost, e_unf, e_sput;
+  bool vox;  // this simulation tallies energy deposition in voxels
   // events of the current collision, aggregated per warp after it
   int vac_bin, repl_bin;
   // current member record
@@ -160,8 +163,10 @@ struct LaneSink
   __device__ void reset_sim()
   {
     n_repl = n_inter = n_subst = n_lost = n_members = n_newton = n_passes = n_fallbacks = 0;
+    n_sput = n_back = 0;
     e_lost.reset();
     e_unf.reset();
+    e_sput.reset();
   }
   __device__ void reset_prim()
   {
@@ -171,22 +176,57 @@ struct LaneSink
   }
 
   // ---- events raised by the collision code (the reference's hooks, trim.h:72-84)
-  __device__ void eel(Real d)
+  // energy-deposition voxel tally (extension): one float atomic per deposit
+  __device__ void deposit(Real x, Real y, Real z, Real e)
+  {
+    if (!vox)
+      return;
+    const int ix = int(floorf(float(x - Real(sim->voxel_origin[0])) * sim->voxel_inv_cell[0]));
+    const int iy = int(floorf(float(y - Real(sim->voxel_origin[1])) * sim->voxel_inv_cell[1]));
+    const int iz = int(floorf(float(z - Real(sim->voxel_origin[2])) * sim->voxel_inv_cell[2]));
+    if (ix < 0 || iy < 0 || iz < 0 || ix >= sim->voxel_n[0] || iy >= sim->voxel_n[1] || iz >= sim->voxel_n[2])
+      return;
+    const long long cell = sim->voxel_base + ((long long)iz * sim->voxel_n[1] + iy) * sim->voxel_n[0] + ix;
+    atomicAdd(prm->voxels + cell, float(e));
+  }
+
+  // electronic loss d over the flight path that starts at (x, y, z)
+  __device__ void eel(Real d, Real x, Real y, Real z)
   {
     a_eel.add(d);
     m_eel.add(d);
+    deposit(x, y, z, d);
   }
   __device__ void newton(int n) { n_newton += (unsigned int)n; }
   __device__ void passes(int n) { n_passes += (unsigned int)n; }
   __device__ void fallback() { ++n_fallbacks; }
   __device__ void numeric() { atomicOr(prm->error_flags, ERRB_NUMERIC); }
-  __device__ void enuc(Real e) { a_enuc.add(e); }
+  // nuclear (phonon) deposit e at (x, y, z)
+  __device__ void enuc(Real e, Real x, Real y, Real z)
+  {
+    a_enuc.add(e);
+    deposit(x, y, z, e);
+  }
   __device__ void unfollowed(Real e) { e_unf.add(e); }
-  __device__ void lost(Real e)
+  // the member left the sample carrying `e` (its own energy plus the recoil dropped
+  // with it, trim.C:357); through the entrance surface a recoil counts as sputtered
+  // when E cos^2 > E_surf, a primary as backscattered
+  template <class P>
+  __device__ void lost(Real e, const P & p)
   {
     ++n_lost;
     e_lost.add(e);
     m_state = ST_LOST;
+    if (p.x < Real(0) && sim->bc[0] == 2)
+    {
+      if (p.gen == 0)
+        ++n_back;
+      else if (sim->surface_binding > 0.0f && Real(p.E) * p.dx * p.dx > Real(sim->surface_binding))
+      {
+        ++n_sput;
+        e_sput.add(Real(p.E));
+      }
+    }
   }
 
   template <class R, class E>
@@ -232,6 +272,7 @@ struct LaneSink
   {
     m_state = state;
     a_enuc.add(Real(p.E));
+    deposit(Real(p.x), Real(p.y), Real(p.z), Real(p.E));
     if (state == ST_INTERSTITIAL)
       ++n_inter;
     else if (state == ST_SUBSTITUTIONAL)
@@ -319,6 +360,12 @@ struct LaneSink
       atomicAdd(&t->Elost, e_lost.value());
     if (e_unf.nonzero())
       atomicAdd(&t->Eunfollowed, e_unf.value());
+    if (n_sput)
+      atomicAdd(&t->sputtered, ull(n_sput));
+    if (n_back)
+      atomicAdd(&t->backscattered, ull(n_back));
+    if (e_sput.nonzero())
+      atomicAdd(&t->Esputtered, e_sput.value());
     reset_sim();
   }
 };
@@ -376,6 +423,7 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
   sink.sim = nullptr;
   sink.gprim = -1;
   sink.range_mode = 0;
+  sink.vox = false;
   sink.reset_prim();
   sink.reset_sim();
   sink.m_vac = 0;
@@ -393,6 +441,7 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
       sim = prm.sims + cur_sim;
       sink.sim = sim;
       sink.range_mode = sim->range_mode;
+      sink.vox = prm.voxels != nullptr && sim->voxel_n[0] > 0;
       sink.gprim = -1;
     }
     if ((long long)p.prim != sink.gprim)

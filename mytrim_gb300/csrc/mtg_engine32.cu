@@ -300,7 +300,7 @@ struct Fp32Policy
     }
     else
       ff_sub(p.E, p.El, dee);
-    sink.eel(dee);
+    sink.eel(dee, p.x, p.y, p.z);
     const float p1 = sqrtf(m.sc->two_m1 * p.E);
     if (den >= p.E)
     {
@@ -362,7 +362,7 @@ struct Fp32Policy
       for (int i = 0; i < 3; ++i)
         if (sim.bc[i] == 2 && (pos[i] > sim.w[i] || pos[i] < 0.0f))
         {
-          sink.lost(p.E + p.El + den);
+          sink.lost(p.E + p.El + den, p);
           return CF_DONE;
         }
     }
@@ -372,7 +372,7 @@ struct Fp32Policy
     int state = ST_MOVING;
     if (recE > el.disp_thresh)
     {
-      sink.enuc(el.Elbind);
+      sink.enuc(el.Elbind, rec.x, rec.y, rec.z);
       const bool follow = sim.range_mode ? (rec.gen < 1) : !sim.primaries_only;
       if (follow)
       {
@@ -395,7 +395,7 @@ struct Fp32Policy
     }
     else
     {
-      sink.enuc(den);
+      sink.enuc(den, rec.x, rec.y, rec.z);
       if (p.E < sim.Ef)
         state = ST_INTERSTITIAL;
     }

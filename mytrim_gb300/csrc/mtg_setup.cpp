@@ -392,6 +392,36 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
     d.inv_hist_vac_bin = s.hist_vac_n > 0 ? 1.0 / s.hist_vac_bin : 0.0;
     d.inv_hist_range_bin_f = float(d.inv_hist_range_bin);
     d.inv_hist_vac_bin_f = float(d.inv_hist_vac_bin);
+    if (!(s.surface_binding >= 0.0))
+    {
+      err = "surface binding energy must be non-negative";
+      return MTG_ERR_BAD_INPUT;
+    }
+    d.surface_binding = float(s.surface_binding);
+    const bool vox = s.voxel_n[0] > 0 || s.voxel_n[1] > 0 || s.voxel_n[2] > 0;
+    if (vox)
+    {
+      long long cells = 1;
+      for (int i = 0; i < 3; ++i)
+      {
+        if (s.voxel_n[i] < 1 || s.voxel_n[i] > 4096 || !(s.voxel_size[i] > 0.0))
+        {
+          err = "voxel tally needs 1..4096 cells and a positive size on every axis";
+          return MTG_ERR_BAD_INPUT;
+        }
+        cells *= s.voxel_n[i];
+        d.voxel_n[i] = s.voxel_n[i];
+        d.voxel_origin[i] = float(s.voxel_origin[i]);
+        d.voxel_inv_cell[i] = float(double(s.voxel_n[i]) / s.voxel_size[i]);
+      }
+      if (cells > (1LL << 28))
+      {
+        err = "at most 2^28 voxels per simulation";
+        return MTG_ERR_BAD_INPUT;
+      }
+      d.voxel_base = out.voxel_total;
+      out.voxel_total += cells;
+    }
     hist += s.hist_range_n + 2LL * s.hist_vac_n;
     prim += s.n_primaries;
     out.prim_end.push_back(prim);

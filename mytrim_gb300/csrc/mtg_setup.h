@@ -20,6 +20,7 @@ struct HostTables
   std::vector<MatConst> mats;
   long long total_primaries = 0;
   long long hist_total = 0;               // entries of the concatenated histograms
+  long long voxel_total = 0;              // cells of the concatenated voxel grids
   uint32_t k0 = 0, k1 = 0;                // Philox key
   double emax = 0.0;                      // largest primary energy
 };

@@ -110,6 +110,11 @@ struct SimDesc
   long long hist_range_base, hist_vac_base;
   double inv_hist_range_bin, inv_hist_vac_bin;
   float inv_hist_range_bin_f, inv_hist_vac_bin_f; // single-precision copies (FP32 engine)
+  // extensions: sputter counting and energy-deposition voxels
+  float surface_binding;   // 0 = off
+  int voxel_n[3];          // 0 = off
+  float voxel_origin[3], voxel_inv_cell[3];
+  long long voxel_base;    // offset into the run's voxel buffer
 };
 
 // Totals per simulation (device accumulators, reduced on the host).
@@ -118,6 +123,8 @@ struct SimTotals
   unsigned long long members, replacements, interstitials, substitutionals, lost;
   unsigned long long newton_iters, rejection_passes, fallbacks;
   double Elost, Eunfollowed;
+  unsigned long long sputtered, backscattered;
+  double Esputtered;
 };
 
 // ---- single-precision copies used by the FP32 engine (built from the tables above)

@@ -56,6 +56,10 @@ class SimSpec:
     hist_range_n: int = 0
     hist_vac_bin: float = 1.0
     hist_vac_n: int = 0
+    surface_binding: float = 0.0         # sputter counting (extension), 0 = off
+    voxel_n: Tuple[int, int, int] = (0, 0, 0)  # energy-deposition voxels (extension)
+    voxel_origin: Tuple[float, float, float] = (0.0, 0.0, 0.0)
+    voxel_size: Tuple[float, float, float] = (0.0, 0.0, 0.0)
 
     def box(self):
         if self.size is not None:
@@ -109,6 +113,11 @@ class SimSpec:
         s.hist_range_n = self.hist_range_n
         s.hist_vac_bin = self.hist_vac_bin
         s.hist_vac_n = self.hist_vac_n
+        s.surface_binding = self.surface_binding
+        for i in range(3):
+            s.voxel_n[i] = self.voxel_n[i]
+            s.voxel_origin[i] = self.voxel_origin[i]
+            s.voxel_size[i] = self.voxel_size[i]
         return s
 
 
@@ -235,6 +244,13 @@ class Engine:
             p(out["eel"], C.c_double), p(out["enuc"], C.c_double), p(out["x"], C.c_double),
             p(out["y"], C.c_double), p(out["z"], C.c_double), p(out["state"], C.c_int)))
         return out
+
+    def voxels(self, sim: int = 0) -> np.ndarray:
+        s = self._sims[sim]
+        nx, ny, nz = s.voxel_n
+        out = np.zeros(nx * ny * nz, dtype=np.float32)
+        self._check(self.lib.mtg_get_voxels(self.ctx, sim, out.ctypes.data_as(C.POINTER(C.c_float)), len(out)))
+        return out.reshape(nz, ny, nx)
 
     def set_record_capacity(self, cap: int):
         self._check(self.lib.mtg_set_record_capacity(self.ctx, cap))

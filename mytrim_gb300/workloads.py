@@ -50,14 +50,18 @@ def silver_into_silicon(n_primaries=10_000_000):
                    hist_range_bin=10.0, hist_range_n=300, hist_vac_bin=10.0, hist_vac_n=300)
 
 
-def gold_deposition(n_primaries=100_000_000):
-    """Au 1 MeV into 50 nm Ag / 200 nm Cu / bulk Si with surface loss (CUT at x < 0)."""
+def gold_deposition(n_primaries=100_000_000, voxels=256):
+    """Au 1 MeV into 50 nm Ag / 200 nm Cu / bulk Si, full cascade, surface loss (CUT at
+    x < 0) with sputter counting (E_surf 3 eV), energy deposition in voxels^3 cells over
+    a 300 nm deep, 100 x 100 nm box around the beam, vacancy depth profile."""
     layers = [LayerSpec(500.0, 10.49, [ElementSpec(47, 107.868, 1.0)]),
               LayerSpec(2000.0, 8.96, [ElementSpec(29, CU, 1.0)]),
               LayerSpec(1e7, 2.33, [ElementSpec(14, SI, 1.0, 15.0, 3.0)])]
     return SimSpec(layers=layers, Z=79, m=196.967, E=1e6, n_primaries=n_primaries, pos=(0.0, 0.0, 0.0),
                    size=(1e9, 1e9, 1e9), bc=(F.BC_CUT, F.BC_INF, F.BC_INF),
-                   hist_range_bin=10.0, hist_range_n=300, hist_vac_bin=10.0, hist_vac_n=300)
+                   hist_range_bin=10.0, hist_range_n=300, hist_vac_bin=10.0, hist_vac_n=300,
+                   surface_binding=3.0, voxel_n=(voxels, voxels, voxels), voxel_origin=(0.0, -500.0, -500.0),
+                   voxel_size=(3000.0, 1000.0, 1000.0))
 
 
 # targets of the batched workload: (name, rho, [(Z, mass, fraction, Edisp)])

@@ -390,6 +390,8 @@ struct Engine
     t.hist_range.assign(s.hist_range_n, 0);
     t.hist_vac.assign(s.hist_vac_n, 0);
     t.hist_repl.assign(s.hist_vac_n, 0);
+    t.spec = &s;
+    t.vox_depth.assign(s.vox_n[0] > 0 ? s.vox_n[0] : 0, 0.0);
     pk0 = s.seed;
     pk1 = 0x4D795452u; // fixed high key word for single-simulation runs
   }
@@ -608,6 +610,7 @@ struct Engine
         {
           t.Enuc += el.Elbind;
           p_enuc += el.Elbind;
+          t.deposit(rec.pos[0], rec.pos[1], rec.pos[2], el.Elbind);
           const bool follow = spec.range_mode ? (rec.gen < 1) : !spec.primaries_only;
           if (follow)
           {
@@ -631,11 +634,15 @@ struct Engine
           const double e = rec.E + el.Elbind;
           t.Enuc += e;
           p_enuc += e;
+          t.deposit(rec.pos[0], rec.pos[1], rec.pos[2], e);
           if (pka.E < pka.Ef)
             pka.state = INTERSTITIAL;
         }
       }
       (void)queued;
+      // electronic loss deposited where the flight started, in the order the
+      // reference's hooks see it (checkPKAState follows the fate hooks)
+      t.deposit(rec.pos[0], rec.pos[1], rec.pos[2], dee);
       check_state(pka, rec.E + el.Elbind);
     } while (pka.state == MOVING);
   }
@@ -686,10 +693,12 @@ struct Engine
     {
       t.lost++;
       t.Elost += pka.E + recoil_energy;
+      t.exit_surface(pka.pos[0], pka.gen, pka.E, pka.dir[0]);
       return;
     }
     t.Enuc += pka.E;
     p_enuc += pka.E;
+    t.deposit(pka.pos[0], pka.pos[1], pka.pos[2], pka.E);
     if (pka.state == INTERSTITIAL)
       t.interstitials++;
     else if (pka.state == SUBSTITUTIONAL)

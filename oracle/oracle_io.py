@@ -20,7 +20,8 @@ TABLES = REPO / "mytrim_gb300" / "data" / "stopping_tables.tsv"
 
 SUM_KEYS = ("primaries", "members", "collisions", "vacancies", "replacements", "interstitials",
             "substitutionals", "lost", "Eel", "Enuc", "Elost", "Eunfollowed", "range_n", "sx", "sxx",
-            "sy", "syy", "sz", "szz", "vac_s2", "eel_s2", "enuc_s2", "coll_s2")
+            "sy", "syy", "sz", "szz", "vac_s2", "eel_s2", "enuc_s2", "coll_s2", "sputtered", "backscattered",
+            "Esputtered", "Evoxel")
 
 
 def build(reference_dir=None):
@@ -52,6 +53,12 @@ def spec_text(sim, seed=1, philox=True, first=0, n=None, records=0, tmin=None):
         lines.append(f"subset {first} {n if n is not None else sim.n_primaries - first}")
     if records:
         lines.append(f"records {records}")
+    if getattr(sim, "surface_binding", 0.0) > 0.0:
+        lines.append(f"sputter {sim.surface_binding!r}")
+    vn = getattr(sim, "voxel_n", (0, 0, 0))
+    if vn[0] > 0:
+        o, z = sim.voxel_origin, sim.voxel_size
+        lines.append(f"voxels {vn[0]} {vn[1]} {vn[2]} {o[0]!r} {o[1]!r} {o[2]!r} {z[0]!r} {z[1]!r} {z[2]!r}")
     return "\n".join(lines) + "\n"
 
 
@@ -69,6 +76,8 @@ def parse(text):
                                        enuc=enuc, x=x, y=y, z=z, state=int(parts[10])))
         elif k.startswith("hist_"):
             out[k] = [int(v) for v in parts[1:]]
+        elif k == "vox_depth":
+            out[k] = [float(v) for v in parts[1:]]
         elif len(parts) == 2:
             v = parts[1]
             out[k] = float(v) if any(c in v for c in ".en") else int(v)
@@ -93,7 +102,7 @@ def merge(parts):
     for p in parts:
         for k in SUM_KEYS:
             out[k] += p.get(k, 0)
-    for h in ("hist_range", "hist_vac", "hist_repl"):
+    for h in ("hist_range", "hist_vac", "hist_repl", "vox_depth"):
         hs = [p.get(h, []) for p in parts]
         if hs and hs[0] is not None:
             out[h] = [sum(v) for v in zip(*hs)] if hs[0] else []

@@ -37,6 +37,8 @@ public:
     t.hist_range.assign(spec.hist_range_n, 0);
     t.hist_vac.assign(spec.hist_vac_n, 0);
     t.hist_repl.assign(spec.hist_vac_n, 0);
+    t.spec = &spec;
+    t.vox_depth.assign(spec.vox_n[0] > 0 ? spec.vox_n[0] : 0, 0.0);
   }
 
   runspec::Tally t;
@@ -54,6 +56,7 @@ protected:
     // TrimPhononOut: the binding energy stays behind where a recoil branches off
     t.Enuc += _element->_Elbind;
     p_enuc += _element->_Elbind;
+    t.deposit(_recoil->_pos(0), _recoil->_pos(1), _recoil->_pos(2), _element->_Elbind);
     bool follow = _spec.range_mode ? (_recoil->_gen < 1) : !_spec.primaries_only;
     if (!follow)
       t.Eunfollowed += _recoil->_E;
@@ -102,6 +105,7 @@ protected:
     const double e = _recoil->_E + _element->_Elbind;
     t.Enuc += e;
     p_enuc += e;
+    t.deposit(_recoil->_pos(0), _recoil->_pos(1), _recoil->_pos(2), e);
   }
 
   void checkPKAState() override
@@ -109,6 +113,8 @@ protected:
     t.collisions++;
     p_coll++;
     p_eel += _dee; // electronic loss of this collision, after the clamp (trim.C:277-289)
+    // deposited where the flight path started: the recoil's position (trim.C:306)
+    t.deposit(_recoil->_pos(0), _recoil->_pos(1), _recoil->_pos(2), _dee);
     const int st = _pka->_state;
     if (st == IonBase::MOVING)
       return;
@@ -118,10 +124,12 @@ protected:
       t.lost++;
       // the projectile's energy and the recoil dropped with it (trim.C:357) leave the sample
       t.Elost += _pka->_E + (_recoil->_E + _element->_Elbind);
+      t.exit_surface(_pka->_pos(0), _pka->_gen, _pka->_E, _pka->_dir(0));
       return;
     }
     t.Enuc += _pka->_E;
     p_enuc += _pka->_E;
+    t.deposit(_pka->_pos(0), _pka->_pos(1), _pka->_pos(2), _pka->_E);
     if (st == IonBase::INTERSTITIAL)
       t.interstitials++;
     else if (st == IonBase::SUBSTITUTIONAL)

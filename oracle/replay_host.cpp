@@ -30,14 +30,18 @@ struct HostSink
   double m_eel = 0.0;
   int range_mode = 0;
 
-  void eel(double d) { m_eel += d; }
+  void eel(double d, double, double, double) { m_eel += d; }
   void newton(int) {}
   void passes(int) {}
   void fallback() {}
   void numeric() {}
-  void enuc(double) {}
+  void enuc(double, double, double, double) {}
   void unfollowed(double) {}
-  void lost(double) { m_state = ST_LOST; }
+  template <class P>
+  void lost(double, const P &)
+  {
+    m_state = ST_LOST;
+  }
   template <class R, class E>
   void vacancy(const R & rec, const E & el)
   {

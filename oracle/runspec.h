@@ -23,6 +23,8 @@
 //   hist_vac <bin_A> <nbins>    histogram of vacancy depth (TrimVacCount bins are 1 A)
 //   subset <first> <count>      run primaries [first, first+count)
 //   records <n>                 emit per-primary records for the first n primaries
+//   sputter <Esurf>             count recoils leaving through x < 0 with E cos^2 > Esurf
+//   voxels nx ny nz ox oy oz sx sy sz   energy-deposition voxel box (depth profile reported)
 #pragma once
 
 #include <cstdio>
@@ -72,6 +74,9 @@ struct Spec
   int hist_vac_n = 0;
   long long first = 0, n = -1;
   int records = 0;
+  double esurf = 0.0;
+  int vox_n[3] = {0, 0, 0};
+  double vox_o[3] = {0, 0, 0}, vox_s[3] = {0, 0, 0};
 
   double total_thickness() const
   {
@@ -187,6 +192,11 @@ parse(std::istream & in, Spec & s, std::string & err)
       ok = bool(ls >> s.first >> s.n);
     else if (key == "records")
       ok = bool(ls >> s.records);
+    else if (key == "sputter")
+      ok = bool(ls >> s.esurf);
+    else if (key == "voxels")
+      ok = bool(ls >> s.vox_n[0] >> s.vox_n[1] >> s.vox_n[2] >> s.vox_o[0] >> s.vox_o[1] >> s.vox_o[2] >>
+                s.vox_s[0] >> s.vox_s[1] >> s.vox_s[2]);
     else
     {
       err = "unknown key '" + key + "' on line " + std::to_string(lineno);
@@ -226,6 +236,41 @@ struct Tally
   // per-primary moments for Monte Carlo error bars
   double vac_s2 = 0.0, eel_s2 = 0.0, enuc_s2 = 0.0, coll_s2 = 0.0;
   std::vector<long long> hist_range, hist_vac, hist_repl;
+  // extensions: sputtering and energy-deposition voxels (depth profile over x cells)
+  long long sputtered = 0, backscattered = 0;
+  double Esputtered = 0.0, Evoxel = 0.0;
+  std::vector<double> vox_depth;
+  const Spec * spec = nullptr;
+
+  void deposit(double x, double y, double z, double e)
+  {
+    if (!spec || spec->vox_n[0] <= 0)
+      return;
+    const double p[3] = {x, y, z};
+    int ix[3];
+    for (int i = 0; i < 3; ++i)
+    {
+      const double q = (p[i] - spec->vox_o[i]) * spec->vox_n[i] / spec->vox_s[i];
+      if (!(q >= 0.0) || q >= spec->vox_n[i])
+        return;
+      ix[i] = int(q);
+    }
+    Evoxel += e;
+    vox_depth[ix[0]] += e;
+  }
+  // a member lost through x < 0 with energy E and direction cosine dx
+  void exit_surface(double x, int gen, double E, double dx)
+  {
+    if (!spec || !(x < 0.0) || spec->bc[0] != 2)
+      return;
+    if (gen == 0)
+      ++backscattered;
+    else if (spec->esurf > 0.0 && E * dx * dx > spec->esurf)
+    {
+      ++sputtered;
+      Esputtered += E;
+    }
+  }
 
   void print(FILE * f) const
   {
@@ -249,6 +294,12 @@ struct Tally
     hist("hist_range", hist_range);
     hist("hist_vac", hist_vac);
     hist("hist_repl", hist_repl);
+    fprintf(f, "sputtered %lld\nbackscattered %lld\nEsputtered %.17g\nEvoxel %.17g\n", sputtered,
+            backscattered, Esputtered, Evoxel);
+    fprintf(f, "vox_depth");
+    for (double v : vox_depth)
+      fprintf(f, " %.17g", v);
+    fprintf(f, "\n");
   }
 };
 

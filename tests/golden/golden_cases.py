@@ -26,6 +26,14 @@ CASES = {
     "he_fe_range": (SimSpec(layers=[LayerSpec(100000.0, 7.8658, [ElementSpec(26, 55.847, 1.0)])], Z=2, m=4.0026,
                             E=20000.0, n_primaries=30, mode="range", hist_range_bin=10.0, hist_range_n=200),
                     11, 30),
+    # gold into Ag / Cu / Si with a CUT surface, sputter counting and deposition voxels
+    "au_agcusi_sputter": (SimSpec(layers=[LayerSpec(50.0, 10.49, [ElementSpec(47, 107.868, 1.0)]),
+                                          LayerSpec(100.0, 8.96, [ElementSpec(29, CU, 1.0)]),
+                                          LayerSpec(100000.0, 2.33, [ElementSpec(14, SI, 1.0, 15.0, 3.0)])],
+                                  Z=79, m=196.967, E=20000.0, n_primaries=6, pos=(0.0, 0.0, 0.0),
+                                  size=(1e9, 1e9, 1e9), bc=(2, 1, 1), surface_binding=3.0,
+                                  voxel_n=(30, 4, 4), voxel_origin=(0.0, -100.0, -100.0),
+                                  voxel_size=(300.0, 200.0, 200.0)), 5, 6),
     # protons into a two-element target
     "h_sic": (SimSpec(layers=[LayerSpec(100000.0, 3.21, [ElementSpec(14, SI, 1.0), ElementSpec(6, 12.011, 1.0)])],
                       Z=1, m=1.008, E=5000.0, n_primaries=40), 12, 40),

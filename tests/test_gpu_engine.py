@@ -267,3 +267,40 @@ def test_multi_simulation_run(engine_lib):
     s1, s2 = summarize(both[1]), summarize(both[2])
     assert both[1]["vacancies"] != both[2]["vacancies"]
     assert _z(s1, s2, "vac_per_ion") < 4.0
+
+
+def test_sputter_and_voxels_match_oracle(oracle_built, engine_lib):
+    """Sputter counts, backscattering and the deposition voxels of the FP64 engine
+    equal the oracle on the same streams (counts exactly; voxel sums to float
+    accumulation accuracy)."""
+    sim = W.gold_deposition(n_primaries=40, voxels=40)
+    sim.E = 100e3
+    e = Engine(precision="fp64", seed=21)
+    g = e.run([sim])[0]
+    vox = e.voxels(0)
+    e.close()
+    o = oracle_built.run(sim, seed=21, philox=True)
+    for k in ("sputtered", "backscattered", "lost", "members", "vacancies"):
+        assert g[k] == o[k], (k, g[k], o[k])
+    assert g["sputtered"] > 0
+    assert math.isclose(g["Esputtered"], o["Esputtered"], rel_tol=1e-9)
+    assert math.isclose(g["Evoxel"], o["Evoxel"], rel_tol=1e-5)
+    depth = vox.sum(axis=(0, 1), dtype=np.float64)
+    ref = np.array(o["vox_depth"])
+    assert np.allclose(depth, ref, rtol=1e-4, atol=1e-3 * ref.max())
+
+
+def test_fp32_voxels_conserve_energy(engine_lib):
+    """FP32: the deposited energy inside a box that contains the whole cascade equals
+    electronic + nuclear loss."""
+    sim = W.gold_deposition(n_primaries=300, voxels=64)
+    sim.E = 50e3
+    sim.voxel_origin = (-2000.0, -4000.0, -4000.0)
+    sim.voxel_size = (10000.0, 8000.0, 8000.0)
+    e = Engine(precision="fp32", seed=22)
+    t = e.run([sim])[0]
+    vox = e.voxels(0)
+    e.close()
+    inside = float(vox.sum(dtype=np.float64))
+    assert math.isclose(inside, t["Evoxel"], rel_tol=1e-6)
+    assert math.isclose(t["Evoxel"], t["Eel"] + t["Enuc"], rel_tol=2e-4)

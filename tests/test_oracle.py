@@ -29,7 +29,8 @@ from mytrim_gb300.engine import ElementSpec, LayerSpec, SimSpec  # noqa: E402
 
 SCALARS = ("primaries", "members", "collisions", "vacancies", "replacements", "interstitials",
            "substitutionals", "lost", "Eel", "Enuc", "Elost", "Eunfollowed", "range_n", "sx", "sxx",
-           "sy", "syy", "sz", "szz", "vac_s2", "eel_s2", "enuc_s2", "coll_s2")
+           "sy", "syy", "sz", "szz", "vac_s2", "eel_s2", "enuc_s2", "coll_s2", "sputtered", "backscattered",
+           "Esputtered", "Evoxel")
 
 
 @pytest.mark.parametrize("case", sorted(CASES))
@@ -39,7 +40,7 @@ def test_restatement_matches_reference_fixture(oracle_built, case):
     got = oracle_built.run(sim, seed=seed, philox=False, records=nrec)
     for k in SCALARS:
         assert got[k] == gold[k], (case, k, got[k], gold[k])
-    for h in ("hist_range", "hist_vac", "hist_repl"):
+    for h in ("hist_range", "hist_vac", "hist_repl", "vox_depth"):
         assert got[h] == gold[h], (case, h)
     assert got["records"] == gold["records"]
 
