@@ -153,6 +153,10 @@ struct LaneSink
   unsigned int n_sput, n_back;
   Acc e_lost, e_unf, e_sput;
   bool vox;  // this simulation tallies energy deposition in voxels
+  // pending voxel deposit: consecutive deposits into one cell are summed in a
+  // register and written with one atomic when the cell changes
+  long long vcell;
+  float vacc;
   // events of the current collision, aggregated per warp after it
   int vac_bin, repl_bin;
   // current member record
@@ -187,7 +191,21 @@ struct LaneSink
     if (ix < 0 || iy < 0 || iz < 0 || ix >= sim->voxel_n[0] || iy >= sim->voxel_n[1] || iz >= sim->voxel_n[2])
       return;
     const long long cell = sim->voxel_base + ((long long)iz * sim->voxel_n[1] + iy) * sim->voxel_n[0] + ix;
-    atomicAdd(prm->voxels + cell, float(e));
+    if (cell == vcell)
+    {
+      vacc += float(e);
+      return;
+    }
+    flush_voxel();
+    vcell = cell;
+    vacc = float(e);
+  }
+  __device__ void flush_voxel()
+  {
+    if (vcell >= 0)
+      atomicAdd(prm->voxels + vcell, vacc);
+    vcell = -1;
+    vacc = 0.0f;
   }
 
   // electronic loss d over the flight path that starts at (x, y, z)
@@ -424,6 +442,8 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
   sink.gprim = -1;
   sink.range_mode = 0;
   sink.vox = false;
+  sink.vcell = -1;
+  sink.vacc = 0.0f;
   sink.reset_prim();
   sink.reset_sim();
   sink.m_vac = 0;
@@ -583,6 +603,7 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
   }
   sink.flush_prim();
   sink.flush_sim(cur_sim);
+  sink.flush_voxel();
 }
 
 } // namespace mtg
