@@ -142,6 +142,9 @@ typedef struct
   unsigned long long seed;
   long long max_collisions_per_member; /* 0 = default (2^24) */
   int stack_capacity;    /* recoil stack entries per warp, 0 = default */
+  int block_threads;     /* threads per block of the cascade kernel: 64 or 128, 0 = 128 */
+  int max_primaries_per_refill; /* fresh primaries one warp takes at a time, 1..32;
+                                   0 = chosen from the batch size and the grid */
 } mtg_config;
 
 /* Results of one simulation. */

@@ -59,7 +59,7 @@ class Sim(C.Structure):
 class Config(C.Structure):
     _fields_ = [("tmin", C.c_double), ("tau", C.c_double), ("cw", C.c_double), ("length_scale", C.c_double),
                 ("precision", C.c_int), ("seed", C.c_ulonglong), ("max_collisions_per_member", C.c_longlong),
-                ("stack_capacity", C.c_int)]
+                ("stack_capacity", C.c_int), ("block_threads", C.c_int), ("max_primaries_per_refill", C.c_int)]
 
 
 class Totals(C.Structure):

@@ -89,6 +89,7 @@ struct mtg_ctx
   std::vector<int> job_first;
   int block = 128, grid = 0;
   size_t smem = 0;
+  int cold_offset = 0;
   int stage = 0;
   int stack_cap = 0;
   long long ovf_cap = 0;
@@ -132,6 +133,8 @@ default_config()
   c.seed = 1;
   c.max_collisions_per_member = 1 << 24;
   c.stack_capacity = 0;
+  c.block_threads = 0;
+  c.max_primaries_per_refill = 0;
   return c;
 }
 
@@ -163,9 +166,14 @@ setup_launch_shape(mtg_ctx * ctx)
     else
       tab = 0;
   }
-  ctx->smem = ctx->stage ? tab : 0;
+  ctx->block = ctx->cfg.block_threads > 0 ? ctx->cfg.block_threads : 128;
+  size_t tables = ctx->stage ? tab : 0;
   if (!ctx->stage && prec == MTG_PREC_FP32_SURROGATE)
-    ctx->smem = surrogate_net_bytes();
+    tables = surrogate_net_bytes();
+  // per-thread tally slots follow the tables, 16-byte aligned
+  ctx->cold_offset = int((tables + 15) / 16 * 16);
+  const size_t slot = prec == MTG_PREC_FP64 ? cold_slot_bytes64() : cold_slot_bytes32();
+  ctx->smem = size_t(ctx->cold_offset) + slot * size_t(ctx->block);
   int bps = 0;
   cudaError_t e = prec == MTG_PREC_FP64 ? occupancy64(ctx->block, ctx->smem, &bps)
                                         : occupancy32(ctx->block, ctx->smem, &bps, prec == MTG_PREC_FP32_SURROGATE);
@@ -213,6 +221,7 @@ fill_params(mtg_ctx * ctx, EngineParams & prm)
     prm.mats = reinterpret_cast<const MatConst *>(ctx->d_mats32.p);
   }
   prm.stage_tables = ctx->stage;
+  prm.cold_offset = ctx->cold_offset;
   prm.n_stage_species = int(t.species.size());
   prm.n_stage_mats = int(t.mats.size());
   prm.total_primaries = t.total_primaries;
@@ -235,6 +244,15 @@ fill_params(mtg_ctx * ctx, EngineParams & prm)
   prm.k1 = t.k1;
   long long mc = ctx->cfg.max_collisions_per_member;
   prm.max_collisions = (unsigned int)(mc <= 0 ? (1 << 24) : std::min<long long>(mc, 0xffffffffLL));
+  // fresh primaries per warp refill: small enough that every warp refills several
+  // times (dynamic load balance across warps), at most one per lane
+  int take = ctx->cfg.max_primaries_per_refill;
+  if (take <= 0)
+  {
+    const long long warps = std::max<long long>(1, (long long)ctx->grid * (ctx->block / 32));
+    take = int(std::min<long long>(32, std::max<long long>(1, t.total_primaries / (warps * 4))));
+  }
+  prm.max_take = take;
   if (ctx->record_cap > 0)
   {
     prm.records = ptr<MemberRecord>(ctx->d_records);
@@ -421,6 +439,10 @@ mtg_configure(mtg_ctx * ctx, const mtg_config * cfg)
     return fail(ctx, MTG_ERR_BAD_INPUT, "unknown precision");
   if (!(cfg->length_scale > 0.0) || !(cfg->tmin > 0.0) || !(cfg->cw > 0.0) || cfg->stack_capacity < 0)
     return fail(ctx, MTG_ERR_BAD_INPUT, "length_scale, tmin and cw must be positive");
+  if (cfg->block_threads != 0 && cfg->block_threads != 64 && cfg->block_threads != 128)
+    return fail(ctx, MTG_ERR_BAD_INPUT, "block_threads must be 0, 64 or 128");
+  if (cfg->max_primaries_per_refill < 0 || cfg->max_primaries_per_refill > 32)
+    return fail(ctx, MTG_ERR_BAD_INPUT, "max_primaries_per_refill must be 0..32");
   ctx->cfg = *cfg;
   ctx->prepared = false;
   return MTG_OK;

@@ -79,6 +79,8 @@ struct EngineParams
   unsigned int * error_flags;
   uint32_t k0, k1;
   unsigned int max_collisions; // per member
+  int max_take;                // fresh primaries one warp takes per refill (load balance)
+  int cold_offset;             // byte offset of the per-thread LaneCold slots in dynamic shared memory
   // optional per-member records (replay checks)
   MemberRecord * records;
   unsigned long long * n_records;
@@ -116,6 +118,7 @@ struct AccF64
   __device__ void add(double x) { s += x; }
   __device__ double value() const { return s; }
   __device__ bool nonzero() const { return s != 0.0; }
+  __device__ void atomic_add_to(double * dst) const { atomicAdd(dst, s); }
 };
 
 // Kahan-compensated FP32 accumulator (FP32 engine): keeps FP64 work out of the
@@ -133,6 +136,40 @@ struct AccKahan32
   }
   __device__ double value() const { return double(s) - double(c); }
   __device__ bool nonzero() const { return s != 0.0f; }
+  // add the sum to a double in global memory without FP64 instructions (float ->
+  // double by exponent rebias on the bit pattern; the engine flushes denormals)
+  __device__ void atomic_add_to(double * dst) const
+  {
+    atomicAdd(dst, widen(s));
+    if (c != 0.0f)
+      atomicAdd(dst, widen(-c));
+  }
+  static __device__ __forceinline__ double widen(float f)
+  {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xffu;
+    if (e == 0u)
+      return 0.0;
+    const unsigned long long bits = ((unsigned long long)(u >> 31) << 63) |
+                                    ((unsigned long long)(e + 896u) << 52) |
+                                    ((unsigned long long)(u & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)bits);
+  }
+};
+
+// Rarely-updated tally state of one lane, kept in a per-thread slot of shared
+// memory instead of registers (the collision loop needs its registers).
+template <class Acc>
+struct LaneCold
+{
+  unsigned int n_repl, n_inter, n_subst, n_lost, n_members, n_passes, n_fallbacks, n_sput, n_back;
+  unsigned int m_vac;
+  int m_state;
+  int pad;
+  Acc e_lost, e_unf, e_sput, m_eel;
+  long long vcell; // pending voxel deposit: cell and value
+  float vacc;
+  float pad2;
 };
 
 // Device tally sink for one lane.
@@ -141,6 +178,7 @@ struct LaneSink
 {
   using Acc = typename Pol::Acc;
   using Real = typename Pol::Real;
+  LaneCold<Acc> * cold;
   const EngineParams * prm;
   const SimDesc * sim;
   long long gprim;     // global primary index of the current member
@@ -148,29 +186,27 @@ struct LaneSink
   // per-primary accumulators
   unsigned int a_vac, a_coll;
   Acc a_eel, a_enuc;
-  // per-simulation accumulators (32-bit per lane; flushed long before they can wrap)
-  unsigned int n_repl, n_inter, n_subst, n_lost, n_members, n_newton, n_passes, n_fallbacks;
-  unsigned int n_sput, n_back;
-  Acc e_lost, e_unf, e_sput;
+  // per-simulation Newton-iteration count (every collision), the rest in `cold`
+  unsigned int n_newton;
   bool vox;  // this simulation tallies energy deposition in voxels
-  // pending voxel deposit: consecutive deposits into one cell are summed in a
-  // register and written with one atomic when the cell changes
-  long long vcell;
-  float vacc;
   // events of the current collision, aggregated per warp after it
   int vac_bin, repl_bin;
-  // current member record
-  unsigned int m_vac;
-  int m_state;
-  Acc m_eel;
 
   __device__ void reset_sim()
   {
-    n_repl = n_inter = n_subst = n_lost = n_members = n_newton = n_passes = n_fallbacks = 0;
-    n_sput = n_back = 0;
-    e_lost.reset();
-    e_unf.reset();
-    e_sput.reset();
+    LaneCold<Acc> & c = *cold;
+    c.n_repl = c.n_inter = c.n_subst = c.n_lost = c.n_members = c.n_passes = c.n_fallbacks = 0;
+    c.n_sput = c.n_back = 0;
+    n_newton = 0;
+    c.e_lost.reset();
+    c.e_unf.reset();
+    c.e_sput.reset();
+  }
+  __device__ void reset_member()
+  {
+    cold->m_vac = 0;
+    cold->m_state = 0;
+    cold->m_eel.reset();
   }
   __device__ void reset_prim()
   {
@@ -191,33 +227,36 @@ struct LaneSink
     if (ix < 0 || iy < 0 || iz < 0 || ix >= sim->voxel_n[0] || iy >= sim->voxel_n[1] || iz >= sim->voxel_n[2])
       return;
     const long long cell = sim->voxel_base + ((long long)iz * sim->voxel_n[1] + iy) * sim->voxel_n[0] + ix;
-    if (cell == vcell)
+    LaneCold<Acc> & c = *cold;
+    if (cell == c.vcell)
     {
-      vacc += float(e);
+      c.vacc += float(e);
       return;
     }
     flush_voxel();
-    vcell = cell;
-    vacc = float(e);
+    c.vcell = cell;
+    c.vacc = float(e);
   }
   __device__ void flush_voxel()
   {
-    if (vcell >= 0)
-      atomicAdd(prm->voxels + vcell, vacc);
-    vcell = -1;
-    vacc = 0.0f;
+    LaneCold<Acc> & c = *cold;
+    if (c.vcell >= 0)
+      atomicAdd(prm->voxels + c.vcell, c.vacc);
+    c.vcell = -1;
+    c.vacc = 0.0f;
   }
 
   // electronic loss d over the flight path that starts at (x, y, z)
   __device__ void eel(Real d, Real x, Real y, Real z)
   {
     a_eel.add(d);
-    m_eel.add(d);
+    if (prm->records)
+      cold->m_eel.add(d);
     deposit(x, y, z, d);
   }
   __device__ void newton(int n) { n_newton += (unsigned int)n; }
-  __device__ void passes(int n) { n_passes += (unsigned int)n; }
-  __device__ void fallback() { ++n_fallbacks; }
+  __device__ void passes(int n) { cold->n_passes += (unsigned int)n; }
+  __device__ void fallback() { ++cold->n_fallbacks; }
   __device__ void numeric() { atomicOr(prm->error_flags, ERRB_NUMERIC); }
   // nuclear (phonon) deposit e at (x, y, z)
   __device__ void enuc(Real e, Real x, Real y, Real z)
@@ -225,24 +264,25 @@ struct LaneSink
     a_enuc.add(e);
     deposit(x, y, z, e);
   }
-  __device__ void unfollowed(Real e) { e_unf.add(e); }
+  __device__ void unfollowed(Real e) { cold->e_unf.add(e); }
   // the member left the sample carrying `e` (its own energy plus the recoil dropped
   // with it, trim.C:357); through the entrance surface a recoil counts as sputtered
   // when E cos^2 > E_surf, a primary as backscattered
   template <class P>
   __device__ void lost(Real e, const P & p)
   {
-    ++n_lost;
-    e_lost.add(e);
-    m_state = ST_LOST;
+    LaneCold<Acc> & c = *cold;
+    ++c.n_lost;
+    c.e_lost.add(e);
+    c.m_state = ST_LOST;
     if (p.x < Real(0) && sim->bc[0] == 2)
     {
       if (p.gen == 0)
-        ++n_back;
+        ++c.n_back;
       else if (sim->surface_binding > 0.0f && Real(p.E) * p.dx * p.dx > Real(sim->surface_binding))
       {
-        ++n_sput;
-        e_sput.add(Real(p.E));
+        ++c.n_sput;
+        c.e_sput.add(Real(p.E));
       }
     }
   }
@@ -269,18 +309,18 @@ struct LaneSink
       else
         add = 1;
       a_vac += add;
-      m_vac += add;
+      cold->m_vac += add;
       return;
     }
     ++a_vac;
-    ++m_vac;
+    ++cold->m_vac;
     vac_bin = depth_bin(Real(rec.x), inv_vac_bin(), sim->hist_vac_n);
     if (vac_bin >= 0)
       vac_bin += int(sim->hist_vac_base);
   }
   __device__ void replacement(Real x)
   {
-    ++n_repl;
+    ++cold->n_repl;
     repl_bin = depth_bin(x, inv_vac_bin(), sim->hist_vac_n);
     if (repl_bin >= 0)
       repl_bin += int(sim->hist_vac_base + sim->hist_vac_n);
@@ -288,13 +328,13 @@ struct LaneSink
   template <class P>
   __device__ void stop(int state, const P & p)
   {
-    m_state = state;
+    cold->m_state = state;
     a_enuc.add(Real(p.E));
     deposit(Real(p.x), Real(p.y), Real(p.z), Real(p.E));
     if (state == ST_INTERSTITIAL)
-      ++n_inter;
+      ++cold->n_inter;
     else if (state == ST_SUBSTITUTIONAL)
-      ++n_subst;
+      ++cold->n_subst;
     if (p.gen == 0)
     {
       prm->prim.fx[gprim] = double(p.x);
@@ -347,9 +387,9 @@ struct LaneSink
     if (a_coll)
       atomicAdd(prm->prim.coll + gprim, (unsigned long long)a_coll);
     if (a_eel.nonzero())
-      atomicAdd(prm->prim.eel + gprim, a_eel.value());
+      a_eel.atomic_add_to(prm->prim.eel + gprim);
     if (a_enuc.nonzero())
-      atomicAdd(prm->prim.enuc + gprim, a_enuc.value());
+      a_enuc.atomic_add_to(prm->prim.enuc + gprim);
     reset_prim();
   }
   __device__ void flush_sim(int s)
@@ -357,33 +397,34 @@ struct LaneSink
     if (s < 0)
       return;
     SimTotals * t = prm->totals + s;
+    const LaneCold<Acc> & c = *cold;
     using ull = unsigned long long;
-    if (n_members)
-      atomicAdd(&t->members, ull(n_members));
-    if (n_repl)
-      atomicAdd(&t->replacements, ull(n_repl));
-    if (n_inter)
-      atomicAdd(&t->interstitials, ull(n_inter));
-    if (n_subst)
-      atomicAdd(&t->substitutionals, ull(n_subst));
-    if (n_lost)
-      atomicAdd(&t->lost, ull(n_lost));
+    if (c.n_members)
+      atomicAdd(&t->members, ull(c.n_members));
+    if (c.n_repl)
+      atomicAdd(&t->replacements, ull(c.n_repl));
+    if (c.n_inter)
+      atomicAdd(&t->interstitials, ull(c.n_inter));
+    if (c.n_subst)
+      atomicAdd(&t->substitutionals, ull(c.n_subst));
+    if (c.n_lost)
+      atomicAdd(&t->lost, ull(c.n_lost));
     if (n_newton)
       atomicAdd(&t->newton_iters, ull(n_newton));
-    if (n_passes)
-      atomicAdd(&t->rejection_passes, ull(n_passes));
-    if (n_fallbacks)
-      atomicAdd(&t->fallbacks, ull(n_fallbacks));
-    if (e_lost.nonzero())
-      atomicAdd(&t->Elost, e_lost.value());
-    if (e_unf.nonzero())
-      atomicAdd(&t->Eunfollowed, e_unf.value());
-    if (n_sput)
-      atomicAdd(&t->sputtered, ull(n_sput));
-    if (n_back)
-      atomicAdd(&t->backscattered, ull(n_back));
-    if (e_sput.nonzero())
-      atomicAdd(&t->Esputtered, e_sput.value());
+    if (c.n_passes)
+      atomicAdd(&t->rejection_passes, ull(c.n_passes));
+    if (c.n_fallbacks)
+      atomicAdd(&t->fallbacks, ull(c.n_fallbacks));
+    if (c.e_lost.nonzero())
+      c.e_lost.atomic_add_to(&t->Elost);
+    if (c.e_unf.nonzero())
+      c.e_unf.atomic_add_to(&t->Eunfollowed);
+    if (c.n_sput)
+      atomicAdd(&t->sputtered, ull(c.n_sput));
+    if (c.n_back)
+      atomicAdd(&t->backscattered, ull(c.n_back));
+    if (c.e_sput.nonzero())
+      c.e_sput.atomic_add_to(&t->Esputtered);
     reset_sim();
   }
 };
@@ -437,18 +478,17 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
   typename Pol::MemberCtx mctx;
 
   LaneSink<Pol> sink;
+  sink.cold = reinterpret_cast<LaneCold<typename Pol::Acc> *>(smem + prm.cold_offset) + threadIdx.x;
+  sink.cold->vcell = -1;
+  sink.cold->vacc = 0.0f;
   sink.prm = &prm;
   sink.sim = nullptr;
   sink.gprim = -1;
   sink.range_mode = 0;
   sink.vox = false;
-  sink.vcell = -1;
-  sink.vacc = 0.0f;
   sink.reset_prim();
   sink.reset_sim();
-  sink.m_vac = 0;
-  sink.m_state = 0;
-  sink.m_eel.reset();
+  sink.reset_member();
 
   auto start_member = [&](const Particle & q) {
     p = q;
@@ -468,15 +508,13 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
     {
       sink.flush_prim();
       sink.gprim = (long long)p.prim;
-      if (sink.n_newton > 0x40000000u || sink.n_passes > 0x40000000u)
+      if (sink.n_newton > 0x40000000u || sink.cold->n_passes > 0x40000000u)
         sink.flush_sim(cur_sim);
     }
     Pol::begin_member(mctx, prm, tab, *sim, p);
     r1 = Pol::first_draw(p.key, prm.k0, prm.k1);
-    sink.m_vac = 0;
-    sink.m_state = 0;
-    sink.m_eel.reset();
-    ++sink.n_members;
+    sink.reset_member();
+    ++sink.cold->n_members;
   };
 
   while (true)
@@ -494,7 +532,9 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
         live = true;
       }
       top -= npop;
-      const int need = nidle - npop;
+      int need = nidle - npop;
+      if (need > prm.max_take)
+        need = prm.max_take;
       if (need > 0 && !work_done)
       {
         unsigned long long base = 0;
@@ -506,7 +546,7 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
         if (avail <= need)
           work_done = true;
         const int r = rank - npop;
-        if (!live && r >= 0 && r < avail)
+        if (!live && r >= 0 && r < need && r < avail)
         {
           const long long g = (long long)base + r;
           if (prm.in_records)
@@ -556,14 +596,14 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
             m.sim = p.sim;
             m.species = p.species;
             m.gen = p.gen;
-            m.state = sink.m_state;
+            m.state = sink.cold->m_state;
             m.ncoll = ic;
-            m.nvac = sink.m_vac;
+            m.nvac = sink.cold->m_vac;
             m.E = double(p.E);
             m.x = double(p.x);
             m.y = double(p.y);
             m.z = double(p.z);
-            m.eel = sink.m_eel.value();
+            m.eel = sink.cold->m_eel.value();
             prm.records[slot] = m;
           }
         }

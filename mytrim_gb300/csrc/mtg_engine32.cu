@@ -466,6 +466,12 @@ record_size32()
   return sizeof(P32);
 }
 
+size_t
+cold_slot_bytes32()
+{
+  return sizeof(LaneCold<AccKahan32>);
+}
+
 // ---- scattering service (FP32 exact and surrogate)
 __global__ void
 scatter32_kernel(const double * eps, const double * b, long long n, double * s2, const SurrogateNet * net,

@@ -117,6 +117,12 @@ record_size64()
   return sizeof(P64);
 }
 
+size_t
+cold_slot_bytes64()
+{
+  return sizeof(LaneCold<AccF64>);
+}
+
 // ---- service kernels
 
 __global__ void

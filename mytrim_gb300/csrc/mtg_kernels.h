@@ -15,6 +15,7 @@ struct PrimaryTallies;
 cudaError_t launch_cascade64(const EngineParams & prm, int grid, int block, size_t smem, cudaStream_t st);
 cudaError_t occupancy64(int block, size_t smem, int * blocks_per_sm);
 size_t record_size64();
+size_t cold_slot_bytes64(); // per-thread shared-memory tally slot
 cudaError_t launch_stopping64(const SpeciesConst * sc, const MatConst * mc, const double * E, long long n,
                               double * out, cudaStream_t st);
 cudaError_t launch_scatter64(const double * eps, const double * b, long long n, double * s2, cudaStream_t st);
@@ -37,6 +38,7 @@ cudaError_t launch_cascade32(const EngineParams & prm, const Fp32Tables & t, int
                              cudaStream_t st, int surrogate);
 cudaError_t occupancy32(int block, size_t smem, int * blocks_per_sm, int surrogate);
 size_t record_size32();
+size_t cold_slot_bytes32();
 cudaError_t launch_scatter32(const double * eps, const double * b, long long n, double * s2, const void * net,
                              int surrogate, cudaStream_t st);
 cudaError_t launch_stopping32(const float * row, float lnE_min, float inv_d, const double * E, long long n,

@@ -159,7 +159,8 @@ class Engine:
 
     def __init__(self, device: int = 0, precision: str = "fp64", seed: int = 1, tmin: float = 0.2,
                  tau: float = 0.0, cw: float = 0.001, length_scale: float = 1.0, max_collisions: int = 0,
-                 stack_capacity: int = 0, tables: Optional[str] = None):
+                 stack_capacity: int = 0, tables: Optional[str] = None, block_threads: int = 0,
+                 max_take: int = 0):
         self.lib = F.load()
         self.ctx = C.c_void_p()
         st = self.lib.mtg_create(device, C.byref(self.ctx))
@@ -168,7 +169,8 @@ class Engine:
         self._check(self.lib.mtg_load_tables(self.ctx, str(tables or TABLES).encode()))
         self.cfg = F.Config()
         self.configure(precision=precision, seed=seed, tmin=tmin, tau=tau, cw=cw, length_scale=length_scale,
-                       max_collisions=max_collisions, stack_capacity=stack_capacity)
+                       max_collisions=max_collisions, stack_capacity=stack_capacity, block_threads=block_threads,
+                       max_take=max_take)
         self._sims: List[SimSpec] = []
 
     def _check(self, st):
@@ -178,13 +180,15 @@ class Engine:
         return st
 
     def configure(self, precision="fp64", seed=1, tmin=0.2, tau=0.0, cw=0.001, length_scale=1.0,
-                  max_collisions=0, stack_capacity=0):
+                  max_collisions=0, stack_capacity=0, block_threads=0, max_take=0):
         c = self.cfg
         c.tmin, c.tau, c.cw, c.length_scale = tmin, tau, cw, length_scale
         c.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
         c.seed = seed
         c.max_collisions_per_member = max_collisions
         c.stack_capacity = stack_capacity
+        c.block_threads = block_threads
+        c.max_primaries_per_refill = max_take
         self._check(self.lib.mtg_configure(self.ctx, C.byref(c)))
 
     def close(self):
