@@ -129,6 +129,9 @@ typedef struct
   int voxel_n[3];         /* energy-deposition voxel tally: cells per axis (all > 0 to enable) */
   double voxel_origin[3]; /* corner of the voxel box [length unit] */
   double voxel_size[3];   /* edge lengths of the voxel box [length unit] */
+  double hist_lateral_bin; /* 2-D histogram of the primaries' stopping points in (y, z) around
+                              the start position: bin width [length unit] */
+  int hist_lateral_n;     /* bins per axis (0 = none); appended after the replacement bins */
 } mtg_sim;
 
 /* Run-wide settings (SimconfType scalars, simconf.h:66). */
@@ -212,7 +215,8 @@ mtg_status mtg_configure(mtg_ctx * ctx, const mtg_config * cfg);
 
 /* Run n_sims simulations to completion (full cascades), host in, host out.
  * totals: n_sims entries.  hist: NULL or, per simulation in order, hist_range_n
- * range bins, then hist_vac_n vacancy bins, then hist_vac_n replacement bins.
+ * range bins, then hist_vac_n vacancy bins, then hist_vac_n replacement bins, then
+ * hist_lateral_n^2 lateral bins (z major).
  * Replaces: the cascade loop computeThread (runmytrim.C:71-93) over
  * TrimBase::trim (trim.C:36-425) with the tally plugins (apps/src/Trim*.C). */
 mtg_status mtg_run(mtg_ctx * ctx, const mtg_sim * sims, int n_sims, mtg_totals * totals,

@@ -53,7 +53,8 @@ class Sim(C.Structure):
                 ("first_primary", C.c_longlong), ("tally_mode", C.c_int),
                 ("primaries_only", C.c_int), ("hist_range_bin", C.c_double), ("hist_range_n", C.c_int),
                 ("hist_vac_bin", C.c_double), ("hist_vac_n", C.c_int), ("surface_binding", C.c_double),
-                ("voxel_n", C.c_int * 3), ("voxel_origin", C.c_double * 3), ("voxel_size", C.c_double * 3)]
+                ("voxel_n", C.c_int * 3), ("voxel_origin", C.c_double * 3), ("voxel_size", C.c_double * 3),
+                ("hist_lateral_bin", C.c_double), ("hist_lateral_n", C.c_int)]
 
 
 class Config(C.Structure):

@@ -344,6 +344,14 @@ struct LaneSink
       const int b = depth_bin(Real(p.x), inv_range_bin(), sim->hist_range_n);
       if (b >= 0)
         atomicAdd(prm->hist + sim->hist_range_base + b, 1ull);
+      if (sim->hist_lat_n > 0)
+      {
+        const float qy = (float(p.y) - sim->lat_y0) * sim->inv_hist_lat_bin;
+        const float qz = (float(p.z) - sim->lat_z0) * sim->inv_hist_lat_bin;
+        const int n = sim->hist_lat_n;
+        if (qy >= 0.0f && qz >= 0.0f && qy < float(n) && qz < float(n))
+          atomicAdd(prm->hist + sim->hist_lat_base + (long long)int(qz) * n + int(qy), 1ull);
+      }
     }
   }
 

@@ -422,7 +422,20 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
       d.voxel_base = out.voxel_total;
       out.voxel_total += cells;
     }
-    hist += s.hist_range_n + 2LL * s.hist_vac_n;
+    if (s.hist_lateral_n < 0 || s.hist_lateral_n > 4096 || (s.hist_lateral_n > 0 && !(s.hist_lateral_bin > 0.0)))
+    {
+      err = "invalid lateral histogram binning";
+      return MTG_ERR_BAD_INPUT;
+    }
+    d.hist_lat_n = s.hist_lateral_n;
+    if (s.hist_lateral_n > 0)
+    {
+      d.inv_hist_lat_bin = float(1.0 / s.hist_lateral_bin);
+      d.lat_y0 = float(s.ion.pos[1] - 0.5 * s.hist_lateral_n * s.hist_lateral_bin);
+      d.lat_z0 = float(s.ion.pos[2] - 0.5 * s.hist_lateral_n * s.hist_lateral_bin);
+    }
+    d.hist_lat_base = hist + s.hist_range_n + 2LL * s.hist_vac_n;
+    hist += s.hist_range_n + 2LL * s.hist_vac_n + (long long)s.hist_lateral_n * s.hist_lateral_n;
     prim += s.n_primaries;
     out.prim_end.push_back(prim);
     out.sims.push_back(d);

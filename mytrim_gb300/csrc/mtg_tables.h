@@ -115,6 +115,10 @@ struct SimDesc
   int voxel_n[3];          // 0 = off
   float voxel_origin[3], voxel_inv_cell[3];
   long long voxel_base;    // offset into the run's voxel buffer
+  // lateral (y, z) histogram of stopping points around the start position
+  int hist_lat_n;
+  float inv_hist_lat_bin, lat_y0, lat_z0; // y0, z0: lower corner of the histogram
+  long long hist_lat_base;
 };
 
 // Totals per simulation (device accumulators, reduced on the host).

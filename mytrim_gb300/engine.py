@@ -60,6 +60,8 @@ class SimSpec:
     voxel_n: Tuple[int, int, int] = (0, 0, 0)  # energy-deposition voxels (extension)
     voxel_origin: Tuple[float, float, float] = (0.0, 0.0, 0.0)
     voxel_size: Tuple[float, float, float] = (0.0, 0.0, 0.0)
+    hist_lateral_bin: float = 10.0       # lateral (y, z) histogram of stopping points
+    hist_lateral_n: int = 0
 
     def box(self):
         if self.size is not None:
@@ -73,7 +75,7 @@ class SimSpec:
         return (0.0, w[1] / 2.0, w[2] / 2.0)
 
     def hist_sizes(self):
-        return self.hist_range_n, self.hist_vac_n, self.hist_vac_n
+        return self.hist_range_n, self.hist_vac_n, self.hist_vac_n, self.hist_lateral_n ** 2
 
     def to_c(self) -> F.Sim:
         if not 1 <= len(self.layers) <= F.MAX_LAYERS:
@@ -114,6 +116,8 @@ class SimSpec:
         s.hist_vac_bin = self.hist_vac_bin
         s.hist_vac_n = self.hist_vac_n
         s.surface_binding = self.surface_binding
+        s.hist_lateral_bin = self.hist_lateral_bin
+        s.hist_lateral_n = self.hist_lateral_n
         for i in range(3):
             s.voxel_n[i] = self.voxel_n[i]
             s.voxel_origin[i] = self.voxel_origin[i]
@@ -223,12 +227,14 @@ class Engine:
         off = 0
         for i, s in enumerate(self._sims):
             d = tot[i].as_dict()
-            hr, hv, hp = s.hist_sizes()
+            hr, hv, hp, hl = s.hist_sizes()
             h = np.frombuffer(hist, dtype=np.int64, count=max(nh, 1))
             d["hist_range"] = h[off:off + hr].copy()
             d["hist_vac"] = h[off + hr:off + hr + hv].copy()
             d["hist_repl"] = h[off + hr + hv:off + hr + hv + hp].copy()
-            off += hr + hv + hp
+            d["hist_lateral"] = h[off + hr + hv + hp:off + hr + hv + hp + hl].copy().reshape(
+                s.hist_lateral_n, s.hist_lateral_n)
+            off += hr + hv + hp + hl
             d["status"] = st
             out.append(d)
         return out

@@ -26,13 +26,14 @@ def cu_self_ion(n_primaries=10_000, E=100e3):
 def sio2_on_si(Z, m, E, n_primaries, tilt_deg=7.0):
     """Ion at `tilt_deg` into 10 nm SiO2 (2.2 g/cm3; Edisp Si 15, O 28) on bulk Si (2.33,
     Edisp 15); backscattered ions leave through the surface (CUT at x < 0);
-    0.5 nm depth histogram to 300 nm."""
+    0.5 nm depth histogram to 300 nm, lateral 1 nm histogram over +-150 nm."""
     t = math.radians(tilt_deg)
     layers = [LayerSpec(100.0, 2.2, [ElementSpec(14, SI, 1.0, 15.0, 3.0), ElementSpec(8, O, 2.0, 28.0, 3.0)]),
               LayerSpec(1e7, 2.33, [ElementSpec(14, SI, 1.0, 15.0, 3.0)])]
     return SimSpec(layers=layers, Z=Z, m=m, E=E, n_primaries=n_primaries, dir=(math.cos(t), math.sin(t), 0.0),
                    pos=(0.0, 0.0, 0.0), size=(1e9, 1e9, 1e9), bc=(F.BC_CUT, F.BC_INF, F.BC_INF),
-                   hist_range_bin=5.0, hist_range_n=600, hist_vac_bin=5.0, hist_vac_n=600)
+                   hist_range_bin=5.0, hist_range_n=600, hist_vac_bin=5.0, hist_vac_n=600,
+                   hist_lateral_bin=10.0, hist_lateral_n=300)
 
 
 def boron_implant(n_primaries=1_000_000):

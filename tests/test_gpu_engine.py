@@ -304,3 +304,18 @@ def test_fp32_voxels_conserve_energy(engine_lib):
     inside = float(vox.sum(dtype=np.float64))
     assert math.isclose(inside, t["Evoxel"], rel_tol=1e-6)
     assert math.isclose(t["Evoxel"], t["Eel"] + t["Enuc"], rel_tol=2e-4)
+
+
+def test_lateral_histogram(engine_lib):
+    """The lateral (y, z) histogram of stopping points holds every stopped primary that
+    lands inside it, and its first moments equal the range tallies'."""
+    sim = W.arsenic_implant(n_primaries=4000)
+    e = Engine(precision="fp32", seed=12)
+    t = e.run([sim])[0]
+    e.close()
+    h = t["hist_lateral"]
+    assert h.shape == (300, 300)
+    assert h.sum() <= t["range_n"] and h.sum() >= 0.99 * t["range_n"]
+    centres = (np.arange(300) + 0.5) * 10.0 - 1500.0
+    my = (h.sum(axis=0) * centres).sum() / h.sum()
+    assert abs(my - t["sy"] / t["range_n"]) < 5.0
