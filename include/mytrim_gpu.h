@@ -132,6 +132,10 @@ typedef struct
   double hist_lateral_bin; /* 2-D histogram of the primaries' stopping points in (y, z) around
                               the start position: bin width [length unit] */
   int hist_lateral_n;     /* bins per axis (0 = none); appended after the replacement bins */
+  int hist_evac_rows;     /* vacancy-energy histogram (TrimVacEnergyCount, apps/src/
+                             TrimVacEnergyCount.C:32-53): rows int(ln E) of the displaced
+                             recoil's energy (below 0 in row 0), hist_vac_n depth columns
+                             each; 0 = none; appended after the lateral bins */
 } mtg_sim;
 
 /* Run-wide settings (SimconfType scalars, simconf.h:66). */
@@ -163,6 +167,9 @@ typedef struct
   long long sputtered, backscattered; /* recoils / primaries lost through x < 0 */
   double Esputtered;                  /* kinetic energy carried out by sputtered atoms */
   double Evoxel;                      /* energy deposited inside the voxel box */
+  long long hist_dropped;             /* vacancy, replacement or vacancy-energy events past the
+                                         last depth bin or energy row (the reference grows its
+                                         histograms instead; rerun with more bins to keep them) */
 } mtg_totals;
 
 /* Per-member trajectory summary (replay checks). */
@@ -216,7 +223,8 @@ mtg_status mtg_configure(mtg_ctx * ctx, const mtg_config * cfg);
 /* Run n_sims simulations to completion (full cascades), host in, host out.
  * totals: n_sims entries.  hist: NULL or, per simulation in order, hist_range_n
  * range bins, then hist_vac_n vacancy bins, then hist_vac_n replacement bins, then
- * hist_lateral_n^2 lateral bins (z major).
+ * hist_lateral_n^2 lateral bins (z major), then hist_evac_rows x hist_vac_n
+ * vacancy-energy bins (row major).
  * Replaces: the cascade loop computeThread (runmytrim.C:71-93) over
  * TrimBase::trim (trim.C:36-425) with the tally plugins (apps/src/Trim*.C). */
 mtg_status mtg_run(mtg_ctx * ctx, const mtg_sim * sims, int n_sims, mtg_totals * totals,
@@ -248,6 +256,49 @@ mtg_status mtg_get_voxels(mtg_ctx * ctx, int sim, float * out, long long n);
 mtg_status mtg_set_record_capacity(mtg_ctx * ctx, long long capacity);
 mtg_status mtg_get_records(mtg_ctx * ctx, mtg_member_record * out, long long capacity,
                            long long * n_written);
+
+/* ---- event log: one record per hook call of the selected kinds ----
+ * The reference streams such events from its hooks: TrimDefectLog (vacancies and
+ * the rest states, trim.C:467-483), TrimPhononOut (binding energy of followed
+ * recoils, dissipated recoil energy and residual energy of stopped members,
+ * trim.C:504-527) and TrimRange (x of every dissipated recoil by Z,
+ * apps/src/TrimRange.C:49-54).  Here the cascade kernel appends them to a device
+ * buffer; the order of the records is not defined (sort them by primary, key).
+ * Members are identified by their path key instead of the reference's sequential
+ * _id. */
+typedef enum
+{
+  MTG_EV_VACANCY = 1,     /* vacancyCreation: the displaced recoil (position, energy E after
+                             the binding energy, Z of the target atom, its generation) */
+  MTG_EV_REPLACEMENT = 2, /* replacementCollision: the displaced recoil */
+  MTG_EV_BRANCH = 3,      /* followRecoil: a displaced recoil (whether followed or not);
+                             aux = binding energy left at its site */
+  MTG_EV_DISSIPATE = 4,   /* dissipateRecoilEnergy: a recoil below the displacement energy;
+                             E = its energy, aux = binding energy (E + aux stays there) */
+  MTG_EV_REST = 5,        /* checkPKAState: the member came to rest; state = 1 replacement,
+                             2 substitutional, 3 interstitial; E = residual energy */
+  MTG_EV_LOST = 6         /* the member left through a CUT boundary; aux = energy of the
+                             recoil dropped with it */
+} mtg_event_kind;
+
+typedef struct
+{
+  double x, y, z;          /* position [length unit] */
+  double E, aux;           /* energies [eV], meaning by kind */
+  unsigned long long key;  /* path key of the member that raised the event */
+  long long primary;       /* primary index within its simulation (first_primary based) */
+  int sim, kind, Z, gen, state, pad;
+} mtg_event;
+
+/* Log events of the kinds whose bit (1 << kind) is set in kind_mask (0 disables)
+ * in subsequent runs, up to `capacity` records; a run that raises more fails with
+ * MTG_ERR_QUEUE_FULL after its tallies are complete.  Logging costs one global
+ * atomic per event. */
+mtg_status mtg_set_event_log(mtg_ctx * ctx, unsigned int kind_mask, long long capacity);
+/* Copy the last run's records; *n_total receives the number logged (may exceed the
+ * capacity when the log overflowed), *n_written the number copied. */
+mtg_status mtg_get_events(mtg_ctx * ctx, mtg_event * out, long long capacity, long long * n_written,
+                          long long * n_total);
 
 /* Electronic stopping [eV/Angstrom] of ion (Z1, m1) in `material` at n energies,
  * evaluated on the GPU in FP64 (precision MTG_PREC_FP64) or through the FP32

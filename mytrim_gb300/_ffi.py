@@ -54,7 +54,7 @@ class Sim(C.Structure):
                 ("primaries_only", C.c_int), ("hist_range_bin", C.c_double), ("hist_range_n", C.c_int),
                 ("hist_vac_bin", C.c_double), ("hist_vac_n", C.c_int), ("surface_binding", C.c_double),
                 ("voxel_n", C.c_int * 3), ("voxel_origin", C.c_double * 3), ("voxel_size", C.c_double * 3),
-                ("hist_lateral_bin", C.c_double), ("hist_lateral_n", C.c_int)]
+                ("hist_lateral_bin", C.c_double), ("hist_lateral_n", C.c_int), ("hist_evac_rows", C.c_int)]
 
 
 class Config(C.Structure):
@@ -72,7 +72,8 @@ class Totals(C.Structure):
                                           "vac_s2", "eel_s2", "enuc_s2", "coll_s2")] + \
                [(n, C.c_longlong) for n in ("newton_iterations", "rejection_passes", "surrogate_fallbacks",
                                             "sputtered", "backscattered")] + \
-               [(n, C.c_double) for n in ("Esputtered", "Evoxel")]
+               [(n, C.c_double) for n in ("Esputtered", "Evoxel")] + \
+               [("hist_dropped", C.c_longlong)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -82,6 +83,16 @@ class MemberRecord(C.Structure):
     _fields_ = [("key", C.c_ulonglong), ("sim", C.c_int), ("species", C.c_int), ("gen", C.c_int),
                 ("state", C.c_int), ("ncoll", C.c_uint), ("nvac", C.c_uint), ("E", C.c_double),
                 ("x", C.c_double), ("y", C.c_double), ("z", C.c_double), ("eel", C.c_double)]
+
+
+class Event(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("x", "y", "z", "E", "aux")] + \
+               [("key", C.c_ulonglong), ("primary", C.c_longlong)] + \
+               [(n, C.c_int) for n in ("sim", "kind", "Z", "gen", "state", "pad")]
+
+
+# event kinds (mtg_event_kind)
+EV_VACANCY, EV_REPLACEMENT, EV_BRANCH, EV_DISSIPATE, EV_REST, EV_LOST = 1, 2, 3, 4, 5, 6
 
 
 class SurrogateConfig(C.Structure):
@@ -123,6 +134,9 @@ SIGNATURES = {
     "mtg_get_voxels": (C.c_int, [_P, C.c_int, C.POINTER(C.c_float), C.c_longlong]),
     "mtg_set_record_capacity": (C.c_int, [_P, C.c_longlong]),
     "mtg_get_records": (C.c_int, [_P, C.POINTER(MemberRecord), C.c_longlong, C.POINTER(C.c_longlong)]),
+    "mtg_set_event_log": (C.c_int, [_P, C.c_uint, C.c_longlong]),
+    "mtg_get_events": (C.c_int, [_P, C.POINTER(Event), C.c_longlong, C.POINTER(C.c_longlong),
+                                 C.POINTER(C.c_longlong)]),
     "mtg_stopping": (C.c_int, [_P, C.c_int, C.c_double, C.POINTER(Material), C.POINTER(C.c_double),
                                C.c_longlong, C.c_int, C.POINTER(C.c_double)]),
     "mtg_scatter": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_longlong, C.c_int,

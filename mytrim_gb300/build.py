@@ -68,6 +68,7 @@ def build(verbose=False, force=False):
     if not force and out.exists():
         newest = max(p.stat().st_mtime for p in srcs + headers + [Path(__file__)])
         if out.stat().st_mtime >= newest:
+            build_frontend()
             return out
     OUT_DIR.mkdir(exist_ok=True)
     OBJ_DIR.mkdir(exist_ok=True)
@@ -85,7 +86,32 @@ def build(verbose=False, force=False):
     if verbose:
         for (u, _), (_, log) in zip(units, results):
             sys.stderr.write(f"== {u}\n{log}")
+    build_frontend(force=True)
     return out
+
+
+FRONTEND_SRC = PKG / "cpp" / "runmytrim_gpu.cpp"
+
+
+def frontend_path():
+    return OUT_DIR / "runmytrim_gpu"
+
+
+def build_frontend(force=False):
+    """Compile the runmytrim front-end (host C++ over the C ABI) next to the library."""
+    exe = frontend_path()
+    deps = [FRONTEND_SRC, PKG / "cpp" / "json_lite.h", INCLUDE / "mytrim_gpu.h", lib_path()]
+    if not force and exe.exists() and exe.stat().st_mtime >= max(p.stat().st_mtime for p in deps):
+        return exe
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    tmp = exe.with_suffix(".tmp")
+    cmd = [cxx, "-O2", "-std=c++17", f"-I{INCLUDE}", f"-I{PKG / 'cpp'}", "-o", str(tmp), str(FRONTEND_SRC),
+           f"-L{OUT_DIR}", "-lmytrim_gpu", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"runmytrim_gpu build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, exe)
+    return exe
 
 
 if __name__ == "__main__":

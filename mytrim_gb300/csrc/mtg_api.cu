@@ -57,6 +57,7 @@ enum Counter
   C_OVF0 = 64, // overflow counts of the two ping-pong lists
   C_OVF1 = 65,
   C_NREC = 66,
+  C_NEV = 67,
   C_COUNT = 68
 };
 constexpr int MAX_PASSES = 64;
@@ -82,7 +83,7 @@ struct mtg_ctx
   DevBuf d_vox, d_vox_range, d_vox_sum; // energy-deposition voxels
   bool sg_ready = false;
   DevBuf p_vac, p_coll, p_eel, p_enuc, p_fx, p_fy, p_fz, p_state;
-  DevBuf d_totals, d_hist, d_err, d_counters, d_stacks, d_ovf0, d_ovf1, d_records;
+  DevBuf d_totals, d_hist, d_err, d_counters, d_stacks, d_ovf0, d_ovf1, d_records, d_events;
   DevBuf d_jobs, d_job_first, d_partials, d_out;
   DevBuf d_tmp0, d_tmp1, d_tmp2, d_tmp3;
   std::vector<ReduceJob> jobs;
@@ -94,6 +95,8 @@ struct mtg_ctx
   int stack_cap = 0;
   long long ovf_cap = 0;
   long long record_cap = 0;
+  long long event_cap = 0;
+  unsigned int event_mask = 0;
   int passes = 0; // cascade passes launched for the current run
   int ovf_last = 0;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -175,8 +178,10 @@ setup_launch_shape(mtg_ctx * ctx)
   const size_t slot = prec == MTG_PREC_FP64 ? cold_slot_bytes64() : cold_slot_bytes32();
   ctx->smem = size_t(ctx->cold_offset) + slot * size_t(ctx->block);
   int bps = 0;
-  cudaError_t e = prec == MTG_PREC_FP64 ? occupancy64(ctx->block, ctx->smem, &bps)
-                                        : occupancy32(ctx->block, ctx->smem, &bps, prec == MTG_PREC_FP32_SURROGATE);
+  const int events = ctx->event_cap > 0 && ctx->event_mask ? 1 : 0;
+  cudaError_t e = prec == MTG_PREC_FP64
+                      ? occupancy64(ctx->block, ctx->smem, &bps, events)
+                      : occupancy32(ctx->block, ctx->smem, &bps, prec == MTG_PREC_FP32_SURROGATE, events);
   if (e != cudaSuccess)
     return fail(ctx, MTG_ERR_CUDA, std::string("occupancy query: ") + cudaGetErrorString(e));
   if (bps < 1)
@@ -259,6 +264,14 @@ fill_params(mtg_ctx * ctx, EngineParams & prm)
     prm.n_records = ptr<unsigned long long>(ctx->d_counters) + C_NREC;
     prm.records_cap = ctx->record_cap;
   }
+  if (ctx->event_cap > 0 && ctx->event_mask)
+  {
+    prm.events = ptr<EventRec>(ctx->d_events);
+    prm.n_events = ptr<unsigned long long>(ctx->d_counters) + C_NEV;
+    prm.events_cap = ctx->event_cap;
+    prm.event_mask = ctx->event_mask;
+  }
+  prm.any_evac = t.any_evac;
 }
 
 // Launch cascade pass `pass` (0 = fresh primaries, >0 = drain of the previous
@@ -383,7 +396,8 @@ mtg_destroy(mtg_ctx * ctx)
                      &ctx->d_stop,   &ctx->p_vac,      &ctx->p_coll,    &ctx->p_eel,     &ctx->p_enuc,
                      &ctx->p_fx,     &ctx->p_fy,       &ctx->p_fz,      &ctx->p_state,   &ctx->d_totals,
                      &ctx->d_hist,   &ctx->d_err,      &ctx->d_counters, &ctx->d_stacks, &ctx->d_ovf0,
-                     &ctx->d_ovf1,   &ctx->d_records,  &ctx->d_jobs,    &ctx->d_job_first, &ctx->d_partials,
+                     &ctx->d_ovf1,   &ctx->d_records,  &ctx->d_events,  &ctx->d_jobs,    &ctx->d_job_first,
+                     &ctx->d_partials,
                      &ctx->d_out,    &ctx->d_tmp0,     &ctx->d_tmp1,    &ctx->d_tmp2,    &ctx->d_tmp3,
                      &ctx->d_species32, &ctx->d_mats32, &ctx->d_sims32, &ctx->d_sg_params, &ctx->d_sg_net,
                      &ctx->d_vox,    &ctx->d_vox_range, &ctx->d_vox_sum};
@@ -549,6 +563,8 @@ mtg_prepare(mtg_ctx * ctx, const mtg_sim * sims, int n_sims)
   }
   if (ctx->record_cap > 0)
     CK(ensure(ctx->d_records, sizeof(MemberRecord) * size_t(ctx->record_cap)));
+  if (ctx->event_cap > 0 && ctx->event_mask)
+    CK(ensure(ctx->d_events, sizeof(EventRec) * size_t(ctx->event_cap)));
   st = setup_launch_shape(ctx);
   if (st != MTG_OK)
     return st;
@@ -708,6 +724,7 @@ mtg_collect(mtg_ctx * ctx, mtg_totals * totals, long long * hist)
       o.backscattered = (long long)tot[s].backscattered;
       o.Esputtered = tot[s].Esputtered;
       o.Evoxel = vsum[s];
+      o.hist_dropped = (long long)tot[s].hist_dropped;
       coll_all += o.collisions;
     }
   ctx->stats.collisions = coll_all;
@@ -723,7 +740,8 @@ mtg_collect(mtg_ctx * ctx, mtg_totals * totals, long long * hist)
                      &ctx->d_stop,   &ctx->p_vac,      &ctx->p_coll,    &ctx->p_eel,     &ctx->p_enuc,
                      &ctx->p_fx,     &ctx->p_fy,       &ctx->p_fz,      &ctx->p_state,   &ctx->d_totals,
                      &ctx->d_hist,   &ctx->d_err,      &ctx->d_counters, &ctx->d_stacks, &ctx->d_ovf0,
-                     &ctx->d_ovf1,   &ctx->d_records,  &ctx->d_jobs,    &ctx->d_job_first, &ctx->d_partials,
+                     &ctx->d_ovf1,   &ctx->d_records,  &ctx->d_events,  &ctx->d_jobs,    &ctx->d_job_first,
+                     &ctx->d_partials,
                      &ctx->d_out,    &ctx->d_species32, &ctx->d_mats32, &ctx->d_sims32, &ctx->d_vox};
   for (DevBuf * b : bufs)
     bytes += b->bytes;
@@ -731,6 +749,9 @@ mtg_collect(mtg_ctx * ctx, mtg_totals * totals, long long * hist)
 
   if (unfinished || (errf & ERRB_QUEUE_FULL))
     return fail(ctx, MTG_ERR_QUEUE_FULL, "recoil overflow list exhausted; results incomplete");
+  if (errf & ERRB_EVENTS_FULL)
+    return fail(ctx, MTG_ERR_QUEUE_FULL,
+                "event log capacity " + std::to_string(ctx->event_cap) + " exceeded; the tallies are complete");
   if (errf & ERRB_BUDGET)
     return fail(ctx, MTG_ERR_TIMEOUT, "a cascade member exceeded the collision budget");
   if (errf & ERRB_NUMERIC)
@@ -834,6 +855,44 @@ mtg_get_records(mtg_ctx * ctx, mtg_member_record * out, long long capacity, long
   *n_written = m;
   if ((long long)n > ctx->record_cap)
     return fail(ctx, MTG_ERR_QUEUE_FULL, "record buffer too small; records truncated");
+  return MTG_OK;
+}
+
+mtg_status
+mtg_set_event_log(mtg_ctx * ctx, unsigned int kind_mask, long long capacity)
+{
+  if (!ctx)
+    return MTG_ERR_BAD_INPUT;
+  if (capacity < 0 || (kind_mask & ~0x7eu))
+    return fail(ctx, MTG_ERR_BAD_INPUT, "event kinds are 1..6 and the capacity must not be negative");
+  ctx->event_cap = capacity;
+  ctx->event_mask = kind_mask;
+  ctx->prepared = false;
+  return MTG_OK;
+}
+
+mtg_status
+mtg_get_events(mtg_ctx * ctx, mtg_event * out, long long capacity, long long * n_written, long long * n_total)
+{
+  mtg_status st = require_device(ctx);
+  if (st != MTG_OK)
+    return st;
+  if ((capacity > 0 && !out) || capacity < 0 || !n_written)
+    return fail(ctx, MTG_ERR_BAD_INPUT, "bad event buffer");
+  *n_written = 0;
+  if (n_total)
+    *n_total = 0;
+  if (ctx->event_cap <= 0 || !ctx->event_mask || !ctx->launched)
+    return MTG_OK;
+  unsigned long long n = 0;
+  CK(cudaMemcpy(&n, ptr<unsigned long long>(ctx->d_counters) + C_NEV, 8, cudaMemcpyDeviceToHost));
+  static_assert(sizeof(mtg_event) == sizeof(EventRec), "event layout");
+  const long long m = std::min<long long>((long long)n, std::min(capacity, ctx->event_cap));
+  if (m > 0)
+    CK(cudaMemcpy(out, ctx->d_events.p, sizeof(EventRec) * m, cudaMemcpyDeviceToHost));
+  *n_written = m;
+  if (n_total)
+    *n_total = (long long)n;
   return MTG_OK;
 }
 

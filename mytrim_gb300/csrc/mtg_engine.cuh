@@ -85,6 +85,12 @@ struct EngineParams
   MemberRecord * records;
   unsigned long long * n_records;
   long long records_cap;
+  // optional event log (mask bit k selects EventKind k; 0 = off)
+  EventRec * events;
+  unsigned long long * n_events;
+  long long events_cap;
+  unsigned int event_mask;
+  int any_evac; // some simulation keeps a vacancy-energy histogram
 };
 
 __device__ __forceinline__ unsigned int
@@ -165,15 +171,16 @@ struct LaneCold
   unsigned int n_repl, n_inter, n_subst, n_lost, n_members, n_passes, n_fallbacks, n_sput, n_back;
   unsigned int m_vac;
   int m_state;
-  int pad;
+  unsigned int n_dropped; // depth-histogram events beyond the last bin
   Acc e_lost, e_unf, e_sput, m_eel;
   long long vcell; // pending voxel deposit: cell and value
   float vacc;
-  float pad2;
+  int evac_bin;    // vacancy-energy bin of the current collision (-1 = none)
 };
 
-// Device tally sink for one lane.
-template <class Pol>
+// Device tally sink for one lane.  EV: the kernel variant that feeds the event
+// log (the default variant carries no event code at all).
+template <class Pol, bool EV>
 struct LaneSink
 {
   using Acc = typename Pol::Acc;
@@ -196,7 +203,7 @@ struct LaneSink
   {
     LaneCold<Acc> & c = *cold;
     c.n_repl = c.n_inter = c.n_subst = c.n_lost = c.n_members = c.n_passes = c.n_fallbacks = 0;
-    c.n_sput = c.n_back = 0;
+    c.n_sput = c.n_back = c.n_dropped = 0;
     n_newton = 0;
     c.e_lost.reset();
     c.e_unf.reset();
@@ -213,6 +220,48 @@ struct LaneSink
     a_vac = a_coll = 0;
     a_eel.reset();
     a_enuc.reset();
+  }
+
+  // ---- event log (opt-in): one entry per selected hook call
+  __device__ void event(int kind, Real x, Real y, Real z, Real E, int Z, int gen, int state, Real aux,
+                        uint64_t key)
+  {
+    if (!(prm->event_mask & (1u << kind)))
+      return;
+    const unsigned long long slot = atomicAdd(prm->n_events, 1ull);
+    if ((long long)slot >= prm->events_cap)
+    {
+      atomicOr(prm->error_flags, ERRB_EVENTS_FULL);
+      return;
+    }
+    EventRec & r = prm->events[slot];
+    r.x = double(x);
+    r.y = double(y);
+    r.z = double(z);
+    r.E = double(E);
+    r.aux = double(aux);
+    r.key = key;
+    r.primary = gprim - sim->prim_begin + sim->key_offset;
+    r.sim = int(sim - prm->sims);
+    r.kind = kind;
+    r.Z = Z;
+    r.gen = gen;
+    r.state = state;
+    r.pad = 0;
+  }
+  // followRecoil (trim.C:362): a displaced recoil, followed or not
+  template <class R>
+  __device__ void branch(const R & rec, int Z2, Real Elbind, uint64_t key)
+  {
+    if constexpr (EV)
+      event(EV_BRANCH, Real(rec.x), Real(rec.y), Real(rec.z), Real(rec.E), Z2, rec.gen, 0, Elbind, key);
+  }
+  // dissipateRecoilEnergy (trim.C:397-401): a recoil below the displacement energy
+  template <class R>
+  __device__ void dissipate(const R & rec, Real Erec, int Z2, Real Elbind, uint64_t key)
+  {
+    if constexpr (EV)
+      event(EV_DISSIPATE, Real(rec.x), Real(rec.y), Real(rec.z), Erec, Z2, rec.gen, 0, Elbind, key);
   }
 
   // ---- events raised by the collision code (the reference's hooks, trim.h:72-84)
@@ -269,9 +318,11 @@ struct LaneSink
   // with it, trim.C:357); through the entrance surface a recoil counts as sputtered
   // when E cos^2 > E_surf, a primary as backscattered
   template <class P>
-  __device__ void lost(Real e, const P & p)
+  __device__ void lost(Real e, const P & p, int Z1)
   {
     LaneCold<Acc> & c = *cold;
+    if constexpr (EV)
+      event(EV_LOST, Real(p.x), Real(p.y), Real(p.z), Real(p.E), Z1, p.gen, ST_LOST, e - Real(p.E), p.key);
     ++c.n_lost;
     c.e_lost.add(e);
     c.m_state = ST_LOST;
@@ -288,14 +339,16 @@ struct LaneSink
   }
 
   template <class R, class E>
-  __device__ void vacancy(const R & rec, const E & el)
+  __device__ void vacancy(const R & rec, const E & el, Real Erec, uint64_t key)
   {
+    if constexpr (EV)
+      event(EV_VACANCY, Real(rec.x), Real(rec.y), Real(rec.z), Erec, el.Z2, rec.gen, 0, Real(el.Elbind), key);
     if (range_mode)
     {
       // TrimRange::vacancyCreation (apps/src/TrimRange.C:32-47): Kinchin-Pease
       // count of the displaced recoil, each increment truncated like the
       // reference's int accumulator
-      const Real Z = Real(el.Z2), m = Real(el.m2), Er = Real(rec.E);
+      const Real Z = Real(el.Z2), m = Real(el.m2), Er = Erec;
       const Real Ed = Real(el.Edisp);
       const Real ed = Real(0.0115) * powr(Z, Real(-7.0 / 3.0)) * Er;
       const Real kd = Real(0.1337) * powr(Z, Real(2.0 / 3.0)) / sqrt(m);
@@ -314,20 +367,42 @@ struct LaneSink
     }
     ++a_vac;
     ++cold->m_vac;
-    vac_bin = depth_bin(Real(rec.x), inv_vac_bin(), sim->hist_vac_n);
-    if (vac_bin >= 0)
-      vac_bin += int(sim->hist_vac_base);
+    const int b = depth_bin(Real(rec.x), inv_vac_bin(), sim->hist_vac_n);
+    if (b >= 0)
+    {
+      vac_bin = int(sim->hist_vac_base) + b;
+      if (sim->hist_evac_rows > 0)
+      {
+        // TrimVacEnergyCount::vacancyCreation (apps/src/TrimVacEnergyCount.C:32-53):
+        // row int(ln E) of the recoil energy, negative rows in row 0
+        int row = int(loge(Erec));
+        row = row < 0 ? 0 : row;
+        if (row < sim->hist_evac_rows)
+          cold->evac_bin = int(sim->hist_evac_base) + row * sim->hist_vac_n + b;
+        else
+          ++cold->n_dropped;
+      }
+    }
+    else if (b == BIN_BEYOND)
+      ++cold->n_dropped;
   }
-  __device__ void replacement(Real x)
+  template <class R, class E>
+  __device__ void replacement(const R & rec, const E & el, Real Erec, uint64_t key)
   {
+    if constexpr (EV)
+      event(EV_REPLACEMENT, Real(rec.x), Real(rec.y), Real(rec.z), Erec, el.Z2, rec.gen, 0, Real(el.Elbind), key);
     ++cold->n_repl;
-    repl_bin = depth_bin(x, inv_vac_bin(), sim->hist_vac_n);
-    if (repl_bin >= 0)
-      repl_bin += int(sim->hist_vac_base + sim->hist_vac_n);
+    const int b = depth_bin(Real(rec.x), inv_vac_bin(), sim->hist_vac_n);
+    if (b >= 0)
+      repl_bin = int(sim->hist_vac_base + sim->hist_vac_n) + b;
+    else if (b == BIN_BEYOND)
+      ++cold->n_dropped;
   }
   template <class P>
-  __device__ void stop(int state, const P & p)
+  __device__ void stop(int state, const P & p, int Z1)
   {
+    if constexpr (EV)
+      event(EV_REST, Real(p.x), Real(p.y), Real(p.z), Real(p.E), Z1, p.gen, state, Real(0), p.key);
     cold->m_state = state;
     a_enuc.add(Real(p.E));
     deposit(Real(p.x), Real(p.y), Real(p.z), Real(p.E));
@@ -356,13 +431,24 @@ struct LaneSink
   }
 
   // truncation toward zero like int(x) in the reference (TrimVacCount.C:36-39),
-  // in the engine's own precision
+  // in the engine's own precision; BIN_BEYOND past the last bin, -1 before the
+  // first (where the reference drops the event too) or without a histogram
+  static constexpr int BIN_BEYOND = -2;
   static __device__ int depth_bin(Real x, Real inv_bin, int n)
   {
     const Real q = x * inv_bin;
-    if (n <= 0 || !(q > Real(-1)) || q >= Real(n))
+    if (n <= 0 || !(q > Real(-1)))
       return -1;
+    if (q >= Real(n))
+      return BIN_BEYOND;
     return int(q);
+  }
+  static __device__ Real loge(Real x)
+  {
+    if constexpr (sizeof(Real) == sizeof(float))
+      return __logf(x);
+    else
+      return log64(x);
   }
   __device__ Real inv_vac_bin() const
   {
@@ -433,6 +519,8 @@ struct LaneSink
       atomicAdd(&t->backscattered, ull(c.n_back));
     if (c.e_sput.nonzero())
       c.e_sput.atomic_add_to(&t->Esputtered);
+    if (c.n_dropped)
+      atomicAdd(&t->hist_dropped, ull(c.n_dropped));
     reset_sim();
   }
 };
@@ -451,7 +539,7 @@ warp_hist_add(unsigned long long * hist, int bin)
   }
 }
 
-template <class Pol>
+template <class Pol, bool EV>
 __global__ void __launch_bounds__(128, Pol::MIN_BLOCKS)
 cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
 {
@@ -485,10 +573,11 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
   const SimDesc * sim = nullptr;
   typename Pol::MemberCtx mctx;
 
-  LaneSink<Pol> sink;
+  LaneSink<Pol, EV> sink;
   sink.cold = reinterpret_cast<LaneCold<typename Pol::Acc> *>(smem + prm.cold_offset) + threadIdx.x;
   sink.cold->vcell = -1;
   sink.cold->vacc = 0.0f;
+  sink.cold->evac_bin = -1;
   sink.prm = &prm;
   sink.sim = nullptr;
   sink.gprim = -1;
@@ -624,6 +713,11 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
     }
     warp_hist_add(prm.hist, sink.vac_bin);
     warp_hist_add(prm.hist, sink.repl_bin);
+    if (prm.any_evac)
+    {
+      warp_hist_add(prm.hist, sink.cold->evac_bin);
+      sink.cold->evac_bin = -1;
+    }
 
     // ---- push displaced recoils onto the warp stack
     const bool push = (flags & CF_PUSH) != 0;

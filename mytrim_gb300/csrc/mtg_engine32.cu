@@ -362,7 +362,7 @@ struct Fp32Policy
       for (int i = 0; i < 3; ++i)
         if (sim.bc[i] == 2 && (pos[i] > sim.w[i] || pos[i] < 0.0f))
         {
-          sink.lost(p.E + p.El + den, p);
+          sink.lost(p.E + p.El + den, p, m.sc->Z1);
           return CF_DONE;
         }
     }
@@ -373,6 +373,7 @@ struct Fp32Policy
     if (recE > el.disp_thresh)
     {
       sink.enuc(el.Elbind, rec.x, rec.y, rec.z);
+      sink.branch(rec, el.Z2, el.Elbind, p.key);
       const bool follow = sim.range_mode ? (rec.gen < 1) : !sim.primaries_only;
       if (follow)
       {
@@ -386,15 +387,16 @@ struct Fp32Policy
       else
         sink.unfollowed(recE);
       if (p.E > el.Edisp)
-        sink.vacancy(rec, el);
+        sink.vacancy(rec, el, recE, p.key);
       else
       {
-        sink.replacement(rec.x);
+        sink.replacement(rec, el, recE, p.key);
         state = (m.sc->Z1 == el.Z2) ? ST_REPLACEMENT : ST_SUBSTITUTIONAL;
       }
     }
     else
     {
+      sink.dissipate(rec, recE, el.Z2, el.Elbind, p.key);
       sink.enuc(den, rec.x, rec.y, rec.z);
       if (p.E < sim.Ef)
         state = ST_INTERSTITIAL;
@@ -403,7 +405,7 @@ struct Fp32Policy
     {
       p.E += p.El;
       p.El = 0.0f;
-      sink.stop(state, p);
+      sink.stop(state, p, m.sc->Z1);
       flags |= CF_DONE;
     }
     else if (!(p.E == p.E))
@@ -427,37 +429,47 @@ launch_cascade32(const EngineParams & prm, const Fp32Tables & t, int grid, int b
   tabs.lnE_min = t.lnE_min;
   tabs.inv_dlnE = t.inv_dlnE;
   tabs.net = reinterpret_cast<const SurrogateNet *>(t.mlp);
-  if (surrogate)
-    cascade_kernel<Fp32Policy<true>><<<grid, block, smem, st>>>(prm, tabs);
+  const bool ev = prm.event_mask != 0;
+  if (surrogate && ev)
+    cascade_kernel<Fp32Policy<true>, true><<<grid, block, smem, st>>>(prm, tabs);
+  else if (surrogate)
+    cascade_kernel<Fp32Policy<true>, false><<<grid, block, smem, st>>>(prm, tabs);
+  else if (ev)
+    cascade_kernel<Fp32Policy<false>, true><<<grid, block, smem, st>>>(prm, tabs);
   else
-    cascade_kernel<Fp32Policy<false>><<<grid, block, smem, st>>>(prm, tabs);
+    cascade_kernel<Fp32Policy<false>, false><<<grid, block, smem, st>>>(prm, tabs);
   return cudaGetLastError();
 }
 
-cudaError_t
-occupancy32(int block, size_t smem, int * blocks_per_sm, int surrogate)
+template <class K>
+static cudaError_t
+occupancy_of(K kernel, int block, size_t smem, int * blocks_per_sm)
 {
-  if (surrogate)
-  {
-    if (smem > 48 * 1024)
-    {
-      cudaError_t e = cudaFuncSetAttribute(cascade_kernel<Fp32Policy<true>>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-      if (e != cudaSuccess)
-        return e;
-    }
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, cascade_kernel<Fp32Policy<true>>, block,
-                                                         smem);
-  }
   if (smem > 48 * 1024)
   {
-    cudaError_t e = cudaFuncSetAttribute(cascade_kernel<Fp32Policy<false>>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess)
       return e;
   }
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, cascade_kernel<Fp32Policy<false>>, block,
-                                                       smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kernel, block, smem);
+}
+
+// residency of the variant the launch will use (both variants get the shared-memory opt-in)
+cudaError_t
+occupancy32(int block, size_t smem, int * blocks_per_sm, int surrogate, int events)
+{
+  int other = 0;
+  if (surrogate)
+  {
+    cudaError_t e = occupancy_of(cascade_kernel<Fp32Policy<true>, true>, block, smem, events ? blocks_per_sm : &other);
+    if (e != cudaSuccess)
+      return e;
+    return occupancy_of(cascade_kernel<Fp32Policy<true>, false>, block, smem, events ? &other : blocks_per_sm);
+  }
+  cudaError_t e = occupancy_of(cascade_kernel<Fp32Policy<false>, true>, block, smem, events ? blocks_per_sm : &other);
+  if (e != cudaSuccess)
+    return e;
+  return occupancy_of(cascade_kernel<Fp32Policy<false>, false>, block, smem, events ? &other : blocks_per_sm);
 }
 
 size_t

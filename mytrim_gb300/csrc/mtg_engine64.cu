@@ -93,22 +93,35 @@ struct Fp64Policy
 cudaError_t
 launch_cascade64(const EngineParams & prm, int grid, int block, size_t smem, cudaStream_t st)
 {
-  cascade_kernel<Fp64Policy><<<grid, block, smem, st>>>(prm, Fp64Policy::Tables{prm.species, prm.mats});
+  if (prm.event_mask)
+    cascade_kernel<Fp64Policy, true><<<grid, block, smem, st>>>(prm, Fp64Policy::Tables{prm.species, prm.mats});
+  else
+    cascade_kernel<Fp64Policy, false><<<grid, block, smem, st>>>(prm, Fp64Policy::Tables{prm.species, prm.mats});
   return cudaGetLastError();
 }
 
-cudaError_t
-occupancy64(int block, size_t smem, int * blocks_per_sm)
+template <class K>
+static cudaError_t
+occupancy_of(K kernel, int block, size_t smem, int * blocks_per_sm)
 {
   if (smem > 48 * 1024)
   {
-    cudaError_t e = cudaFuncSetAttribute(cascade_kernel<Fp64Policy>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess)
       return e;
   }
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, cascade_kernel<Fp64Policy>,
-                                                       block, smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kernel, block, smem);
+}
+
+// residency of the variant the launch will use (both variants get the shared-memory opt-in)
+cudaError_t
+occupancy64(int block, size_t smem, int * blocks_per_sm, int events)
+{
+  int other = 0;
+  cudaError_t e = occupancy_of(cascade_kernel<Fp64Policy, true>, block, smem, events ? blocks_per_sm : &other);
+  if (e != cudaSuccess)
+    return e;
+  return occupancy_of(cascade_kernel<Fp64Policy, false>, block, smem, events ? &other : blocks_per_sm);
 }
 
 size_t

@@ -436,6 +436,16 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
     }
     d.hist_lat_base = hist + s.hist_range_n + 2LL * s.hist_vac_n;
     hist += s.hist_range_n + 2LL * s.hist_vac_n + (long long)s.hist_lateral_n * s.hist_lateral_n;
+    if (s.hist_evac_rows < 0 || s.hist_evac_rows > 64)
+    {
+      err = "hist_evac_rows must be 0..64";
+      return MTG_ERR_BAD_INPUT;
+    }
+    d.hist_evac_rows = s.hist_vac_n > 0 ? s.hist_evac_rows : 0;
+    d.hist_evac_base = hist;
+    hist += (long long)d.hist_evac_rows * s.hist_vac_n;
+    if (d.hist_evac_rows > 0)
+      out.any_evac = 1;
     prim += s.n_primaries;
     out.prim_end.push_back(prim);
     out.sims.push_back(d);
@@ -444,6 +454,12 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
   if (prim > 0xffffffffLL)
   {
     err = "at most 2^32 - 1 primaries per run";
+    return MTG_ERR_BAD_INPUT;
+  }
+  if (hist >= (1LL << 31))
+  {
+    // bins are addressed with 32-bit indices on the device
+    err = "histograms of one run must hold fewer than 2^31 bins";
     return MTG_ERR_BAD_INPUT;
   }
   out.total_primaries = prim;

@@ -23,6 +23,7 @@ struct HostTables
   long long voxel_total = 0;              // cells of the concatenated voxel grids
   uint32_t k0 = 0, k1 = 0;                // Philox key
   double emax = 0.0;                      // largest primary energy
+  int any_evac = 0;                       // some simulation keeps a vacancy-energy histogram
 };
 
 // Build the tables; returns MTG_OK or MTG_ERR_BAD_INPUT with `err` set.

@@ -119,6 +119,10 @@ struct SimDesc
   int hist_lat_n;
   float inv_hist_lat_bin, lat_y0, lat_z0; // y0, z0: lower corner of the histogram
   long long hist_lat_base;
+  // vacancy-energy histogram (TrimVacEnergyCount): rows by int(ln E) of the
+  // recoil, columns the vacancy depth bins
+  int hist_evac_rows;
+  long long hist_evac_base;
 };
 
 // Totals per simulation (device accumulators, reduced on the host).
@@ -129,6 +133,27 @@ struct SimTotals
   double Elost, Eunfollowed;
   unsigned long long sputtered, backscattered;
   double Esputtered;
+  unsigned long long hist_dropped; // depth-histogram events beyond the last bin
+};
+
+// One entry of the event log (layout of mtg_event).
+struct EventRec
+{
+  double x, y, z, E, aux;
+  uint64_t key;
+  long long primary;
+  int sim, kind, Z, gen, state, pad;
+};
+
+// event kinds (bit k of the log's mask selects kind k)
+enum EventKind : int
+{
+  EV_VACANCY = 1,
+  EV_REPLACEMENT = 2,
+  EV_BRANCH = 3,
+  EV_DISSIPATE = 4,
+  EV_REST = 5,
+  EV_LOST = 6
 };
 
 // ---- single-precision copies used by the FP32 engine (built from the tables above)
@@ -185,7 +210,8 @@ enum ErrorBits : unsigned int
   ERRB_QUEUE_FULL = 1u,
   ERRB_NUMERIC = 2u,
   ERRB_BUDGET = 4u,
-  ERRB_BAD_INDEX = 8u
+  ERRB_BAD_INDEX = 8u,
+  ERRB_EVENTS_FULL = 16u
 };
 
 } // namespace mtg

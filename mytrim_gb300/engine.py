@@ -62,6 +62,7 @@ class SimSpec:
     voxel_size: Tuple[float, float, float] = (0.0, 0.0, 0.0)
     hist_lateral_bin: float = 10.0       # lateral (y, z) histogram of stopping points
     hist_lateral_n: int = 0
+    hist_evac_rows: int = 0              # vacancy-energy histogram rows (int(ln E))
 
     def box(self):
         if self.size is not None:
@@ -75,7 +76,8 @@ class SimSpec:
         return (0.0, w[1] / 2.0, w[2] / 2.0)
 
     def hist_sizes(self):
-        return self.hist_range_n, self.hist_vac_n, self.hist_vac_n, self.hist_lateral_n ** 2
+        evac = self.hist_evac_rows * self.hist_vac_n if self.hist_vac_n > 0 else 0
+        return self.hist_range_n, self.hist_vac_n, self.hist_vac_n, self.hist_lateral_n ** 2, evac
 
     def to_c(self) -> F.Sim:
         if not 1 <= len(self.layers) <= F.MAX_LAYERS:
@@ -118,6 +120,7 @@ class SimSpec:
         s.surface_binding = self.surface_binding
         s.hist_lateral_bin = self.hist_lateral_bin
         s.hist_lateral_n = self.hist_lateral_n
+        s.hist_evac_rows = self.hist_evac_rows
         for i in range(3):
             s.voxel_n[i] = self.voxel_n[i]
             s.voxel_origin[i] = self.voxel_origin[i]
@@ -227,14 +230,15 @@ class Engine:
         off = 0
         for i, s in enumerate(self._sims):
             d = tot[i].as_dict()
-            hr, hv, hp, hl = s.hist_sizes()
+            hr, hv, hp, hl, he = s.hist_sizes()
             h = np.frombuffer(hist, dtype=np.int64, count=max(nh, 1))
             d["hist_range"] = h[off:off + hr].copy()
             d["hist_vac"] = h[off + hr:off + hr + hv].copy()
             d["hist_repl"] = h[off + hr + hv:off + hr + hv + hp].copy()
-            d["hist_lateral"] = h[off + hr + hv + hp:off + hr + hv + hp + hl].copy().reshape(
-                s.hist_lateral_n, s.hist_lateral_n)
-            off += hr + hv + hp + hl
+            o = off + hr + hv + hp
+            d["hist_lateral"] = h[o:o + hl].copy().reshape(s.hist_lateral_n, s.hist_lateral_n)
+            d["hist_evac"] = h[o + hl:o + hl + he].copy().reshape(s.hist_evac_rows if he else 0, hv if he else 0)
+            off += hr + hv + hp + hl + he
             d["status"] = st
             out.append(d)
         return out
@@ -276,6 +280,27 @@ class Engine:
                        ("z", "<f8"), ("eel", "<f8")])
         assert dt.itemsize == C.sizeof(F.MemberRecord)
         return np.frombuffer(bytes(buf)[: n.value * dt.itemsize], dtype=dt).copy()
+
+    def set_event_log(self, kinds, capacity: int):
+        """Log events of the given kinds (F.EV_* numbers) in subsequent runs."""
+        mask = 0
+        for k in kinds:
+            mask |= 1 << int(k)
+        self._check(self.lib.mtg_set_event_log(self.ctx, mask, capacity))
+        self._event_cap = capacity if mask else 0
+
+    def events(self) -> np.ndarray:
+        """The last run's event records as a structured array (unordered)."""
+        cap = getattr(self, "_event_cap", 0)
+        dt = np.dtype([("x", "<f8"), ("y", "<f8"), ("z", "<f8"), ("E", "<f8"), ("aux", "<f8"), ("key", "<u8"),
+                       ("primary", "<i8"), ("sim", "<i4"), ("kind", "<i4"), ("Z", "<i4"), ("gen", "<i4"),
+                       ("state", "<i4"), ("pad", "<i4")])
+        assert dt.itemsize == C.sizeof(F.Event)
+        out = np.zeros(max(cap, 1), dtype=dt)
+        n, total = C.c_longlong(0), C.c_longlong(0)
+        self._check(self.lib.mtg_get_events(self.ctx, out.ctypes.data_as(C.POINTER(F.Event)), cap, C.byref(n),
+                                            C.byref(total)))
+        return out[: n.value].copy()
 
     def stopping(self, Z1, m1, layer: LayerSpec, energies, precision="fp64") -> np.ndarray:
         e = np.ascontiguousarray(energies, dtype=np.float64)

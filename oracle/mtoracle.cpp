@@ -364,6 +364,7 @@ struct Engine
   std::vector<double> thick;
   double tmin = 0.2, tau = 0.0, cw = 0.001;
   runspec::Tally t;
+  runspec::PluginOut out; // runmytrim output plugin (spec key "output")
   // current primary
   long long p_vac = 0, p_coll = 0;
   double p_enuc = 0.0, p_eel = 0.0;
@@ -392,6 +393,8 @@ struct Engine
     t.hist_repl.assign(s.hist_vac_n, 0);
     t.spec = &s;
     t.vox_depth.assign(s.vox_n[0] > 0 ? s.vox_n[0] : 0, 0.0);
+    out.type = s.out_type;
+    out.base = s.out_base;
     pk0 = s.seed;
     pk1 = 0x4D795452u; // fixed high key word for single-simulation runs
   }
@@ -632,6 +635,7 @@ struct Engine
         else
         {
           const double e = rec.E + el.Elbind;
+          out.dissipate(rec.Z, rec.pos[0]);
           t.Enuc += e;
           p_enuc += e;
           t.deposit(rec.pos[0], rec.pos[1], rec.pos[2], e);
@@ -669,6 +673,7 @@ struct Engine
     }
     t.vacancies++;
     p_vac++;
+    out.vacancy(rec.pos[0], rec.E);
     const int b = runspec::bin_of(rec.pos[0], spec.hist_vac_bin, spec.hist_vac_n);
     if (b >= 0)
       t.hist_vac[b]++;
@@ -677,6 +682,7 @@ struct Engine
   void replacement(const Ion & rec)
   {
     t.replacements++;
+    out.replacement(rec.pos[0]);
     const int b = runspec::bin_of(rec.pos[0], spec.hist_vac_bin, spec.hist_vac_n);
     if (b >= 0)
       t.hist_repl[b]++;
@@ -809,5 +815,10 @@ main(int argc, char ** argv)
   auto t1 = std::chrono::steady_clock::now();
   eng.t.print(stdout);
   printf("wall_s %.6f\n", std::chrono::duration<double>(t1 - t0).count());
+  if (!spec.out_type.empty() && !eng.out.write())
+  {
+    fprintf(stderr, "mtoracle: cannot write %s output\n", spec.out_type.c_str());
+    return 1;
+  }
   return 0;
 }

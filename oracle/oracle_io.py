@@ -16,6 +16,7 @@ ORACLE_DIR = Path(__file__).resolve().parent
 REPO = ORACLE_DIR.parent
 MTORACLE = ORACLE_DIR / "_build" / "mtoracle"
 REF_DRIVER = ORACLE_DIR / "_ref" / "ref_driver"
+REF_RUNMYTRIM = ORACLE_DIR / "_ref" / "ref_runmytrim"
 TABLES = REPO / "mytrim_gb300" / "data" / "stopping_tables.tsv"
 
 SUM_KEYS = ("primaries", "members", "collisions", "vacancies", "replacements", "interstitials",
@@ -33,7 +34,7 @@ def build(reference_dir=None):
         subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "ref", f"REF={ref}"], check=True, env=env)
 
 
-def spec_text(sim, seed=1, philox=True, first=0, n=None, records=0, tmin=None):
+def spec_text(sim, seed=1, philox=True, first=0, n=None, records=0, tmin=None, output=None, scale=1.0):
     w = sim.box()
     p = sim.start()
     lines = [f"seed {seed}", f"seeding {'philox' if philox else 'compat'}",
@@ -53,6 +54,10 @@ def spec_text(sim, seed=1, philox=True, first=0, n=None, records=0, tmin=None):
         lines.append(f"subset {first} {n if n is not None else sim.n_primaries - first}")
     if records:
         lines.append(f"records {records}")
+    if output is not None:
+        lines.append(f"output {output[0]} {output[1]}")
+    if scale != 1.0:
+        lines.append(f"scale {scale!r}")
     if getattr(sim, "surface_binding", 0.0) > 0.0:
         lines.append(f"sputter {sim.surface_binding!r}")
     vn = getattr(sim, "voxel_n", (0, 0, 0))
@@ -95,6 +100,28 @@ def run(sim, seed=1, philox=True, first=0, n=None, records=0, reference=False, t
     if r.returncode != 0:
         raise RuntimeError(f"oracle failed: {r.stderr}")
     return parse(r.stdout)
+
+
+def write_outputs(sim, output_type, base, seed=1, philox=True, reference=False, cwd=None, timeout=None,
+                  scale=1.0):
+    """Run one oracle process that writes runmytrim's output file <base>_*.dat in
+    `cwd`: the restatement (mtoracle) or, with reference=True, the reference's own
+    plugins (oracle/_ref/ref_runmytrim, compat seeding only).  Returns the parsed
+    tallies (mtoracle only, else {}) and the stderr text (ref_runmytrim prints
+    runmytrim's summary lines there)."""
+    if reference:
+        args = [str(REF_RUNMYTRIM)]
+        exe = REF_RUNMYTRIM
+    else:
+        args = [str(MTORACLE), str(TABLES)]
+        exe = MTORACLE
+    if not exe.exists():
+        raise RuntimeError(f"{exe} is not built")
+    txt = spec_text(sim, seed=seed, philox=philox, output=(output_type, base), scale=scale)
+    r = subprocess.run(args, input=txt, capture_output=True, text=True, timeout=timeout, cwd=cwd)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle failed: {r.stderr}")
+    return (parse(r.stdout) if not reference else {}), r.stderr
 
 
 def merge(parts):

@@ -37,17 +37,25 @@ struct HostSink
   void numeric() {}
   void enuc(double, double, double, double) {}
   void unfollowed(double) {}
+  template <class R>
+  void branch(const R &, int, double, uint64_t)
+  {
+  }
+  template <class R>
+  void dissipate(const R &, double, int, double, uint64_t)
+  {
+  }
   template <class P>
-  void lost(double, const P &)
+  void lost(double, const P &, int)
   {
     m_state = ST_LOST;
   }
   template <class R, class E>
-  void vacancy(const R & rec, const E & el)
+  void vacancy(const R &, const E & el, double Erec, uint64_t)
   {
     if (range_mode)
     {
-      const double Z = double(el.Z2), m = el.m2, Er = double(rec.E);
+      const double Z = double(el.Z2), m = el.m2, Er = Erec;
       const double Ed = el.Edisp;
       const double ed = 0.0115 * pow64(Z, -7.0 / 3.0) * Er;
       const double kd = 0.1337 * pow64(Z, 2.0 / 3.0) / sqrt(m);
@@ -65,9 +73,12 @@ struct HostSink
     }
     ++m_vac;
   }
-  void replacement(double) {}
+  template <class R, class E>
+  void replacement(const R &, const E &, double, uint64_t)
+  {
+  }
   template <class P>
-  void stop(int state, const P &)
+  void stop(int state, const P &, int)
   {
     m_state = state;
   }

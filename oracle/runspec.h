@@ -25,11 +25,16 @@
 //   records <n>                 emit per-primary records for the first n primaries
 //   sputter <Esurf>             count recoils leaving through x < 0 with E cos^2 > Esurf
 //   voxels nx ny nz ox oy oz sx sy sz   energy-deposition voxel box (depth profile reported)
+//   output <type> <base>        write runmytrim's output file for type vaccount,
+//                               vacenergycount or range as <base>_vac.dat, _evac.dat
+//                               or _ranges.dat (runmytrim.C:185-206, 309)
 #pragma once
 
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <cmath>
+#include <algorithm>
 #include <string>
 #include <vector>
 #include <sstream>
@@ -77,6 +82,7 @@ struct Spec
   double esurf = 0.0;
   int vox_n[3] = {0, 0, 0};
   double vox_o[3] = {0, 0, 0}, vox_s[3] = {0, 0, 0};
+  std::string out_type, out_base;
 
   double total_thickness() const
   {
@@ -194,6 +200,9 @@ parse(std::istream & in, Spec & s, std::string & err)
       ok = bool(ls >> s.records);
     else if (key == "sputter")
       ok = bool(ls >> s.esurf);
+    else if (key == "output")
+      ok = bool(ls >> s.out_type >> s.out_base) &&
+           (s.out_type == "vaccount" || s.out_type == "vacenergycount" || s.out_type == "range");
     else if (key == "voxels")
       ok = bool(ls >> s.vox_n[0] >> s.vox_n[1] >> s.vox_n[2] >> s.vox_o[0] >> s.vox_o[1] >> s.vox_o[2] >>
                 s.vox_s[0] >> s.vox_s[1] >> s.vox_s[2]);
@@ -300,6 +309,123 @@ struct Tally
     for (double v : vox_depth)
       fprintf(f, " %.17g", v);
     fprintf(f, "\n");
+  }
+};
+
+// The tallies of runmytrim's three output plugins, grown on demand as the
+// reference grows them, and their file writers: a restatement of
+// apps/src/TrimVacCount.C:32-79, apps/src/TrimVacEnergyCount.C:32-81 and
+// apps/src/TrimRange.C:49-121 (same bins, same text through std::ostream).
+struct PluginOut
+{
+  std::string type, base;
+  std::vector<unsigned int> vac, repl;          // by int(x) of the recoil
+  std::vector<std::vector<unsigned int>> evac;  // by int(ln E) of the recoil, then int(x)
+  std::vector<std::vector<double>> range = std::vector<std::vector<double>>(112); // x by recoil Z
+
+  static void bump(std::vector<unsigned int> & h, int x)
+  {
+    if (x >= int(h.size()))
+      h.resize(x + 1, 0);
+    h[x]++;
+  }
+  // vacancyCreation of a TrimVacCount / TrimVacEnergyCount run
+  void vacancy(double rx, double rE)
+  {
+    const int x = int(rx);
+    if (x < 0)
+      return;
+    if (type == "vaccount")
+      bump(vac, x);
+    else if (type == "vacenergycount")
+    {
+      int e = int(std::log(rE));
+      e = e < 0 ? 0 : e;
+      if (e >= int(evac.size()))
+        evac.resize(e + 1);
+      bump(evac[e], x);
+    }
+  }
+  // replacementCollision of a TrimVacCount run
+  void replacement(double rx)
+  {
+    const int x = int(rx);
+    if (type == "vaccount" && x >= 0)
+      bump(repl, x);
+  }
+  // dissipateRecoilEnergy of a TrimRange run
+  void dissipate(int Z, double rx)
+  {
+    if (type == "range" && Z >= 0 && Z < int(range.size()))
+      range[Z].push_back(rx);
+  }
+
+  bool write() const
+  {
+    if (type == "vaccount")
+    {
+      const size_t n = std::max(vac.size(), repl.size());
+      std::ofstream out(base + "_vac.dat");
+      for (size_t x = 0; x < n; ++x)
+        out << x << ' ' << (x < vac.size() ? vac[x] : 0u) << ' ' << (x < repl.size() ? repl[x] : 0u) << '\n';
+      return bool(out);
+    }
+    if (type == "vacenergycount")
+    {
+      std::ofstream out(base + "_evac.dat");
+      for (size_t e = 0; e < evac.size(); ++e)
+      {
+        for (size_t x = 0; x < evac[e].size(); ++x)
+          out << e << ' ' << x << ' ' << evac[e][x] << '\n';
+        out << '\n';
+      }
+      return bool(out);
+    }
+    if (type == "range")
+    {
+      // histogram extent and bin width as TrimRange::writeOutput chooses them
+      unsigned int max_samples = 0;
+      double x_min = 0.0, x_max = 0.0;
+      for (auto & r : range)
+      {
+        if (r.size() > max_samples)
+          max_samples = (unsigned int)r.size();
+        for (double x : r)
+        {
+          x_min = std::min(x_min, x);
+          x_max = std::max(x_max, x);
+        }
+      }
+      std::ofstream out(base + "_ranges.dat");
+      out << "#x";
+      for (size_t Z = 0; Z < range.size(); ++Z)
+        if (!range[Z].empty())
+          out << " Z" << Z;
+      out << '\n';
+      const double xwidth = x_max - x_min;
+      if (max_samples == 0 || !(xwidth > 0.0))
+        return bool(out); // no extent: header only
+      const double bin = std::min(xwidth * 100.0 / max_samples, xwidth / 10.0);
+      const unsigned int nbin = (unsigned int)(xwidth / bin + 1);
+      std::vector<std::vector<unsigned int>> h;
+      for (auto & r : range)
+      {
+        if (r.empty())
+          continue;
+        h.emplace_back(nbin, 0u);
+        for (double x : r)
+          h.back()[(size_t)std::floor((x - x_min) / bin)]++;
+      }
+      for (unsigned int n = 0; n < nbin; ++n)
+      {
+        out << (n * bin + x_min);
+        for (auto & c : h)
+          out << ' ' << c[n];
+        out << '\n';
+      }
+      return bool(out);
+    }
+    return true;
   }
 };
 

@@ -319,3 +319,91 @@ def test_lateral_histogram(engine_lib):
     centres = (np.arange(300) + 0.5) * 10.0 - 1500.0
     my = (h.sum(axis=0) * centres).sum() / h.sum()
     assert abs(my - t["sy"] / t["range_n"]) < 5.0
+
+
+ALL_EVENTS = [F.EV_VACANCY, F.EV_REPLACEMENT, F.EV_BRANCH, F.EV_DISSIPATE, F.EV_REST, F.EV_LOST]
+
+
+def _cu_sim(n=200, E=5000.0, **kw):
+    return SimSpec(layers=[LayerSpec(1e5, 8.96, [ElementSpec(29, 63.546, 1.0, 25.0, 3.0)])], Z=29, m=63.546, E=E,
+                   n_primaries=n, hist_vac_bin=1.0, hist_vac_n=2000, **kw)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_event_log_matches_tallies(engine_lib, prec):
+    """Every hook call is logged once: counts and energies of the log add up to
+    the run's tallies, and the tallies do not change when the log is on."""
+    sim = _cu_sim()
+    e = Engine(precision=prec, seed=5)
+    t0 = e.run([sim])[0]
+    e.set_event_log(ALL_EVENTS, 10_000_000)
+    t = e.run([sim])[0]
+    ev = e.events()
+    e.close()
+    for key in ("vacancies", "replacements", "collisions", "members", "Eel", "Enuc"):
+        assert t[key] == t0[key], key
+    k = ev["kind"]
+    assert (k == F.EV_VACANCY).sum() == t["vacancies"]
+    assert (k == F.EV_REPLACEMENT).sum() == t["replacements"]
+    rest = ev[k == F.EV_REST]
+    assert (rest["state"] == 3).sum() == t["interstitials"]
+    assert (rest["state"] == 2).sum() == t["substitutionals"]
+    assert len(rest) + (k == F.EV_LOST).sum() == t["members"]
+    assert set(np.unique(ev["primary"])) == set(range(sim.n_primaries))
+    # TrimPhononOut's split of the nuclear deposit (trim.C:504-527): binding energy of
+    # every displaced recoil, dissipated recoils' energy plus binding, residual
+    # energy of the members that came to rest
+    enuc = (ev["aux"][k == F.EV_BRANCH].sum() + (ev["E"] + ev["aux"])[k == F.EV_DISSIPATE].sum()
+            + rest["E"].sum())
+    assert enuc == pytest.approx(t["Enuc"], rel=1e-9 if prec == "fp64" else 1e-5)
+    if prec == "fp64":
+        # the vacancy depth histogram from the logged recoil positions, int(x) bins
+        x = ev["x"][k == F.EV_VACANCY]
+        x = x[(x > -1.0) & (x < 2000.0)]
+        assert np.array_equal(np.bincount(np.trunc(x).astype(np.int64), minlength=2000), t["hist_vac"])
+
+
+def test_event_log_overflow_keeps_tallies(engine_lib):
+    sim = _cu_sim(n=100)
+    e = Engine(precision="fp32", seed=6)
+    t0 = e.run([sim])[0]
+    e.set_event_log([F.EV_DISSIPATE], 50)
+    with pytest.raises(F.EngineError) as err:
+        e.run([sim])
+    assert err.value.status == 4  # MTG_ERR_QUEUE_FULL
+    t = e.run([sim], check=False)[0]
+    assert len(e.events()) == 50
+    e.close()
+    for key in ("vacancies", "collisions", "Eel"):
+        assert t[key] == t0[key]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_vacancy_energy_histogram(engine_lib, prec):
+    """TrimVacEnergyCount rows: int(ln E) of the displaced recoil; summed over the
+    rows they give the vacancy depth histogram; rows past the last count as dropped."""
+    sim = SimSpec(layers=[LayerSpec(1e5, 2.33, [ElementSpec(14, 28.086, 1.0, 15.0, 3.0)])], Z=79, m=196.967,
+                  E=20000.0, n_primaries=60, hist_vac_bin=1.0, hist_vac_n=3000, hist_evac_rows=12)
+    e = Engine(precision=prec, seed=8)
+    e.set_event_log([F.EV_VACANCY], 10_000_000)
+    t = e.run([sim])[0]
+    ev = e.events()
+    h = t["hist_evac"]
+    assert h.shape == (12, 3000)
+    assert np.array_equal(h.sum(axis=0), t["hist_vac"])
+    assert t["hist_dropped"] == 0
+    x, E = ev["x"], ev["E"]
+    keep = (x > -1.0) & (x < 3000.0)
+    rows = np.maximum(np.trunc(np.log(E[keep])).astype(np.int64), 0)
+    ref = np.zeros_like(h)
+    np.add.at(ref, (rows, np.trunc(x[keep]).astype(np.int64)), 1)
+    if prec == "fp64":
+        assert np.array_equal(ref, h)
+    else:
+        assert np.abs(ref - h).sum() <= 1e-3 * h.sum() + 2  # float log at row edges
+    # two rows only: the higher-energy vacancies are dropped and counted
+    sim.hist_evac_rows = 2
+    t2 = e.run([sim])[0]
+    e.close()
+    assert t2["hist_evac"].sum() + t2["hist_dropped"] == t["hist_vac"].sum()
+    assert t2["hist_dropped"] == h[2:].sum()
