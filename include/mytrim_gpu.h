@@ -151,7 +151,8 @@ typedef struct
   int stack_capacity;    /* recoil stack entries per warp, 0 = default */
   int block_threads;     /* threads per block of the cascade kernel: 64 or 128, 0 = 128 */
   int max_primaries_per_refill; /* fresh primaries one warp takes at a time, 1..32;
-                                   0 = chosen from the batch size and the grid */
+                                   0 = chosen from the expected cascade size (one for
+                                   large cascades), the batch size and the grid */
 } mtg_config;
 
 /* Results of one simulation. */
@@ -194,6 +195,8 @@ typedef struct
   size_t device_bytes;     /* device memory held by the context */
   long long h2d_bytes;     /* host-to-device bytes of the last prepare */
   long long d2h_bytes;     /* device-to-host bytes of the last collect */
+  long long warp_steps;    /* collision-loop iterations of all warps in the last run; the
+                              lane occupancy is collisions / (32 warp_steps) */
 } mtg_stats;
 
 typedef struct mtg_ctx mtg_ctx;

@@ -111,7 +111,7 @@ class Stats(C.Structure):
     _fields_ = [("kernel_ms", C.c_double), ("reduce_ms", C.c_double), ("launches", C.c_int),
                 ("drains", C.c_int), ("grid", C.c_int), ("block", C.c_int), ("stack_capacity", C.c_int),
                 ("overflowed", C.c_longlong), ("collisions", C.c_longlong), ("device_bytes", C.c_size_t),
-                ("h2d_bytes", C.c_longlong), ("d2h_bytes", C.c_longlong)]
+                ("h2d_bytes", C.c_longlong), ("d2h_bytes", C.c_longlong), ("warp_steps", C.c_longlong)]
 
 
 # symbol -> (restype, argtypes); must match include/mytrim_gpu.h

@@ -58,7 +58,8 @@ enum Counter
   C_OVF1 = 65,
   C_NREC = 66,
   C_NEV = 67,
-  C_COUNT = 68
+  C_STEPS = 68,
+  C_COUNT = 72
 };
 constexpr int MAX_PASSES = 64;
 
@@ -249,13 +250,18 @@ fill_params(mtg_ctx * ctx, EngineParams & prm)
   prm.k1 = t.k1;
   long long mc = ctx->cfg.max_collisions_per_member;
   prm.max_collisions = (unsigned int)(mc <= 0 ? (1 << 24) : std::min<long long>(mc, 0xffffffffLL));
-  // fresh primaries per warp refill: small enough that every warp refills several
-  // times (dynamic load balance across warps), at most one per lane
+  // fresh primaries per warp refill.  A warp that follows few cascades at a time
+  // switches primary (and flushes the per-primary tallies) rarely, so large cascades
+  // want one primary per refill, while small ones need several to keep 32 lanes
+  // busy: about 64 expected members per refill.  At most a quarter of a warp's fair
+  // share of the batch, so that every warp refills several times (load balance).
   int take = ctx->cfg.max_primaries_per_refill;
   if (take <= 0)
   {
     const long long warps = std::max<long long>(1, (long long)ctx->grid * (ctx->block / 32));
-    take = int(std::min<long long>(32, std::max<long long>(1, t.total_primaries / (warps * 4))));
+    const long long balance = std::max<long long>(1, t.total_primaries / (warps * 4));
+    const long long fill = std::max<long long>(1, llround(64.0 / std::max(t.members_est, 1.0)));
+    take = int(std::min<long long>(32, std::min(balance, fill)));
   }
   prm.max_take = take;
   if (ctx->record_cap > 0)
@@ -272,6 +278,7 @@ fill_params(mtg_ctx * ctx, EngineParams & prm)
     prm.event_mask = ctx->event_mask;
   }
   prm.any_evac = t.any_evac;
+  prm.warp_steps = ptr<unsigned long long>(ctx->d_counters) + C_STEPS;
 }
 
 // Launch cascade pass `pass` (0 = fresh primaries, >0 = drain of the previous
@@ -664,6 +671,7 @@ mtg_collect(mtg_ctx * ctx, mtg_totals * totals, long long * hist)
     ctx->stats.reduce_ms = ms;
   }
   ctx->stats.drains = ctx->passes - 1;
+  ctx->stats.warp_steps = (long long)cnt[C_STEPS];
   ctx->stats.grid = ctx->grid;
   ctx->stats.block = ctx->block;
   ctx->stats.stack_capacity = ctx->stack_cap;

@@ -116,6 +116,23 @@ u24f(uint32_t x)
   return float((x >> 8) + 1u) * (1.0f / 16777216.0f);
 }
 
+// The uniform r1 of a member's first free flight (trim.C:71, 93-94), taken from
+// the bits of its path key.  A key is the output of a 64-bit mixing function of
+// (parent key, collision) or (simulation, primary), so its bits are as random as a
+// generator draw and independent of the Philox draws keyed by it; a member start
+// then needs no generator call.  FP64 takes 53 bits, FP32 the leading 24 of them.
+MTG_HD double
+key_u53(uint64_t key)
+{
+  return u53(uint32_t(key >> 32), uint32_t(key));
+}
+
+MTG_HD float
+key_u24f(uint64_t key)
+{
+  return u24f(uint32_t(key >> 32));
+}
+
 // ------------------------------------------------------------------ FP64 math
 MTG_HD double
 bits_to_double(uint64_t b)

@@ -19,8 +19,8 @@
 //
 // Tallies: per-lane accumulators flushed to per-primary arrays when a lane
 // switches primary (vacancies, collisions, electronic and nuclear energy), the
-// primary's stopping point written once, depth histograms through warp-aggregated
-// atomics (__match_any_sync), per-simulation counters flushed once per lane.
+// primary's stopping point written once, depth histograms through per-lane
+// atomics, per-simulation counters flushed once per lane.
 #pragma once
 
 #include "mtg_tables.h"
@@ -91,6 +91,7 @@ struct EngineParams
   long long events_cap;
   unsigned int event_mask;
   int any_evac; // some simulation keeps a vacancy-energy histogram
+  unsigned long long * warp_steps; // loop iterations of all warps (lane occupancy = collisions / 32 steps)
 };
 
 __device__ __forceinline__ unsigned int
@@ -127,8 +128,35 @@ struct AccF64
   __device__ void atomic_add_to(double * dst) const { atomicAdd(dst, s); }
 };
 
-// Kahan-compensated FP32 accumulator (FP32 engine): keeps FP64 work out of the
-// per-collision path while the sum stays accurate to ~1e-14 relative
+// float -> double by exponent rebias on the bit pattern (no FP64 instruction; the
+// FP32 engine flushes denormals, so a zero exponent means zero)
+__device__ __forceinline__ double
+widen_f32(float f)
+{
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xffu;
+  if (e == 0u)
+    return 0.0;
+  const unsigned long long bits = ((unsigned long long)(u >> 31) << 63) | ((unsigned long long)(e + 896u) << 52) |
+                                  ((unsigned long long)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+
+// Plain FP32 accumulator for the per-collision energy sums of the FP32 engine;
+// the engine hands it to the FP64 per-primary arrays every few dozen collisions
+// (Pol::FLUSH_EVERY), so each float sum stays short and accurate to ~1e-7
+struct AccF32
+{
+  float s;
+  __device__ void reset() { s = 0.0f; }
+  __device__ void add(float x) { s += x; }
+  __device__ double value() const { return double(s); }
+  __device__ bool nonzero() const { return s != 0.0f; }
+  __device__ void atomic_add_to(double * dst) const { atomicAdd(dst, widen_f32(s)); }
+};
+
+// Kahan-compensated FP32 accumulator (FP32 engine, long-lived rare sums): keeps
+// FP64 work out of the engine while the sum stays accurate to ~1e-14 relative
 struct AccKahan32
 {
   float s, c;
@@ -142,24 +170,12 @@ struct AccKahan32
   }
   __device__ double value() const { return double(s) - double(c); }
   __device__ bool nonzero() const { return s != 0.0f; }
-  // add the sum to a double in global memory without FP64 instructions (float ->
-  // double by exponent rebias on the bit pattern; the engine flushes denormals)
+  // add the sum to a double in global memory without FP64 instructions
   __device__ void atomic_add_to(double * dst) const
   {
-    atomicAdd(dst, widen(s));
+    atomicAdd(dst, widen_f32(s));
     if (c != 0.0f)
-      atomicAdd(dst, widen(-c));
-  }
-  static __device__ __forceinline__ double widen(float f)
-  {
-    const uint32_t u = __float_as_uint(f);
-    const uint32_t e = (u >> 23) & 0xffu;
-    if (e == 0u)
-      return 0.0;
-    const unsigned long long bits = ((unsigned long long)(u >> 31) << 63) |
-                                    ((unsigned long long)(e + 896u) << 52) |
-                                    ((unsigned long long)(u & 0x7fffffu) << 29);
-    return __longlong_as_double((long long)bits);
+      atomicAdd(dst, widen_f32(-c));
   }
 };
 
@@ -183,7 +199,8 @@ struct LaneCold
 template <class Pol, bool EV>
 struct LaneSink
 {
-  using Acc = typename Pol::Acc;
+  using Acc = typename Pol::Acc;       // rare sums (kept in shared memory)
+  using AccHot = typename Pol::AccHot; // per-collision sums (registers)
   using Real = typename Pol::Real;
   LaneCold<Acc> * cold;
   const EngineParams * prm;
@@ -192,7 +209,7 @@ struct LaneSink
   int range_mode;
   // per-primary accumulators
   unsigned int a_vac, a_coll;
-  Acc a_eel, a_enuc;
+  AccHot a_eel, a_enuc;
   // per-simulation Newton-iteration count (every collision), the rest in `cold`
   unsigned int n_newton;
   bool vox;  // this simulation tallies energy deposition in voxels
@@ -472,6 +489,22 @@ struct LaneSink
       return pow64(x, y);
   }
 
+  // every Pol::FLUSH_EVERY collisions of a lane, hand the energy sums to the
+  // per-primary arrays (no-op for FLUSH_EVERY = 0)
+  __device__ void tick()
+  {
+    if constexpr (Pol::FLUSH_EVERY > 0)
+      if ((a_coll & unsigned(Pol::FLUSH_EVERY - 1)) == 0u)
+      {
+        if (a_eel.nonzero())
+          a_eel.atomic_add_to(prm->prim.eel + gprim);
+        if (a_enuc.nonzero())
+          a_enuc.atomic_add_to(prm->prim.enuc + gprim);
+        a_eel.reset();
+        a_enuc.reset();
+      }
+  }
+
   __device__ void flush_prim()
   {
     if (gprim < 0)
@@ -524,20 +557,6 @@ struct LaneSink
     reset_sim();
   }
 };
-
-// warp-aggregated histogram increment: lanes with the same bin add once
-__device__ __forceinline__ void
-warp_hist_add(unsigned long long * hist, int bin)
-{
-  const unsigned int active = __ballot_sync(0xffffffffu, bin >= 0);
-  if (bin >= 0)
-  {
-    const unsigned int peers = __match_any_sync(active, bin);
-    const int leader = __ffs(peers) - 1;
-    if ((threadIdx.x & 31) == leader)
-      atomicAdd(hist + bin, (unsigned long long)__popc(peers));
-  }
-}
 
 template <class Pol, bool EV>
 __global__ void __launch_bounds__(128, Pol::MIN_BLOCKS)
@@ -614,8 +633,10 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
     ++sink.cold->n_members;
   };
 
+  unsigned int steps = 0;
   while (true)
   {
+    ++steps;
     // ---- refill idle lanes: recoils from the warp stack first, then new work
     const unsigned int idle = __ballot_sync(FULL, !live);
     if (idle)
@@ -675,6 +696,7 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
     flags = Pol::collide(live, p, ic, r1, mctx, prm.k0, prm.k1, rec, sink);
     if (live)
     {
+      sink.tick();
       if (!(flags & CF_DONE) && ic >= prm.max_collisions)
       {
         atomicOr(prm.error_flags, ERRB_BUDGET);
@@ -711,11 +733,18 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
         rec.prim = p.prim;
       }
     }
-    warp_hist_add(prm.hist, sink.vac_bin);
-    warp_hist_add(prm.hist, sink.repl_bin);
+    // depth histograms: a collision makes a vacancy or a replacement, never both;
+    // about one lane in ten has an event, so each adds its own count (aggregating
+    // lanes with __match_any_sync cost more than it saved)
+    {
+      const int hb = sink.vac_bin >= 0 ? sink.vac_bin : sink.repl_bin;
+      if (hb >= 0)
+        atomicAdd(prm.hist + hb, 1ull);
+    }
     if (prm.any_evac)
     {
-      warp_hist_add(prm.hist, sink.cold->evac_bin);
+      if (sink.cold->evac_bin >= 0)
+        atomicAdd(prm.hist + sink.cold->evac_bin, 1ull);
       sink.cold->evac_bin = -1;
     }
 
@@ -746,6 +775,8 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
   sink.flush_prim();
   sink.flush_sim(cur_sim);
   sink.flush_voxel();
+  if (lane == 0)
+    atomicAdd(prm.warp_steps, (unsigned long long)(steps - 1)); // the last pass finds no work
 }
 
 } // namespace mtg

@@ -82,6 +82,8 @@ struct Fp32Policy
   using Particle = P32;
   using Real = float;
   using Acc = AccKahan32;
+  using AccHot = AccF32;
+  static constexpr int FLUSH_EVERY = 64; // collisions per hand-over of the hot energy sums (power of 2)
   using Tables = Tables32;
   // resident 128-thread blocks per SM the register budget is cut for (the
   // surrogate's tensor-core fragments need more registers)
@@ -159,10 +161,9 @@ struct Fp32Policy
     m.net = t.net;
   }
 
-  static __device__ __forceinline__ float first_draw(uint64_t key, uint32_t k0, uint32_t k1)
+  static __device__ __forceinline__ float first_draw(uint64_t key, uint32_t, uint32_t)
   {
-    const U4 d = draw_block(key, 0u, 0u, k0, k1);
-    return u24f(d.x);
+    return key_u24f(key);
   }
 
   static __device__ __forceinline__ P32 make_primary(const SimDesc & s, int si, long long g)

@@ -14,6 +14,8 @@ struct Fp64Policy
   using Particle = P64;
   using Real = double;
   using Acc = AccF64;
+  using AccHot = AccF64;
+  static constexpr int FLUSH_EVERY = 0;
   static constexpr int MIN_BLOCKS = 3; // <= 170 registers: 12 warps per SM
 
   struct Tables
@@ -56,10 +58,9 @@ struct Fp64Policy
     m.mrow = t.mats + mbase + p.species * sim.n_mat;
   }
 
-  static __device__ __forceinline__ double first_draw(uint64_t key, uint32_t k0, uint32_t k1)
+  static __device__ __forceinline__ double first_draw(uint64_t key, uint32_t, uint32_t)
   {
-    const U4 d = draw_block(key, 0u, 0u, k0, k1);
-    return u53(d.x, d.y);
+    return key_u53(key);
   }
 
   static __device__ __forceinline__ P64 make_primary(const SimDesc & s, int si, long long g)

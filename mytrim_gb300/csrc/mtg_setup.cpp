@@ -266,6 +266,40 @@ build_fp32_tables(const HostTables & t, std::vector<Species32> & species, std::v
   }
 }
 
+// Expected cascade members per primary, for the launch heuristics only: one plus
+// the Norgett-Robinson-Torrens displacement estimate 0.8 T_dam / (2 E_d), with the
+// damage energy T_dam from Lindhard's partition in Robinson's fit (M. J. Norgett,
+// M. T. Robinson, I. M. Torrens, Nucl. Eng. Des. 33 (1975) 50), evaluated against
+// the first layer's fraction-weighted mean target atom.
+static double
+expected_members(const mtg_sim & s)
+{
+  if (s.tally_mode == MTG_TALLY_RANGE || s.primaries_only)
+    return 1.0;
+  const mtg_material & m = s.sample.material[0];
+  double tt = 0.0, Z2 = 0.0, M2 = 0.0, Ed = 0.0;
+  for (int j = 0; j < m.n_elements; ++j)
+  {
+    const double t = std::max(m.elements[j].t, 0.0);
+    tt += t;
+    Z2 += t * m.elements[j].Z;
+    M2 += t * m.elements[j].m;
+    Ed += t * m.elements[j].Edisp;
+  }
+  if (!(tt > 0.0) || !(Ed > 0.0))
+    return 1.0;
+  Z2 /= tt;
+  M2 /= tt;
+  Ed /= tt;
+  const double Z1 = s.ion.Z, M1 = s.ion.m, E = s.ion.E;
+  const double EL = 30.724 * Z1 * Z2 * std::sqrt(std::pow(Z1, 2.0 / 3.0) + std::pow(Z2, 2.0 / 3.0)) * (M1 + M2) / M2;
+  const double eps = E / EL;
+  const double k = 0.1337 * std::pow(Z1, 1.0 / 6.0) * std::sqrt(Z1 / M1);
+  const double g = 3.4008 * std::pow(eps, 1.0 / 6.0) + 0.40244 * std::pow(eps, 0.75) + eps;
+  const double Tdam = E / (1.0 + k * g);
+  return 1.0 + std::max(0.0, 0.8 * Tdam / (2.0 * Ed));
+}
+
 int
 build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim * sims, int n_sims,
              HostTables & out, std::string & err)
@@ -446,6 +480,7 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
     hist += (long long)d.hist_evac_rows * s.hist_vac_n;
     if (d.hist_evac_rows > 0)
       out.any_evac = 1;
+    out.members_est += double(s.n_primaries) * expected_members(s);
     prim += s.n_primaries;
     out.prim_end.push_back(prim);
     out.sims.push_back(d);
@@ -463,6 +498,7 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
     return MTG_ERR_BAD_INPUT;
   }
   out.total_primaries = prim;
+  out.members_est = prim > 0 ? out.members_est / double(prim) : 1.0;
   out.hist_total = hist;
   return MTG_OK;
 }

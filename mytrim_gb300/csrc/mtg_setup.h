@@ -24,6 +24,7 @@ struct HostTables
   uint32_t k0 = 0, k1 = 0;                // Philox key
   double emax = 0.0;                      // largest primary energy
   int any_evac = 0;                       // some simulation keeps a vacancy-energy histogram
+  double members_est = 1.0;               // expected cascade members per primary (launch heuristics)
 };
 
 // Build the tables; returns MTG_OK or MTG_ERR_BAD_INPUT with `err` set.

@@ -141,13 +141,9 @@ struct PhiloxDraw
 {
   uint32_t k0, k1;
   uint64_t member;
-  // block 0 of collision 0: r1 (trim.C:71)
-  double r1() const
-  {
-    uint32_t c[4] = {uint32_t(member), uint32_t(member >> 32), 0u, 0u};
-    philox4x32_10(c, k0, k1);
-    return u53(c[0], c[1]);
-  }
+  // r1 of the first flight (trim.C:71): the bits of the member's path key, which
+  // mix64 has already mixed
+  double r1() const { return u53(uint32_t(member >> 32), uint32_t(member)); }
   // block 0 of collision ic: impact parameter and target-atom draws (trim.C:143,147)
   void pair(uint32_t ic, double & r2, double & hh) const
   {

@@ -218,8 +218,7 @@ main(int argc, char ** argv)
       stack.pop_back();
       const SpeciesConst & sc = t.species[sd.species_base + m.species];
       const MatConst * mrow = &t.mats[sd.mat_base + m.species * sd.n_mat];
-      const U4 d = draw_block(m.key, 0u, 0u, t.k0, t.k1);
-      const double r1 = u53(d.x, d.y);
+      const double r1 = key_u53(m.key);
       HostSink sink;
       sink.sim = &sd;
       sink.range_mode = sd.range_mode;
