@@ -80,7 +80,7 @@ def args_parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--batch", type=int, default=1 << 17, help="primaries per step")
+    p.add_argument("--batch", type=int, default=1 << 20, help="primaries per step")
     p.add_argument("--precision", default="auto", choices=["auto", "fp32", "surrogate", "fp64"])
     p.add_argument("--fp64-batch", type=int, default=8192)
     p.add_argument("--cpu-per-core", type=int, default=0, help="primaries per core in the CPU sample")

@@ -75,6 +75,9 @@ struct mtg_ctx
   bool have_tables = false;
   mtg_config cfg;
   HostTables tables;
+  std::vector<Species32> sp32; // single-precision copies (FP32 engine), storage kept across batches
+  std::vector<Mat32> mc32;
+  std::vector<Sim32> sm32;
   bool prepared = false;
   bool launched = false;
   // device buffers
@@ -162,7 +165,7 @@ setup_launch_shape(mtg_ctx * ctx)
       tab = sizeof(SpeciesConst) * t.species.size() + sizeof(MatConst) * t.mats.size();
     else
       tab = sizeof(Species32) * t.species.size() + sizeof(Mat32) * t.mats.size() +
-            sizeof(float) * STOP_N * t.mats.size();
+            sizeof(float) * STOP_N * t.stop_row_mat.size();
     if (prec == MTG_PREC_FP32_SURROGATE)
       tab += surrogate_net_bytes();
     if (tab <= 160 * 1024)
@@ -230,6 +233,7 @@ fill_params(mtg_ctx * ctx, EngineParams & prm)
   prm.cold_offset = ctx->cold_offset;
   prm.n_stage_species = int(t.species.size());
   prm.n_stage_mats = int(t.mats.size());
+  prm.n_stage_stop_rows = int(t.stop_row_mat.size());
   prm.total_primaries = t.total_primaries;
   prm.stacks = ctx->d_stacks.p;
   prm.stack_cap = ctx->stack_cap;
@@ -301,6 +305,7 @@ launch_pass(mtg_ctx * ctx, int pass)
     prm.in_count = cnt + (out_list ? C_OVF0 : C_OVF1);
     prm.in_cap = ctx->ovf_cap;
   }
+
   cudaError_t e;
   const int prec = ctx->cfg.precision;
   if (prec == MTG_PREC_FP64)
@@ -543,23 +548,23 @@ mtg_prepare(mtg_ctx * ctx, const mtg_sim * sims, int n_sims)
 
   if (ctx->cfg.precision != MTG_PREC_FP64)
   {
-    // FP32 path: stopping tables evaluated on the device in FP64
-    std::vector<int> row_species(t.mats.size());
-    for (size_t s = 0; s < ns; ++s)
-      for (int sp = 0; sp < t.sims[s].n_species; ++sp)
-        for (int k = 0; k < t.sims[s].n_mat; ++k)
-          row_species[t.sims[s].mat_base + sp * t.sims[s].n_mat + k] = t.sims[s].species_base + sp;
-    CK(ensure(ctx->d_row_species, sizeof(int) * row_species.size()));
-    CK(ensure(ctx->d_stop, sizeof(float) * STOP_N * t.mats.size()));
-    CK(h2d(ctx, ctx->d_row_species.p, row_species.data(), sizeof(int) * row_species.size()));
+    // FP32 path: stopping tables evaluated on the device in FP64, one row per
+    // distinct (species, material) of the run
+    const size_t nrows = t.stop_row_mat.size();
+    CK(ensure(ctx->d_row_species, 2 * sizeof(int) * nrows));
+    CK(ensure(ctx->d_stop, sizeof(float) * STOP_N * nrows));
+    int * d_row_species = ptr<int>(ctx->d_row_species);
+    int * d_row_mat = d_row_species + nrows;
+    CK(h2d(ctx, d_row_species, t.stop_row_species.data(), sizeof(int) * nrows));
+    CK(h2d(ctx, d_row_mat, t.stop_row_mat.data(), sizeof(int) * nrows));
     const double lo = std::log(STOP_EMIN), hi = std::log(t.emax * 1.05);
-    CK(launch_build_stop_tables(ptr<SpeciesConst>(ctx->d_species), ptr<MatConst>(ctx->d_mats), nullptr, 0,
-                                int(t.mats.size()), ptr<int>(ctx->d_row_species), ptr<float>(ctx->d_stop), lo,
-                                (hi - lo) / (STOP_N - 1), nullptr));
+    CK(launch_build_stop_tables(ptr<SpeciesConst>(ctx->d_species), ptr<MatConst>(ctx->d_mats), d_row_mat,
+                                int(nrows), d_row_species, ptr<float>(ctx->d_stop), lo, (hi - lo) / (STOP_N - 1),
+                                nullptr));
     CK(cudaDeviceSynchronize());
-    std::vector<Species32> sp32;
-    std::vector<Mat32> mc32;
-    std::vector<Sim32> sm32;
+    std::vector<Species32> & sp32 = ctx->sp32;
+    std::vector<Mat32> & mc32 = ctx->mc32;
+    std::vector<Sim32> & sm32 = ctx->sm32;
     build_fp32_tables(t, sp32, mc32, sm32);
     CK(ensure(ctx->d_species32, sizeof(Species32) * sp32.size()));
     CK(ensure(ctx->d_mats32, sizeof(Mat32) * mc32.size()));
@@ -947,7 +952,7 @@ mtg_stopping(mtg_ctx * ctx, int Z1, double m1, const mtg_material * material, co
     int zero = 0;
     int * d_rs = reinterpret_cast<int *>(reinterpret_cast<char *>(ctx->d_tmp3.p) + sizeof(float) * STOP_N);
     CK(cudaMemcpy(d_rs, &zero, sizeof zero, cudaMemcpyHostToDevice));
-    CK(launch_build_stop_tables(d_sc, d_mc, nullptr, 0, 1, d_rs, ptr<float>(ctx->d_tmp3), lo, dl, nullptr));
+    CK(launch_build_stop_tables(d_sc, d_mc, nullptr, 1, d_rs, ptr<float>(ctx->d_tmp3), lo, dl, nullptr));
     CK(launch_stopping32(ptr<float>(ctx->d_tmp3), float(lo), float(1.0 / dl), ptr<double>(ctx->d_tmp1), n,
                          ptr<double>(ctx->d_tmp2), nullptr));
   }

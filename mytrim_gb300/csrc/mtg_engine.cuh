@@ -58,6 +58,7 @@ struct EngineParams
   const MatConst * mats;
   int stage_tables;               // stage species+mats of simulation 0 into shared memory
   int n_stage_species, n_stage_mats;
+  int n_stage_stop_rows;          // FP32 stopping-table rows of the run
   long long total_primaries;
   unsigned long long * next_primary;
   // drain mode: members read from `in_records` (count in device memory) instead
@@ -584,6 +585,15 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
 
   int top = 0;
   bool work_done = false; // no more primaries / input records for this warp
+  // members per refill: the launch's choice for fresh primaries; for the records of
+  // a drain pass, a quarter of a warp's fair share (at most one per lane)
+  int max_take = prm.max_take;
+  if (prm.in_records)
+  {
+    const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+    const long long share = n_work / (nwarps * 4);
+    max_take = share < 1 ? 1 : (share > 32 ? 32 : int(share));
+  }
   bool live = false;
   Particle p;
   uint32_t ic = 0;
@@ -651,8 +661,8 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
       }
       top -= npop;
       int need = nidle - npop;
-      if (need > prm.max_take)
-        need = prm.max_take;
+      if (need > max_take)
+        need = max_take;
       if (need > 0 && !work_done)
       {
         unsigned long long base = 0;
@@ -771,12 +781,15 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
       if (top > prm.stack_cap)
         top = prm.stack_cap;
     }
+
   }
   sink.flush_prim();
   sink.flush_sim(cur_sim);
   sink.flush_voxel();
   if (lane == 0)
+  {
     atomicAdd(prm.warp_steps, (unsigned long long)(steps - 1)); // the last pass finds no work
+  }
 }
 
 } // namespace mtg

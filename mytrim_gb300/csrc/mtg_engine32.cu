@@ -125,7 +125,7 @@ struct Fp32Policy
     float * s_st = reinterpret_cast<float *>(q);
     const int n1 = int(sizeof(Species32) / 4) * ns;
     const int n2 = int(sizeof(Mat32) / 4) * nm;
-    const int n3 = STOP_N * nm;
+    const int n3 = STOP_N * prm.n_stage_stop_rows;
     for (int i = threadIdx.x; i < n1; i += blockDim.x)
       reinterpret_cast<float *>(s_sp)[i] = reinterpret_cast<const float *>(g.species)[i];
     for (int i = threadIdx.x; i < n2; i += blockDim.x)
@@ -155,7 +155,7 @@ struct Fp32Policy
     m.sim = s;
     m.sc = t.species + sbase + p.species;
     m.mrow = t.mats + mbase + p.species * s->n_mat;
-    m.stop = t.stop + (long long)(mbase + p.species * s->n_mat) * STOP_N;
+    m.stop = t.stop;
     m.lnE_min = t.lnE_min;
     m.inv_dlnE = t.inv_dlnE;
     m.net = t.net;
@@ -245,7 +245,7 @@ struct Fp32Policy
     a.b = pimp * mc.el[nn].inv_ai;
 
     // electronic loss from the stopping table (material.C:114-121)
-    a.dee = ls * stop_lookup(m.stop + (long long)k * STOP_N, m.lnE_min, m.inv_dlnE, E);
+    a.dee = ls * stop_lookup(m.stop + (long long)mc.row * STOP_N, m.lnE_min, m.inv_dlnE, E);
     return a;
   }
 

@@ -190,7 +190,7 @@ namespace mtg
 // FP32-path stopping tables: S(E) of every (species, material) row on a grid
 // uniform in ln E, evaluated with the FP64 stopping above.
 __global__ void
-build_stop_tables_kernel(const SpeciesConst * species, const MatConst * mats, int n_rows,
+build_stop_tables_kernel(const SpeciesConst * species, const MatConst * mats, const int * row_mat, int n_rows,
                          const int * row_species, float * out, double lnE_min, double dlnE)
 {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -199,19 +199,19 @@ build_stop_tables_kernel(const SpeciesConst * species, const MatConst * mats, in
   const int row = int(i / STOP_N);
   const int j = int(i % STOP_N);
   const double E = exp64(lnE_min + dlnE * double(j));
-  out[i] = float(material_stop64(species[row_species[row]], mats[row], E));
+  const MatConst & mc = mats[row_mat ? row_mat[row] : row];
+  out[i] = float(material_stop64(species[row_species[row]], mc, E));
 }
 
 cudaError_t
-launch_build_stop_tables(const SpeciesConst * species, const MatConst * mats, const SimDesc * /*sims*/,
-                         int /*n_sims*/, int n_rows, const int * row_species, float * out, double lnE_min,
-                         double dlnE, cudaStream_t st)
+launch_build_stop_tables(const SpeciesConst * species, const MatConst * mats, const int * row_mat, int n_rows,
+                         const int * row_species, float * out, double lnE_min, double dlnE, cudaStream_t st)
 {
   const long long n = (long long)n_rows * STOP_N;
   const int block = 256;
   if (n > 0)
     build_stop_tables_kernel<<<(unsigned int)((n + block - 1) / block), block, 0, st>>>(
-        species, mats, n_rows, row_species, out, lnE_min, dlnE);
+        species, mats, row_mat, n_rows, row_species, out, lnE_min, dlnE);
   return cudaGetLastError();
 }
 

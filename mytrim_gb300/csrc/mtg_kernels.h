@@ -31,8 +31,8 @@ struct Fp32Tables
   const void * mlp;     // surrogate weights, NULL without the surrogate
   const void * sims32;  // Sim32 per simulation
 };
-cudaError_t launch_build_stop_tables(const SpeciesConst * species, const MatConst * mats, const SimDesc * sims,
-                                     int n_sims, int n_rows, const int * row_species, float * out, double lnE_min,
+cudaError_t launch_build_stop_tables(const SpeciesConst * species, const MatConst * mats, const int * row_mat,
+                                     int n_rows, const int * row_species, float * out, double lnE_min,
                                      double dlnE, cudaStream_t st);
 cudaError_t launch_cascade32(const EngineParams & prm, const Fp32Tables & t, int grid, int block, size_t smem,
                              cudaStream_t st, int surrogate);

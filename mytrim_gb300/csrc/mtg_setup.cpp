@@ -6,6 +6,8 @@
 #include <cstring>
 #include <fstream>
 #include <sstream>
+#include <string>
+#include <unordered_map>
 
 namespace mtg
 {
@@ -218,7 +220,7 @@ build_fp32_tables(const HostTables & t, std::vector<Species32> & species, std::v
     o.epsdg = float(m.epsdg);
     o.inv_pi_arho = float(1.0 / (3.14159265358979323846 * m.arho));
     o.nel = m.nel;
-    o.row = int(i);
+    o.row = m.row;
     for (int j = 0; j < m.nel; ++j)
     {
       const ElemConst & e = m.el[j];
@@ -304,7 +306,18 @@ int
 build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim * sims, int n_sims,
              HostTables & out, std::string & err)
 {
-  out = HostTables();
+  // clear, keeping the vectors' storage for the next batch
+  out.sims.clear();
+  out.prim_end.clear();
+  out.species.clear();
+  out.mats.clear();
+  out.stop_row_mat.clear();
+  out.stop_row_species.clear();
+  out.total_primaries = out.hist_total = out.voxel_total = 0;
+  out.k0 = out.k1 = 0;
+  out.emax = 0.0;
+  out.any_evac = 0;
+  out.members_est = 1.0;
   if (n_sims < 1 || !sims)
   {
     err = "need at least one simulation";
@@ -317,6 +330,45 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
   }
   seed_key(cfg.seed, out.k0, out.k1);
   long long prim = 0, hist = 0;
+  {
+    // at most (1 + elements) species and layers x species materials per simulation
+    size_t nsp = 0, nmat = 0;
+    for (int si = 0; si < n_sims; ++si)
+    {
+      const mtg_sample & smp = sims[si].sample;
+      const int nl = std::max(0, std::min(smp.n_layers, int(MAX_LAYERS)));
+      size_t ne = 1;
+      for (int k = 0; k < nl; ++k)
+        ne += size_t(std::max(0, std::min(smp.material[k].n_elements, int(MAX_EL))));
+      nsp += ne;
+      nmat += ne * size_t(nl);
+    }
+    out.species.reserve(nsp);
+    out.mats.reserve(nmat);
+    out.sims.reserve(size_t(n_sims));
+    out.prim_end.reserve(size_t(n_sims));
+  }
+  // (species, material) -> index of its first MatConst: equal pairs across the
+  // simulations of a batch share the derived constants and the stopping-table row
+  std::unordered_map<std::string, int> mat_cache;
+  auto mat_key = [](const SpeciesConst & sc, const mtg_material & m) {
+    std::string k;
+    auto put = [&k](const void * p, size_t n) { k.append(reinterpret_cast<const char *>(p), n); };
+    put(&sc.Z1, sizeof sc.Z1);
+    put(&sc.m1, sizeof sc.m1);
+    put(&m.rho, sizeof m.rho);
+    put(&m.n_elements, sizeof m.n_elements);
+    for (int j = 0; j < m.n_elements && j < MAX_EL; ++j)
+    {
+      const mtg_element & e = m.elements[j];
+      put(&e.Z, sizeof e.Z);
+      put(&e.m, sizeof e.m);
+      put(&e.t, sizeof e.t);
+      put(&e.Edisp, sizeof e.Edisp);
+      put(&e.Elbind, sizeof e.Elbind);
+    }
+    return k;
+  };
   for (int si = 0; si < n_sims; ++si)
   {
     const mtg_sim & s = sims[si];
@@ -377,10 +429,23 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
     for (int sidx = 0; sidx < d.n_species; ++sidx)
       for (int k = 0; k < smp.n_layers; ++k)
       {
+        const SpeciesConst & sc = out.species[d.species_base + sidx];
+        const std::string key = mat_key(sc, smp.material[k]);
+        const auto it = mat_cache.find(key);
         MatConst mc;
-        int rc = make_material(rows, out.species[d.species_base + sidx], smp.material[k], cfg.tmin, mc, err);
-        if (rc != MTG_OK)
-          return rc;
+        if (it != mat_cache.end())
+          mc = out.mats[size_t(it->second)];
+        else
+        {
+          int rc = make_material(rows, sc, smp.material[k], cfg.tmin, mc, err);
+          if (rc != MTG_OK)
+            return rc;
+          mc.row = int(out.stop_row_mat.size());
+          out.stop_row_mat.push_back(int(out.mats.size()));
+          out.stop_row_species.push_back(d.species_base + sidx);
+          mat_cache.emplace(key, int(out.mats.size()));
+        }
+        // the recoil species are numbered within each simulation
         for (int j = 0; j < mc.nel; ++j)
           mc.el[j].rspecies = species_of(mc.el[j].Z2, mc.el[j].m2);
         out.mats.push_back(mc);

@@ -25,6 +25,9 @@ struct HostTables
   double emax = 0.0;                      // largest primary energy
   int any_evac = 0;                       // some simulation keeps a vacancy-energy histogram
   double members_est = 1.0;               // expected cascade members per primary (launch heuristics)
+  // stopping-table rows of the FP32 engine, one per distinct (species, material):
+  // the MatConst entry and the species each row is built from
+  std::vector<int> stop_row_mat, stop_row_species;
 };
 
 // Build the tables; returns MTG_OK or MTG_ERR_BAD_INPUT with `err` set.

@@ -77,7 +77,7 @@ struct MatConst
   double a, f, epsdg, arho;
   double am, az;
   int nel;
-  int pad;
+  int row; // stopping-table row (FP32 engine); equal (species, material) pairs share one
   ElemConst el[MAX_EL];
   StopPair sp[MAX_EL];
 };
