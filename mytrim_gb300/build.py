@@ -90,28 +90,32 @@ def build(verbose=False, force=False):
     return out
 
 
-FRONTEND_SRC = PKG / "cpp" / "runmytrim_gpu.cpp"
+FRONTENDS = ("runmytrim_gpu", "runstopping_gpu")
 
 
-def frontend_path():
-    return OUT_DIR / "runmytrim_gpu"
+def frontend_path(name="runmytrim_gpu"):
+    return OUT_DIR / name
 
 
-def build_frontend(force=False):
-    """Compile the runmytrim front-end (host C++ over the C ABI) next to the library."""
-    exe = frontend_path()
-    deps = [FRONTEND_SRC, PKG / "cpp" / "json_lite.h", INCLUDE / "mytrim_gpu.h", lib_path()]
-    if not force and exe.exists() and exe.stat().st_mtime >= max(p.stat().st_mtime for p in deps):
-        return exe
+def build_frontend(force=False, name=None):
+    """Compile the command-line front-ends (host C++ over the C ABI) next to the
+    library: runmytrim_gpu and runstopping_gpu.  Returns the path of `name`
+    (default runmytrim_gpu)."""
     cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
-    tmp = exe.with_suffix(".tmp")
-    cmd = [cxx, "-O2", "-std=c++17", f"-I{INCLUDE}", f"-I{PKG / 'cpp'}", "-o", str(tmp), str(FRONTEND_SRC),
-           f"-L{OUT_DIR}", "-lmytrim_gpu", "-Wl,-rpath,$ORIGIN"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"runmytrim_gpu build failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, exe)
-    return exe
+    for fe in FRONTENDS:
+        exe = frontend_path(fe)
+        src = PKG / "cpp" / f"{fe}.cpp"
+        deps = [src, PKG / "cpp" / "json_lite.h", INCLUDE / "mytrim_gpu.h", lib_path()]
+        if not force and exe.exists() and exe.stat().st_mtime >= max(p.stat().st_mtime for p in deps):
+            continue
+        tmp = exe.with_suffix(".tmp")
+        cmd = [cxx, "-O2", "-std=c++17", f"-I{INCLUDE}", f"-I{PKG / 'cpp'}", "-o", str(tmp), str(src),
+               f"-L{OUT_DIR}", "-lmytrim_gpu", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"{fe} build failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, exe)
+    return frontend_path(name or "runmytrim_gpu")
 
 
 if __name__ == "__main__":

@@ -17,6 +17,7 @@ REPO = ORACLE_DIR.parent
 MTORACLE = ORACLE_DIR / "_build" / "mtoracle"
 REF_DRIVER = ORACLE_DIR / "_ref" / "ref_driver"
 REF_RUNMYTRIM = ORACLE_DIR / "_ref" / "ref_runmytrim"
+REF_RUNSTOPPING = ORACLE_DIR / "_ref" / "ref_runstopping"
 TABLES = REPO / "mytrim_gb300" / "data" / "stopping_tables.tsv"
 
 SUM_KEYS = ("primaries", "members", "collisions", "vacancies", "replacements", "interstitials",
@@ -175,3 +176,14 @@ def stopping(Z1, m1, layer, energies):
             k += 1
         out.append(se * arho)
     return out
+
+
+def runstopping_reference(Z1, m1, layer, energies):
+    """What runstopping prints for the request, computed by the reference library
+    (oracle/_ref/ref_runstopping; needs the reference build)."""
+    lines = [f"ion {Z1} {m1!r}", f"rho {layer.rho!r}"]
+    lines += [f"element {e.Z} {e.m!r} {e.t!r}" for e in layer.elements]
+    lines.append("energies " + " ".join(repr(float(E)) for E in energies))
+    r = subprocess.run([str(REF_RUNSTOPPING)], input="\n".join(lines) + "\n", capture_output=True, text=True,
+                       check=True)
+    return r.stdout
