@@ -86,8 +86,20 @@ typedef struct
   mtg_element elements[MTG_MAX_ELEMENTS];
 } mtg_material;
 
+typedef enum
+{
+  MTG_GEOM_LAYERS = 0,  /* SampleLayers / SampleSolid */
+  MTG_GEOM_CLUSTERS = 1 /* sampleClusters (sample_clusters.h:30-57) */
+} mtg_geometry;
+
 /* SampleLayers (sample_layers.h:33-43) or SampleSolid (n_layers = 1): layers stacked
- * along x from 0; x < 0 belongs to layer 0, the last layer extends to +infinity. */
+ * along x from 0; x < 0 belongs to layer 0, the last layer extends to +infinity.
+ * With geometry MTG_GEOM_CLUSTERS the sample is sampleClusters: material[0] fills the
+ * box w, material[1] fills spheres (x, y, z, r) listed in `clusters` (host memory,
+ * read during mtg_prepare / mtg_run), found through a spatial hash of
+ * cluster_hash[0..2] cells (sampleClusters::initSpatialhash, addCluster); n_layers
+ * must be 2 and thickness is not used.  A member that reaches a CUT boundary's
+ * outside at the start of a collision is dropped without a tally, as in trim.C:81-83. */
 typedef struct
 {
   int n_layers;
@@ -95,6 +107,10 @@ typedef struct
   mtg_material material[MTG_MAX_LAYERS];
   double w[3];
   int bc[3];
+  int geometry;            /* mtg_geometry */
+  int cluster_hash[3];     /* spatial-hash cells per axis (clusters only) */
+  long long n_clusters;
+  const double * clusters; /* n_clusters x (x, y, z, r) */
 } mtg_sample;
 
 /* IonBase template of the primaries (ion.h:30-85, runmytrim.C:263-304). */

@@ -38,9 +38,14 @@ class Material(C.Structure):
     _fields_ = [("rho", C.c_double), ("n_elements", C.c_int), ("elements", Element * MAX_ELEMENTS)]
 
 
+GEOM_LAYERS, GEOM_CLUSTERS = 0, 1
+
+
 class Sample(C.Structure):
     _fields_ = [("n_layers", C.c_int), ("thickness", C.c_double * MAX_LAYERS),
-                ("material", Material * MAX_LAYERS), ("w", C.c_double * 3), ("bc", C.c_int * 3)]
+                ("material", Material * MAX_LAYERS), ("w", C.c_double * 3), ("bc", C.c_int * 3),
+                ("geometry", C.c_int), ("cluster_hash", C.c_int * 3), ("n_clusters", C.c_longlong),
+                ("clusters", C.POINTER(C.c_double))]
 
 
 class Ion(C.Structure):

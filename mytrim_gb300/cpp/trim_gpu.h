@@ -143,6 +143,43 @@ private:
 #ifdef MYTRIM_TRIM_H
 #include "sample_layers.h"
 #include "sample_solid.h"
+#include "sample_clusters.h"
+
+namespace mtg
+{
+
+// sampleClusters (sample_clusters.h:30-57): material[0] the matrix, material[1] the
+// clusters, the cluster centres and radii c[0..3][0..cn) interleaved into
+// `storage` (which must outlive the call that reads the sample), the hash cells kn.
+inline mtg_sample
+flatten_clusters(const MyTRIM_NS::sampleClusters & sample, std::vector<double> & storage)
+{
+  if (sample.material.size() != 2)
+    throw std::invalid_argument("TrimGPU: a cluster sample needs two materials (matrix, cluster)");
+  mtg_sample o{};
+  o.n_layers = 2;
+  for (int k = 0; k < 2; ++k)
+  {
+    o.thickness[k] = sample.w[0];
+    o.material[k] = flatten_material(*sample.material[k]);
+  }
+  for (int i = 0; i < 3; ++i)
+  {
+    o.w[i] = sample.w[i];
+    o.bc[i] = int(sample.bc[i]);
+    o.cluster_hash[i] = sample.kn[i];
+  }
+  storage.resize(4 * size_t(sample.cn));
+  for (int l = 0; l < sample.cn; ++l)
+    for (int i = 0; i < 4; ++i)
+      storage[4 * size_t(l) + i] = sample.c[i][l];
+  o.geometry = MTG_GEOM_CLUSTERS;
+  o.n_clusters = sample.cn;
+  o.clusters = storage.data();
+  return o;
+}
+
+} // namespace mtg
 
 namespace MyTRIM_NS
 {
@@ -176,12 +213,15 @@ public:
     cfg.seed = seed;
     _ctx.check(mtg_configure(_ctx.get(), &cfg));
     mtg_sim sim{};
+    std::vector<double> cluster_storage;
     if (auto * layers = dynamic_cast<SampleLayers *>(_sample))
       sim.sample = mtg::flatten_sample(*layers, &layers->layerThickness);
     else if (dynamic_cast<SampleSolid *>(_sample))
       sim.sample = mtg::flatten_sample(*_sample, nullptr);
+    else if (auto * clusters = dynamic_cast<sampleClusters *>(_sample))
+      sim.sample = mtg::flatten_clusters(*clusters, cluster_storage);
     else
-      throw std::invalid_argument("TrimGPU supports SampleSolid and SampleLayers");
+      throw std::invalid_argument("TrimGPU supports SampleSolid, SampleLayers and sampleClusters");
     sim.ion = mtg::flatten_ion(*pka);
     sim.n_primaries = n;
     sim.first_primary = first_primary;

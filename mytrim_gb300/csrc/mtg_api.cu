@@ -85,6 +85,8 @@ struct mtg_ctx
   DevBuf d_species32, d_mats32, d_sims32;
   DevBuf d_sg_params, d_sg_net; // surrogate network
   DevBuf d_vox, d_vox_range, d_vox_sum; // energy-deposition voxels
+  DevBuf d_cl, d_cl32, d_cl_next, d_cl_head; // sampleClusters geometry
+  std::vector<SimDesc> sims_dev;             // SimDesc copies with device cluster pointers
   bool sg_ready = false;
   DevBuf p_vac, p_coll, p_eel, p_enuc, p_fx, p_fy, p_fz, p_state;
   DevBuf d_totals, d_hist, d_err, d_counters, d_stacks, d_ovf0, d_ovf1, d_records, d_events;
@@ -183,9 +185,10 @@ setup_launch_shape(mtg_ctx * ctx)
   ctx->smem = size_t(ctx->cold_offset) + slot * size_t(ctx->block);
   int bps = 0;
   const int events = ctx->event_cap > 0 && ctx->event_mask ? 1 : 0;
+  const int clusters = t.any_clusters;
   cudaError_t e = prec == MTG_PREC_FP64
-                      ? occupancy64(ctx->block, ctx->smem, &bps, events)
-                      : occupancy32(ctx->block, ctx->smem, &bps, prec == MTG_PREC_FP32_SURROGATE, events);
+                      ? occupancy64(ctx->block, ctx->smem, &bps, events, clusters)
+                      : occupancy32(ctx->block, ctx->smem, &bps, prec == MTG_PREC_FP32_SURROGATE, events, clusters);
   if (e != cudaSuccess)
     return fail(ctx, MTG_ERR_CUDA, std::string("occupancy query: ") + cudaGetErrorString(e));
   if (bps < 1)
@@ -282,6 +285,7 @@ fill_params(mtg_ctx * ctx, EngineParams & prm)
     prm.event_mask = ctx->event_mask;
   }
   prm.any_evac = t.any_evac;
+  prm.any_clusters = t.any_clusters;
   prm.warp_steps = ptr<unsigned long long>(ctx->d_counters) + C_STEPS;
 }
 
@@ -412,7 +416,8 @@ mtg_destroy(mtg_ctx * ctx)
                      &ctx->d_partials,
                      &ctx->d_out,    &ctx->d_tmp0,     &ctx->d_tmp1,    &ctx->d_tmp2,    &ctx->d_tmp3,
                      &ctx->d_species32, &ctx->d_mats32, &ctx->d_sims32, &ctx->d_sg_params, &ctx->d_sg_net,
-                     &ctx->d_vox,    &ctx->d_vox_range, &ctx->d_vox_sum};
+                     &ctx->d_vox,    &ctx->d_vox_range, &ctx->d_vox_sum, &ctx->d_cl,     &ctx->d_cl32,
+                     &ctx->d_cl_next, &ctx->d_cl_head};
   for (DevBuf * b : bufs)
     if (b->p)
       cudaFree(b->p);
@@ -522,7 +527,22 @@ mtg_prepare(mtg_ctx * ctx, const mtg_sim * sims, int n_sims)
     CK(ensure(ctx->d_vox_sum, sizeof(double) * ns));
     CK(h2d(ctx, ctx->d_vox_range.p, vr.data(), sizeof(long long) * vr.size()));
   }
-  CK(h2d(ctx, ctx->d_sims.p, t.sims.data(), sizeof(SimDesc) * ns));
+  // cluster samples: the cluster arrays, and the simulations pointing at them
+  ctx->sims_dev = t.sims;
+  if (!t.clusters.empty() || !t.cl_head.empty())
+  {
+    CK(ensure(ctx->d_cl, sizeof(Cl4d) * std::max<size_t>(t.clusters.size(), 1)));
+    CK(ensure(ctx->d_cl_next, sizeof(int) * std::max<size_t>(t.cl_next.size(), 1)));
+    CK(ensure(ctx->d_cl_head, sizeof(int) * std::max<size_t>(t.cl_head.size(), 1)));
+    if (!t.clusters.empty())
+    {
+      CK(h2d(ctx, ctx->d_cl.p, t.clusters.data(), sizeof(Cl4d) * t.clusters.size()));
+      CK(h2d(ctx, ctx->d_cl_next.p, t.cl_next.data(), sizeof(int) * t.cl_next.size()));
+    }
+    CK(h2d(ctx, ctx->d_cl_head.p, t.cl_head.data(), sizeof(int) * t.cl_head.size()));
+    patch_cluster_pointers(ctx->sims_dev, ptr<Cl4d>(ctx->d_cl), ptr<int>(ctx->d_cl_next), ptr<int>(ctx->d_cl_head));
+  }
+  CK(h2d(ctx, ctx->d_sims.p, ctx->sims_dev.data(), sizeof(SimDesc) * ns));
   CK(h2d(ctx, ctx->d_prim_end.p, t.prim_end.data(), sizeof(long long) * ns));
   CK(h2d(ctx, ctx->d_species.p, t.species.data(), sizeof(SpeciesConst) * t.species.size()));
   CK(h2d(ctx, ctx->d_mats.p, t.mats.data(), sizeof(MatConst) * t.mats.size()));
@@ -566,6 +586,23 @@ mtg_prepare(mtg_ctx * ctx, const mtg_sim * sims, int n_sims)
     std::vector<Mat32> & mc32 = ctx->mc32;
     std::vector<Sim32> & sm32 = ctx->sm32;
     build_fp32_tables(t, sp32, mc32, sm32);
+    if (!t.clusters.empty() || !t.cl_head.empty())
+    {
+      std::vector<Cl4f> c32(t.clusters.size());
+      for (size_t l = 0; l < c32.size(); ++l)
+        c32[l] = Cl4f{float(t.clusters[l].x), float(t.clusters[l].y), float(t.clusters[l].z),
+                      float(t.clusters[l].r)};
+      CK(ensure(ctx->d_cl32, sizeof(Cl4f) * std::max<size_t>(c32.size(), 1)));
+      if (!c32.empty())
+        CK(h2d(ctx, ctx->d_cl32.p, c32.data(), sizeof(Cl4f) * c32.size()));
+      for (size_t i = 0; i < sm32.size(); ++i)
+        if (sm32[i].geometry == 1)
+        {
+          sm32[i].cl = ptr<Cl4f>(ctx->d_cl32) + t.sims[i].cl_base;
+          sm32[i].cl_next = ptr<int>(ctx->d_cl_next) + t.sims[i].cl_base;
+          sm32[i].cl_head = ptr<int>(ctx->d_cl_head) + t.sims[i].cell_base;
+        }
+    }
     CK(ensure(ctx->d_species32, sizeof(Species32) * sp32.size()));
     CK(ensure(ctx->d_mats32, sizeof(Mat32) * mc32.size()));
     CK(ensure(ctx->d_sims32, sizeof(Sim32) * sm32.size()));

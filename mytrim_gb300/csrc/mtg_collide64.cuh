@@ -22,6 +22,7 @@
 #pragma once
 
 #include "mtg_common.cuh"
+#include "mtg_geometry.cuh"
 #include "mtg_tables.h"
 
 namespace mtg
@@ -185,16 +186,31 @@ scatter64(double eps, double b, double & s2, double & ct, double & st, int & nit
 // One collision.  `mats` points at this species' MatConst row of the simulation
 // (n_mat entries), ic is the 1-based collision index, r1 the member's first-flight
 // draw.  Sink receives the tally events (see the engine and the host replay).
-template <class Sink>
+template <bool GEO, class Sink>
 MTG_HD int
 collide64(P64 & p, uint32_t ic, double r1, const SimDesc & sim, const SpeciesConst & sc,
           const MatConst * mats, uint32_t k0, uint32_t k1, P64 & rec, Sink & sink)
 {
-  // which material (SampleLayers::lookupLayer, sample_layers.C:27-43)
-  int layer = 0;
-  while (layer < sim.n_layers - 1 && !(p.x < sim.layer_end[layer]))
-    ++layer;
-  const MatConst & mc = mats[sim.layer_mat[layer]];
+  // which material: SampleLayers::lookupLayer (sample_layers.C:27-43) or
+  // sampleClusters::lookupMaterial (sample_clusters.C:42-53)
+  int mat_index;
+  if (GEO && sim.geometry == 1)
+  {
+    const double pos[3] = {p.x, p.y, p.z};
+    const int l = cluster_lookup<double>(pos, sim.w, sim.bc, sim.kn, sim.kd, sim.cmr, sim.cl, sim.cl_next,
+                                         sim.cl_head, sim.n_clusters);
+    if (l == -2)
+      return CF_DONE | CF_VOID; // no material: the member is dropped (trim.C:81-83)
+    mat_index = l >= 0 ? 1 : 0;
+  }
+  else
+  {
+    int layer = 0;
+    while (layer < sim.n_layers - 1 && !(p.x < sim.layer_end[layer]))
+      ++layer;
+    mat_index = sim.layer_mat[layer];
+  }
+  const MatConst & mc = mats[mat_index];
 
   // normalise direction (trim.C:85)
   {

@@ -92,6 +92,7 @@ struct EngineParams
   long long events_cap;
   unsigned int event_mask;
   int any_evac; // some simulation keeps a vacancy-energy histogram
+  int any_clusters; // some simulation has the cluster geometry
   unsigned long long * warp_steps; // loop iterations of all warps (lane occupancy = collisions / 32 steps)
 };
 
@@ -559,7 +560,9 @@ struct LaneSink
   }
 };
 
-template <class Pol, bool EV>
+// EV: the event-log variant; GEO: the variant that knows the cluster geometry
+// (the layered-sample kernel carries neither)
+template <class Pol, bool EV, bool GEO>
 __global__ void __launch_bounds__(128, Pol::MIN_BLOCKS)
 cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
 {
@@ -703,9 +706,11 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
     }
     // every lane takes part (a policy may evaluate warp-collective code); lanes
     // without a member do no work and get no flags
-    flags = Pol::collide(live, p, ic, r1, mctx, prm.k0, prm.k1, rec, sink);
+    flags = Pol::template collide<GEO>(live, p, ic, r1, mctx, prm.k0, prm.k1, rec, sink);
     if (live)
     {
+      if (flags & CF_VOID)
+        --sink.a_coll; // the member left without a collision (no checkPKAState)
       sink.tick();
       if (!(flags & CF_DONE) && ic >= prm.max_collisions)
       {

@@ -18,6 +18,7 @@
 #include "mtg_common.cuh"
 #include "mtg_collide64.cuh"
 #include "mtg_engine.cuh"
+#include "mtg_geometry.cuh"
 #include "mtg_kernels.h"
 #include "mtg_scatter32.cuh"
 #include "mtg_surrogate.cuh"
@@ -193,19 +194,35 @@ struct Fp32Policy
     float eps, b;  // reduced energy and impact parameter
     float ls, dee; // flight length and electronic loss
     uint32_t azimuth;
+    bool gone;     // outside the sample: no collision, the member is dropped
   };
 
   // flight, target atom and electronic loss (trim.C:80-170)
+  template <bool GEO>
   static __device__ __forceinline__ PhaseA phase_a(P32 & p, uint32_t ic, float r1, const MemberCtx & m, uint32_t k0,
                                                    uint32_t k1)
   {
     const Sim32 & sim = *m.sim;
-    // material lookup (sample_layers.C:27-43)
-    int layer = 0;
-    while (layer < sim.n_layers - 1 && !(p.x < sim.layer_end[layer]))
-      ++layer;
-    const int k = sim.layer_mat[layer];
     PhaseA a;
+    // material lookup: SampleLayers (sample_layers.C:27-43) or sampleClusters
+    // (sample_clusters.C:42-53)
+    int k;
+    a.gone = false;
+    if (GEO && sim.geometry == 1)
+    {
+      const float pos[3] = {p.x, p.y, p.z};
+      const int l = cluster_lookup<float>(pos, sim.w, sim.bc, sim.kn, sim.kd, sim.cmr, sim.cl, sim.cl_next,
+                                          sim.cl_head, sim.n_clusters);
+      a.gone = l == -2; // no material: the member is dropped (trim.C:81-83)
+      k = l >= 0 ? 1 : 0;
+    }
+    else
+    {
+      int layer = 0;
+      while (layer < sim.n_layers - 1 && !(p.x < sim.layer_end[layer]))
+        ++layer;
+      k = sim.layer_mat[layer];
+    }
     a.mc = m.mrow + k;
     const Mat32 & mc = *a.mc;
 
@@ -249,7 +266,7 @@ struct Fp32Policy
     return a;
   }
 
-  template <class Sink>
+  template <bool GEO, class Sink>
   static __device__ __forceinline__ int collide(bool live, P32 & p, uint32_t ic, float r1, const MemberCtx & m,
                                                 uint32_t k0, uint32_t k1, P32 & rec, Sink & sink)
   {
@@ -261,13 +278,15 @@ struct Fp32Policy
       bool nn = false;
       if (live)
       {
-        a = phase_a(p, ic, r1, m, k0, k1);
-        nn = surrogate_in_domain(a.eps, a.b);
+        a = phase_a<GEO>(p, ic, r1, m, k0, k1);
+        nn = !a.gone && surrogate_in_domain(a.eps, a.b);
       }
       // every lane of the warp, with or without a member, evaluates the network
       const float o0 = surrogate_eval_warp(m.net, nn ? surrogate_x1(a.eps) : 0.0f, nn ? surrogate_x2(a.b) : 0.0f);
       if (!live)
         return 0;
+      if (a.gone)
+        return CF_DONE | CF_VOID;
       if (nn)
         surrogate_s2_from(a.eps, a.b, o0, s2, c2);
       else
@@ -280,7 +299,9 @@ struct Fp32Policy
     {
       if (!live)
         return 0;
-      a = phase_a(p, ic, r1, m, k0, k1);
+      a = phase_a<GEO>(p, ic, r1, m, k0, k1);
+      if (a.gone)
+        return CF_DONE | CF_VOID;
       scatter32(a.eps, a.b, s2, c2, niter);
     }
     sink.newton(niter);
@@ -430,15 +451,23 @@ launch_cascade32(const EngineParams & prm, const Fp32Tables & t, int grid, int b
   tabs.lnE_min = t.lnE_min;
   tabs.inv_dlnE = t.inv_dlnE;
   tabs.net = reinterpret_cast<const SurrogateNet *>(t.mlp);
-  const bool ev = prm.event_mask != 0;
-  if (surrogate && ev)
-    cascade_kernel<Fp32Policy<true>, true><<<grid, block, smem, st>>>(prm, tabs);
-  else if (surrogate)
-    cascade_kernel<Fp32Policy<true>, false><<<grid, block, smem, st>>>(prm, tabs);
-  else if (ev)
-    cascade_kernel<Fp32Policy<false>, true><<<grid, block, smem, st>>>(prm, tabs);
+  const int v = (prm.event_mask != 0 ? 1 : 0) + (prm.any_clusters != 0 ? 2 : 0);
+  if (surrogate)
+    switch (v)
+    {
+      case 0: cascade_kernel<Fp32Policy<true>, false, false><<<grid, block, smem, st>>>(prm, tabs); break;
+      case 1: cascade_kernel<Fp32Policy<true>, true, false><<<grid, block, smem, st>>>(prm, tabs); break;
+      case 2: cascade_kernel<Fp32Policy<true>, false, true><<<grid, block, smem, st>>>(prm, tabs); break;
+      default: cascade_kernel<Fp32Policy<true>, true, true><<<grid, block, smem, st>>>(prm, tabs); break;
+    }
   else
-    cascade_kernel<Fp32Policy<false>, false><<<grid, block, smem, st>>>(prm, tabs);
+    switch (v)
+    {
+      case 0: cascade_kernel<Fp32Policy<false>, false, false><<<grid, block, smem, st>>>(prm, tabs); break;
+      case 1: cascade_kernel<Fp32Policy<false>, true, false><<<grid, block, smem, st>>>(prm, tabs); break;
+      case 2: cascade_kernel<Fp32Policy<false>, false, true><<<grid, block, smem, st>>>(prm, tabs); break;
+      default: cascade_kernel<Fp32Policy<false>, true, true><<<grid, block, smem, st>>>(prm, tabs); break;
+    }
   return cudaGetLastError();
 }
 
@@ -455,22 +484,29 @@ occupancy_of(K kernel, int block, size_t smem, int * blocks_per_sm)
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kernel, block, smem);
 }
 
-// residency of the variant the launch will use (both variants get the shared-memory opt-in)
-cudaError_t
-occupancy32(int block, size_t smem, int * blocks_per_sm, int surrogate, int events)
+template <bool SG>
+static cudaError_t
+occupancy_variants(int block, size_t smem, int * occ)
 {
-  int other = 0;
-  if (surrogate)
-  {
-    cudaError_t e = occupancy_of(cascade_kernel<Fp32Policy<true>, true>, block, smem, events ? blocks_per_sm : &other);
-    if (e != cudaSuccess)
-      return e;
-    return occupancy_of(cascade_kernel<Fp32Policy<true>, false>, block, smem, events ? &other : blocks_per_sm);
-  }
-  cudaError_t e = occupancy_of(cascade_kernel<Fp32Policy<false>, true>, block, smem, events ? blocks_per_sm : &other);
+  cudaError_t e;
+  if ((e = occupancy_of(cascade_kernel<Fp32Policy<SG>, false, false>, block, smem, &occ[0])) != cudaSuccess ||
+      (e = occupancy_of(cascade_kernel<Fp32Policy<SG>, true, false>, block, smem, &occ[1])) != cudaSuccess ||
+      (e = occupancy_of(cascade_kernel<Fp32Policy<SG>, false, true>, block, smem, &occ[2])) != cudaSuccess)
+    return e;
+  return occupancy_of(cascade_kernel<Fp32Policy<SG>, true, true>, block, smem, &occ[3]);
+}
+
+// residency of the variant the launch will use; every variant gets the
+// shared-memory opt-in
+cudaError_t
+occupancy32(int block, size_t smem, int * blocks_per_sm, int surrogate, int events, int clusters)
+{
+  int occ[4] = {0, 0, 0, 0};
+  cudaError_t e = surrogate ? occupancy_variants<true>(block, smem, occ) : occupancy_variants<false>(block, smem, occ);
   if (e != cudaSuccess)
     return e;
-  return occupancy_of(cascade_kernel<Fp32Policy<false>, false>, block, smem, events ? &other : blocks_per_sm);
+  *blocks_per_sm = occ[(events ? 1 : 0) + (clusters ? 2 : 0)];
+  return cudaSuccess;
 }
 
 size_t

@@ -81,23 +81,29 @@ struct Fp64Policy
     return p;
   }
 
-  template <class Sink>
+  template <bool GEO, class Sink>
   static __device__ __forceinline__ int collide(bool live, P64 & p, uint32_t ic, double r1, const MemberCtx & m,
                                                 uint32_t k0, uint32_t k1, P64 & rec, Sink & sink)
   {
     if (!live)
       return 0;
-    return collide64(p, ic, r1, *m.sim, *m.sc, m.mrow, k0, k1, rec, sink);
+    return collide64<GEO>(p, ic, r1, *m.sim, *m.sc, m.mrow, k0, k1, rec, sink);
   }
 };
 
 cudaError_t
 launch_cascade64(const EngineParams & prm, int grid, int block, size_t smem, cudaStream_t st)
 {
-  if (prm.event_mask)
-    cascade_kernel<Fp64Policy, true><<<grid, block, smem, st>>>(prm, Fp64Policy::Tables{prm.species, prm.mats});
+  const Fp64Policy::Tables tabs{prm.species, prm.mats};
+  const bool ev = prm.event_mask != 0, geo = prm.any_clusters != 0;
+  if (ev && geo)
+    cascade_kernel<Fp64Policy, true, true><<<grid, block, smem, st>>>(prm, tabs);
+  else if (ev)
+    cascade_kernel<Fp64Policy, true, false><<<grid, block, smem, st>>>(prm, tabs);
+  else if (geo)
+    cascade_kernel<Fp64Policy, false, true><<<grid, block, smem, st>>>(prm, tabs);
   else
-    cascade_kernel<Fp64Policy, false><<<grid, block, smem, st>>>(prm, Fp64Policy::Tables{prm.species, prm.mats});
+    cascade_kernel<Fp64Policy, false, false><<<grid, block, smem, st>>>(prm, tabs);
   return cudaGetLastError();
 }
 
@@ -114,15 +120,20 @@ occupancy_of(K kernel, int block, size_t smem, int * blocks_per_sm)
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kernel, block, smem);
 }
 
-// residency of the variant the launch will use (both variants get the shared-memory opt-in)
+// residency of the variant the launch will use; every variant gets the
+// shared-memory opt-in
 cudaError_t
-occupancy64(int block, size_t smem, int * blocks_per_sm, int events)
+occupancy64(int block, size_t smem, int * blocks_per_sm, int events, int clusters)
 {
-  int other = 0;
-  cudaError_t e = occupancy_of(cascade_kernel<Fp64Policy, true>, block, smem, events ? blocks_per_sm : &other);
-  if (e != cudaSuccess)
+  int occ[4] = {0, 0, 0, 0};
+  cudaError_t e;
+  if ((e = occupancy_of(cascade_kernel<Fp64Policy, false, false>, block, smem, &occ[0])) != cudaSuccess ||
+      (e = occupancy_of(cascade_kernel<Fp64Policy, true, false>, block, smem, &occ[1])) != cudaSuccess ||
+      (e = occupancy_of(cascade_kernel<Fp64Policy, false, true>, block, smem, &occ[2])) != cudaSuccess ||
+      (e = occupancy_of(cascade_kernel<Fp64Policy, true, true>, block, smem, &occ[3])) != cudaSuccess)
     return e;
-  return occupancy_of(cascade_kernel<Fp64Policy, false>, block, smem, events ? &other : blocks_per_sm);
+  *blocks_per_sm = occ[(events ? 1 : 0) + (clusters ? 2 : 0)];
+  return cudaSuccess;
 }
 
 size_t

@@ -198,6 +198,17 @@ make_material(const mtg_scoef_row * rows, const SpeciesConst & sc, const mtg_mat
 }
 
 void
+patch_cluster_pointers(std::vector<SimDesc> & sims, const Cl4d * cl, const int * next, const int * head)
+{
+  for (SimDesc & d : sims)
+  {
+    d.cl = d.geometry == 1 && cl ? cl + d.cl_base : nullptr;
+    d.cl_next = d.geometry == 1 && next ? next + d.cl_base : nullptr;
+    d.cl_head = d.geometry == 1 && head ? head + d.cell_base : nullptr;
+  }
+}
+
+void
 build_fp32_tables(const HostTables & t, std::vector<Species32> & species, std::vector<Mat32> & mats,
                   std::vector<Sim32> & sims)
 {
@@ -265,6 +276,15 @@ build_fp32_tables(const HostTables & t, std::vector<Species32> & species, std::v
     o.cw = float(d.cw);
     o.range_mode = d.range_mode;
     o.primaries_only = d.primaries_only;
+    o.geometry = d.geometry;
+    o.n_clusters = d.n_clusters;
+    for (int k = 0; k < 3; ++k)
+    {
+      o.kn[k] = d.kn[k];
+      o.kd[k] = float(d.kd[k]);
+    }
+    o.cmr = float(d.cmr);
+    // cluster pointers: set where the device copies are made
   }
 }
 
@@ -313,10 +333,14 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
   out.mats.clear();
   out.stop_row_mat.clear();
   out.stop_row_species.clear();
+  out.clusters.clear();
+  out.cl_next.clear();
+  out.cl_head.clear();
   out.total_primaries = out.hist_total = out.voxel_total = 0;
   out.k0 = out.k1 = 0;
   out.emax = 0.0;
   out.any_evac = 0;
+  out.any_clusters = 0;
   out.members_est = 1.0;
   if (n_sims < 1 || !sims)
   {
@@ -377,6 +401,42 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
     {
       err = "a sample needs 1 to 8 layers";
       return MTG_ERR_BAD_INPUT;
+    }
+    if (smp.geometry != MTG_GEOM_LAYERS && smp.geometry != MTG_GEOM_CLUSTERS)
+    {
+      err = "unknown sample geometry";
+      return MTG_ERR_BAD_INPUT;
+    }
+    if (smp.geometry == MTG_GEOM_CLUSTERS)
+    {
+      if (smp.n_layers != 2)
+      {
+        err = "a cluster sample needs two materials (matrix, cluster)";
+        return MTG_ERR_BAD_INPUT;
+      }
+      long long cells = 1;
+      for (int i = 0; i < 3; ++i)
+      {
+        if (smp.cluster_hash[i] < 1 || !(smp.w[i] > 0.0))
+        {
+          err = "a cluster sample needs a positive box and at least one hash cell per axis";
+          return MTG_ERR_BAD_INPUT;
+        }
+        cells *= smp.cluster_hash[i];
+      }
+      if (cells > (1LL << 26) || smp.n_clusters < 0 || smp.n_clusters > (1LL << 26) ||
+          (smp.n_clusters > 0 && !smp.clusters))
+      {
+        err = "cluster sample: at most 2^26 hash cells and 2^26 clusters, with a cluster array";
+        return MTG_ERR_BAD_INPUT;
+      }
+      for (long long l = 0; l < smp.n_clusters; ++l)
+        if (!(smp.clusters[4 * l + 3] >= 0.0) || !std::isfinite(smp.clusters[4 * l]) ||
+            !std::isfinite(smp.clusters[4 * l + 1]) || !std::isfinite(smp.clusters[4 * l + 2]))
+        {
+          err = "cluster coordinates must be finite and radii non-negative";
+          return MTG_ERR_BAD_INPUT;
+        }
     }
     if (s.ion.Z < 1 || s.ion.Z > MTG_SCOEF_ROWS || !(s.ion.m > 0.0) || !(s.ion.E > 0.0))
     {
@@ -539,6 +599,48 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
     {
       err = "hist_evac_rows must be 0..64";
       return MTG_ERR_BAD_INPUT;
+    }
+    if (smp.geometry == MTG_GEOM_CLUSTERS)
+    {
+      // sampleClusters::initSpatialhash + addCluster (sample_clusters.C:139-225): the
+      // cell of a cluster is floor(c * kn / w) mod kn; each cell lists its clusters
+      // in insertion order
+      d.geometry = 1;
+      out.any_clusters = 1;
+      d.n_clusters = int(smp.n_clusters);
+      d.cl_base = (long long)out.clusters.size();
+      d.cell_base = (long long)out.cl_head.size();
+      long long cells = 1;
+      for (int i = 0; i < 3; ++i)
+      {
+        d.kn[i] = smp.cluster_hash[i];
+        d.kd[i] = smp.w[i] / double(d.kn[i]);
+        cells *= d.kn[i];
+      }
+      out.cl_head.resize(size_t(d.cell_base + cells), -1);
+      std::vector<int> tail(size_t(cells), -1);
+      d.cmr = 0.0;
+      for (long long l = 0; l < smp.n_clusters; ++l)
+      {
+        const double * c = smp.clusters + 4 * l;
+        int k[3];
+        for (int i = 0; i < 3; ++i)
+        {
+          k[i] = int(std::floor((c[i] * d.kn[i]) / smp.w[i])) % d.kn[i];
+          k[i] = k[i] < 0 ? k[i] + d.kn[i] : k[i];
+        }
+        const long long cell = k[0] + (long long)d.kn[0] * (k[1] + (long long)d.kn[1] * k[2]);
+        const int idx = int(l); // index within this sample
+        if (tail[size_t(cell)] < 0)
+          out.cl_head[size_t(d.cell_base + cell)] = idx;
+        else
+          out.cl_next[size_t(d.cl_base + tail[size_t(cell)])] = idx;
+        tail[size_t(cell)] = idx;
+        out.clusters.push_back(Cl4d{c[0], c[1], c[2], c[3]});
+        out.cl_next.push_back(-1);
+        if (c[3] > d.cmr)
+          d.cmr = c[3];
+      }
     }
     d.hist_evac_rows = s.hist_vac_n > 0 ? s.hist_evac_rows : 0;
     d.hist_evac_base = hist;

@@ -24,11 +24,19 @@ struct HostTables
   uint32_t k0 = 0, k1 = 0;                // Philox key
   double emax = 0.0;                      // largest primary energy
   int any_evac = 0;                       // some simulation keeps a vacancy-energy histogram
+  int any_clusters = 0;                   // some simulation has the cluster geometry
   double members_est = 1.0;               // expected cascade members per primary (launch heuristics)
   // stopping-table rows of the FP32 engine, one per distinct (species, material):
   // the MatConst entry and the species each row is built from
   std::vector<int> stop_row_mat, stop_row_species;
+  // clusters of all cluster samples of the run (SimDesc::cl_base / cell_base index them)
+  std::vector<Cl4d> clusters;
+  std::vector<int> cl_next, cl_head;
 };
+
+// Point the simulations' cluster pointers at arrays holding HostTables::clusters,
+// cl_next and cl_head (host or device copies).
+void patch_cluster_pointers(std::vector<SimDesc> & sims, const Cl4d * cl, const int * next, const int * head);
 
 // Build the tables; returns MTG_OK or MTG_ERR_BAD_INPUT with `err` set.
 int build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim * sims,

@@ -123,6 +123,28 @@ struct SimDesc
   // recoil, columns the vacancy depth bins
   int hist_evac_rows;
   long long hist_evac_base;
+  // sampleClusters geometry (geometry 1): spatial hash of kn cells of size kd,
+  // largest radius cmr; cluster arrays of the run (x, y, z, r; next in cell list;
+  // first cluster per cell) patched in as pointers where the tables live
+  int geometry;
+  int kn[3];
+  int n_clusters;
+  double kd[3];
+  double cmr;
+  long long cl_base, cell_base; // offsets into the run's cluster and cell arrays
+  const struct Cl4d * cl;
+  const int * cl_next;
+  const int * cl_head;
+};
+
+// one cluster: centre and radius
+struct Cl4d
+{
+  double x, y, z, r;
+};
+struct Cl4f
+{
+  float x, y, z, r;
 };
 
 // Totals per simulation (device accumulators, reduced on the host).
@@ -185,7 +207,15 @@ struct Sim32
   int bc[3];
   int n_layers, n_mat, mat_base, species_base;
   float Ef, flscale, tau, cw; // flscale = 1 / length scale
-  int range_mode, primaries_only, any_cut, pad;
+  int range_mode, primaries_only, any_cut, geometry;
+  // sampleClusters geometry (see SimDesc)
+  int kn[3];
+  int n_clusters;
+  float kd[3];
+  float cmr;
+  const Cl4f * cl;
+  const int * cl_next;
+  const int * cl_head;
 };
 
 // final state of a cascade member (IonBase::StateType, ion.h:75-84)
@@ -202,7 +232,8 @@ enum MemberState : int
 enum CollideFlags : int
 {
   CF_PUSH = 1, // the collision displaced a recoil to follow
-  CF_DONE = 2  // the member came to rest or left the sample
+  CF_DONE = 2, // the member came to rest or left the sample
+  CF_VOID = 4  // no collision happened: the member found no material and was dropped
 };
 
 enum ErrorBits : unsigned int

@@ -63,6 +63,12 @@ class SimSpec:
     hist_lateral_bin: float = 10.0       # lateral (y, z) histogram of stopping points
     hist_lateral_n: int = 0
     hist_evac_rows: int = 0              # vacancy-energy histogram rows (int(ln E))
+    # sampleClusters geometry: layers[0] is the matrix, layers[1] the cluster
+    # material; clusters is an (n, 4) array of x, y, z, r; cluster_hash the
+    # spatial-hash cells per axis (sampleClusters::initSpatialhash)
+    geometry: str = "layers"
+    clusters: Optional[np.ndarray] = None
+    cluster_hash: Tuple[int, int, int] = (1, 1, 1)
 
     def box(self):
         if self.size is not None:
@@ -101,6 +107,19 @@ class SimSpec:
         for i in range(3):
             s.sample.w[i] = w[i]
             s.sample.bc[i] = self.bc[i]
+        if self.geometry == "clusters":
+            if len(self.layers) != 2:
+                raise ValueError("a cluster sample needs two materials (matrix, cluster)")
+            cl = np.ascontiguousarray(self.clusters if self.clusters is not None else np.zeros((0, 4)),
+                                      dtype=np.float64).reshape(-1, 4)
+            s.sample.geometry = F.GEOM_CLUSTERS
+            for i in range(3):
+                s.sample.cluster_hash[i] = int(self.cluster_hash[i])
+            s.sample.n_clusters = len(cl)
+            s.sample.clusters = cl.ctypes.data_as(C.POINTER(C.c_double))
+            s._keep = cl  # the array must outlive the call that reads it
+        elif self.geometry != "layers":
+            raise ValueError("geometry is 'layers' or 'clusters'")
         s.ion.Z = self.Z
         s.ion.m = self.m
         s.ion.E = self.E
@@ -211,9 +230,11 @@ class Engine:
 
     # ---- runs
     def prepare(self, sims: Sequence[SimSpec]):
-        arr = (F.Sim * len(sims))(*[s.to_c() for s in sims])
+        cs = [s.to_c() for s in sims]
+        arr = (F.Sim * len(sims))(*cs)
         self._sims = list(sims)
         self._check(self.lib.mtg_prepare(self.ctx, arr, len(sims)))
+        del cs  # held until here: cluster arrays are read during mtg_prepare
 
     def launch(self, stream: Optional[int] = None):
         self._check(self.lib.mtg_launch_async(self.ctx, C.c_void_p(stream or 0)))

@@ -391,6 +391,8 @@ struct Engine
     t.vox_depth.assign(s.vox_n[0] > 0 ? s.vox_n[0] : 0, 0.0);
     out.type = s.out_type;
     out.base = s.out_base;
+    if (s.clusters)
+      hash.build(s);
     pk0 = s.seed;
     pk1 = 0x4D795452u; // fixed high key word for single-simulation runs
   }
@@ -402,6 +404,18 @@ struct Engine
     uint16.reset();
   }
   double drand() { return ureal(mt); }
+
+  runspec::ClusterHash hash; // cluster samples only
+
+  // material index at pos: SampleLayers::lookupLayer (sample_layers.C:27-43) or
+  // sampleClusters::lookupMaterial (sample_clusters.C:42-53; -1 = no material)
+  int material_at(const double pos[3]) const
+  {
+    if (!spec.clusters)
+      return layer_of(pos[0]);
+    const int l = hash.lookup(pos);
+    return l == -2 ? -1 : (l >= 0 ? 1 : 0);
+  }
 
   // SampleLayers::lookupLayer (sample_layers.C:27-43)
   int layer_of(double x) const
@@ -444,7 +458,10 @@ struct Engine
     do
     {
       ++ic;
-      Mat & mat = mats[layer_of(pka.pos[0])];
+      const int mi = material_at(pka.pos);
+      if (mi < 0)
+        break; // outside the sample: the member is dropped (trim.C:81-83)
+      Mat & mat = mats[mi];
       norm3(pka.dir);
 
       // maximum impact parameter and free flight (trim.C:88-94)

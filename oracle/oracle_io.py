@@ -57,6 +57,11 @@ def spec_text(sim, seed=1, philox=True, first=0, n=None, records=0, tmin=None, o
         lines.append(f"records {records}")
     if output is not None:
         lines.append(f"output {output[0]} {output[1]}")
+    if getattr(sim, "geometry", "layers") == "clusters":
+        k = sim.cluster_hash
+        lines.append(f"clusters {k[0]} {k[1]} {k[2]}")
+        for c in sim.clusters:
+            lines.append("cluster " + " ".join(repr(float(v)) for v in c))
     if scale != 1.0:
         lines.append(f"scale {scale!r}")
     if getattr(sim, "surface_binding", 0.0) > 0.0:

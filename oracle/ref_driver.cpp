@@ -19,6 +19,7 @@
 #include "element.h"
 #include "material.h"
 #include "sample_layers.h"
+#include "sample_clusters.h"
 #include "ion.h"
 #include "trim.h"
 
@@ -175,9 +176,19 @@ main()
   simconf.tmin = 0.2;
   simconf.setLengthScale(spec.scale);
 
-  SampleLayers sample(spec.size[0], spec.size[1], spec.size[2]);
+  // SampleLayers, or sampleClusters with the spec's clusters (material 0 the
+  // matrix, material 1 the clusters)
+  SampleLayers layers(spec.size[0], spec.size[1], spec.size[2]);
+  sampleClusters clusters(spec.size[0], spec.size[1], spec.size[2]);
+  SampleBase & sample = spec.clusters ? static_cast<SampleBase &>(clusters) : static_cast<SampleBase &>(layers);
   for (int i = 0; i < 3; ++i)
     sample.bc[i] = SampleBase::sampleBoundary(spec.bc[i]);
+  if (spec.clusters)
+  {
+    clusters.initSpatialhash(spec.kn[0], spec.kn[1], spec.kn[2]);
+    for (size_t l = 0; l + 3 < spec.cl.size(); l += 4)
+      clusters.addCluster(spec.cl[l], spec.cl[l + 1], spec.cl[l + 2], spec.cl[l + 3]);
+  }
   for (auto & l : spec.layers)
   {
     MaterialBase * material = new MaterialBase(&simconf, l.rho);
@@ -193,7 +204,7 @@ main()
     }
     material->prepare();
     sample.material.push_back(material);
-    sample.layerThickness.push_back(l.thickness);
+    layers.layerThickness.push_back(l.thickness);
   }
 
   OracleTrim trim(&simconf, &sample, spec);

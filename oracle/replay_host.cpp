@@ -181,6 +181,14 @@ main(int argc, char ** argv)
   sim.first_primary = 0;
   sim.tally_mode = spec.range_mode ? MTG_TALLY_RANGE : MTG_TALLY_VACCOUNT;
   sim.primaries_only = spec.primaries_only;
+  if (spec.clusters)
+  {
+    sim.sample.geometry = MTG_GEOM_CLUSTERS;
+    for (int i = 0; i < 3; ++i)
+      sim.sample.cluster_hash[i] = spec.kn[i];
+    sim.sample.n_clusters = (long long)(spec.cl.size() / 4);
+    sim.sample.clusters = spec.cl.data();
+  }
   mtg_config cfg;
   memset(&cfg, 0, sizeof cfg);
   cfg.tmin = 0.2;
@@ -194,6 +202,7 @@ main(int argc, char ** argv)
     fprintf(stderr, "replay_host: %s\n", err.c_str());
     return 2;
   }
+  patch_cluster_pointers(t.sims, t.clusters.data(), t.cl_next.data(), t.cl_head.data());
   const SimDesc & sd = t.sims[0];
   std::vector<P64> stack;
   for (long long n = spec.first; n < spec.first + spec.n; ++n)
@@ -228,7 +237,7 @@ main(int argc, char ** argv)
       {
         ++ic;
         P64 rec;
-        flags = collide64(m, ic, r1, sd, sc, mrow, t.k0, t.k1, rec, sink);
+        flags = collide64<true>(m, ic, r1, sd, sc, mrow, t.k0, t.k1, rec, sink);
         if (flags & CF_PUSH)
         {
           rec.sim = m.sim;

@@ -25,6 +25,10 @@
 //   records <n>                 emit per-primary records for the first n primaries
 //   sputter <Esurf>             count recoils leaving through x < 0 with E cos^2 > Esurf
 //   voxels nx ny nz ox oy oz sx sy sz   energy-deposition voxel box (depth profile reported)
+//   clusters <kx> <ky> <kz>     sampleClusters geometry (sample_clusters.C): the first
+//                               layer is the matrix, the second the cluster material;
+//                               kx ky kz spatial-hash cells (initSpatialhash)
+//   cluster <x> <y> <z> <r>     appends a spherical cluster (addCluster)
 //   output <type> <base>        write runmytrim's output file for type vaccount,
 //                               vacenergycount or range as <base>_vac.dat, _evac.dat
 //                               or _ranges.dat (runmytrim.C:185-206, 309)
@@ -83,6 +87,9 @@ struct Spec
   int vox_n[3] = {0, 0, 0};
   double vox_o[3] = {0, 0, 0}, vox_s[3] = {0, 0, 0};
   std::string out_type, out_base;
+  bool clusters = false;
+  int kn[3] = {1, 1, 1};
+  std::vector<double> cl; // x, y, z, r per cluster
 
   double total_thickness() const
   {
@@ -200,6 +207,17 @@ parse(std::istream & in, Spec & s, std::string & err)
       ok = bool(ls >> s.records);
     else if (key == "sputter")
       ok = bool(ls >> s.esurf);
+    else if (key == "clusters")
+    {
+      ok = bool(ls >> s.kn[0] >> s.kn[1] >> s.kn[2]) && s.kn[0] > 0 && s.kn[1] > 0 && s.kn[2] > 0;
+      s.clusters = true;
+    }
+    else if (key == "cluster")
+    {
+      double v[4];
+      ok = bool(ls >> v[0] >> v[1] >> v[2] >> v[3]);
+      s.cl.insert(s.cl.end(), v, v + 4);
+    }
     else if (key == "output")
       ok = bool(ls >> s.out_type >> s.out_base) &&
            (s.out_type == "vaccount" || s.out_type == "vacenergycount" || s.out_type == "range");
@@ -228,9 +246,115 @@ parse(std::istream & in, Spec & s, std::string & err)
       err = "layer without elements";
       return false;
     }
+  if (s.clusters && s.layers.size() != 2)
+  {
+    err = "a cluster sample needs two materials (matrix, cluster)";
+    return false;
+  }
   s.finalize();
   return true;
 }
+
+// The spatial hash of sampleClusters (sample_clusters.C:139-225): per cell the
+// head of a linked list of clusters in insertion order.
+struct ClusterHash
+{
+  int kn[3] = {1, 1, 1};
+  double w[3] = {1, 1, 1}, kd[3] = {1, 1, 1}, cmr = 0.0;
+  int bc[3] = {0, 0, 0};
+  std::vector<double> c; // x, y, z, r
+  std::vector<int> next, head;
+
+  void build(const Spec & s)
+  {
+    for (int i = 0; i < 3; ++i)
+    {
+      kn[i] = s.kn[i];
+      w[i] = s.size[i];
+      bc[i] = s.bc[i];
+      kd[i] = w[i] / double(kn[i]);
+    }
+    c = s.cl;
+    const size_t n = c.size() / 4;
+    next.assign(n, -1);
+    head.assign(size_t(kn[0]) * kn[1] * kn[2], -1);
+    std::vector<int> tail(head.size(), -1);
+    cmr = 0.0;
+    for (size_t l = 0; l < n; ++l)
+    {
+      int k[3];
+      for (int i = 0; i < 3; ++i)
+      {
+        k[i] = int(std::floor((c[4 * l + i] * kn[i]) / w[i])) % kn[i];
+        k[i] = k[i] < 0 ? k[i] + kn[i] : k[i];
+      }
+      const int cell = k[0] + kn[0] * (k[1] + kn[1] * k[2]);
+      if (head[cell] < 0)
+        head[cell] = int(l);
+      else
+        next[tail[cell]] = int(l);
+      tail[cell] = int(l);
+      if (c[4 * l + 3] > cmr)
+        cmr = c[4 * l + 3];
+    }
+  }
+
+  // sampleClusters::lookupCluster with dr = 0 (sample_clusters.C:60-130): the
+  // cluster containing pos, -1 in the matrix, -2 outside a CUT boundary
+  int lookup(const double pos[3]) const
+  {
+    int k[3], k1[3], k2[3];
+    for (int i = 0; i < 3; ++i)
+    {
+      k[i] = int(std::floor((pos[i] * kn[i]) / w[i]));
+      if (pos[i] < 0.0 || pos[i] >= w[i])
+      {
+        if (bc[i] == 2)
+          return -2;
+        if (bc[i] == 1)
+          return -1;
+        k[i] = k[i] % kn[i];
+        if (k[i] < 0)
+          k[i] += kn[i];
+      }
+      const int ks = int((cmr + 0.0) / kd[i]) + 1;
+      k1[i] = k[i] - ks;
+      k2[i] = k[i] + ks;
+      if (k1[i] < 0 && bc[i] != 0)
+        k1[i] = 0;
+      if (k2[i] >= kn[i] && bc[i] != 0)
+        k2[i] = kn[i] - 1;
+    }
+    int j[3];
+    for (j[0] = k1[0]; j[0] <= k2[0]; ++j[0])
+      for (j[1] = k1[1]; j[1] <= k2[1]; ++j[1])
+        for (j[2] = k1[2]; j[2] <= k2[2]; ++j[2])
+        {
+          int m[3];
+          for (int i = 0; i < 3; ++i)
+          {
+            m[i] = j[i] % kn[i];
+            if (m[i] < 0)
+              m[i] += kn[i];
+          }
+          for (int l = head[m[0] + kn[0] * (m[1] + kn[1] * m[2])]; l >= 0; l = next[l])
+          {
+            double dif[3];
+            for (int i = 0; i < 3; ++i)
+            {
+              dif[i] = pos[i] - c[4 * l + i];
+              if (bc[i] == 0)
+                dif[i] -= std::round(dif[i] / w[i]) * w[i];
+            }
+            const double r2 = dif[0] * dif[0] + dif[1] * dif[1] + dif[2] * dif[2];
+            const double rr = c[4 * l + 3] + 0.0;
+            if (r2 < rr * rr)
+              return l;
+          }
+        }
+    return -1;
+  }
+};
 
 // Tallies reported by both oracles (one line per key on stdout).
 struct Tally

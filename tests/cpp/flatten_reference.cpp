@@ -4,6 +4,7 @@
 #include "simconf.h"
 #include "material.h"
 #include "sample_layers.h"
+#include "sample_clusters.h"
 #include "trim_gpu.h"
 
 #include <cstdio>
@@ -50,5 +51,17 @@ int main()
              s.material[k].elements[j].Elbind);
   printf("ion %d %.17g %.17g %.17g %.17g %.17g %.17g\n", ion.Z, ion.m, ion.E, ion.Ef, ion.dir[0], ion.dir[1],
          ion.pos[1]);
+
+  // a cluster sample built with the reference's own hash and insertion
+  sampleClusters cs(400.0, 300.0, 200.0);
+  cs.initSpatialhash(8, 6, 4);
+  cs.addCluster(10.0, 20.0, 30.0, 5.0);
+  cs.addCluster(200.0, 150.0, 100.0, 7.5);
+  cs.material.push_back(m2);
+  cs.material.push_back(m1);
+  std::vector<double> storage;
+  mtg_sample c = mtg::flatten_clusters(cs, storage);
+  printf("clusters %d %d %lld %d %d %d %.17g %.17g\n", c.geometry, c.n_layers, c.n_clusters, c.cluster_hash[0],
+         c.cluster_hash[1], c.cluster_hash[2], c.clusters[4], c.clusters[7]);
   return 0;
 }

@@ -4,7 +4,29 @@ Each case: (SimSpec, master seed, number of per-primary records kept).
 """
 import math
 
+import numpy as np
+
 from mytrim_gb300.engine import ElementSpec, LayerSpec, SimSpec
+
+
+def random_clusters(n, r, gap, box, seed):
+    """n non-overlapping spheres of radius r, surfaces at least `gap` apart in a
+    periodic box (the placement rule of sampleClusters::addRandomClusters,
+    sample_clusters.C:228-250, with numpy's generator)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    while len(out) < n:
+        p = rng.uniform(0.0, 1.0, 3) * np.asarray(box)
+        ok = True
+        for q in out:
+            d = p - q[:3]
+            d -= np.round(d / box) * box
+            if d @ d < (2 * r + gap) ** 2:
+                ok = False
+                break
+        if ok:
+            out.append(np.array([p[0], p[1], p[2], r]))
+    return np.array(out)
 
 SI, O, CU = 28.086, 15.999, 63.546
 
@@ -34,6 +56,13 @@ CASES = {
                                   size=(1e9, 1e9, 1e9), bc=(2, 1, 1), surface_binding=3.0,
                                   voxel_n=(30, 4, 4), voxel_origin=(0.0, -100.0, -100.0),
                                   voxel_size=(300.0, 200.0, 200.0)), 5, 6),
+    # xenon into UO2 holding xenon bubbles (sampleClusters, periodic 400 A box)
+    "xe_uo2_clusters": (SimSpec(layers=[LayerSpec(400.0, 10.0, [ElementSpec(92, 235.0, 1.0), ElementSpec(8, 16.0, 2.0)]),
+                                        LayerSpec(400.0, 3.5, [ElementSpec(54, 132.0, 1.0)])],
+                                Z=54, m=132.0, E=30000.0, n_primaries=16, pos=(0.0, 200.0, 200.0),
+                                size=(400.0, 400.0, 400.0), geometry="clusters",
+                                clusters=random_clusters(40, 20.0, 25.0, (400.0, 400.0, 400.0), 3),
+                                cluster_hash=(19, 19, 19), hist_range_bin=10.0, hist_range_n=100), 5, 16),
     # protons into a two-element target
     "h_sic": (SimSpec(layers=[LayerSpec(100000.0, 3.21, [ElementSpec(14, SI, 1.0), ElementSpec(6, 12.011, 1.0)])],
                       Z=1, m=1.008, E=5000.0, n_primaries=40), 12, 40),

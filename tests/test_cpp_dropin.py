@@ -7,7 +7,7 @@ import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
 REF_SRCS = ["element.C", "material.C", "sample.C", "ion.C", "trim.C", "simconf.C", "sample_solid.C",
-            "sample_layers.C", "shim/point.C"]
+            "sample_layers.C", "sample_clusters.C", "shim/point.C"]
 
 
 def test_flatten_reference_objects(tmp_path):
@@ -27,5 +27,8 @@ def test_flatten_reference_objects(tmp_path):
     assert layers[5:8] == ["2", "0", "0"]
     el = [l.split() for l in out if l.startswith("el ")]
     assert [(int(e[4]), float(e[7])) for e in el] == [(14, 15.0), (8, 28.0), (14, 15.0)]
-    ion = out[-2].split()
+    ion = [l for l in out if l.startswith("ion ")][0].split()
     assert ion[1] == "33" and float(ion[3]) == 50000.0 and float(ion[4]) == 5.0
+    cl = [l for l in out if l.startswith("clusters ")][0].split()
+    # geometry 1, two materials, two clusters, hash 8x6x4, second centre x, second radius
+    assert cl[1:7] == ["1", "2", "2", "8", "6", "4"] and float(cl[7]) == 200.0 and float(cl[8]) == 7.5

@@ -407,3 +407,35 @@ def test_vacancy_energy_histogram(engine_lib, prec):
     e.close()
     assert t2["hist_evac"].sum() + t2["hist_dropped"] == t["hist_vac"].sum()
     assert t2["hist_dropped"] == h[2:].sum()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_cluster_sample_without_clusters_is_the_matrix(engine_lib, prec):
+    """A cluster sample with no clusters is the matrix everywhere: the same
+    trajectories, hence the same tallies, as a one-layer sample of it."""
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    from golden_cases import CASES as GC
+    base = GC["xe_uo2_clusters"][0]
+    empty = SimSpec(**{**base.__dict__, "clusters": np.zeros((0, 4)), "n_primaries": 30})
+    solid = SimSpec(**{**base.__dict__, "geometry": "layers", "layers": [base.layers[0]], "clusters": None,
+                       "n_primaries": 30})
+    e = Engine(precision=prec, seed=21)
+    a = e.run([empty])[0]
+    b = e.run([solid])[0]
+    e.close()
+    for k in ("members", "collisions", "vacancies", "replacements", "interstitials", "range_n", "Eel", "Enuc"):
+        assert a[k] == b[k], k
+
+
+def test_cluster_fp32_matches_fp64(engine_lib):
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    from golden_cases import CASES as GC
+    sim = SimSpec(**{**GC["xe_uo2_clusters"][0].__dict__, "n_primaries": 2000})
+    r = {}
+    for prec in ("fp64", "fp32"):
+        e = Engine(precision=prec, seed=33)
+        r[prec] = summarize(e.run([sim])[0])
+        e.close()
+    for key in ("vac_per_ion", "eel_per_ion", "range_mean"):
+        a, b = r["fp32"], r["fp64"]
+        assert _z(a, b, key) < 3.5 or abs(a[key] - b[key]) < 0.01 * abs(b[key]), key
