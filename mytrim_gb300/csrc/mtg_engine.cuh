@@ -228,8 +228,11 @@ struct LaneSink
     c.e_unf.reset();
     c.e_sput.reset();
   }
+  // per-member summaries feed the optional member records only
   __device__ void reset_member()
   {
+    if (!prm->records)
+      return;
     cold->m_vac = 0;
     cold->m_state = 0;
     cold->m_eel.reset();
@@ -344,7 +347,8 @@ struct LaneSink
       event(EV_LOST, Real(p.x), Real(p.y), Real(p.z), Real(p.E), Z1, p.gen, ST_LOST, e - Real(p.E), p.key);
     ++c.n_lost;
     c.e_lost.add(e);
-    c.m_state = ST_LOST;
+    if (prm->records)
+      c.m_state = ST_LOST;
     if (p.x < Real(0) && sim->bc[0] == 2)
     {
       if (p.gen == 0)
@@ -381,16 +385,18 @@ struct LaneSink
       else
         add = 1;
       a_vac += add;
-      cold->m_vac += add;
+      if (prm->records)
+        cold->m_vac += add;
       return;
     }
     ++a_vac;
-    ++cold->m_vac;
+    if (prm->records)
+      ++cold->m_vac;
     const int b = depth_bin(Real(rec.x), inv_vac_bin(), sim->hist_vac_n);
     if (b >= 0)
     {
       vac_bin = int(sim->hist_vac_base) + b;
-      if (sim->hist_evac_rows > 0)
+      if (prm->any_evac && sim->hist_evac_rows > 0)
       {
         // TrimVacEnergyCount::vacancyCreation (apps/src/TrimVacEnergyCount.C:32-53):
         // row int(ln E) of the recoil energy, negative rows in row 0
@@ -422,7 +428,8 @@ struct LaneSink
   {
     if constexpr (EV)
       event(EV_REST, Real(p.x), Real(p.y), Real(p.z), Real(p.E), Z1, p.gen, state, Real(0), p.key);
-    cold->m_state = state;
+    if (prm->records)
+      cold->m_state = state;
     a_enuc.add(Real(p.E));
     deposit(Real(p.x), Real(p.y), Real(p.z), Real(p.E));
     if (state == ST_INTERSTITIAL)
