@@ -304,6 +304,7 @@ typedef struct
 {
   double x, y, z;          /* position [length unit] */
   double E, aux;           /* energies [eV], meaning by kind */
+  double m;                /* mass [u] of the atom the event describes */
   unsigned long long key;  /* path key of the member that raised the event */
   long long primary;       /* primary index within its simulation (first_primary based) */
   int sim, kind, Z, gen, state, pad;

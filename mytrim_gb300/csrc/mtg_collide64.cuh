@@ -327,7 +327,7 @@ collide64(P64 & p, uint32_t ic, double r1, const SimDesc & sim, const SpeciesCon
   for (int i = 0; i < 3; ++i)
     if (sim.bc[i] == 2 && (pos[i] > sim.w[i] || pos[i] < 0.0))
     {
-      sink.lost(p.E + den, p, sc.Z1);
+      sink.lost(p.E + den, p, sc.Z1, sc.m1);
       return CF_DONE;
     }
 
@@ -337,7 +337,7 @@ collide64(P64 & p, uint32_t ic, double r1, const SimDesc & sim, const SpeciesCon
   if (rec.E > el.Edisp - el.Elbind)
   {
     sink.enuc(el.Elbind, rec.x, rec.y, rec.z);
-    sink.branch(rec, el.Z2, el.Elbind, p.key);
+    sink.branch(rec, el, p.key);
     const bool follow = sim.range_mode ? (rec.gen < 1) : !sim.primaries_only;
     if (follow)
     {
@@ -360,14 +360,14 @@ collide64(P64 & p, uint32_t ic, double r1, const SimDesc & sim, const SpeciesCon
   }
   else
   {
-    sink.dissipate(rec, rec.E, el.Z2, el.Elbind, p.key);
+    sink.dissipate(rec, rec.E, el, p.key);
     sink.enuc(rec.E + el.Elbind, rec.x, rec.y, rec.z);
     if (p.E < sim.Ef)
       state = ST_INTERSTITIAL;
   }
   if (state != ST_MOVING)
   {
-    sink.stop(state, p, sc.Z1);
+    sink.stop(state, p, sc.Z1, sc.m1);
     flags |= CF_DONE;
   }
   else if (!(p.E == p.E))

@@ -245,7 +245,7 @@ struct LaneSink
   }
 
   // ---- event log (opt-in): one entry per selected hook call
-  __device__ void event(int kind, Real x, Real y, Real z, Real E, int Z, int gen, int state, Real aux,
+  __device__ void event(int kind, Real x, Real y, Real z, Real E, int Z, Real m, int gen, int state, Real aux,
                         uint64_t key)
   {
     if (!(prm->event_mask & (1u << kind)))
@@ -267,23 +267,26 @@ struct LaneSink
     r.sim = int(sim - prm->sims);
     r.kind = kind;
     r.Z = Z;
+    r.m = double(m);
     r.gen = gen;
     r.state = state;
     r.pad = 0;
   }
   // followRecoil (trim.C:362): a displaced recoil, followed or not
-  template <class R>
-  __device__ void branch(const R & rec, int Z2, Real Elbind, uint64_t key)
+  template <class R, class E>
+  __device__ void branch(const R & rec, const E & el, uint64_t key)
   {
     if constexpr (EV)
-      event(EV_BRANCH, Real(rec.x), Real(rec.y), Real(rec.z), Real(rec.E), Z2, rec.gen, 0, Elbind, key);
+      event(EV_BRANCH, Real(rec.x), Real(rec.y), Real(rec.z), Real(rec.E), el.Z2, Real(el.m2), rec.gen, 0,
+            Real(el.Elbind), key);
   }
   // dissipateRecoilEnergy (trim.C:397-401): a recoil below the displacement energy
-  template <class R>
-  __device__ void dissipate(const R & rec, Real Erec, int Z2, Real Elbind, uint64_t key)
+  template <class R, class E>
+  __device__ void dissipate(const R & rec, Real Erec, const E & el, uint64_t key)
   {
     if constexpr (EV)
-      event(EV_DISSIPATE, Real(rec.x), Real(rec.y), Real(rec.z), Erec, Z2, rec.gen, 0, Elbind, key);
+      event(EV_DISSIPATE, Real(rec.x), Real(rec.y), Real(rec.z), Erec, el.Z2, Real(el.m2), rec.gen, 0,
+            Real(el.Elbind), key);
   }
 
   // ---- events raised by the collision code (the reference's hooks, trim.h:72-84)
@@ -340,11 +343,11 @@ struct LaneSink
   // with it, trim.C:357); through the entrance surface a recoil counts as sputtered
   // when E cos^2 > E_surf, a primary as backscattered
   template <class P>
-  __device__ void lost(Real e, const P & p, int Z1)
+  __device__ void lost(Real e, const P & p, int Z1, Real m1)
   {
     LaneCold<Acc> & c = *cold;
     if constexpr (EV)
-      event(EV_LOST, Real(p.x), Real(p.y), Real(p.z), Real(p.E), Z1, p.gen, ST_LOST, e - Real(p.E), p.key);
+      event(EV_LOST, Real(p.x), Real(p.y), Real(p.z), Real(p.E), Z1, m1, p.gen, ST_LOST, e - Real(p.E), p.key);
     ++c.n_lost;
     c.e_lost.add(e);
     if (prm->records)
@@ -365,7 +368,8 @@ struct LaneSink
   __device__ void vacancy(const R & rec, const E & el, Real Erec, uint64_t key)
   {
     if constexpr (EV)
-      event(EV_VACANCY, Real(rec.x), Real(rec.y), Real(rec.z), Erec, el.Z2, rec.gen, 0, Real(el.Elbind), key);
+      event(EV_VACANCY, Real(rec.x), Real(rec.y), Real(rec.z), Erec, el.Z2, Real(el.m2), rec.gen, 0,
+            Real(el.Elbind), key);
     if (range_mode)
     {
       // TrimRange::vacancyCreation (apps/src/TrimRange.C:32-47): Kinchin-Pease
@@ -415,7 +419,8 @@ struct LaneSink
   __device__ void replacement(const R & rec, const E & el, Real Erec, uint64_t key)
   {
     if constexpr (EV)
-      event(EV_REPLACEMENT, Real(rec.x), Real(rec.y), Real(rec.z), Erec, el.Z2, rec.gen, 0, Real(el.Elbind), key);
+      event(EV_REPLACEMENT, Real(rec.x), Real(rec.y), Real(rec.z), Erec, el.Z2, Real(el.m2), rec.gen, 0,
+            Real(el.Elbind), key);
     ++cold->n_repl;
     const int b = depth_bin(Real(rec.x), inv_vac_bin(), sim->hist_vac_n);
     if (b >= 0)
@@ -424,10 +429,10 @@ struct LaneSink
       ++cold->n_dropped;
   }
   template <class P>
-  __device__ void stop(int state, const P & p, int Z1)
+  __device__ void stop(int state, const P & p, int Z1, Real m1)
   {
     if constexpr (EV)
-      event(EV_REST, Real(p.x), Real(p.y), Real(p.z), Real(p.E), Z1, p.gen, state, Real(0), p.key);
+      event(EV_REST, Real(p.x), Real(p.y), Real(p.z), Real(p.E), Z1, m1, p.gen, state, Real(0), p.key);
     if (prm->records)
       cold->m_state = state;
     a_enuc.add(Real(p.E));

@@ -384,7 +384,7 @@ struct Fp32Policy
       for (int i = 0; i < 3; ++i)
         if (sim.bc[i] == 2 && (pos[i] > sim.w[i] || pos[i] < 0.0f))
         {
-          sink.lost(p.E + p.El + den, p, m.sc->Z1);
+          sink.lost(p.E + p.El + den, p, m.sc->Z1, m.sc->m1);
           return CF_DONE;
         }
     }
@@ -395,7 +395,7 @@ struct Fp32Policy
     if (recE > el.disp_thresh)
     {
       sink.enuc(el.Elbind, rec.x, rec.y, rec.z);
-      sink.branch(rec, el.Z2, el.Elbind, p.key);
+      sink.branch(rec, el, p.key);
       const bool follow = sim.range_mode ? (rec.gen < 1) : !sim.primaries_only;
       if (follow)
       {
@@ -418,7 +418,7 @@ struct Fp32Policy
     }
     else
     {
-      sink.dissipate(rec, recE, el.Z2, el.Elbind, p.key);
+      sink.dissipate(rec, recE, el, p.key);
       sink.enuc(den, rec.x, rec.y, rec.z);
       if (p.E < sim.Ef)
         state = ST_INTERSTITIAL;
@@ -427,7 +427,7 @@ struct Fp32Policy
     {
       p.E += p.El;
       p.El = 0.0f;
-      sink.stop(state, p, m.sc->Z1);
+      sink.stop(state, p, m.sc->Z1, m.sc->m1);
       flags |= CF_DONE;
     }
     else if (!(p.E == p.E))

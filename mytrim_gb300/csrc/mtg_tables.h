@@ -161,7 +161,7 @@ struct SimTotals
 // One entry of the event log (layout of mtg_event).
 struct EventRec
 {
-  double x, y, z, E, aux;
+  double x, y, z, E, aux, m;
   uint64_t key;
   long long primary;
   int sim, kind, Z, gen, state, pad;

@@ -1,0 +1,73 @@
+"""Text streams of the reference's event-logging TrimBase subclasses, written from
+the engine's event log (``Engine.set_event_log`` / ``Engine.events``).
+
+* ``defect_log`` -- TrimDefectLog (trim.C:467-483): "V <ion>" for every vacancy
+  (the displaced recoil), "I", "S" or "R" <ion> for every member that came to rest
+  as an interstitial, substitutional or replacement;
+* ``phonon_log`` -- TrimPhononOut (trim.C:504-527): "<E> <ion>" for every energy
+  left in the lattice: the binding energy of each displaced recoil, the energy plus
+  binding energy of each recoil below the displacement energy, the residual energy
+  of each member that came to rest.
+
+``<ion>`` is IonBase's stream form (ion.C:74-79): x y z Z m E id gen tag, numbers as
+std::ostream prints them (six significant digits).  The engine has no sequential
+ion ids and no cluster tags: the member's path key stands in for the id (of the
+member that raised the event) and the tag is -1.  The GPU writes events in no
+particular order; the lines are sorted by simulation, primary, path key and kind.
+"""
+from typing import Iterable, TextIO
+
+import numpy as np
+
+from . import _ffi as F
+
+_REST_LETTER = {1: "R", 2: "S", 3: "I"}  # IonBase::StateType (ion.h:75-84)
+
+
+def _g(v: float) -> str:
+    return "%g" % v
+
+
+def _ion(e) -> str:
+    return (f"{_g(e['x'])} {_g(e['y'])} {_g(e['z'])} {int(e['Z'])} {_g(e['m'])} {_g(e['E'])} "
+            f"{int(e['key'])} {int(e['gen'])} -1 ")
+
+
+def _sorted(events: np.ndarray) -> np.ndarray:
+    order = np.lexsort((events["kind"], events["key"], events["primary"], events["sim"]))
+    return events[order]
+
+
+def defect_log(events: np.ndarray) -> Iterable[str]:
+    """Lines of TrimDefectLog for events logged with kinds EV_VACANCY and EV_REST."""
+    for e in _sorted(events):
+        k = int(e["kind"])
+        if k == F.EV_VACANCY:
+            yield "V " + _ion(e)
+        elif k == F.EV_REST and int(e["state"]) in _REST_LETTER:
+            yield _REST_LETTER[int(e["state"])] + " " + _ion(e)
+
+
+def phonon_log(events: np.ndarray) -> Iterable[str]:
+    """Lines of TrimPhononOut for events logged with kinds EV_BRANCH, EV_DISSIPATE
+    and EV_REST."""
+    for e in _sorted(events):
+        k = int(e["kind"])
+        if k == F.EV_BRANCH:
+            yield f"{_g(e['aux'])} " + _ion(e)
+        elif k == F.EV_DISSIPATE:
+            yield f"{_g(e['E'] + e['aux'])} " + _ion(e)
+        elif k == F.EV_REST:
+            yield f"{_g(e['E'])} " + _ion(e)
+
+
+def write(lines: Iterable[str], out: TextIO) -> int:
+    n = 0
+    for line in lines:
+        out.write(line + "\n")
+        n += 1
+    return n
+
+
+DEFECT_KINDS = (F.EV_VACANCY, F.EV_REST)
+PHONON_KINDS = (F.EV_BRANCH, F.EV_DISSIPATE, F.EV_REST)

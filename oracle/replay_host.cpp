@@ -37,16 +37,16 @@ struct HostSink
   void numeric() {}
   void enuc(double, double, double, double) {}
   void unfollowed(double) {}
-  template <class R>
-  void branch(const R &, int, double, uint64_t)
+  template <class R, class E>
+  void branch(const R &, const E &, uint64_t)
   {
   }
-  template <class R>
-  void dissipate(const R &, double, int, double, uint64_t)
+  template <class R, class E>
+  void dissipate(const R &, double, const E &, uint64_t)
   {
   }
   template <class P>
-  void lost(double, const P &, int)
+  void lost(double, const P &, int, double)
   {
     m_state = ST_LOST;
   }
@@ -78,7 +78,7 @@ struct HostSink
   {
   }
   template <class P>
-  void stop(int state, const P &, int)
+  void stop(int state, const P &, int, double)
   {
     m_state = state;
   }

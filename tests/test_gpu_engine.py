@@ -439,3 +439,23 @@ def test_cluster_fp32_matches_fp64(engine_lib):
     for key in ("vac_per_ion", "eel_per_ion", "range_mean"):
         a, b = r["fp32"], r["fp64"]
         assert _z(a, b, key) < 3.5 or abs(a[key] - b[key]) < 0.01 * abs(b[key]), key
+
+
+def test_event_streams(engine_lib):
+    """TrimDefectLog / TrimPhononOut text from the event log: one V line per vacancy,
+    one I/S/R line per member at rest with that state, ten fields per ion."""
+    from mytrim_gb300 import streams
+    sim = _cu_sim(n=50)
+    e = Engine(precision="fp64", seed=19)
+    e.set_event_log(set(streams.DEFECT_KINDS) | set(streams.PHONON_KINDS), 5_000_000)
+    t = e.run([sim])[0]
+    ev = e.events()
+    e.close()
+    d = list(streams.defect_log(ev))
+    assert sum(l.startswith("V ") for l in d) == t["vacancies"]
+    assert sum(l.startswith("I ") for l in d) == t["interstitials"]
+    assert sum(l.startswith("S ") for l in d) == t["substitutionals"]
+    assert all(len(l.split()) == 10 for l in d)
+    p = list(streams.phonon_log(ev))
+    assert all(len(l.split()) == 10 for l in p)
+    assert sum(float(l.split()[0]) for l in p) == pytest.approx(t["Enuc"], rel=1e-4)  # 6-digit text
