@@ -13,6 +13,8 @@
 #include <math.h>
 #include <string.h>
 
+#include "mtg_fp64_tables.h"
+
 #if defined(__CUDACC__)
 #define MTG_HD __host__ __device__ __forceinline__
 #else
@@ -165,9 +167,35 @@ pow2i(int k)
   return bits_to_double(uint64_t(k + 1023) << 52);
 }
 
-// e^x.  Cody-Waite reduction x = k ln2 + r with ln2 split into a 42-bit head
-// (k * head is exact for |k| < 2^11) and a tail, |r| <= ln2/2, then the Taylor
-// series of e^r to degree 13 (truncation below 5e-18 relative), scaled by 2^k.
+// ---- table-driven FP64 exp and log (P. T. P. Tang, ACM TOMS 15 (1989) 144; 16
+// (1990) 378).  Tables from gen_fp64_tables.py (mtg_fp64_tables.h); the device
+// reads its own copies in global memory, the host build (replay) the same values.
+namespace fp64tab
+{
+#if defined(__CUDACC__)
+static __device__ const double d_exp_hi[64] = {MTG_EXP_TABLE_HI};
+static __device__ const double d_exp_lo[64] = {MTG_EXP_TABLE_LO};
+static __device__ const double d_log_invc[92] = {MTG_LOG_INVC};
+static __device__ const double d_log_hi[92] = {MTG_LOG_TABLE_HI};
+static __device__ const double d_log_lo[92] = {MTG_LOG_TABLE_LO};
+#endif
+static const double h_exp_hi[64] = {MTG_EXP_TABLE_HI};
+static const double h_exp_lo[64] = {MTG_EXP_TABLE_LO};
+static const double h_log_invc[92] = {MTG_LOG_INVC};
+static const double h_log_hi[92] = {MTG_LOG_TABLE_HI};
+static const double h_log_lo[92] = {MTG_LOG_TABLE_LO};
+} // namespace fp64tab
+
+#if defined(__CUDA_ARCH__)
+#define MTG_TAB(name) fp64tab::d_##name
+#else
+#define MTG_TAB(name) fp64tab::h_##name
+#endif
+
+// e^x.  x = (64 m + j) ln2/64 + r with n = 64 m + j = rint(64 x / ln2), |r| <= ln2/128
+// (ln2/64 in two parts, the first with 29 significant bits so that n times it is
+// exact); e^x = 2^m (S_j + S_j p(r)), S_j = 2^(j/64) as a double pair and p the
+// Taylor polynomial of e^r - 1 to degree 6 (truncation below 3e-20 relative).
 MTG_HD double
 exp64(double x)
 {
@@ -175,34 +203,32 @@ exp64(double x)
     return 0.0;
   if (x > 709.7)
     return HUGE_VAL;
-  const double k = rint(x * 0x1.71547652b82fep+0);
-  double r = fma(-k, 0x1.62e42fefa3800p-1, x);
-  r = fma(-k, 0x1.ef35793c76730p-45, r);
-  double p = 0x1.6124613a86d09p-33; // 1/13!
-  p = fma(p, r, 0x1.1eed8eff8d898p-29); // 1/12!
-  p = fma(p, r, 0x1.ae64567f544e4p-26); // 1/11!
-  p = fma(p, r, 0x1.27e4fb7789f5cp-22); // 1/10!
-  p = fma(p, r, 0x1.71de3a556c734p-19); // 1/9!
-  p = fma(p, r, 0x1.a01a01a01a01ap-16); // 1/8!
-  p = fma(p, r, 0x1.a01a01a01a01ap-13); // 1/7!
-  p = fma(p, r, 0x1.6c16c16c16c17p-10); // 1/6!
-  p = fma(p, r, 0x1.1111111111111p-7);  // 1/5!
-  p = fma(p, r, 0x1.5555555555555p-5);  // 1/4!
-  p = fma(p, r, 0x1.5555555555555p-3);  // 1/3!
+  const double k = rint(x * MTG_EXP_INV_L);
+  double r = fma(-k, MTG_EXP_L1, x);
+  r = fma(-k, MTG_EXP_L2, r);
+  const int n = int(k);
+  const int j = n & 63;
+  const int m = (n - j) / 64;
+  double p = 0x1.6c16c16c16c17p-10;   // 1/720
+  p = fma(p, r, 0x1.1111111111111p-7); // 1/120
+  p = fma(p, r, 0x1.5555555555555p-5); // 1/24
+  p = fma(p, r, 0x1.5555555555555p-3); // 1/6
   p = fma(p, r, 0.5);
-  p = fma(p, r, 1.0);
-  p = fma(p, r, 1.0);
-  const int ki = int(k);
-  if (ki >= -1022)
-    return p * pow2i(ki);
+  p = fma(p, r * r, r);
+  const double sh = MTG_TAB(exp_hi)[j];
+  const double y = sh + fma(sh, p, MTG_TAB(exp_lo)[j]);
+  if (m >= -1022)
+    return y * pow2i(m);
   // subnormal results: scale in two steps
-  return (p * pow2i(ki + 600)) * pow2i(-600);
+  return (y * pow2i(m + 600)) * pow2i(-600);
 }
 
-// natural logarithm for finite x > 0.  x = m 2^e with m in (sqrt(1/2), sqrt(2)],
-// f = m - 1, s = f / (2 + f); log(1 + f) = 2 atanh(s) is summed as
-// f - hf + s (hf + R) with hf = f^2/2 and R = sum_{k=1..12} 2 s^{2k} / (2k + 1)
-// (the series tail is below 1e-19 relative for |s| <= 0.1716).
+// natural logarithm for finite x > 0.  x = 2^e m with m in (sqrt(1/2), sqrt(2)];
+// m falls in interval j of 0.703125 + j/128, whose approximate reciprocal inv_c has
+// at most 10 significant bits, so u = m inv_c - 1 is a single rounding (|u| < 1/128,
+// u = m - 1 exactly around 1); log x = e ln2 - log(inv_c) + log1p(u) with the
+// first two summed exactly (both multiples of 2^-42) and log1p(u) its Taylor
+// polynomial to degree 9 (truncation below 1e-20 relative).
 MTG_HD double
 log64(double x)
 {
@@ -222,26 +248,23 @@ log64(double x)
     m *= 0.5;
     e += 1;
   }
-  const double f = m - 1.0;
-  const double s = f / (2.0 + f);
-  const double z = s * s;
-  double R = 0x1.47ae147ae147bp-4;      // 2/25
-  R = fma(R, z, 0x1.642c8590b2164p-4);  // 2/23
-  R = fma(R, z, 0x1.8618618618618p-4);  // 2/21
-  R = fma(R, z, 0x1.af286bca1af28p-4);  // 2/19
-  R = fma(R, z, 0x1.e1e1e1e1e1e1ep-4);  // 2/17
-  R = fma(R, z, 0x1.1111111111111p-3);  // 2/15
-  R = fma(R, z, 0x1.3b13b13b13b14p-3);  // 2/13
-  R = fma(R, z, 0x1.745d1745d1746p-3);  // 2/11
-  R = fma(R, z, 0x1.c71c71c71c71cp-3);  // 2/9
-  R = fma(R, z, 0x1.2492492492492p-2);  // 2/7
-  R = fma(R, z, 0x1.999999999999ap-2);  // 2/5
-  R = fma(R, z, 0x1.5555555555555p-1);  // 2/3
-  R = R * z;
-  const double hf = 0.5 * f * f;
+  int j = int((m - 0.703125) * 128.0);
+  j = j < 0 ? 0 : (j > 91 ? 91 : j);
+  const double u = fma(m, MTG_TAB(log_invc)[j], -1.0);
+  // log1p(u) - u = u^2 (-1/2 + u/3 - u^2/4 + ... + u^7/9), Horner from the top
+  double q = 0x1.c71c71c71c71cp-4;      // 1/9
+  q = fma(q, u, -0x1.0000000000000p-3); // -1/8
+  q = fma(q, u, 0x1.2492492492492p-3);  // 1/7
+  q = fma(q, u, -0x1.5555555555555p-3); // -1/6
+  q = fma(q, u, 0x1.999999999999ap-3);  // 1/5
+  q = fma(q, u, -0x1.0000000000000p-2); // -1/4
+  q = fma(q, u, 0x1.5555555555555p-2);  // 1/3
+  q = fma(q, u, -0.5);                  // -1/2
+  q = q * (u * u);
   const double de = double(e);
-  return fma(de, 0x1.62e42fefa3800p-1,
-             f - (hf - fma(s, hf + R, de * 0x1.ef35793c76730p-45)));
+  const double hi = fma(de, MTG_LOG_LN2_HI, MTG_TAB(log_hi)[j]);
+  const double lo = fma(de, MTG_LOG_LN2_LO, MTG_TAB(log_lo)[j]);
+  return hi + (u + (lo + q));
 }
 
 // x^y for x >= 0 (every use in the engine has a positive base)
