@@ -167,7 +167,7 @@ def run_reference(a):
     oracle_io.build(None)
     reference = have_reference_build()
     per_core = a.cpu_per_core or 48
-    sim = W.silver_into_silicon(n_primaries=1)
+    sim = make_sim(a.workload, 1)
     rates = []
     cores = os.cpu_count() or 1
     for i in range(a.warmup + a.steps):
@@ -180,7 +180,8 @@ def run_reference(a):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": 1e3 * per_core * cores / value, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "primaries_per_step": per_core * cores, "path": "CPU, FP64, mt19937"},
+        "config": {"workload": WORKLOADS[a.workload][0], "primaries_per_step": per_core * cores,
+                   "path": "CPU, FP64, mt19937"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
                          "sample": f"{per_core} primaries per core x {cores} independent processes per step"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
