@@ -97,6 +97,7 @@ struct mtg_ctx
   int block = 128, grid = 0;
   size_t smem = 0;
   int cold_offset = 0;
+  int hist_smem_bins = 0, hist_smem_offset = 0;
   int stage = 0;
   int stack_cap = 0;
   long long ovf_cap = 0;
@@ -179,18 +180,37 @@ setup_launch_shape(mtg_ctx * ctx)
   size_t tables = ctx->stage ? tab : 0;
   if (!ctx->stage && prec == MTG_PREC_FP32_SURROGATE)
     tables = surrogate_net_bytes();
-  // per-thread tally slots follow the tables, 16-byte aligned
+  // per-thread tally slots follow the tables, 16-byte aligned, then the shared
+  // vacancy / replacement histogram of a single-simulation run with few bins
   ctx->cold_offset = int((tables + 15) / 16 * 16);
   const size_t slot = prec == MTG_PREC_FP64 ? cold_slot_bytes64() : cold_slot_bytes32();
   ctx->smem = size_t(ctx->cold_offset) + slot * size_t(ctx->block);
+  ctx->hist_smem_bins = 0;
   int bps = 0;
   const int events = ctx->event_cap > 0 && ctx->event_mask ? 1 : 0;
   const int clusters = t.any_clusters;
-  cudaError_t e = prec == MTG_PREC_FP64
-                      ? occupancy64(ctx->block, ctx->smem, &bps, events, clusters)
-                      : occupancy32(ctx->block, ctx->smem, &bps, prec == MTG_PREC_FP32_SURROGATE, events, clusters);
+  auto occupancy = [&](size_t smem, int * b) {
+    return prec == MTG_PREC_FP64
+               ? occupancy64(ctx->block, smem, b, events, clusters)
+               : occupancy32(ctx->block, smem, b, prec == MTG_PREC_FP32_SURROGATE, events, clusters);
+  };
+  cudaError_t e = occupancy(ctx->smem, &bps);
   if (e != cudaSuccess)
     return fail(ctx, MTG_ERR_CUDA, std::string("occupancy query: ") + cudaGetErrorString(e));
+  if (t.sims.size() == 1 && t.sims[0].hist_vac_n > 0 && 2 * t.sims[0].hist_vac_n <= HIST_SMEM_MAX)
+  {
+    // only where it leaves the resident blocks per SM unchanged
+    const int off = int((ctx->smem + 15) / 16 * 16);
+    const size_t smem2 = size_t(off) + sizeof(unsigned int) * 2 * size_t(t.sims[0].hist_vac_n);
+    int bps2 = 0;
+    if (occupancy(smem2, &bps2) == cudaSuccess && bps2 >= bps)
+    {
+      ctx->hist_smem_offset = off;
+      ctx->hist_smem_bins = 2 * t.sims[0].hist_vac_n;
+      ctx->smem = smem2;
+      bps = bps2;
+    }
+  }
   if (bps < 1)
     return fail(ctx, MTG_ERR_CUDA, "cascade kernel cannot be resident with this launch shape");
   ctx->grid = ctx->n_sm * bps;
@@ -234,6 +254,9 @@ fill_params(mtg_ctx * ctx, EngineParams & prm)
   }
   prm.stage_tables = ctx->stage;
   prm.cold_offset = ctx->cold_offset;
+  prm.hist_smem_bins = ctx->hist_smem_bins;
+  prm.hist_smem_offset = ctx->hist_smem_offset;
+  prm.hist_smem_base = ctx->hist_smem_bins ? t.sims[0].hist_vac_base : 0;
   prm.n_stage_species = int(t.species.size());
   prm.n_stage_mats = int(t.mats.size());
   prm.n_stage_stop_rows = int(t.stop_row_mat.size());

@@ -94,7 +94,16 @@ struct EngineParams
   int any_evac; // some simulation keeps a vacancy-energy histogram
   int any_clusters; // some simulation has the cluster geometry
   unsigned long long * warp_steps; // loop iterations of all warps (lane occupancy = collisions / 32 steps)
+  // single-simulation runs with few depth bins count vacancies and replacements in
+  // a per-block shared-memory histogram (hist_smem_bins counters from byte offset
+  // hist_smem_offset), added to the global one when the block ends; 0 = global atomics
+  int hist_smem_bins;
+  int hist_smem_offset;
+  long long hist_smem_base; // global index of shared bin 0
 };
+
+// largest vacancy + replacement histogram counted in shared memory (u32 counters)
+constexpr int HIST_SMEM_MAX = 2048;
 
 __device__ __forceinline__ unsigned int
 lanemask_lt()
@@ -582,6 +591,12 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
   extern __shared__ __align__(16) unsigned char smem[];
 
   // stage the tables of a single-simulation run in shared memory
+  // per-block vacancy / replacement counters (zeroed before the staging barrier)
+  unsigned int * s_hist = reinterpret_cast<unsigned int *>(smem + prm.hist_smem_offset);
+  for (int i = threadIdx.x; i < prm.hist_smem_bins; i += blockDim.x)
+    s_hist[i] = 0u;
+  if (prm.hist_smem_bins)
+    __syncthreads();
   const typename Pol::Tables tab = Pol::stage(prm, tabs, smem);
 
   const unsigned int FULL = 0xffffffffu;
@@ -766,7 +781,12 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
     {
       const int hb = sink.vac_bin >= 0 ? sink.vac_bin : sink.repl_bin;
       if (hb >= 0)
-        atomicAdd(prm.hist + hb, 1ull);
+      {
+        if (prm.hist_smem_bins)
+          atomicAdd(s_hist + (hb - prm.hist_smem_base), 1u);
+        else
+          atomicAdd(prm.hist + hb, 1ull);
+      }
     }
     if (prm.any_evac)
     {
@@ -803,6 +823,14 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
   sink.flush_prim();
   sink.flush_sim(cur_sim);
   sink.flush_voxel();
+  if (prm.hist_smem_bins)
+  {
+    // every warp of the block has left its loop: add the block's counts
+    __syncthreads();
+    for (int i = threadIdx.x; i < prm.hist_smem_bins; i += blockDim.x)
+      if (s_hist[i])
+        atomicAdd(prm.hist + prm.hist_smem_base + i, (unsigned long long)s_hist[i]);
+  }
   if (lane == 0)
   {
     atomicAdd(prm.warp_steps, (unsigned long long)(steps - 1)); // the last pass finds no work
