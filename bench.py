@@ -16,7 +16,9 @@ Printed JSON line (rank 0):
                totals out, uploads and read-back inside the timed region)
   fp64         the plain FP64 exact-scattering path on the same workload, and the
                relative difference of mean projected range fast vs FP64
-  roofline     the cascade kernel against the FP32 issue rate
+  roofline     the cascade kernel: 391 algorithmic operations per collision (300 + 91
+               per target element) against the FP32 issue rate, SMs x 128 lanes x
+               the measured SM clock
   cpu_baseline the CPU oracle (reference algorithm and RNG) on the host cores
 --impl reference times the reference's CPU implementation of the path (the
 reference library itself where it was built from source, else the oracle port
