@@ -191,6 +191,20 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
+def hbm_line(traffic, kernel_ms):
+    """The cascade kernel against the measured HBM copy bandwidth: the DRAM bytes of
+    one launch (ncu, profiles/cascade_fp32_agsi.md) over its CUDA-event time."""
+    peaks = ROOT / "MEASURED_PEAKS.json"
+    if traffic is None or not peaks.exists() or not kernel_ms:
+        return None
+    peak = json.loads(peaks.read_text()).get("hbm_gbs")
+    if not peak:
+        return None
+    achieved = traffic / (kernel_ms / 1e3) / 1e9
+    return {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
+
+
 def dist_setup(a):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -396,7 +410,8 @@ def main():
                      "peak_source": f"derived: {props.multi_processor_count} SMs x 128 FP32 lanes x "
                                     f"{sm_mhz:.0f} MHz measured (MEASURED_PEAKS.json has no FP32 figure)",
                      "work": f"{W_COLL} ops per collision x {per_launch_coll:.4g} collisions per launch",
-                     "kernel_ms": kms},
+                     "kernel_ms": kms,
+                     "hbm": hbm_line(traffic, kms)},
     }
     if not a.no_cpu and world == 1:
         cores = os.cpu_count() or 1
