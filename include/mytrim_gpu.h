@@ -57,8 +57,13 @@ typedef enum
 typedef enum
 {
   MTG_TALLY_VACCOUNT = 0, /* TrimVacCount semantics (apps/src/TrimVacCount.C:32-54) */
-  MTG_TALLY_RANGE = 1     /* TrimRange semantics: no recoil followed, Kinchin-Pease
+  MTG_TALLY_RANGE = 1,    /* TrimRange semantics: no recoil followed, Kinchin-Pease
                              vacancies (apps/src/TrimRange.C:32-47) */
+  MTG_TALLY_PRIMARIES = 2 /* TrimPrimaries (max_generation 1) / TrimRecoils (2): recoils
+                             of a generation below max_generation are followed; every
+                             displaced recoil is a vacancy, and one of generation
+                             max_generation adds the modified Kinchin-Pease count with
+                             the material's mean Z and mass (trim.C:446-464) */
 } mtg_tally_mode;
 
 /* One row of the stopping tables (SimconfType::ScoefLine, simconf.h:71-90). */
@@ -148,6 +153,8 @@ typedef struct
   double hist_lateral_bin; /* 2-D histogram of the primaries' stopping points in (y, z) around
                               the start position: bin width [length unit] */
   int hist_lateral_n;     /* bins per axis (0 = none); appended after the replacement bins */
+  int max_generation;     /* MTG_TALLY_PRIMARIES: TrimPrimaries::maxGen (1 for TrimPrimaries,
+                             2 for TrimRecoils, trim.h:113-133); ignored otherwise */
   int hist_evac_rows;     /* vacancy-energy histogram (TrimVacEnergyCount, apps/src/
                              TrimVacEnergyCount.C:32-53): rows int(ln E) of the displaced
                              recoil's energy (below 0 in row 0), hist_vac_n depth columns

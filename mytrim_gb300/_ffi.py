@@ -20,7 +20,7 @@ STATUS_NAMES = {
 
 PREC_FP64, PREC_FP32, PREC_FP32_SURROGATE = 0, 1, 2
 BC_PBC, BC_INF, BC_CUT = 0, 1, 2
-TALLY_VACCOUNT, TALLY_RANGE = 0, 1
+TALLY_VACCOUNT, TALLY_RANGE, TALLY_PRIMARIES = 0, 1, 2
 
 
 class ScoefRow(C.Structure):
@@ -59,7 +59,8 @@ class Sim(C.Structure):
                 ("primaries_only", C.c_int), ("hist_range_bin", C.c_double), ("hist_range_n", C.c_int),
                 ("hist_vac_bin", C.c_double), ("hist_vac_n", C.c_int), ("surface_binding", C.c_double),
                 ("voxel_n", C.c_int * 3), ("voxel_origin", C.c_double * 3), ("voxel_size", C.c_double * 3),
-                ("hist_lateral_bin", C.c_double), ("hist_lateral_n", C.c_int), ("hist_evac_rows", C.c_int)]
+                ("hist_lateral_bin", C.c_double), ("hist_lateral_n", C.c_int), ("max_generation", C.c_int),
+                ("hist_evac_rows", C.c_int)]
 
 
 class Config(C.Structure):

@@ -198,11 +198,12 @@ public:
   }
 
   // Full cascades of n primaries cloned from `pka` (direction and position as
-  // set on the template), tallied like TrimVacCount (or TrimRange with
-  // mode MTG_TALLY_RANGE) with TrimPhononOut energy accounting.
+  // set on the template), tallied like TrimVacCount (or TrimRange with mode
+  // MTG_TALLY_RANGE, TrimPrimaries / TrimRecoils with MTG_TALLY_PRIMARIES and
+  // max_generation 1 / 2) with TrimPhononOut energy accounting.
   mtg_totals runPrimaries(IonBase * pka, long long n, unsigned long long seed = 1,
                           int mode = MTG_TALLY_VACCOUNT, bool primaries_only = false,
-                          long long first_primary = 0)
+                          long long first_primary = 0, int max_generation = 1)
   {
     mtg_config cfg{};
     cfg.tmin = _simconf->tmin;
@@ -227,6 +228,7 @@ public:
     sim.first_primary = first_primary;
     sim.tally_mode = mode;
     sim.primaries_only = primaries_only ? 1 : 0;
+    sim.max_generation = max_generation;
     mtg_totals t{};
     _ctx.check(mtg_run(_ctx.get(), &sim, 1, &t, nullptr));
     _simconf->vacancies_created += int(t.vacancies);

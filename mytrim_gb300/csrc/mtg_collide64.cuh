@@ -338,7 +338,7 @@ collide64(P64 & p, uint32_t ic, double r1, const SimDesc & sim, const SpeciesCon
   {
     sink.enuc(el.Elbind, rec.x, rec.y, rec.z);
     sink.branch(rec, el, p.key);
-    const bool follow = sim.range_mode ? (rec.gen < 1) : !sim.primaries_only;
+    const bool follow = rec.gen < sim.follow_gen;
     if (follow)
     {
       const double s = 1.0 / sqrt(rec.dx * rec.dx + rec.dy * rec.dy + rec.dz * rec.dz);

@@ -379,6 +379,26 @@ struct LaneSink
     if constexpr (EV)
       event(EV_VACANCY, Real(rec.x), Real(rec.y), Real(rec.z), Erec, el.Z2, Real(el.m2), rec.gen, 0,
             Real(el.Elbind), key);
+    if (range_mode == 2)
+    {
+      // TrimPrimaries::vacancyCreation (trim.C:446-464): one vacancy per displaced
+      // recoil and, for a recoil of the cutoff generation (not followed), the
+      // modified Kinchin-Pease count with the material's mean Z and mass
+      unsigned int add = 1;
+      if (rec.gen == sim->kp_gen)
+      {
+        const Real az = Real(el.maz), am = Real(el.mam), Er = Erec;
+        const Real ed = Real(0.0115) * powr(az, Real(-7.0 / 3.0)) * Er;
+        const Real g = Real(3.4008) * powr(ed, Real(1.0 / 6.0)) + Real(0.40244) * powr(ed, Real(3.0 / 4.0)) + ed;
+        const Real kd = Real(0.1337) * powr(az, Real(2.0 / 3.0)) / sqrt(am);
+        const Real Ev = Er / (Real(1) + kd * g);
+        add += (unsigned int)(int(Real(0.8) * Ev / (Real(2) * Real(el.Edisp))));
+      }
+      a_vac += add;
+      if (prm->records)
+        cold->m_vac += add;
+      return;
+    }
     if (range_mode)
     {
       // TrimRange::vacancyCreation (apps/src/TrimRange.C:32-47): Kinchin-Pease

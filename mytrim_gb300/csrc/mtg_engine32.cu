@@ -396,7 +396,7 @@ struct Fp32Policy
     {
       sink.enuc(el.Elbind, rec.x, rec.y, rec.z);
       sink.branch(rec, el, p.key);
-      const bool follow = sim.range_mode ? (rec.gen < 1) : !sim.primaries_only;
+      const bool follow = rec.gen < sim.follow_gen;
       if (follow)
       {
         const float s = rsqrtf(rec.dx * rec.dx + rec.dy * rec.dy + rec.dz * rec.dz);

@@ -190,6 +190,8 @@ make_material(const mtg_scoef_row * rows, const SpeciesConst & sc, const mtg_mat
     ec.Edisp = e.Edisp;
     ec.Elbind = e.Elbind;
     ec.m2 = e.m;
+    ec.maz = az;
+    ec.mam = am;
     ec.Z2 = e.Z;
     ec.rspecies = -1;
     mc.sp[i] = make_stop_pair(rows, sc, e.Z);
@@ -245,6 +247,8 @@ build_fp32_tables(const HostTables & t, std::vector<Species32> & species, std::v
       f.Elbind = float(e.Elbind);
       f.m2 = float(e.m2);
       f.disp_thresh = float(e.Edisp - e.Elbind);
+      f.maz = float(e.maz);
+      f.mam = float(e.mam);
       f.Z2 = e.Z2;
       f.rspecies = e.rspecies;
     }
@@ -276,6 +280,8 @@ build_fp32_tables(const HostTables & t, std::vector<Species32> & species, std::v
     o.cw = float(d.cw);
     o.range_mode = d.range_mode;
     o.primaries_only = d.primaries_only;
+    o.follow_gen = d.follow_gen;
+    o.kp_gen = d.kp_gen;
     o.geometry = d.geometry;
     o.n_clusters = d.n_clusters;
     for (int k = 0; k < 3; ++k)
@@ -296,7 +302,8 @@ build_fp32_tables(const HostTables & t, std::vector<Species32> & species, std::v
 static double
 expected_members(const mtg_sim & s)
 {
-  if (s.tally_mode == MTG_TALLY_RANGE || s.primaries_only)
+  if (s.tally_mode == MTG_TALLY_RANGE || s.primaries_only ||
+      (s.tally_mode == MTG_TALLY_PRIMARIES && s.max_generation <= 1))
     return 1.0;
   const mtg_material & m = s.sample.material[0];
   double tt = 0.0, Z2 = 0.0, M2 = 0.0, Ed = 0.0;
@@ -537,8 +544,24 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
     d.invscale = 1.0 / cfg.length_scale;
     d.tau = cfg.tau;
     d.cw = cfg.cw;
-    d.range_mode = s.tally_mode == MTG_TALLY_RANGE;
+    if (s.tally_mode < MTG_TALLY_VACCOUNT || s.tally_mode > MTG_TALLY_PRIMARIES ||
+        (s.tally_mode == MTG_TALLY_PRIMARIES && s.max_generation < 1))
+    {
+      err = "unknown tally mode, or a generation cutoff below 1";
+      return MTG_ERR_BAD_INPUT;
+    }
+    d.range_mode = s.tally_mode;
     d.primaries_only = s.primaries_only != 0;
+    // which displaced recoils are followed (followRecoil): ThreadedTrimBase all, or
+    // none with primaries_only; TrimRange none (only generation 0 moves);
+    // TrimPrimaries / TrimRecoils those of a generation below maxGen (trim.h:113-133)
+    if (s.tally_mode == MTG_TALLY_RANGE)
+      d.follow_gen = 1;
+    else if (s.tally_mode == MTG_TALLY_PRIMARIES)
+      d.follow_gen = s.max_generation;
+    else
+      d.follow_gen = d.primaries_only ? 1 : 0x7fffffff;
+    d.kp_gen = s.tally_mode == MTG_TALLY_PRIMARIES ? s.max_generation : -1;
     d.prim_begin = prim;
     d.n_primaries = s.n_primaries;
     d.sim_key = uint64_t(si);

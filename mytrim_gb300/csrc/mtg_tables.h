@@ -67,6 +67,7 @@ struct ElemConst
   double ai;        // screening length with Z1
   double fi;        // reduced-energy factor with Z1
   double Edisp, Elbind, m2;
+  double maz, mam;  // the material's mean Z and mass (MaterialBase::_az, _am), for TrimPrimaries
   int Z2;
   int rspecies;     // species index (within the simulation) of a recoil of this element
 };
@@ -99,8 +100,10 @@ struct SimDesc
   double dir[3], pos[3];
   // run control
   double scale, invscale, tau, cw;
-  int range_mode;       // TrimRange semantics: no recoil followed, KP vacancies
+  int range_mode;       // tally mode: 0 TrimVacCount, 1 TrimRange, 2 TrimPrimaries / TrimRecoils
   int primaries_only;   // ThreadedTrimBase::_primaries_only
+  int follow_gen;       // a displaced recoil is followed iff its generation is below this
+  int kp_gen;           // TrimPrimaries: generation whose displaced recoils add a KP count
   long long prim_begin; // first global primary index of this simulation
   long long n_primaries;
   uint64_t sim_key;     // simulation number used in the member keys
@@ -183,7 +186,8 @@ struct Elem32
 {
   float t, my, ec, inv_ai, fi, Edisp, Elbind, m2;
   float disp_thresh; // Edisp - Elbind (trim.C:359)
-  int Z2, rspecies, pad;
+  float maz, mam;    // material mean Z and mass (TrimPrimaries)
+  int Z2, rspecies;
 };
 
 struct Mat32
@@ -208,6 +212,7 @@ struct Sim32
   int n_layers, n_mat, mat_base, species_base;
   float Ef, flscale, tau, cw; // flscale = 1 / length scale
   int range_mode, primaries_only, any_cut, geometry;
+  int follow_gen, kp_gen, pad0, pad1;
   // sampleClusters geometry (see SimDesc)
   int kn[3];
   int n_clusters;

@@ -50,7 +50,8 @@ class SimSpec:
     pos: Optional[Tuple[float, float, float]] = None  # default (0, w1/2, w2/2) as runmytrim.C:298
     size: Optional[Tuple[float, float, float]] = None  # default (total thickness, 100, 100)
     bc: Tuple[int, int, int] = (F.BC_PBC, F.BC_PBC, F.BC_PBC)
-    mode: str = "vaccount"               # or "range"
+    mode: str = "vaccount"               # or "range", or "primaries" (TrimPrimaries / TrimRecoils)
+    max_generation: int = 1              # mode "primaries": TrimPrimaries::maxGen
     primaries_only: bool = False
     hist_range_bin: float = 10.0
     hist_range_n: int = 0
@@ -130,7 +131,9 @@ class SimSpec:
             s.ion.pos[i] = p[i]
         s.n_primaries = self.n_primaries
         s.first_primary = self.first_primary
-        s.tally_mode = F.TALLY_RANGE if self.mode == "range" else F.TALLY_VACCOUNT
+        s.tally_mode = {"vaccount": F.TALLY_VACCOUNT, "range": F.TALLY_RANGE,
+                        "primaries": F.TALLY_PRIMARIES}[self.mode]
+        s.max_generation = self.max_generation
         s.primaries_only = int(self.primaries_only)
         s.hist_range_bin = self.hist_range_bin
         s.hist_range_n = self.hist_range_n

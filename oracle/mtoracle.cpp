@@ -627,7 +627,11 @@ struct Engine
           t.Enuc += el.Elbind;
           p_enuc += el.Elbind;
           t.deposit(rec.pos[0], rec.pos[1], rec.pos[2], el.Elbind);
-          const bool follow = spec.range_mode ? (rec.gen < 1) : !spec.primaries_only;
+          // followRecoil: TrimRange (TrimRange.h:16), TrimPrimaries / TrimRecoils
+          // (trim.h:119), ThreadedTrimBase (ThreadedTrimBase.h:12)
+          const bool follow = spec.range_mode       ? (rec.gen < 1)
+                              : spec.primaries_mode ? (rec.gen < spec.max_gen)
+                                                    : !spec.primaries_only;
           if (follow)
           {
             norm3(rec.dir);
@@ -638,7 +642,7 @@ struct Engine
           else
             t.Eunfollowed += rec.E;
           if (pka.E > el.Edisp)
-            vacancy(rec, el);
+            vacancy(rec, el, mat);
           else
           {
             replacement(rec);
@@ -664,8 +668,24 @@ struct Engine
     } while (pka.state == MOVING);
   }
 
-  void vacancy(const Ion & rec, const Elem & el)
+  void vacancy(const Ion & rec, const Elem & el, const Mat & mat)
   {
+    if (spec.primaries_mode)
+    {
+      // TrimPrimaries::vacancyCreation (trim.C:446-464)
+      long long add = 1;
+      if (rec.gen == spec.max_gen)
+      {
+        const double ed = 0.0115 * std::pow(mat.az, -7.0 / 3.0) * rec.E;
+        const double g = 3.4008 * std::pow(ed, 1.0 / 6.0) + 0.40244 * std::pow(ed, 3.0 / 4.0) + ed;
+        const double kd = 0.1337 * std::pow(mat.az, 2.0 / 3.0) / std::sqrt(mat.am);
+        const double Ev = rec.E / (1.0 + kd * g);
+        add += int(0.8 * Ev / (2.0 * el.Edisp));
+      }
+      t.vacancies += add;
+      p_vac += add;
+      return;
+    }
     if (spec.range_mode)
     {
       const double Ed = el.Edisp;

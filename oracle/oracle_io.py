@@ -44,7 +44,8 @@ def spec_text(sim, seed=1, philox=True, first=0, n=None, records=0, tmin=None, o
              f"pos {p[0]!r} {p[1]!r} {p[2]!r}",
              f"size {w[0]!r} {w[1]!r} {w[2]!r}",
              f"bc {sim.bc[0]} {sim.bc[1]} {sim.bc[2]}",
-             f"mode {sim.mode}", f"primaries_only {int(sim.primaries_only)}",
+             f"mode {sim.mode}" + (f" {sim.max_generation}" if sim.mode == "primaries" else ""),
+             f"primaries_only {int(sim.primaries_only)}",
              f"hist_range {sim.hist_range_bin!r} {sim.hist_range_n}",
              f"hist_vac {sim.hist_vac_bin!r} {sim.hist_vac_n}"]
     for l in sim.layers:

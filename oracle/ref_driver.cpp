@@ -29,11 +29,15 @@
 
 using namespace MyTRIM_NS;
 
-class OracleTrim : public TrimBase
+// The tally hooks over a reference trim class: TrimBase, or TrimPrimaries /
+// TrimRecoils (trim.h:113-133), whose own followRecoil and vacancyCreation then
+// decide and count.
+template <class Base>
+class OracleTrimT : public Base
 {
 public:
-  OracleTrim(SimconfType * simconf, SampleBase * sample, const runspec::Spec & spec)
-    : TrimBase(simconf, sample), _spec(spec)
+  OracleTrimT(SimconfType * simconf, SampleBase * sample, const runspec::Spec & spec)
+    : Base(simconf, sample), _spec(spec)
   {
     t.hist_range.assign(spec.hist_range_n, 0);
     t.hist_vac.assign(spec.hist_vac_n, 0);
@@ -50,6 +54,11 @@ public:
   int last_state = 0;
 
 protected:
+  using Base::_dee;
+  using Base::_element;
+  using Base::_pka;
+  using Base::_recoil;
+  using Base::_simconf;
   const runspec::Spec & _spec;
 
   bool followRecoil() override
@@ -58,7 +67,9 @@ protected:
     t.Enuc += _element->_Elbind;
     p_enuc += _element->_Elbind;
     t.deposit(_recoil->_pos(0), _recoil->_pos(1), _recoil->_pos(2), _element->_Elbind);
-    bool follow = _spec.range_mode ? (_recoil->_gen < 1) : !_spec.primaries_only;
+    bool follow = _spec.primaries_mode ? Base::followRecoil()
+                  : _spec.range_mode   ? (_recoil->_gen < 1)
+                                       : !_spec.primaries_only;
     if (!follow)
       t.Eunfollowed += _recoil->_E;
     return follow;
@@ -66,6 +77,16 @@ protected:
 
   void vacancyCreation() override
   {
+    if (_spec.primaries_mode)
+    {
+      // the reference class counts into vacancies_created (an int)
+      const int before = _simconf->vacancies_created;
+      Base::vacancyCreation();
+      const long long add = (long long)_simconf->vacancies_created - before;
+      t.vacancies += add;
+      p_vac += add;
+      return;
+    }
     if (_spec.range_mode)
     {
       // TrimRange::vacancyCreation (apps/src/TrimRange.C:32-47); the reference adds
@@ -155,59 +176,12 @@ protected:
   }
 };
 
+// runmytrim's loop (runmytrim.C:71-93, 288-302) over one trim class
+template <class Trim>
 int
-main()
+run_with(SimconfType & simconf, SampleBase & sample, const runspec::Spec & spec)
 {
-  runspec::Spec spec;
-  std::string err;
-  if (!runspec::parse(std::cin, spec, err))
-  {
-    fprintf(stderr, "ref_driver: %s\n", err.c_str());
-    return 2;
-  }
-  if (spec.philox)
-  {
-    fprintf(stderr, "ref_driver: the reference library only has mt19937 streams\n");
-    return 2;
-  }
-
-  SimconfType simconf;
-  simconf.fullTraj = false;
-  simconf.tmin = 0.2;
-  simconf.setLengthScale(spec.scale);
-
-  // SampleLayers, or sampleClusters with the spec's clusters (material 0 the
-  // matrix, material 1 the clusters)
-  SampleLayers layers(spec.size[0], spec.size[1], spec.size[2]);
-  sampleClusters clusters(spec.size[0], spec.size[1], spec.size[2]);
-  SampleBase & sample = spec.clusters ? static_cast<SampleBase &>(clusters) : static_cast<SampleBase &>(layers);
-  for (int i = 0; i < 3; ++i)
-    sample.bc[i] = SampleBase::sampleBoundary(spec.bc[i]);
-  if (spec.clusters)
-  {
-    clusters.initSpatialhash(spec.kn[0], spec.kn[1], spec.kn[2]);
-    for (size_t l = 0; l + 3 < spec.cl.size(); l += 4)
-      clusters.addCluster(spec.cl[l], spec.cl[l + 1], spec.cl[l + 2], spec.cl[l + 3]);
-  }
-  for (auto & l : spec.layers)
-  {
-    MaterialBase * material = new MaterialBase(&simconf, l.rho);
-    for (auto & e : l.el)
-    {
-      Element el;
-      el._Z = e.Z;
-      el._m = e.m;
-      el._t = e.t;
-      el._Edisp = e.Edisp;
-      el._Elbind = e.Elbind;
-      material->_element.push_back(el);
-    }
-    material->prepare();
-    sample.material.push_back(material);
-    layers.layerThickness.push_back(l.thickness);
-  }
-
-  OracleTrim trim(&simconf, &sample, spec);
+  Trim trim(&simconf, &sample, spec);
 
   // per-primary seeds from the master stream, as runmytrim.C:288-302 does
   simconf.seed(spec.seed);
@@ -264,4 +238,66 @@ main()
   trim.t.print(stdout);
   printf("wall_s %.6f\n", std::chrono::duration<double>(t1 - t0).count());
   return 0;
+}
+
+int
+main()
+{
+  runspec::Spec spec;
+  std::string err;
+  if (!runspec::parse(std::cin, spec, err))
+  {
+    fprintf(stderr, "ref_driver: %s\n", err.c_str());
+    return 2;
+  }
+  if (spec.philox)
+  {
+    fprintf(stderr, "ref_driver: the reference library only has mt19937 streams\n");
+    return 2;
+  }
+
+  SimconfType simconf;
+  simconf.fullTraj = false;
+  simconf.tmin = 0.2;
+  simconf.setLengthScale(spec.scale);
+
+  // SampleLayers, or sampleClusters with the spec's clusters (material 0 the
+  // matrix, material 1 the clusters)
+  SampleLayers layers(spec.size[0], spec.size[1], spec.size[2]);
+  sampleClusters clusters(spec.size[0], spec.size[1], spec.size[2]);
+  SampleBase & sample = spec.clusters ? static_cast<SampleBase &>(clusters) : static_cast<SampleBase &>(layers);
+  for (int i = 0; i < 3; ++i)
+    sample.bc[i] = SampleBase::sampleBoundary(spec.bc[i]);
+  if (spec.clusters)
+  {
+    clusters.initSpatialhash(spec.kn[0], spec.kn[1], spec.kn[2]);
+    for (size_t l = 0; l + 3 < spec.cl.size(); l += 4)
+      clusters.addCluster(spec.cl[l], spec.cl[l + 1], spec.cl[l + 2], spec.cl[l + 3]);
+  }
+  for (auto & l : spec.layers)
+  {
+    MaterialBase * material = new MaterialBase(&simconf, l.rho);
+    for (auto & e : l.el)
+    {
+      Element el;
+      el._Z = e.Z;
+      el._m = e.m;
+      el._t = e.t;
+      el._Edisp = e.Edisp;
+      el._Elbind = e.Elbind;
+      material->_element.push_back(el);
+    }
+    material->prepare();
+    sample.material.push_back(material);
+    layers.layerThickness.push_back(l.thickness);
+  }
+
+  if (!spec.primaries_mode)
+    return run_with<OracleTrimT<TrimBase>>(simconf, sample, spec);
+  if (spec.max_gen == 1)
+    return run_with<OracleTrimT<TrimPrimaries>>(simconf, sample, spec);
+  if (spec.max_gen == 2)
+    return run_with<OracleTrimT<TrimRecoils>>(simconf, sample, spec);
+  fprintf(stderr, "ref_driver: the reference has TrimPrimaries (1) and TrimRecoils (2) only\n");
+  return 2;
 }

@@ -51,8 +51,24 @@ struct HostSink
     m_state = ST_LOST;
   }
   template <class R, class E>
-  void vacancy(const R &, const E & el, double Erec, uint64_t)
+  void vacancy(const R & rec, const E & el, double Erec, uint64_t)
   {
+    if (range_mode == 2)
+    {
+      // TrimPrimaries::vacancyCreation, as the engine's sink
+      unsigned int add = 1;
+      if (rec.gen == sim->kp_gen)
+      {
+        const double az = el.maz, am = el.mam;
+        const double ed = 0.0115 * pow64(az, -7.0 / 3.0) * Erec;
+        const double g = 3.4008 * pow64(ed, 1.0 / 6.0) + 0.40244 * pow64(ed, 3.0 / 4.0) + ed;
+        const double kd = 0.1337 * pow64(az, 2.0 / 3.0) / sqrt(am);
+        const double Ev = Erec / (1.0 + kd * g);
+        add += (unsigned int)(int(0.8 * Ev / (2.0 * el.Edisp)));
+      }
+      m_vac += add;
+      return;
+    }
     if (range_mode)
     {
       const double Z = double(el.Z2), m = el.m2, Er = Erec;
@@ -179,7 +195,8 @@ main(int argc, char ** argv)
   sim.ion.Ef = spec.Ef;
   sim.n_primaries = spec.count;
   sim.first_primary = 0;
-  sim.tally_mode = spec.range_mode ? MTG_TALLY_RANGE : MTG_TALLY_VACCOUNT;
+  sim.tally_mode = spec.primaries_mode ? MTG_TALLY_PRIMARIES : (spec.range_mode ? MTG_TALLY_RANGE : MTG_TALLY_VACCOUNT);
+  sim.max_generation = spec.max_gen;
   sim.primaries_only = spec.primaries_only;
   if (spec.clusters)
   {

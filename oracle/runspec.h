@@ -17,7 +17,9 @@
 //   scale <l>                   length scale (simconf.C:75-80)
 //   layer <thickness> <rho>     appends a layer
 //   element <Z> <mass> <fraction> [<Edisp> <Elbind>]   appends to the last layer
-//   mode vaccount|range         vaccount: TrimVacCount; range: TrimRange (KP, gen cut)
+//   mode vaccount|range|primaries [<maxgen>]
+//                               vaccount: TrimVacCount; range: TrimRange (KP, gen cut);
+//                               primaries: TrimPrimaries (maxgen 1) / TrimRecoils (2)
 //   primaries_only 0|1          ThreadedTrimBase::_primaries_only
 //   hist_range <bin_A> <nbins>  histogram of primary stopping depth
 //   hist_vac <bin_A> <nbins>    histogram of vacancy depth (TrimVacCount bins are 1 A)
@@ -76,6 +78,8 @@ struct Spec
   double scale = 1.0;
   std::vector<LayerSpec> layers;
   bool range_mode = false;
+  bool primaries_mode = false; // TrimPrimaries / TrimRecoils
+  int max_gen = 1;
   bool primaries_only = false;
   double hist_range_bin = 10.0;
   int hist_range_n = 0;
@@ -190,6 +194,10 @@ parse(std::istream & in, Spec & s, std::string & err)
       std::string v;
       ok = bool(ls >> v);
       s.range_mode = (v == "range");
+      s.primaries_mode = (v == "primaries");
+      int g;
+      if (s.primaries_mode && (ls >> g))
+        s.max_gen = g;
     }
     else if (key == "primaries_only")
     {

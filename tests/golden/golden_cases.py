@@ -63,6 +63,16 @@ CASES = {
                                 size=(400.0, 400.0, 400.0), geometry="clusters",
                                 clusters=random_clusters(40, 20.0, 25.0, (400.0, 400.0, 400.0), 3),
                                 cluster_hash=(19, 19, 19), hist_range_bin=10.0, hist_range_n=100), 5, 16),
+    # TrimPrimaries / TrimRecoils: generation cutoff 1 and 2 with the modified
+    # Kinchin-Pease count at the cutoff (trim.C:446-464), into a two-element target
+    "xe_sic_primaries": (SimSpec(layers=[LayerSpec(100000.0, 3.21, [ElementSpec(14, SI, 1.0, 35.0, 3.0),
+                                                                     ElementSpec(6, 12.011, 1.0, 20.0, 3.0)])],
+                                 Z=54, m=131.29, E=30000.0, n_primaries=30, mode="primaries", max_generation=1,
+                                 hist_range_bin=10.0, hist_range_n=100), 17, 30),
+    "xe_sic_recoils": (SimSpec(layers=[LayerSpec(100000.0, 3.21, [ElementSpec(14, SI, 1.0, 35.0, 3.0),
+                                                                   ElementSpec(6, 12.011, 1.0, 20.0, 3.0)])],
+                               Z=54, m=131.29, E=30000.0, n_primaries=30, mode="primaries", max_generation=2,
+                               hist_range_bin=10.0, hist_range_n=100), 18, 30),
     # protons into a two-element target
     "h_sic": (SimSpec(layers=[LayerSpec(100000.0, 3.21, [ElementSpec(14, SI, 1.0), ElementSpec(6, 12.011, 1.0)])],
                       Z=1, m=1.008, E=5000.0, n_primaries=40), 12, 40),
