@@ -91,6 +91,15 @@ typedef struct
   mtg_element elements[MTG_MAX_ELEMENTS];
 } mtg_material;
 
+/* TrimBase::Potential (trim.h:63-69): the screened interatomic potential of the
+ * scattering, with its magic-formula constants (trim.C:194-258). */
+typedef enum
+{
+  MTG_POT_UNIVERSAL = 0, /* ZBL universal (the reference's default, trim.h:40) */
+  MTG_POT_MOLIERE = 1,
+  MTG_POT_CKR = 2        /* C-Kr, with the reference's derivative coefficients as written */
+} mtg_potential;
+
 typedef enum
 {
   MTG_GEOM_LAYERS = 0,  /* SampleLayers / SampleSolid */
@@ -159,6 +168,9 @@ typedef struct
                              TrimVacEnergyCount.C:32-53): rows int(ln E) of the displaced
                              recoil's energy (below 0 in row 0), hist_vac_n depth columns
                              each; 0 = none; appended after the lateral bins */
+  int potential;          /* TrimBase::_potential, an mtg_potential value; 0 = universal.  The
+                             learned surrogate covers the universal potential only: the
+                             other two scatter exactly on the surrogate path as well */
 } mtg_sim;
 
 /* Run-wide settings (SimconfType scalars, simconf.h:66). */
@@ -340,6 +352,11 @@ mtg_status mtg_stopping(mtg_ctx * ctx, int Z1, double m1, const mtg_material * m
  * Replaces: the scattering block of TrimBase::trim (trim.C:172-271). */
 mtg_status mtg_scatter(mtg_ctx * ctx, const double * eps, const double * b, long long n,
                        int precision, double * s2);
+/* mtg_scatter in the potential given as an mtg_potential value; the surrogate
+ * precision accepts only MTG_POT_UNIVERSAL.
+ * Replaces: the same block with TrimBase::_potential set (trim.C:194-258). */
+mtg_status mtg_scatter_potential(mtg_ctx * ctx, const double * eps, const double * b, long long n,
+                                 int precision, int potential, double * s2);
 
 /* Counters of the last run. */
 mtg_status mtg_get_stats(const mtg_ctx * ctx, mtg_stats * out);

@@ -39,6 +39,7 @@ class Material(C.Structure):
 
 
 GEOM_LAYERS, GEOM_CLUSTERS = 0, 1
+POT_UNIVERSAL, POT_MOLIERE, POT_CKR = 0, 1, 2
 
 
 class Sample(C.Structure):
@@ -60,7 +61,7 @@ class Sim(C.Structure):
                 ("hist_vac_bin", C.c_double), ("hist_vac_n", C.c_int), ("surface_binding", C.c_double),
                 ("voxel_n", C.c_int * 3), ("voxel_origin", C.c_double * 3), ("voxel_size", C.c_double * 3),
                 ("hist_lateral_bin", C.c_double), ("hist_lateral_n", C.c_int), ("max_generation", C.c_int),
-                ("hist_evac_rows", C.c_int)]
+                ("hist_evac_rows", C.c_int), ("potential", C.c_int)]
 
 
 class Config(C.Structure):
@@ -147,6 +148,8 @@ SIGNATURES = {
                                C.c_longlong, C.c_int, C.POINTER(C.c_double)]),
     "mtg_scatter": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_longlong, C.c_int,
                               C.POINTER(C.c_double)]),
+    "mtg_scatter_potential": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_longlong, C.c_int,
+                                        C.c_int, C.POINTER(C.c_double)]),
     "mtg_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "mtg_surrogate_train": (C.c_int, [_P, C.POINTER(SurrogateConfig), C.POINTER(SurrogateReport)]),
     "mtg_surrogate_get_params": (C.c_int, [_P, C.POINTER(C.c_float), C.c_longlong]),

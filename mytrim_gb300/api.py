@@ -103,7 +103,8 @@ class TrimGPU:
     """Drop-in for a runmytrim TrimBase subclass (TrimVacCount / TrimRange with
     TrimPhononOut energy accounting), running every primary's full cascade on the GPU."""
 
-    UNIVERSAL = 0
+    # TrimBase::Potential (trim.h:63-69); assign one to _potential
+    UNIVERSAL, MOLIERE, CKR = 0, 1, 2
 
     def __init__(self, simconf: SimconfType, sample: SampleBase, precision: str = "fp64", device: int = 0,
                  output: str = "vaccount", primaries_only: bool = False):
@@ -123,7 +124,7 @@ class TrimGPU:
                        dir=tuple(pka._dir), pos=tuple(pka._pos) if pka._pos else None, size=tuple(s.w),
                        bc=tuple(s.bc), mode=self._output, primaries_only=self._primaries_only,
                        hist_range_bin=hist_range[0], hist_range_n=hist_range[1], hist_vac_bin=hist_vac[0],
-                       hist_vac_n=hist_vac[1])
+                       hist_vac_n=hist_vac[1], potential=("universal", "moliere", "ckr")[self._potential])
         r = self._engine.run([spec])[0]
         sc = self._simconf
         sc.EelTotal += r["Eel"]

@@ -200,7 +200,8 @@ public:
   // Full cascades of n primaries cloned from `pka` (direction and position as
   // set on the template), tallied like TrimVacCount (or TrimRange with mode
   // MTG_TALLY_RANGE, TrimPrimaries / TrimRecoils with MTG_TALLY_PRIMARIES and
-  // max_generation 1 / 2) with TrimPhononOut energy accounting.
+  // max_generation 1 / 2) with TrimPhononOut energy accounting, scattering in the
+  // potential set in _potential.
   mtg_totals runPrimaries(IonBase * pka, long long n, unsigned long long seed = 1,
                           int mode = MTG_TALLY_VACCOUNT, bool primaries_only = false,
                           long long first_primary = 0, int max_generation = 1)
@@ -229,6 +230,7 @@ public:
     sim.tally_mode = mode;
     sim.primaries_only = primaries_only ? 1 : 0;
     sim.max_generation = max_generation;
+    sim.potential = int(_potential); // TrimBase's public member (trim.h:63-69)
     mtg_totals t{};
     _ctx.check(mtg_run(_ctx.get(), &sim, 1, &t, nullptr));
     _simconf->vacancies_created += int(t.vacancies);

@@ -1023,11 +1023,21 @@ mtg_stopping(mtg_ctx * ctx, int Z1, double m1, const mtg_material * material, co
 mtg_status
 mtg_scatter(mtg_ctx * ctx, const double * eps, const double * b, long long n, int precision, double * s2)
 {
+  return mtg_scatter_potential(ctx, eps, b, n, precision, MTG_POT_UNIVERSAL, s2);
+}
+
+mtg_status
+mtg_scatter_potential(mtg_ctx * ctx, const double * eps, const double * b, long long n, int precision,
+                      int potential, double * s2)
+{
   mtg_status st = require_device(ctx);
   if (st != MTG_OK)
     return st;
   if (n < 0 || (n > 0 && (!eps || !b || !s2)))
     return fail(ctx, MTG_ERR_BAD_INPUT, "bad scatter request");
+  if (potential < MTG_POT_UNIVERSAL || potential > MTG_POT_CKR ||
+      (precision == MTG_PREC_FP32_SURROGATE && potential != MTG_POT_UNIVERSAL))
+    return fail(ctx, MTG_ERR_BAD_INPUT, "invalid potential for this precision");
   if (n == 0)
     return MTG_OK;
   CK(ensure(ctx->d_tmp1, 8 * size_t(n)));
@@ -1036,10 +1046,11 @@ mtg_scatter(mtg_ctx * ctx, const double * eps, const double * b, long long n, in
   CK(cudaMemcpy(ctx->d_tmp1.p, eps, 8 * n, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_tmp2.p, b, 8 * n, cudaMemcpyHostToDevice));
   if (precision == MTG_PREC_FP64)
-    CK(launch_scatter64(ptr<double>(ctx->d_tmp1), ptr<double>(ctx->d_tmp2), n, ptr<double>(ctx->d_tmp3), nullptr));
+    CK(launch_scatter64(ptr<double>(ctx->d_tmp1), ptr<double>(ctx->d_tmp2), n, ptr<double>(ctx->d_tmp3), potential,
+                        nullptr));
   else if (precision == MTG_PREC_FP32)
-    CK(launch_scatter32(ptr<double>(ctx->d_tmp1), ptr<double>(ctx->d_tmp2), n, ptr<double>(ctx->d_tmp3), nullptr,
-                        0, nullptr));
+    CK(launch_scatter32(ptr<double>(ctx->d_tmp1), ptr<double>(ctx->d_tmp2), n, ptr<double>(ctx->d_tmp3), potential,
+                        nullptr));
   else
   {
     if (!ctx->sg_ready)

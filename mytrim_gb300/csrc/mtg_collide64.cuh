@@ -132,10 +132,13 @@ material_stop64(const SpeciesConst & sc, const MatConst & mc, double E)
   return se * mc.arho;
 }
 
-// Universal-potential scattering (trim.C:172-271).  Returns s2 = sin^2(theta_cm/2)
-// and ct, st = cos, sin of theta_cm; niter counts Newton iterations.
+// Scattering (trim.C:172-271) for the universal (pot 0), Moliere (1) or C-Kr (2)
+// screened potential, each with its magic-formula constants; the reference's
+// expressions as written, the C-Kr derivative coefficients included.  Returns
+// s2 = sin^2(theta_cm/2) and ct, st = cos, sin of theta_cm; niter counts Newton
+// iterations.
 MTG_HD void
-scatter64(double eps, double b, double & s2, double & ct, double & st, int & niter)
+scatter64(double eps, double b, double & s2, double & ct, double & st, int & niter, int pot = 0)
 {
   niter = 0;
   if (eps > 10.0)
@@ -158,12 +161,36 @@ scatter64(double eps, double b, double & s2, double & ct, double & st, int & nit
   double v, v1, q;
   do
   {
-    const double ex1 = 0.18175 * exp64(-3.1998 * r);
-    const double ex2 = 0.50986 * exp64(-0.94229 * r);
-    const double ex3 = 0.28022 * exp64(-0.4029 * r);
-    const double ex4 = 0.028171 * exp64(-0.20162 * r);
-    v = (ex1 + ex2 + ex3 + ex4) / r;
-    v1 = -(v + 3.1998 * ex1 + 0.94229 * ex2 + 0.4029 * ex3 + 0.20162 * ex4) / r;
+    if (pot == 1)
+    {
+      // Moliere (trim.C:206-213); Utility::pow<4> and pow<5> as the reference's
+      // shim/pow.h multiplies: (x x)(x x) and x ((x x)(x x))
+      const double ex1 = exp64(-0.3 * r);
+      const double e1s = ex1 * ex1;
+      const double ex2 = e1s * e1s;
+      const double e2s = ex2 * ex2;
+      const double ex3 = ex2 * (e2s * e2s);
+      v = (0.35 * ex1 + 0.55 * ex2 + 0.1 * ex3) / r;
+      v1 = -(v + 0.105 * ex1 + 0.66 * ex2 + 0.6 * ex3) / r;
+    }
+    else if (pot == 2)
+    {
+      // C-Kr (trim.C:215-222)
+      const double ex1 = exp64(-0.279 * r);
+      const double ex2 = exp64(-0.637 * r);
+      const double ex3 = exp64(-1.1919 * r);
+      v = (0.191 * ex1 + 0.474 * ex2 + 0.335 * ex3) / r;
+      v1 = -(v + 0.531865 * ex1 + 0.30181 * ex2 + 0.6437 * ex3) / r;
+    }
+    else
+    {
+      const double ex1 = 0.18175 * exp64(-3.1998 * r);
+      const double ex2 = 0.50986 * exp64(-0.94229 * r);
+      const double ex3 = 0.28022 * exp64(-0.4029 * r);
+      const double ex4 = 0.028171 * exp64(-0.20162 * r);
+      v = (ex1 + ex2 + ex3 + ex4) / r;
+      v1 = -(v + 3.1998 * ex1 + 0.94229 * ex2 + 0.4029 * ex3 + 0.20162 * ex4) / r;
+    }
     const double fr = b * b / r + v * r / eps - r;
     const double fr1 = -b * b / (r * r) + (v + v1 * r) / eps - 1.0;
     q = fr / fr1;
@@ -172,9 +199,25 @@ scatter64(double eps, double b, double & s2, double & ct, double & st, int & nit
   } while (fabs(q / r) > 0.001 && niter < 100);
   const double roc = -2.0 * (eps - v) / v1;
   const double sqe = sqrt(eps);
-  const double cc = (0.011615 + sqe) / (0.0071222 + sqe);
-  const double aa = 2.0 * eps * (1.0 + (0.99229 / sqe)) * pow64(b, cc);
-  const double ff = (sqrt(aa * aa + 1.0) - aa) * ((9.3066 + eps) / (14.813 + eps));
+  double cc, aa, ff;
+  if (pot == 1)
+  {
+    cc = (0.009611 + sqe) / (0.005175 + sqe);
+    aa = 2.0 * eps * (1.0 + (0.6743 / sqe)) * pow64(b, cc);
+    ff = (sqrt(aa * aa + 1.0) - aa) * ((6.314 + eps) / (10.0 + eps));
+  }
+  else if (pot == 2)
+  {
+    cc = (0.235809 + sqe) / (0.126000 + sqe);
+    aa = 2.0 * eps * (1.0 + (1.0144 / sqe)) * pow64(b, cc);
+    ff = (sqrt(aa * aa + 1.0) - aa) * ((6935.0 + eps) / (83550.0 + eps));
+  }
+  else
+  {
+    cc = (0.011615 + sqe) / (0.0071222 + sqe);
+    aa = 2.0 * eps * (1.0 + (0.99229 / sqe)) * pow64(b, cc);
+    ff = (sqrt(aa * aa + 1.0) - aa) * ((9.3066 + eps) / (14.813 + eps));
+  }
   const double delta = (r - b) * aa * ff / (ff + 1.0);
   const double co = (b + delta + roc) / (r + roc);
   const double c2 = co * co;
@@ -249,7 +292,7 @@ collide64(P64 & p, uint32_t ic, double r1, const SimDesc & sim, const SpeciesCon
 
   double s2, ct, st;
   int niter;
-  scatter64(eps, b, s2, ct, st, niter);
+  scatter64(eps, b, s2, ct, st, niter, sim.potential);
   sink.newton(niter);
 
   // energy transfer, electronic loss, momenta (trim.C:275-296)

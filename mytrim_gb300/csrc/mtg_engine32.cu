@@ -279,7 +279,8 @@ struct Fp32Policy
       if (live)
       {
         a = phase_a<GEO>(p, ic, r1, m, k0, k1);
-        nn = !a.gone && surrogate_in_domain(a.eps, a.b);
+        // the network is trained on the universal potential only
+        nn = !a.gone && m.sim->potential == 0 && surrogate_in_domain(a.eps, a.b);
       }
       // every lane of the warp, with or without a member, evaluates the network
       const float o0 = surrogate_eval_warp(m.net, nn ? surrogate_x1(a.eps) : 0.0f, nn ? surrogate_x2(a.b) : 0.0f);
@@ -292,7 +293,7 @@ struct Fp32Policy
       else
       {
         sink.fallback();
-        scatter32(a.eps, a.b, s2, c2, niter);
+        scatter32(a.eps, a.b, s2, c2, niter, m.sim->potential);
       }
     }
     else
@@ -302,7 +303,7 @@ struct Fp32Policy
       a = phase_a<GEO>(p, ic, r1, m, k0, k1);
       if (a.gone)
         return CF_DONE | CF_VOID;
-      scatter32(a.eps, a.b, s2, c2, niter);
+      scatter32(a.eps, a.b, s2, c2, niter, m.sim->potential);
     }
     sink.newton(niter);
     const Sim32 & sim = *m.sim;
@@ -521,10 +522,9 @@ cold_slot_bytes32()
   return sizeof(LaneCold<AccKahan32>);
 }
 
-// ---- scattering service (FP32 exact and surrogate)
+// ---- scattering service (FP32 exact)
 __global__ void
-scatter32_kernel(const double * eps, const double * b, long long n, double * s2, const SurrogateNet * net,
-                 int surrogate)
+scatter32_kernel(const double * eps, const double * b, long long n, double * s2, int potential)
 {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n)
@@ -532,18 +532,16 @@ scatter32_kernel(const double * eps, const double * b, long long n, double * s2,
   const float e = float(eps[i]), bb = float(b[i]);
   float s, c;
   int it;
-  scatter32(e, bb, s, c, it);
+  scatter32(e, bb, s, c, it, potential);
   s2[i] = double(s);
 }
 
 cudaError_t
-launch_scatter32(const double * eps, const double * b, long long n, double * s2, const void * net, int surrogate,
-                 cudaStream_t st)
+launch_scatter32(const double * eps, const double * b, long long n, double * s2, int potential, cudaStream_t st)
 {
   const int block = 256;
   if (n > 0)
-    scatter32_kernel<<<(unsigned int)((n + block - 1) / block), block, 0, st>>>(
-        eps, b, n, s2, reinterpret_cast<const SurrogateNet *>(net), surrogate);
+    scatter32_kernel<<<(unsigned int)((n + block - 1) / block), block, 0, st>>>(eps, b, n, s2, potential);
   return cudaGetLastError();
 }
 

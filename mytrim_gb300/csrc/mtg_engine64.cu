@@ -171,25 +171,26 @@ launch_stopping64(const SpeciesConst * sc, const MatConst * mc, const double * E
 }
 
 __global__ void
-scatter64_kernel(const double * eps, const double * b, long long n, double * s2)
+scatter64_kernel(const double * eps, const double * b, long long n, double * s2, int potential)
 {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n)
   {
     double ct, st, s;
     int it;
-    scatter64(eps[i], b[i], s, ct, st, it);
+    scatter64(eps[i], b[i], s, ct, st, it, potential);
     s2[i] = s;
   }
 }
 
 cudaError_t
-launch_scatter64(const double * eps, const double * b, long long n, double * s2, cudaStream_t st)
+launch_scatter64(const double * eps, const double * b, long long n, double * s2, int potential,
+                 cudaStream_t st)
 {
   const int block = 256;
   const long long grid = (n + block - 1) / block;
   if (grid > 0)
-    scatter64_kernel<<<(unsigned int)grid, block, 0, st>>>(eps, b, n, s2);
+    scatter64_kernel<<<(unsigned int)grid, block, 0, st>>>(eps, b, n, s2, potential);
   return cudaGetLastError();
 }
 

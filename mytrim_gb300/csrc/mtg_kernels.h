@@ -18,7 +18,8 @@ size_t record_size64();
 size_t cold_slot_bytes64(); // per-thread shared-memory tally slot
 cudaError_t launch_stopping64(const SpeciesConst * sc, const MatConst * mc, const double * E, long long n,
                               double * out, cudaStream_t st);
-cudaError_t launch_scatter64(const double * eps, const double * b, long long n, double * s2, cudaStream_t st);
+cudaError_t launch_scatter64(const double * eps, const double * b, long long n, double * s2, int potential,
+                             cudaStream_t st);
 
 // FP32 path (mtg_engine32.cu)
 constexpr int STOP_N = 2048;      // points per stopping table (uniform in ln E)
@@ -39,8 +40,8 @@ cudaError_t launch_cascade32(const EngineParams & prm, const Fp32Tables & t, int
 cudaError_t occupancy32(int block, size_t smem, int * blocks_per_sm, int surrogate, int events, int clusters);
 size_t record_size32();
 size_t cold_slot_bytes32();
-cudaError_t launch_scatter32(const double * eps, const double * b, long long n, double * s2, const void * net,
-                             int surrogate, cudaStream_t st);
+cudaError_t launch_scatter32(const double * eps, const double * b, long long n, double * s2, int potential,
+                             cudaStream_t st);
 cudaError_t launch_stopping32(const float * row, float lnE_min, float inv_d, const double * E, long long n,
                               double * out, cudaStream_t st);
 

@@ -1,16 +1,78 @@
-// Universal-potential scattering in FP32, shared by the FP32 engine and the
+// Screened-potential scattering in FP32, shared by the FP32 engine and the
 // scattering service.  The same Newton steps as trim.C:192-233, iterated on
 // d = r - b (no cancellation for distant collisions), and sin^2(theta/2) formed as
 // (1 - co)(1 + co) with 1 - co = d (1 - A F / (F + 1)) / (r + roc), algebraically
 // equal to 1 - co^2 of trim.C:266-269.
+//
+// Each potential is phi(r) = sum_i w_i exp(-k_i r) with v = phi / r and
+// v1 = -(v + sum_i c_i exp(-k_i r)) / r (trim.C:197-222), so that
+// f'(r) = -b^2/r^2 - (sum_i c_i exp(-k_i r)) / eps - 1.  c_i = k_i w_i for the
+// universal and Moliere potentials; for C-Kr the reference writes c_i that are
+// not the derivative's, and they are kept as written.  The Moliere terms
+// exp(-0.3 r)^4 and exp(-0.3 r)^20 are evaluated as exp(-1.2 r) and exp(-6 r).
 #pragma once
 
 namespace mtg
 {
 
-// Returns s2 = sin^2(theta/2) and c2 = cos^2(theta/2).
+template <int POT>
 __device__ __forceinline__ void
-scatter32(float eps, float b, float & s2, float & c2, int & niter)
+screening32(float r, float & phi, float & tk)
+{
+  if constexpr (POT == 1)
+  {
+    // Moliere (trim.C:206-213)
+    const float e1 = __expf(-0.3f * r);
+    const float e2 = __expf(-1.2f * r);
+    const float e3 = __expf(-6.0f * r);
+    phi = 0.35f * e1 + 0.55f * e2 + 0.1f * e3;
+    tk = 0.105f * e1 + 0.66f * e2 + 0.6f * e3;
+  }
+  else if constexpr (POT == 2)
+  {
+    // C-Kr (trim.C:215-222)
+    const float e1 = __expf(-0.279f * r);
+    const float e2 = __expf(-0.637f * r);
+    const float e3 = __expf(-1.1919f * r);
+    phi = 0.191f * e1 + 0.474f * e2 + 0.335f * e3;
+    tk = 0.531865f * e1 + 0.30181f * e2 + 0.6437f * e3;
+  }
+  else
+  {
+    // universal (trim.C:197-204)
+    const float ex1 = 0.18175f * __expf(-3.1998f * r);
+    const float ex2 = 0.50986f * __expf(-0.94229f * r);
+    const float ex3 = 0.28022f * __expf(-0.4029f * r);
+    const float ex4 = 0.028171f * __expf(-0.20162f * r);
+    phi = ex1 + ex2 + ex3 + ex4;
+    tk = 3.1998f * ex1 + 0.94229f * ex2 + 0.4029f * ex3 + 0.20162f * ex4;
+  }
+}
+
+// magic-formula constants (trim.C:236-258): beta = (m0 + sqe) / (m1 + sqe),
+// A = 2 eps (1 + m2 / sqe) b^beta, F = (sqrt(A^2 + 1) - A) (m3 + eps) / (m4 + eps)
+template <int POT>
+struct Magic32;
+template <>
+struct Magic32<0>
+{
+  static constexpr float m0 = 0.011615f, m1 = 0.0071222f, m2 = 0.99229f, m3 = 9.3066f, m4 = 14.813f;
+};
+template <>
+struct Magic32<1>
+{
+  static constexpr float m0 = 0.009611f, m1 = 0.005175f, m2 = 0.6743f, m3 = 6.314f, m4 = 10.0f;
+};
+template <>
+struct Magic32<2>
+{
+  static constexpr float m0 = 0.235809f, m1 = 0.126000f, m2 = 1.0144f, m3 = 6935.0f, m4 = 83550.0f;
+};
+
+// Returns s2 = sin^2(theta/2) and c2 = cos^2(theta/2).
+template <int POT>
+__device__ __forceinline__ void
+scatter32_pot(float eps, float b, float & s2, float & c2, int & niter)
 {
   niter = 0;
   if (eps > 10.0f)
@@ -35,12 +97,8 @@ scatter32(float eps, float b, float & s2, float & c2, int & niter)
   do
   {
     r = b + d;
-    const float ex1 = 0.18175f * __expf(-3.1998f * r);
-    const float ex2 = 0.50986f * __expf(-0.94229f * r);
-    const float ex3 = 0.28022f * __expf(-0.4029f * r);
-    const float ex4 = 0.028171f * __expf(-0.20162f * r);
-    const float phi = ex1 + ex2 + ex3 + ex4;
-    const float tk = 3.1998f * ex1 + 0.94229f * ex2 + 0.4029f * ex3 + 0.20162f * ex4;
+    float phi, tk;
+    screening32<POT>(r, phi, tk);
     const float ir = 1.0f / r;
     v = phi * ir;
     v1 = -(v + tk) * ir;
@@ -53,14 +111,34 @@ scatter32(float eps, float b, float & s2, float & c2, int & niter)
     ++niter;
   } while (fabsf(q) > 0.001f * fabsf(b + d) && niter < 100);
   r = b + d;
+  using M = Magic32<POT>;
   const float roc = -2.0f * (eps - v) / v1;
   const float sqe = sqrtf(eps);
-  const float cc = (0.011615f + sqe) / (0.0071222f + sqe);
-  const float aa = 2.0f * eps * (1.0f + (0.99229f / sqe)) * __expf(cc * __logf(b));
-  const float ff = (1.0f / (sqrtf(aa * aa + 1.0f) + aa)) * ((9.3066f + eps) / (14.813f + eps));
+  const float cc = (M::m0 + sqe) / (M::m1 + sqe);
+  const float aa = 2.0f * eps * (1.0f + (M::m2 / sqe)) * __expf(cc * __logf(b));
+  const float ff = (1.0f / (sqrtf(aa * aa + 1.0f) + aa)) * ((M::m3 + eps) / (M::m4 + eps));
   const float omc = d * (1.0f - aa * ff / (ff + 1.0f)) / (r + roc);
   s2 = omc * (2.0f - omc);
   c2 = 1.0f - s2;
+}
+
+// universal potential (the default)
+__device__ __forceinline__ void
+scatter32(float eps, float b, float & s2, float & c2, int & niter)
+{
+  scatter32_pot<0>(eps, b, s2, c2, niter);
+}
+
+// potential chosen at run time (TrimBase::Potential: 0 universal, 1 Moliere, 2 C-Kr)
+__device__ __forceinline__ void
+scatter32(float eps, float b, float & s2, float & c2, int & niter, int pot)
+{
+  if (pot == 1)
+    scatter32_pot<1>(eps, b, s2, c2, niter);
+  else if (pot == 2)
+    scatter32_pot<2>(eps, b, s2, c2, niter);
+  else
+    scatter32_pot<0>(eps, b, s2, c2, niter);
 }
 
 } // namespace mtg

@@ -282,6 +282,7 @@ build_fp32_tables(const HostTables & t, std::vector<Species32> & species, std::v
     o.primaries_only = d.primaries_only;
     o.follow_gen = d.follow_gen;
     o.kp_gen = d.kp_gen;
+    o.potential = d.potential;
     o.geometry = d.geometry;
     o.n_clusters = d.n_clusters;
     for (int k = 0; k < 3; ++k)
@@ -562,6 +563,12 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
     else
       d.follow_gen = d.primaries_only ? 1 : 0x7fffffff;
     d.kp_gen = s.tally_mode == MTG_TALLY_PRIMARIES ? s.max_generation : -1;
+    if (s.potential < MTG_POT_UNIVERSAL || s.potential > MTG_POT_CKR)
+    {
+      err = "invalid potential"; // trim.C:224-226 exits on the same condition
+      return MTG_ERR_BAD_INPUT;
+    }
+    d.potential = s.potential;
     d.prim_begin = prim;
     d.n_primaries = s.n_primaries;
     d.sim_key = uint64_t(si);

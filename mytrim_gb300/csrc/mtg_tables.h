@@ -104,6 +104,8 @@ struct SimDesc
   int primaries_only;   // ThreadedTrimBase::_primaries_only
   int follow_gen;       // a displaced recoil is followed iff its generation is below this
   int kp_gen;           // TrimPrimaries: generation whose displaced recoils add a KP count
+  int potential;        // TrimBase::Potential: 0 universal, 1 Moliere, 2 C-Kr
+  int pad_potential;
   long long prim_begin; // first global primary index of this simulation
   long long n_primaries;
   uint64_t sim_key;     // simulation number used in the member keys
@@ -212,7 +214,7 @@ struct Sim32
   int n_layers, n_mat, mat_base, species_base;
   float Ef, flscale, tau, cw; // flscale = 1 / length scale
   int range_mode, primaries_only, any_cut, geometry;
-  int follow_gen, kp_gen, pad0, pad1;
+  int follow_gen, kp_gen, potential, pad1;
   // sampleClusters geometry (see SimDesc)
   int kn[3];
   int n_clusters;

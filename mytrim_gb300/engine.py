@@ -18,6 +18,8 @@ DATA_DIR = Path(__file__).resolve().parent / "data"
 TABLES = DATA_DIR / "stopping_tables.tsv"
 
 PRECISIONS = {"fp64": F.PREC_FP64, "fp32": F.PREC_FP32, "surrogate": F.PREC_FP32_SURROGATE}
+# TrimBase::Potential (trim.h:63-69)
+POTENTIALS = {"universal": F.POT_UNIVERSAL, "moliere": F.POT_MOLIERE, "ckr": F.POT_CKR}
 
 
 @dataclass
@@ -64,6 +66,7 @@ class SimSpec:
     hist_lateral_bin: float = 10.0       # lateral (y, z) histogram of stopping points
     hist_lateral_n: int = 0
     hist_evac_rows: int = 0              # vacancy-energy histogram rows (int(ln E))
+    potential: str = "universal"         # TrimBase::_potential: "universal", "moliere" or "ckr"
     # sampleClusters geometry: layers[0] is the matrix, layers[1] the cluster
     # material; clusters is an (n, 4) array of x, y, z, r; cluster_hash the
     # spatial-hash cells per axis (sampleClusters::initSpatialhash)
@@ -143,6 +146,7 @@ class SimSpec:
         s.hist_lateral_bin = self.hist_lateral_bin
         s.hist_lateral_n = self.hist_lateral_n
         s.hist_evac_rows = self.hist_evac_rows
+        s.potential = POTENTIALS[self.potential]
         for i in range(3):
             s.voxel_n[i] = self.voxel_n[i]
             s.voxel_origin[i] = self.voxel_origin[i]
@@ -335,13 +339,14 @@ class Engine:
                                           len(e), prec, out.ctypes.data_as(C.POINTER(C.c_double))))
         return out
 
-    def scatter(self, eps, b, precision="fp64") -> np.ndarray:
+    def scatter(self, eps, b, precision="fp64", potential="universal") -> np.ndarray:
         e = np.ascontiguousarray(eps, dtype=np.float64)
         bb = np.ascontiguousarray(b, dtype=np.float64)
         out = np.zeros_like(e)
         prec = PRECISIONS[precision] if isinstance(precision, str) else precision
+        pot = POTENTIALS[potential] if isinstance(potential, str) else potential
         pd = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
-        self._check(self.lib.mtg_scatter(self.ctx, pd(e), pd(bb), len(e), prec, pd(out)))
+        self._check(self.lib.mtg_scatter_potential(self.ctx, pd(e), pd(bb), len(e), prec, pot, pd(out)))
         return out
 
     # ---- learned scattering surrogate

@@ -36,6 +36,66 @@
 namespace mto
 {
 
+// ---------------------------------------------------------------- potentials
+// v(r) and v'(r) of the screened potential (trim.C:194-226): 0 universal,
+// 1 Moliere (Utility::pow<4> and pow<5> multiply as (x x)(x x) and x (x^4),
+// shim/pow.h), 2 C-Kr with the reference's derivative coefficients as written.
+static inline void
+screening(int pot, double r, double & v, double & v1)
+{
+  if (pot == 1)
+  {
+    const double ex1 = std::exp(-0.3 * r);
+    const double e1s = ex1 * ex1;
+    const double ex2 = e1s * e1s;
+    const double e2s = ex2 * ex2;
+    const double ex3 = ex2 * (e2s * e2s);
+    v = (0.35 * ex1 + 0.55 * ex2 + 0.1 * ex3) / r;
+    v1 = -(v + 0.105 * ex1 + 0.66 * ex2 + 0.6 * ex3) / r;
+  }
+  else if (pot == 2)
+  {
+    const double ex1 = std::exp(-0.279 * r);
+    const double ex2 = std::exp(-0.637 * r);
+    const double ex3 = std::exp(-1.1919 * r);
+    v = (0.191 * ex1 + 0.474 * ex2 + 0.335 * ex3) / r;
+    v1 = -(v + 0.531865 * ex1 + 0.30181 * ex2 + 0.6437 * ex3) / r;
+  }
+  else
+  {
+    const double ex1 = 0.18175 * std::exp(-3.1998 * r);
+    const double ex2 = 0.50986 * std::exp(-0.94229 * r);
+    const double ex3 = 0.28022 * std::exp(-0.4029 * r);
+    const double ex4 = 0.028171 * std::exp(-0.20162 * r);
+    v = (ex1 + ex2 + ex3 + ex4) / r;
+    v1 = -(v + 3.1998 * ex1 + 0.94229 * ex2 + 0.4029 * ex3 + 0.20162 * ex4) / r;
+  }
+}
+
+// magic-formula A and F of each potential (trim.C:236-258)
+static inline void
+magic(int pot, double eps, double sqe, double b, double & aa, double & ff)
+{
+  if (pot == 1)
+  {
+    const double cc = (0.009611 + sqe) / (0.005175 + sqe);
+    aa = 2.0 * eps * (1.0 + (0.6743 / sqe)) * std::pow(b, cc);
+    ff = (std::sqrt(aa * aa + 1.0) - aa) * ((6.314 + eps) / (10.0 + eps));
+  }
+  else if (pot == 2)
+  {
+    const double cc = (0.235809 + sqe) / (0.126000 + sqe);
+    aa = 2.0 * eps * (1.0 + (1.0144 / sqe)) * std::pow(b, cc);
+    ff = (std::sqrt(aa * aa + 1.0) - aa) * ((6935.0 + eps) / (83550.0 + eps));
+  }
+  else
+  {
+    const double cc = (0.011615 + sqe) / (0.0071222 + sqe);
+    aa = 2.0 * eps * (1.0 + (0.99229 / sqe)) * std::pow(b, cc);
+    ff = (std::sqrt(aa * aa + 1.0) - aa) * ((9.3066 + eps) / (14.813 + eps));
+  }
+}
+
 // ---------------------------------------------------------------- data tables
 struct Coef
 {
@@ -500,7 +560,7 @@ struct Engine
       const double see = material_stopping(mat, pka.Z, pka.m, pka.E);
       double dee = ls * see;
 
-      // scattering angle (trim.C:172-271), universal potential
+      // scattering angle (trim.C:172-271) in the chosen potential (trim.C:194-258)
       double s2, c2, ct, st;
       if (eps > 10.0)
       {
@@ -523,12 +583,7 @@ struct Engine
         double v, v1, q;
         do
         {
-          const double ex1 = 0.18175 * std::exp(-3.1998 * r);
-          const double ex2 = 0.50986 * std::exp(-0.94229 * r);
-          const double ex3 = 0.28022 * std::exp(-0.4029 * r);
-          const double ex4 = 0.028171 * std::exp(-0.20162 * r);
-          v = (ex1 + ex2 + ex3 + ex4) / r;
-          v1 = -(v + 3.1998 * ex1 + 0.94229 * ex2 + 0.4029 * ex3 + 0.20162 * ex4) / r;
+          screening(spec.potential, r, v, v1);
           const double fr = b * b / r + v * r / eps - r;
           const double fr1 = -b * b / (r * r) + (v + v1 * r) / eps - 1.0;
           q = fr / fr1;
@@ -536,9 +591,8 @@ struct Engine
         } while (std::abs(q / r) > 0.001);
         const double roc = -2.0 * (eps - v) / v1;
         const double sqe = std::sqrt(eps);
-        const double cc = (0.011615 + sqe) / (0.0071222 + sqe);
-        const double aa = 2.0 * eps * (1.0 + (0.99229 / sqe)) * std::pow(b, cc);
-        const double ff = (std::sqrt(aa * aa + 1.0) - aa) * ((9.3066 + eps) / (14.813 + eps));
+        double aa, ff;
+        magic(spec.potential, eps, sqe, b, aa, ff);
         const double delta = (r - b) * aa * ff / (ff + 1.0);
         const double co = (b + delta + roc) / (r + roc);
         c2 = co * co;

@@ -35,6 +35,9 @@ def build(reference_dir=None):
         subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "ref", f"REF={ref}"], check=True, env=env)
 
 
+POTENTIALS = {"universal": 0, "moliere": 1, "ckr": 2}  # TrimBase::Potential (trim.h:63-69)
+
+
 def spec_text(sim, seed=1, philox=True, first=0, n=None, records=0, tmin=None, output=None, scale=1.0):
     w = sim.box()
     p = sim.start()
@@ -46,6 +49,7 @@ def spec_text(sim, seed=1, philox=True, first=0, n=None, records=0, tmin=None, o
              f"bc {sim.bc[0]} {sim.bc[1]} {sim.bc[2]}",
              f"mode {sim.mode}" + (f" {sim.max_generation}" if sim.mode == "primaries" else ""),
              f"primaries_only {int(sim.primaries_only)}",
+             f"potential {POTENTIALS[getattr(sim, 'potential', 'universal')]}",
              f"hist_range {sim.hist_range_bin!r} {sim.hist_range_n}",
              f"hist_vac {sim.hist_vac_bin!r} {sim.hist_vac_n}"]
     for l in sim.layers:

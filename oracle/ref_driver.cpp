@@ -182,6 +182,7 @@ int
 run_with(SimconfType & simconf, SampleBase & sample, const runspec::Spec & spec)
 {
   Trim trim(&simconf, &sample, spec);
+  trim._potential = typename Trim::Potential(spec.potential); // the public member (trim.h:63-69)
 
   // per-primary seeds from the master stream, as runmytrim.C:288-302 does
   simconf.seed(spec.seed);

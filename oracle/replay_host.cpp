@@ -145,13 +145,14 @@ main(int argc, char ** argv)
   }
   if (argc >= 3 && std::string(argv[2]) == "--scatter")
   {
-    // lines "eps b" -> s2
+    // lines "eps b" -> s2; an optional argument after --scatter picks the potential
+    const int pot = argc >= 4 ? atoi(argv[3]) : 0;
     double eps, b;
     while (std::cin >> eps >> b)
     {
       double s2, ct, st;
       int it;
-      scatter64(eps, b, s2, ct, st, it);
+      scatter64(eps, b, s2, ct, st, it, pot);
       printf("%a\n", s2);
     }
     return 0;
@@ -198,6 +199,7 @@ main(int argc, char ** argv)
   sim.tally_mode = spec.primaries_mode ? MTG_TALLY_PRIMARIES : (spec.range_mode ? MTG_TALLY_RANGE : MTG_TALLY_VACCOUNT);
   sim.max_generation = spec.max_gen;
   sim.primaries_only = spec.primaries_only;
+  sim.potential = spec.potential;
   if (spec.clusters)
   {
     sim.sample.geometry = MTG_GEOM_CLUSTERS;

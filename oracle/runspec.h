@@ -21,6 +21,7 @@
 //                               vaccount: TrimVacCount; range: TrimRange (KP, gen cut);
 //                               primaries: TrimPrimaries (maxgen 1) / TrimRecoils (2)
 //   primaries_only 0|1          ThreadedTrimBase::_primaries_only
+//   potential 0|1|2             TrimBase::_potential: universal, Moliere, C-Kr (trim.h:63-69)
 //   hist_range <bin_A> <nbins>  histogram of primary stopping depth
 //   hist_vac <bin_A> <nbins>    histogram of vacancy depth (TrimVacCount bins are 1 A)
 //   subset <first> <count>      run primaries [first, first+count)
@@ -81,6 +82,7 @@ struct Spec
   bool primaries_mode = false; // TrimPrimaries / TrimRecoils
   int max_gen = 1;
   bool primaries_only = false;
+  int potential = 0;
   double hist_range_bin = 10.0;
   int hist_range_n = 0;
   double hist_vac_bin = 1.0;
@@ -205,6 +207,8 @@ parse(std::istream & in, Spec & s, std::string & err)
       ok = bool(ls >> v);
       s.primaries_only = v != 0;
     }
+    else if (key == "potential")
+      ok = bool(ls >> s.potential) && s.potential >= 0 && s.potential <= 2;
     else if (key == "hist_range")
       ok = bool(ls >> s.hist_range_bin >> s.hist_range_n);
     else if (key == "hist_vac")

@@ -73,6 +73,13 @@ CASES = {
                                                                    ElementSpec(6, 12.011, 1.0, 20.0, 3.0)])],
                                Z=54, m=131.29, E=30000.0, n_primaries=30, mode="primaries", max_generation=2,
                                hist_range_bin=10.0, hist_range_n=100), 18, 30),
+    # the other two potentials of TrimBase::_potential (trim.C:194-258)
+    "cu_cu_moliere": (SimSpec(layers=[LayerSpec(100000.0, 8.92, [ElementSpec(29, CU, 1.0)])], Z=29, m=CU,
+                              E=5000.0, n_primaries=30, potential="moliere", hist_range_bin=5.0,
+                              hist_range_n=100), 21, 30),
+    "kr_c_ckr": (SimSpec(layers=[LayerSpec(100000.0, 2.26, [ElementSpec(6, 12.011, 1.0, 28.0, 3.0)])], Z=36,
+                         m=83.798, E=10000.0, n_primaries=30, potential="ckr", hist_range_bin=5.0,
+                         hist_range_n=100), 22, 30),
     # protons into a two-element target
     "h_sic": (SimSpec(layers=[LayerSpec(100000.0, 3.21, [ElementSpec(14, SI, 1.0), ElementSpec(6, 12.011, 1.0)])],
                       Z=1, m=1.008, E=5000.0, n_primaries=40), 12, 40),

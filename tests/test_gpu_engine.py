@@ -11,6 +11,7 @@
 * properties at full size: energy conservation, sharding invariance, overflow
   drains, error returns instead of hangs.
 """
+import ctypes as C
 import math
 import subprocess
 import sys
@@ -85,27 +86,44 @@ def test_stopping_fp64_bitwise_vs_host_build(gpu_engine, target):
         assert bad.size == 0, (target, Z1, E[bad[:5]], got[bad[:5]], want[bad[:5]])
 
 
-def test_scatter_fp64_bitwise_vs_host_build(gpu_engine):
-    rng = np.random.default_rng(3)
+POTENTIALS = ["universal", "moliere", "ckr"]
+
+
+@pytest.mark.parametrize("pot", range(3))
+def test_scatter_fp64_bitwise_vs_host_build(gpu_engine, pot):
+    rng = np.random.default_rng(3 + pot)
     eps = 10 ** rng.uniform(-5, 1.5, 20000)
     b = rng.uniform(0, 1, 20000) ** 0.5 * 40 + 1e-6
-    want = _host(["--scatter"], "\n".join(f"{float(x)!r} {float(y)!r}" for x, y in zip(eps, b)) + "\n")
-    got = gpu_engine.scatter(eps, b, precision="fp64")
+    want = _host(["--scatter", str(pot)], "\n".join(f"{float(x)!r} {float(y)!r}" for x, y in zip(eps, b)) + "\n")
+    got = gpu_engine.scatter(eps, b, precision="fp64", potential=POTENTIALS[pot])
     bad = np.nonzero(got != want)[0]
     assert bad.size == 0, (eps[bad[:5]], b[bad[:5]], got[bad[:5]], want[bad[:5]])
 
 
-def test_scatter_fp32_matches_fp64(gpu_engine):
+@pytest.mark.parametrize("pot", POTENTIALS)
+def test_scatter_fp32_matches_fp64(gpu_engine, pot):
     rng = np.random.default_rng(4)
     eps = 10 ** rng.uniform(-4, 1.5, 50000)
     b = rng.uniform(0, 1, 50000) ** 0.5 * 30 + 1e-4
-    s64 = gpu_engine.scatter(eps, b, precision="fp64")
-    s32 = gpu_engine.scatter(eps, b, precision="fp32")
+    s64 = gpu_engine.scatter(eps, b, precision="fp64", potential=pot)
+    s32 = gpu_engine.scatter(eps, b, precision="fp32", potential=pot)
     big = s64 > 1e-3
     rel = np.abs(s32 - s64) / s64
     # the FP32 form has no cancellation: large angles to 1e-4, small angles to 1e-2
-    assert np.quantile(rel[big], 0.99) < 1e-4
-    assert np.quantile(rel, 0.99) < 1e-2
+    assert np.quantile(rel[big], 0.99) < 1e-4, np.quantile(rel[big], [0.5, 0.9, 0.99])
+    assert np.quantile(rel, 0.99) < 1e-2, np.quantile(rel, [0.5, 0.9, 0.99])
+
+
+def test_potentials_change_the_scattering(gpu_engine):
+    """The three potentials give different angles in the screened regime and the
+    same Rutherford limit above reduced energy 10 (trim.C:172-179)."""
+    eps = np.array([0.01, 0.1, 1.0, 20.0])
+    b = np.array([1.0, 1.0, 1.0, 0.05])
+    s = [gpu_engine.scatter(eps, b, precision="fp64", potential=p) for p in POTENTIALS]
+    assert np.all(s[0][:3] != s[1][:3]) and np.all(s[0][:3] != s[2][:3])
+    assert s[0][3] == s[1][3] == s[2][3]
+    with pytest.raises(F.EngineError):
+        gpu_engine.scatter(eps, b, precision="fp64", potential=3)
 
 
 def _replay(oracle_built, sim, seed):
@@ -186,6 +204,29 @@ def test_fp32_matches_fp64(engine_lib, name):
         a, b = r["fp32"], r["fp64"]
         rel = abs(a[key] - b[key]) / abs(b[key])
         assert _z(a, b, key) < 3.5 or rel < 0.01, (name, key, a[key], b[key])
+
+
+@pytest.mark.parametrize("case", ["cu_cu_moliere", "kr_c_ckr"])
+def test_fp32_matches_fp64_other_potentials(engine_lib, case):
+    sim = SimSpec(**{**CASES[case][0].__dict__, "n_primaries": 3000})
+    r = {}
+    for prec in ("fp64", "fp32"):
+        e = Engine(precision=prec, seed=9)
+        r[prec] = summarize(e.run([sim])[0])
+        e.close()
+    for key in ("vac_per_ion", "eel_per_ion", "range_mean", "straggle", "lateral"):
+        a, b = r["fp32"], r["fp64"]
+        rel = abs(a[key] - b[key]) / abs(b[key])
+        assert _z(a, b, key) < 3.5 or rel < 0.01, (case, key, a[key], b[key])
+
+
+def test_invalid_potential_is_rejected(engine_lib):
+    sim = SimSpec(**{**CASES["cu_cu_moliere"][0].__dict__, "n_primaries": 4})
+    s = sim.to_c()
+    s.potential = 3
+    e = Engine(precision="fp64")
+    assert e.lib.mtg_prepare(e.ctx, C.byref(s), 1) == 1  # MTG_ERR_BAD_INPUT
+    e.close()
 
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])

@@ -209,3 +209,22 @@ def test_surrogate_engine_matches_fp64(committed):
         rel = abs(g[key] - f[key]) / abs(f[key])
         z = abs(g[key] - f[key]) / math.hypot(g[key + "_err"], f[key + "_err"])
         assert z < 5 or rel < 0.05, (key, g[key], f[key])
+
+
+def test_surrogate_path_scatters_other_potentials_exactly(committed):
+    """The network covers the universal potential only: a Moliere simulation on the
+    surrogate path scatters every collision with the exact FP32 form."""
+    from mytrim_gb300.engine import ElementSpec, LayerSpec, SimSpec
+    e = committed
+    sim = SimSpec(layers=[LayerSpec(1e5, 8.92, [ElementSpec(29, 63.546, 1.0)])], Z=29, m=63.546, E=5e3,
+                  n_primaries=1000, potential="moliere")
+    e.configure(precision="surrogate", seed=8)
+    g = e.run([sim])[0]
+    e.configure(precision="fp32", seed=8)
+    f = e.run([sim])[0]
+    assert g["surrogate_fallbacks"] == g["collisions"]
+    gs, fs = summarize(g), summarize(f)
+    for key in ("vac_per_ion", "range_mean", "eel_per_ion"):
+        assert abs(gs[key] - fs[key]) <= 1e-3 * abs(fs[key]) + 3 * math.hypot(gs[key + "_err"], fs[key + "_err"])
+    with pytest.raises(Exception):
+        e.scatter(np.array([0.1]), np.array([1.0]), precision="surrogate", potential="moliere")
