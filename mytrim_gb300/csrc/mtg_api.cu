@@ -188,11 +188,11 @@ setup_launch_shape(mtg_ctx * ctx)
   ctx->hist_smem_bins = 0;
   int bps = 0;
   const int events = ctx->event_cap > 0 && ctx->event_mask ? 1 : 0;
-  const int clusters = t.any_clusters;
+  const int extended = t.any_extended;
   auto occupancy = [&](size_t smem, int * b) {
     return prec == MTG_PREC_FP64
-               ? occupancy64(ctx->block, smem, b, events, clusters)
-               : occupancy32(ctx->block, smem, b, prec == MTG_PREC_FP32_SURROGATE, events, clusters);
+               ? occupancy64(ctx->block, smem, b, events, extended)
+               : occupancy32(ctx->block, smem, b, prec == MTG_PREC_FP32_SURROGATE, events, extended);
   };
   cudaError_t e = occupancy(ctx->smem, &bps);
   if (e != cudaSuccess)
@@ -308,7 +308,7 @@ fill_params(mtg_ctx * ctx, EngineParams & prm)
     prm.event_mask = ctx->event_mask;
   }
   prm.any_evac = t.any_evac;
-  prm.any_clusters = t.any_clusters;
+  prm.any_extended = t.any_extended;
   prm.warp_steps = ptr<unsigned long long>(ctx->d_counters) + C_STEPS;
 }
 

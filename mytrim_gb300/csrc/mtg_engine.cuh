@@ -92,7 +92,7 @@ struct EngineParams
   long long events_cap;
   unsigned int event_mask;
   int any_evac; // some simulation keeps a vacancy-energy histogram
-  int any_clusters; // some simulation has the cluster geometry
+  int any_extended; // some simulation has the cluster geometry or a non-universal potential
   unsigned long long * warp_steps; // loop iterations of all warps (lane occupancy = collisions / 32 steps)
   // single-simulation runs with few depth bins count vacancies and replacements in
   // a per-block shared-memory histogram (hist_smem_bins counters from byte offset
@@ -601,9 +601,10 @@ struct LaneSink
   }
 };
 
-// EV: the event-log variant; GEO: the variant that knows the cluster geometry
+// EV: the event-log variant; EXT: the variant that knows the cluster geometry and the
+// Moliere and C-Kr potentials (the others scatter in the universal potential only)
 // (the layered-sample kernel carries neither)
-template <class Pol, bool EV, bool GEO>
+template <class Pol, bool EV, bool EXT>
 __global__ void __launch_bounds__(128, Pol::MIN_BLOCKS)
 cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
 {
@@ -753,7 +754,7 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
     }
     // every lane takes part (a policy may evaluate warp-collective code); lanes
     // without a member do no work and get no flags
-    flags = Pol::template collide<GEO>(live, p, ic, r1, mctx, prm.k0, prm.k1, rec, sink);
+    flags = Pol::template collide<EXT>(live, p, ic, r1, mctx, prm.k0, prm.k1, rec, sink);
     if (live)
     {
       if (flags & CF_VOID)

@@ -198,7 +198,7 @@ struct Fp32Policy
   };
 
   // flight, target atom and electronic loss (trim.C:80-170)
-  template <bool GEO>
+  template <bool EXT>
   static __device__ __forceinline__ PhaseA phase_a(P32 & p, uint32_t ic, float r1, const MemberCtx & m, uint32_t k0,
                                                    uint32_t k1)
   {
@@ -208,7 +208,7 @@ struct Fp32Policy
     // (sample_clusters.C:42-53)
     int k;
     a.gone = false;
-    if (GEO && sim.geometry == 1)
+    if (EXT && sim.geometry == 1)
     {
       const float pos[3] = {p.x, p.y, p.z};
       const int l = cluster_lookup<float>(pos, sim.w, sim.bc, sim.kn, sim.kd, sim.cmr, sim.cl, sim.cl_next,
@@ -266,7 +266,7 @@ struct Fp32Policy
     return a;
   }
 
-  template <bool GEO, class Sink>
+  template <bool EXT, class Sink>
   static __device__ __forceinline__ int collide(bool live, P32 & p, uint32_t ic, float r1, const MemberCtx & m,
                                                 uint32_t k0, uint32_t k1, P32 & rec, Sink & sink)
   {
@@ -278,9 +278,9 @@ struct Fp32Policy
       bool nn = false;
       if (live)
       {
-        a = phase_a<GEO>(p, ic, r1, m, k0, k1);
+        a = phase_a<EXT>(p, ic, r1, m, k0, k1);
         // the network is trained on the universal potential only
-        nn = !a.gone && m.sim->potential == 0 && surrogate_in_domain(a.eps, a.b);
+        nn = !a.gone && (!EXT || m.sim->potential == 0) && surrogate_in_domain(a.eps, a.b);
       }
       // every lane of the warp, with or without a member, evaluates the network
       const float o0 = surrogate_eval_warp(m.net, nn ? surrogate_x1(a.eps) : 0.0f, nn ? surrogate_x2(a.b) : 0.0f);
@@ -293,17 +293,17 @@ struct Fp32Policy
       else
       {
         sink.fallback();
-        scatter32(a.eps, a.b, s2, c2, niter, m.sim->potential);
+        scatter32(a.eps, a.b, s2, c2, niter, EXT ? m.sim->potential : 0);
       }
     }
     else
     {
       if (!live)
         return 0;
-      a = phase_a<GEO>(p, ic, r1, m, k0, k1);
+      a = phase_a<EXT>(p, ic, r1, m, k0, k1);
       if (a.gone)
         return CF_DONE | CF_VOID;
-      scatter32(a.eps, a.b, s2, c2, niter, m.sim->potential);
+      scatter32(a.eps, a.b, s2, c2, niter, EXT ? m.sim->potential : 0);
     }
     sink.newton(niter);
     const Sim32 & sim = *m.sim;
@@ -452,7 +452,7 @@ launch_cascade32(const EngineParams & prm, const Fp32Tables & t, int grid, int b
   tabs.lnE_min = t.lnE_min;
   tabs.inv_dlnE = t.inv_dlnE;
   tabs.net = reinterpret_cast<const SurrogateNet *>(t.mlp);
-  const int v = (prm.event_mask != 0 ? 1 : 0) + (prm.any_clusters != 0 ? 2 : 0);
+  const int v = (prm.event_mask != 0 ? 1 : 0) + (prm.any_extended != 0 ? 2 : 0);
   if (surrogate)
     switch (v)
     {
@@ -500,13 +500,13 @@ occupancy_variants(int block, size_t smem, int * occ)
 // residency of the variant the launch will use; every variant gets the
 // shared-memory opt-in
 cudaError_t
-occupancy32(int block, size_t smem, int * blocks_per_sm, int surrogate, int events, int clusters)
+occupancy32(int block, size_t smem, int * blocks_per_sm, int surrogate, int events, int extended)
 {
   int occ[4] = {0, 0, 0, 0};
   cudaError_t e = surrogate ? occupancy_variants<true>(block, smem, occ) : occupancy_variants<false>(block, smem, occ);
   if (e != cudaSuccess)
     return e;
-  *blocks_per_sm = occ[(events ? 1 : 0) + (clusters ? 2 : 0)];
+  *blocks_per_sm = occ[(events ? 1 : 0) + (extended ? 2 : 0)];
   return cudaSuccess;
 }
 

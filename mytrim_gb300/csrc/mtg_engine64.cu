@@ -81,13 +81,13 @@ struct Fp64Policy
     return p;
   }
 
-  template <bool GEO, class Sink>
+  template <bool EXT, class Sink>
   static __device__ __forceinline__ int collide(bool live, P64 & p, uint32_t ic, double r1, const MemberCtx & m,
                                                 uint32_t k0, uint32_t k1, P64 & rec, Sink & sink)
   {
     if (!live)
       return 0;
-    return collide64<GEO>(p, ic, r1, *m.sim, *m.sc, m.mrow, k0, k1, rec, sink);
+    return collide64<EXT>(p, ic, r1, *m.sim, *m.sc, m.mrow, k0, k1, rec, sink);
   }
 };
 
@@ -95,12 +95,12 @@ cudaError_t
 launch_cascade64(const EngineParams & prm, int grid, int block, size_t smem, cudaStream_t st)
 {
   const Fp64Policy::Tables tabs{prm.species, prm.mats};
-  const bool ev = prm.event_mask != 0, geo = prm.any_clusters != 0;
-  if (ev && geo)
+  const bool ev = prm.event_mask != 0, ext = prm.any_extended != 0;
+  if (ev && ext)
     cascade_kernel<Fp64Policy, true, true><<<grid, block, smem, st>>>(prm, tabs);
   else if (ev)
     cascade_kernel<Fp64Policy, true, false><<<grid, block, smem, st>>>(prm, tabs);
-  else if (geo)
+  else if (ext)
     cascade_kernel<Fp64Policy, false, true><<<grid, block, smem, st>>>(prm, tabs);
   else
     cascade_kernel<Fp64Policy, false, false><<<grid, block, smem, st>>>(prm, tabs);
@@ -123,7 +123,7 @@ occupancy_of(K kernel, int block, size_t smem, int * blocks_per_sm)
 // residency of the variant the launch will use; every variant gets the
 // shared-memory opt-in
 cudaError_t
-occupancy64(int block, size_t smem, int * blocks_per_sm, int events, int clusters)
+occupancy64(int block, size_t smem, int * blocks_per_sm, int events, int extended)
 {
   int occ[4] = {0, 0, 0, 0};
   cudaError_t e;
@@ -132,7 +132,7 @@ occupancy64(int block, size_t smem, int * blocks_per_sm, int events, int cluster
       (e = occupancy_of(cascade_kernel<Fp64Policy, false, true>, block, smem, &occ[2])) != cudaSuccess ||
       (e = occupancy_of(cascade_kernel<Fp64Policy, true, true>, block, smem, &occ[3])) != cudaSuccess)
     return e;
-  *blocks_per_sm = occ[(events ? 1 : 0) + (clusters ? 2 : 0)];
+  *blocks_per_sm = occ[(events ? 1 : 0) + (extended ? 2 : 0)];
   return cudaSuccess;
 }
 

@@ -348,7 +348,7 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
   out.k0 = out.k1 = 0;
   out.emax = 0.0;
   out.any_evac = 0;
-  out.any_clusters = 0;
+  out.any_extended = 0;
   out.members_est = 1.0;
   if (n_sims < 1 || !sims)
   {
@@ -569,6 +569,8 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
       return MTG_ERR_BAD_INPUT;
     }
     d.potential = s.potential;
+    if (s.potential != MTG_POT_UNIVERSAL)
+      out.any_extended = 1;
     d.prim_begin = prim;
     d.n_primaries = s.n_primaries;
     d.sim_key = uint64_t(si);
@@ -636,7 +638,7 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
       // cell of a cluster is floor(c * kn / w) mod kn; each cell lists its clusters
       // in insertion order
       d.geometry = 1;
-      out.any_clusters = 1;
+      out.any_extended = 1;
       d.n_clusters = int(smp.n_clusters);
       d.cl_base = (long long)out.clusters.size();
       d.cell_base = (long long)out.cl_head.size();

@@ -24,7 +24,8 @@ struct HostTables
   uint32_t k0 = 0, k1 = 0;                // Philox key
   double emax = 0.0;                      // largest primary energy
   int any_evac = 0;                       // some simulation keeps a vacancy-energy histogram
-  int any_clusters = 0;                   // some simulation has the cluster geometry
+  int any_extended = 0;                   // some simulation has the cluster geometry or a
+                                          // potential other than the universal one
   double members_est = 1.0;               // expected cascade members per primary (launch heuristics)
   // stopping-table rows of the FP32 engine, one per distinct (species, material):
   // the MatConst entry and the species each row is built from
