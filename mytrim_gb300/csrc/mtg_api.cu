@@ -154,6 +154,18 @@ record_size(int precision)
   return precision == MTG_PREC_FP64 ? record_size64() : record_size32();
 }
 
+// the smallest cascade-kernel variant (KernelLevel) with every feature the run uses
+int
+kernel_level(const mtg_ctx * ctx)
+{
+  const HostTables & t = ctx->tables;
+  if ((ctx->event_cap > 0 && ctx->event_mask) || t.any_extended)
+    return LVL_FULL;
+  if (ctx->record_cap > 0 || t.voxel_total > 0 || t.any_evac || t.any_mode)
+    return LVL_MID;
+  return LVL_LEAN;
+}
+
 mtg_status
 setup_launch_shape(mtg_ctx * ctx)
 {
@@ -187,12 +199,10 @@ setup_launch_shape(mtg_ctx * ctx)
   ctx->smem = size_t(ctx->cold_offset) + slot * size_t(ctx->block);
   ctx->hist_smem_bins = 0;
   int bps = 0;
-  const int events = ctx->event_cap > 0 && ctx->event_mask ? 1 : 0;
-  const int extended = t.any_extended;
+  const int level = kernel_level(ctx);
   auto occupancy = [&](size_t smem, int * b) {
-    return prec == MTG_PREC_FP64
-               ? occupancy64(ctx->block, smem, b, events, extended)
-               : occupancy32(ctx->block, smem, b, prec == MTG_PREC_FP32_SURROGATE, events, extended);
+    return prec == MTG_PREC_FP64 ? occupancy64(ctx->block, smem, b, level)
+                                 : occupancy32(ctx->block, smem, b, prec == MTG_PREC_FP32_SURROGATE, level);
   };
   cudaError_t e = occupancy(ctx->smem, &bps);
   if (e != cudaSuccess)
@@ -308,7 +318,7 @@ fill_params(mtg_ctx * ctx, EngineParams & prm)
     prm.event_mask = ctx->event_mask;
   }
   prm.any_evac = t.any_evac;
-  prm.any_extended = t.any_extended;
+  prm.level = kernel_level(ctx);
   prm.warp_steps = ptr<unsigned long long>(ctx->d_counters) + C_STEPS;
 }
 

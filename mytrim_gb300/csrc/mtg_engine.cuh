@@ -92,7 +92,7 @@ struct EngineParams
   long long events_cap;
   unsigned int event_mask;
   int any_evac; // some simulation keeps a vacancy-energy histogram
-  int any_extended; // some simulation has the cluster geometry or a non-universal potential
+  int level;    // KernelLevel of the launched variant
   unsigned long long * warp_steps; // loop iterations of all warps (lane occupancy = collisions / 32 steps)
   // single-simulation runs with few depth bins count vacancies and replacements in
   // a per-block shared-memory histogram (hist_smem_bins counters from byte offset
@@ -205,11 +205,27 @@ struct LaneCold
   int evac_bin;    // vacancy-energy bin of the current collision (-1 = none)
 };
 
-// Device tally sink for one lane.  EV: the kernel variant that feeds the event
-// log (the default variant carries no event code at all).
-template <class Pol, bool EV>
+// Kernel feature levels.  Code for a feature a run does not use still costs the
+// collision loop (instruction fetch, registers), so the cascade kernel comes in
+// three variants and each run takes the smallest that has what it needs:
+//   LVL_LEAN  layered samples, universal potential, TrimVacCount tallies (depth,
+//             range and lateral histograms), CUT boundaries and sputter counting;
+//   LVL_MID   + member records, deposition voxels, the vacancy-energy histogram,
+//             TrimRange / TrimPrimaries tally modes;
+//   LVL_FULL  + the event log, the cluster geometry, the Moliere and C-Kr potentials.
+enum KernelLevel : int
+{
+  LVL_LEAN = 0,
+  LVL_MID = 1,
+  LVL_FULL = 2
+};
+
+// Device tally sink for one lane of a kernel of level LVL.
+template <class Pol, int LVL>
 struct LaneSink
 {
+  static constexpr bool EV = LVL >= LVL_FULL; // feeds the event log
+  static constexpr bool MID = LVL >= LVL_MID;
   using Acc = typename Pol::Acc;       // rare sums (kept in shared memory)
   using AccHot = typename Pol::AccHot; // per-collision sums (registers)
   using Real = typename Pol::Real;
@@ -240,7 +256,7 @@ struct LaneSink
   // per-member summaries feed the optional member records only
   __device__ void reset_member()
   {
-    if (!prm->records)
+    if (!MID || !prm->records)
       return;
     cold->m_vac = 0;
     cold->m_state = 0;
@@ -302,7 +318,7 @@ struct LaneSink
   // energy-deposition voxel tally (extension): one float atomic per deposit
   __device__ void deposit(Real x, Real y, Real z, Real e)
   {
-    if (!vox)
+    if (!MID || !vox)
       return;
     const int ix = int(floorf(float(x - Real(sim->voxel_origin[0])) * sim->voxel_inv_cell[0]));
     const int iy = int(floorf(float(y - Real(sim->voxel_origin[1])) * sim->voxel_inv_cell[1]));
@@ -322,6 +338,8 @@ struct LaneSink
   }
   __device__ void flush_voxel()
   {
+    if constexpr (!MID)
+      return;
     LaneCold<Acc> & c = *cold;
     if (c.vcell >= 0)
       atomicAdd(prm->voxels + c.vcell, c.vacc);
@@ -333,7 +351,7 @@ struct LaneSink
   __device__ void eel(Real d, Real x, Real y, Real z)
   {
     a_eel.add(d);
-    if (prm->records)
+    if (MID && prm->records)
       cold->m_eel.add(d);
     deposit(x, y, z, d);
   }
@@ -359,7 +377,7 @@ struct LaneSink
       event(EV_LOST, Real(p.x), Real(p.y), Real(p.z), Real(p.E), Z1, m1, p.gen, ST_LOST, e - Real(p.E), p.key);
     ++c.n_lost;
     c.e_lost.add(e);
-    if (prm->records)
+    if (MID && prm->records)
       c.m_state = ST_LOST;
     if (p.x < Real(0) && sim->bc[0] == 2)
     {
@@ -379,7 +397,7 @@ struct LaneSink
     if constexpr (EV)
       event(EV_VACANCY, Real(rec.x), Real(rec.y), Real(rec.z), Erec, el.Z2, Real(el.m2), rec.gen, 0,
             Real(el.Elbind), key);
-    if (range_mode == 2)
+    if (MID && range_mode == 2)
     {
       // TrimPrimaries::vacancyCreation (trim.C:446-464): one vacancy per displaced
       // recoil and, for a recoil of the cutoff generation (not followed), the
@@ -399,7 +417,7 @@ struct LaneSink
         cold->m_vac += add;
       return;
     }
-    if (range_mode)
+    if (MID && range_mode)
     {
       // TrimRange::vacancyCreation (apps/src/TrimRange.C:32-47): Kinchin-Pease
       // count of the displaced recoil, each increment truncated like the
@@ -423,13 +441,13 @@ struct LaneSink
       return;
     }
     ++a_vac;
-    if (prm->records)
+    if (MID && prm->records)
       ++cold->m_vac;
     const int b = depth_bin(Real(rec.x), inv_vac_bin(), sim->hist_vac_n);
     if (b >= 0)
     {
       vac_bin = int(sim->hist_vac_base) + b;
-      if (prm->any_evac && sim->hist_evac_rows > 0)
+      if (MID && prm->any_evac && sim->hist_evac_rows > 0)
       {
         // TrimVacEnergyCount::vacancyCreation (apps/src/TrimVacEnergyCount.C:32-53):
         // row int(ln E) of the recoil energy, negative rows in row 0
@@ -462,7 +480,7 @@ struct LaneSink
   {
     if constexpr (EV)
       event(EV_REST, Real(p.x), Real(p.y), Real(p.z), Real(p.E), Z1, m1, p.gen, state, Real(0), p.key);
-    if (prm->records)
+    if (MID && prm->records)
       cold->m_state = state;
     a_enuc.add(Real(p.E));
     deposit(Real(p.x), Real(p.y), Real(p.z), Real(p.E));
@@ -601,13 +619,14 @@ struct LaneSink
   }
 };
 
-// EV: the event-log variant; EXT: the variant that knows the cluster geometry and the
-// Moliere and C-Kr potentials (the others scatter in the universal potential only)
-// (the layered-sample kernel carries neither)
-template <class Pol, bool EV, bool EXT>
+// LVL: the feature level (KernelLevel); the collision code knows the cluster
+// geometry and the non-universal potentials at LVL_FULL only
+template <class Pol, int LVL>
 __global__ void __launch_bounds__(128, Pol::MIN_BLOCKS)
 cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
 {
+  constexpr bool MID = LVL >= LVL_MID;
+  constexpr bool EXT = LVL >= LVL_FULL;
   using Particle = typename Pol::Particle;
   extern __shared__ __align__(16) unsigned char smem[];
 
@@ -653,7 +672,7 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
   const SimDesc * sim = nullptr;
   typename Pol::MemberCtx mctx;
 
-  LaneSink<Pol, EV> sink;
+  LaneSink<Pol, LVL> sink;
   sink.cold = reinterpret_cast<LaneCold<typename Pol::Acc> *>(smem + prm.cold_offset) + threadIdx.x;
   sink.cold->vcell = -1;
   sink.cold->vacc = 0.0f;
@@ -678,7 +697,7 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
       sim = prm.sims + cur_sim;
       sink.sim = sim;
       sink.range_mode = sim->range_mode;
-      sink.vox = prm.voxels != nullptr && sim->voxel_n[0] > 0;
+      sink.vox = MID && prm.voxels != nullptr && sim->voxel_n[0] > 0;
       sink.gprim = -1;
     }
     if ((long long)p.prim != sink.gprim)
@@ -768,7 +787,7 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
       if (flags & CF_DONE)
       {
         live = false;
-        if (prm.records)
+        if (MID && prm.records)
         {
           const unsigned long long slot = atomicAdd(prm.n_records, 1ull);
           if ((long long)slot < prm.records_cap)
@@ -809,7 +828,7 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
           atomicAdd(prm.hist + hb, 1ull);
       }
     }
-    if (prm.any_evac)
+    if (MID && prm.any_evac)
     {
       if (sink.cold->evac_bin >= 0)
         atomicAdd(prm.hist + sink.cold->evac_bin, 1ull);

@@ -452,22 +452,19 @@ launch_cascade32(const EngineParams & prm, const Fp32Tables & t, int grid, int b
   tabs.lnE_min = t.lnE_min;
   tabs.inv_dlnE = t.inv_dlnE;
   tabs.net = reinterpret_cast<const SurrogateNet *>(t.mlp);
-  const int v = (prm.event_mask != 0 ? 1 : 0) + (prm.any_extended != 0 ? 2 : 0);
   if (surrogate)
-    switch (v)
+    switch (prm.level)
     {
-      case 0: cascade_kernel<Fp32Policy<true>, false, false><<<grid, block, smem, st>>>(prm, tabs); break;
-      case 1: cascade_kernel<Fp32Policy<true>, true, false><<<grid, block, smem, st>>>(prm, tabs); break;
-      case 2: cascade_kernel<Fp32Policy<true>, false, true><<<grid, block, smem, st>>>(prm, tabs); break;
-      default: cascade_kernel<Fp32Policy<true>, true, true><<<grid, block, smem, st>>>(prm, tabs); break;
+      case LVL_LEAN: cascade_kernel<Fp32Policy<true>, LVL_LEAN><<<grid, block, smem, st>>>(prm, tabs); break;
+      case LVL_MID: cascade_kernel<Fp32Policy<true>, LVL_MID><<<grid, block, smem, st>>>(prm, tabs); break;
+      default: cascade_kernel<Fp32Policy<true>, LVL_FULL><<<grid, block, smem, st>>>(prm, tabs); break;
     }
   else
-    switch (v)
+    switch (prm.level)
     {
-      case 0: cascade_kernel<Fp32Policy<false>, false, false><<<grid, block, smem, st>>>(prm, tabs); break;
-      case 1: cascade_kernel<Fp32Policy<false>, true, false><<<grid, block, smem, st>>>(prm, tabs); break;
-      case 2: cascade_kernel<Fp32Policy<false>, false, true><<<grid, block, smem, st>>>(prm, tabs); break;
-      default: cascade_kernel<Fp32Policy<false>, true, true><<<grid, block, smem, st>>>(prm, tabs); break;
+      case LVL_LEAN: cascade_kernel<Fp32Policy<false>, LVL_LEAN><<<grid, block, smem, st>>>(prm, tabs); break;
+      case LVL_MID: cascade_kernel<Fp32Policy<false>, LVL_MID><<<grid, block, smem, st>>>(prm, tabs); break;
+      default: cascade_kernel<Fp32Policy<false>, LVL_FULL><<<grid, block, smem, st>>>(prm, tabs); break;
     }
   return cudaGetLastError();
 }
@@ -490,23 +487,22 @@ static cudaError_t
 occupancy_variants(int block, size_t smem, int * occ)
 {
   cudaError_t e;
-  if ((e = occupancy_of(cascade_kernel<Fp32Policy<SG>, false, false>, block, smem, &occ[0])) != cudaSuccess ||
-      (e = occupancy_of(cascade_kernel<Fp32Policy<SG>, true, false>, block, smem, &occ[1])) != cudaSuccess ||
-      (e = occupancy_of(cascade_kernel<Fp32Policy<SG>, false, true>, block, smem, &occ[2])) != cudaSuccess)
+  if ((e = occupancy_of(cascade_kernel<Fp32Policy<SG>, LVL_LEAN>, block, smem, &occ[0])) != cudaSuccess ||
+      (e = occupancy_of(cascade_kernel<Fp32Policy<SG>, LVL_MID>, block, smem, &occ[1])) != cudaSuccess)
     return e;
-  return occupancy_of(cascade_kernel<Fp32Policy<SG>, true, true>, block, smem, &occ[3]);
+  return occupancy_of(cascade_kernel<Fp32Policy<SG>, LVL_FULL>, block, smem, &occ[2]);
 }
 
-// residency of the variant the launch will use; every variant gets the
-// shared-memory opt-in
+// residency of the variant of feature level `level` (KernelLevel); every variant
+// gets the shared-memory opt-in
 cudaError_t
-occupancy32(int block, size_t smem, int * blocks_per_sm, int surrogate, int events, int extended)
+occupancy32(int block, size_t smem, int * blocks_per_sm, int surrogate, int level)
 {
-  int occ[4] = {0, 0, 0, 0};
+  int occ[3] = {0, 0, 0};
   cudaError_t e = surrogate ? occupancy_variants<true>(block, smem, occ) : occupancy_variants<false>(block, smem, occ);
   if (e != cudaSuccess)
     return e;
-  *blocks_per_sm = occ[(events ? 1 : 0) + (extended ? 2 : 0)];
+  *blocks_per_sm = occ[level < 0 ? 0 : (level > 2 ? 2 : level)];
   return cudaSuccess;
 }
 

@@ -95,15 +95,12 @@ cudaError_t
 launch_cascade64(const EngineParams & prm, int grid, int block, size_t smem, cudaStream_t st)
 {
   const Fp64Policy::Tables tabs{prm.species, prm.mats};
-  const bool ev = prm.event_mask != 0, ext = prm.any_extended != 0;
-  if (ev && ext)
-    cascade_kernel<Fp64Policy, true, true><<<grid, block, smem, st>>>(prm, tabs);
-  else if (ev)
-    cascade_kernel<Fp64Policy, true, false><<<grid, block, smem, st>>>(prm, tabs);
-  else if (ext)
-    cascade_kernel<Fp64Policy, false, true><<<grid, block, smem, st>>>(prm, tabs);
-  else
-    cascade_kernel<Fp64Policy, false, false><<<grid, block, smem, st>>>(prm, tabs);
+  switch (prm.level)
+  {
+    case LVL_LEAN: cascade_kernel<Fp64Policy, LVL_LEAN><<<grid, block, smem, st>>>(prm, tabs); break;
+    case LVL_MID: cascade_kernel<Fp64Policy, LVL_MID><<<grid, block, smem, st>>>(prm, tabs); break;
+    default: cascade_kernel<Fp64Policy, LVL_FULL><<<grid, block, smem, st>>>(prm, tabs); break;
+  }
   return cudaGetLastError();
 }
 
@@ -120,19 +117,18 @@ occupancy_of(K kernel, int block, size_t smem, int * blocks_per_sm)
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kernel, block, smem);
 }
 
-// residency of the variant the launch will use; every variant gets the
-// shared-memory opt-in
+// residency of the variant of feature level `level` (KernelLevel); every variant
+// gets the shared-memory opt-in
 cudaError_t
-occupancy64(int block, size_t smem, int * blocks_per_sm, int events, int extended)
+occupancy64(int block, size_t smem, int * blocks_per_sm, int level)
 {
-  int occ[4] = {0, 0, 0, 0};
+  int occ[3] = {0, 0, 0};
   cudaError_t e;
-  if ((e = occupancy_of(cascade_kernel<Fp64Policy, false, false>, block, smem, &occ[0])) != cudaSuccess ||
-      (e = occupancy_of(cascade_kernel<Fp64Policy, true, false>, block, smem, &occ[1])) != cudaSuccess ||
-      (e = occupancy_of(cascade_kernel<Fp64Policy, false, true>, block, smem, &occ[2])) != cudaSuccess ||
-      (e = occupancy_of(cascade_kernel<Fp64Policy, true, true>, block, smem, &occ[3])) != cudaSuccess)
+  if ((e = occupancy_of(cascade_kernel<Fp64Policy, LVL_LEAN>, block, smem, &occ[0])) != cudaSuccess ||
+      (e = occupancy_of(cascade_kernel<Fp64Policy, LVL_MID>, block, smem, &occ[1])) != cudaSuccess ||
+      (e = occupancy_of(cascade_kernel<Fp64Policy, LVL_FULL>, block, smem, &occ[2])) != cudaSuccess)
     return e;
-  *blocks_per_sm = occ[(events ? 1 : 0) + (extended ? 2 : 0)];
+  *blocks_per_sm = occ[level < 0 ? 0 : (level > 2 ? 2 : level)];
   return cudaSuccess;
 }
 

@@ -13,7 +13,7 @@ struct PrimaryTallies;
 
 // FP64 exact path (mtg_engine64.cu)
 cudaError_t launch_cascade64(const EngineParams & prm, int grid, int block, size_t smem, cudaStream_t st);
-cudaError_t occupancy64(int block, size_t smem, int * blocks_per_sm, int events, int extended);
+cudaError_t occupancy64(int block, size_t smem, int * blocks_per_sm, int level);
 size_t record_size64();
 size_t cold_slot_bytes64(); // per-thread shared-memory tally slot
 cudaError_t launch_stopping64(const SpeciesConst * sc, const MatConst * mc, const double * E, long long n,
@@ -37,7 +37,7 @@ cudaError_t launch_build_stop_tables(const SpeciesConst * species, const MatCons
                                      double dlnE, cudaStream_t st);
 cudaError_t launch_cascade32(const EngineParams & prm, const Fp32Tables & t, int grid, int block, size_t smem,
                              cudaStream_t st, int surrogate);
-cudaError_t occupancy32(int block, size_t smem, int * blocks_per_sm, int surrogate, int events, int extended);
+cudaError_t occupancy32(int block, size_t smem, int * blocks_per_sm, int surrogate, int level);
 size_t record_size32();
 size_t cold_slot_bytes32();
 cudaError_t launch_scatter32(const double * eps, const double * b, long long n, double * s2, int potential,

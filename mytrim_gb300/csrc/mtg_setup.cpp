@@ -348,6 +348,7 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
   out.k0 = out.k1 = 0;
   out.emax = 0.0;
   out.any_evac = 0;
+  out.any_mode = 0;
   out.any_extended = 0;
   out.members_est = 1.0;
   if (n_sims < 1 || !sims)
@@ -552,6 +553,8 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
       return MTG_ERR_BAD_INPUT;
     }
     d.range_mode = s.tally_mode;
+    if (s.tally_mode != MTG_TALLY_VACCOUNT)
+      out.any_mode = 1;
     d.primaries_only = s.primaries_only != 0;
     // which displaced recoils are followed (followRecoil): ThreadedTrimBase all, or
     // none with primaries_only; TrimRange none (only generation 0 moves);

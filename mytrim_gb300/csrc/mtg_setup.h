@@ -24,6 +24,7 @@ struct HostTables
   uint32_t k0 = 0, k1 = 0;                // Philox key
   double emax = 0.0;                      // largest primary energy
   int any_evac = 0;                       // some simulation keeps a vacancy-energy histogram
+  int any_mode = 0;                       // some simulation tallies in TrimRange / TrimPrimaries mode
   int any_extended = 0;                   // some simulation has the cluster geometry or a
                                           // potential other than the universal one
   double members_est = 1.0;               // expected cascade members per primary (launch heuristics)

@@ -230,6 +230,34 @@ def test_invalid_potential_is_rejected(engine_lib):
 
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_kernel_levels_agree(engine_lib, prec):
+    """The lean, mid and full kernel variants (chosen by the features a run uses:
+    none, member records, the event log) give the same tallies on the same streams."""
+    sim = SimSpec(**{**CASES["as_sio2_si_cut"][0].__dict__, "n_primaries": 400})
+    out = []
+    for level in ("lean", "mid", "full"):
+        e = Engine(precision=prec, seed=4)
+        if level == "mid":
+            e.set_record_capacity(1 << 20)
+        if level == "full":
+            e.set_event_log([F.EV_VACANCY], 1 << 20)
+        out.append(e.run([sim])[0])
+        e.close()
+    for r in out[1:]:
+        if prec == "fp64":
+            # the same FP64 arithmetic in every variant: identical trajectories
+            for k in ("members", "collisions", "vacancies", "replacements", "interstitials", "lost", "range_n"):
+                assert r[k] == out[0][k], k
+            for k in ("Eel", "Enuc", "Elost"):
+                assert math.isclose(r[k], out[0][k], rel_tol=1e-9), k
+            assert list(r["hist_range"]) == list(out[0]["hist_range"])
+        else:
+            # FP32: the compiler may contract differently per variant; same statistics
+            for k in ("members", "collisions", "vacancies", "Eel", "Enuc"):
+                assert abs(r[k] - out[0][k]) <= 0.03 * abs(out[0][k]), k
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
 def test_energy_conservation(engine_lib, prec):
     sim = W.arsenic_implant(n_primaries=2000)
     e = Engine(precision=prec, seed=3)
