@@ -622,7 +622,7 @@ struct LaneSink
 // LVL: the feature level (KernelLevel); the collision code knows the cluster
 // geometry and the non-universal potentials at LVL_FULL only
 template <class Pol, int LVL>
-__global__ void __launch_bounds__(128, Pol::MIN_BLOCKS)
+__global__ void __launch_bounds__(128, Pol::min_blocks(LVL))
 cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
 {
   constexpr bool MID = LVL >= LVL_MID;

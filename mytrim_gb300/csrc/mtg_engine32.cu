@@ -23,8 +23,14 @@
 #include "mtg_scatter32.cuh"
 #include "mtg_surrogate.cuh"
 
+// resident 128-thread blocks per SM the register budget is cut for: the lean
+// variant fits 72 registers without spills and gains from the seventh block; the
+// larger variants keep 80 registers
 #ifndef MTG_FP32_MIN_BLOCKS
 #define MTG_FP32_MIN_BLOCKS 6
+#endif
+#ifndef MTG_FP32_MIN_BLOCKS_LEAN
+#define MTG_FP32_MIN_BLOCKS_LEAN 7
 #endif
 
 namespace mtg
@@ -86,9 +92,12 @@ struct Fp32Policy
   using AccHot = AccF32;
   static constexpr int FLUSH_EVERY = 64; // collisions per hand-over of the hot energy sums (power of 2)
   using Tables = Tables32;
-  // resident 128-thread blocks per SM the register budget is cut for (the
-  // surrogate's tensor-core fragments need more registers)
-  static constexpr int MIN_BLOCKS = SURROGATE ? 4 : MTG_FP32_MIN_BLOCKS;
+  // resident 128-thread blocks per SM the register budget of the variant of level
+  // `lvl` is cut for (the surrogate's tensor-core fragments need more registers)
+  static constexpr int min_blocks(int lvl)
+  {
+    return SURROGATE ? 4 : (lvl == LVL_LEAN ? MTG_FP32_MIN_BLOCKS_LEAN : MTG_FP32_MIN_BLOCKS);
+  }
 
   struct MemberCtx
   {

@@ -16,7 +16,7 @@ struct Fp64Policy
   using Acc = AccF64;
   using AccHot = AccF64;
   static constexpr int FLUSH_EVERY = 0;
-  static constexpr int MIN_BLOCKS = 3; // <= 170 registers: 12 warps per SM
+  static constexpr int min_blocks(int) { return 3; } // <= 170 registers: 12 warps per SM
 
   struct Tables
   {
