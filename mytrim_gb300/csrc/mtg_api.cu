@@ -178,11 +178,10 @@ setup_launch_shape(mtg_ctx * ctx)
   {
     if (prec == MTG_PREC_FP64)
       tab = sizeof(SpeciesConst) * t.species.size() + sizeof(MatConst) * t.mats.size();
+    else if (prec == MTG_PREC_FP32_SURROGATE)
+      tab = stage_net_offset(int(t.species.size()), int(t.mats.size())) + surrogate_net_bytes();
     else
-      tab = sizeof(Species32) * t.species.size() + sizeof(Mat32) * t.mats.size() +
-            sizeof(float) * STOP_N * t.stop_row_mat.size();
-    if (prec == MTG_PREC_FP32_SURROGATE)
-      tab += surrogate_net_bytes();
+      tab = sizeof(Species32) * t.species.size() + sizeof(Mat32) * t.mats.size();
     if (tab <= 160 * 1024)
       ctx->stage = 1;
     else
@@ -269,7 +268,6 @@ fill_params(mtg_ctx * ctx, EngineParams & prm)
   prm.hist_smem_base = ctx->hist_smem_bins ? t.sims[0].hist_vac_base : 0;
   prm.n_stage_species = int(t.species.size());
   prm.n_stage_mats = int(t.mats.size());
-  prm.n_stage_stop_rows = int(t.stop_row_mat.size());
   prm.total_primaries = t.total_primaries;
   prm.stacks = ctx->d_stacks.p;
   prm.stack_cap = ctx->stack_cap;

@@ -58,7 +58,6 @@ struct EngineParams
   const MatConst * mats;
   int stage_tables;               // stage species+mats of simulation 0 into shared memory
   int n_stage_species, n_stage_mats;
-  int n_stage_stop_rows;          // FP32 stopping-table rows of the run
   long long total_primaries;
   unsigned long long * next_primary;
   // drain mode: members read from `in_records` (count in device memory) instead

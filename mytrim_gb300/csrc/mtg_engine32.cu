@@ -24,13 +24,13 @@
 #include "mtg_surrogate.cuh"
 
 // resident 128-thread blocks per SM the register budget is cut for: the lean
-// variant fits 72 registers without spills and gains from the seventh block; the
+// variant fits 64 registers without spills and gains from the eighth block; the
 // larger variants keep 80 registers
 #ifndef MTG_FP32_MIN_BLOCKS
 #define MTG_FP32_MIN_BLOCKS 6
 #endif
 #ifndef MTG_FP32_MIN_BLOCKS_LEAN
-#define MTG_FP32_MIN_BLOCKS_LEAN 7
+#define MTG_FP32_MIN_BLOCKS_LEAN 8
 #endif
 
 namespace mtg
@@ -132,19 +132,17 @@ struct Fp32Policy
     q += sizeof(Species32) * ns;
     Mat32 * s_mc = reinterpret_cast<Mat32 *>(q);
     q += sizeof(Mat32) * nm;
-    float * s_st = reinterpret_cast<float *>(q);
     const int n1 = int(sizeof(Species32) / 4) * ns;
     const int n2 = int(sizeof(Mat32) / 4) * nm;
-    const int n3 = STOP_N * prm.n_stage_stop_rows;
     for (int i = threadIdx.x; i < n1; i += blockDim.x)
       reinterpret_cast<float *>(s_sp)[i] = reinterpret_cast<const float *>(g.species)[i];
     for (int i = threadIdx.x; i < n2; i += blockDim.x)
       reinterpret_cast<float *>(s_mc)[i] = reinterpret_cast<const float *>(g.mats)[i];
-    for (int i = threadIdx.x; i < n3; i += blockDim.x)
-      s_st[i] = g.stop[i];
+    // the stopping tables stay in global memory (L1-resident): the shared memory
+    // they would take is worth more as an eighth resident block
     if (SURROGATE)
     {
-      SurrogateNet * s_net = reinterpret_cast<SurrogateNet *>(s_st + n3);
+      SurrogateNet * s_net = reinterpret_cast<SurrogateNet *>(smem + stage_net_offset(ns, nm));
       for (int i = threadIdx.x; i < int(sizeof(SurrogateNet) / 4); i += blockDim.x)
         reinterpret_cast<float *>(s_net)[i] = reinterpret_cast<const float *>(g.net)[i];
       t.net = s_net;
@@ -152,7 +150,6 @@ struct Fp32Policy
     __syncthreads();
     t.species = s_sp;
     t.mats = s_mc;
-    t.stop = s_st;
     return t;
   }
 

@@ -205,6 +205,17 @@ struct Species32
   int Z1, pad;
 };
 
+// byte offset of the surrogate network in the FP32 engine's staged shared-memory
+// tables: after the species and material rows, 16-byte aligned
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline size_t
+stage_net_offset(int n_species, int n_mats)
+{
+  return (sizeof(Species32) * size_t(n_species) + sizeof(Mat32) * size_t(n_mats) + 15) / 16 * 16;
+}
+
 struct Sim32
 {
   float layer_end[MAX_LAYERS];
