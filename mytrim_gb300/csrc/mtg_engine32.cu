@@ -23,11 +23,15 @@
 #include "mtg_scatter32.cuh"
 #include "mtg_surrogate.cuh"
 
-// resident 128-thread blocks per SM the register budget is cut for: the lean
-// variant fits 64 registers without spills and gains from the eighth block; the
-// larger variants keep 80 registers
+// resident 128-thread blocks per SM the register budget of each feature level is
+// cut for: lean 8 (64 registers), mid 7 (72), full 6 (80), each the most that
+// compiles without spilling in the collision loop (the full level's cluster lookup
+// spills a few words even at 80)
 #ifndef MTG_FP32_MIN_BLOCKS
 #define MTG_FP32_MIN_BLOCKS 6
+#endif
+#ifndef MTG_FP32_MIN_BLOCKS_MID
+#define MTG_FP32_MIN_BLOCKS_MID 7
 #endif
 #ifndef MTG_FP32_MIN_BLOCKS_LEAN
 #define MTG_FP32_MIN_BLOCKS_LEAN 8
@@ -96,7 +100,9 @@ struct Fp32Policy
   // `lvl` is cut for (the surrogate's tensor-core fragments need more registers)
   static constexpr int min_blocks(int lvl)
   {
-    return SURROGATE ? 4 : (lvl == LVL_LEAN ? MTG_FP32_MIN_BLOCKS_LEAN : MTG_FP32_MIN_BLOCKS);
+    return SURROGATE ? 4
+                     : (lvl == LVL_LEAN ? MTG_FP32_MIN_BLOCKS_LEAN
+                                        : (lvl == LVL_MID ? MTG_FP32_MIN_BLOCKS_MID : MTG_FP32_MIN_BLOCKS));
   }
 
   struct MemberCtx
