@@ -196,8 +196,9 @@ static const double h_log_lo[92] = {MTG_LOG_TABLE_LO};
 // (ln2/64 in two parts, the first with 29 significant bits so that n times it is
 // exact); e^x = 2^m (S_j + S_j p(r)), S_j = 2^(j/64) as a double pair and p the
 // Taylor polynomial of e^r - 1 to degree 6 (truncation below 3e-20 relative).
+// This is the full-range form; exp64 below takes a shorter route for |x| < 704.
 MTG_HD double
-exp64(double x)
+exp64_wide(double x)
 {
   if (x < -745.2)
     return 0.0;
@@ -223,6 +224,42 @@ exp64(double x)
   return (y * pow2i(m + 600)) * pow2i(-600);
 }
 
+// e^x with the same arithmetic as exp64_wide, hence the same result for every x.
+// For |x| < 704 (judged on the high word, no FP64 compare) the result is a normal
+// number 2^m y with -1017 <= m <= 1016: n = rint(64 x / ln2) comes from adding and
+// subtracting 1.5 * 2^52 (the sum's low word is n), and the scaling by 2^m is an
+// integer add to the exponent field.  The FP64 unit is the narrow one on GB300, so
+// this keeps the compares, conversions and the scaling multiply off it.
+MTG_HD double
+exp64(double x)
+{
+  const uint64_t bx = double_to_bits(x);
+  if ((uint32_t(bx >> 32) & 0x7fffffffu) >= 0x40860000u) // |x| >= 704, inf, NaN
+    return exp64_wide(x);
+  // rint(x * 64/ln2) + 1.5 * 2^52, the product rounded first as in exp64_wide
+  // (never contracted to an fma, whatever the translation unit's flags)
+#if defined(__CUDA_ARCH__)
+  const double t = __dadd_rn(__dmul_rn(x, MTG_EXP_INV_L), 0x1.8p52);
+#else
+  const double t = x * MTG_EXP_INV_L + 0x1.8p52; // host builds use -ffp-contract=off
+#endif
+  const double k = t - 0x1.8p52;
+  const int n = int(uint32_t(double_to_bits(t)));
+  double r = fma(-k, MTG_EXP_L1, x);
+  r = fma(-k, MTG_EXP_L2, r);
+  const int j = n & 63;
+  const int m = n >> 6; // floor(n / 64)
+  double p = 0x1.6c16c16c16c17p-10;   // 1/720
+  p = fma(p, r, 0x1.1111111111111p-7); // 1/120
+  p = fma(p, r, 0x1.5555555555555p-5); // 1/24
+  p = fma(p, r, 0x1.5555555555555p-3); // 1/6
+  p = fma(p, r, 0.5);
+  p = fma(p, r * r, r);
+  const double sh = MTG_TAB(exp_hi)[j];
+  const double y = sh + fma(sh, p, MTG_TAB(exp_lo)[j]);
+  return bits_to_double(double_to_bits(y) + (uint64_t(int64_t(m)) << 52));
+}
+
 // natural logarithm for finite x > 0.  x = 2^e m with m in (sqrt(1/2), sqrt(2)];
 // m falls in interval j of 0.703125 + j/128, whose approximate reciprocal inv_c has
 // at most 10 significant bits, so u = m inv_c - 1 is a single rounding (|u| < 1/128,
@@ -230,7 +267,7 @@ exp64(double x)
 // first two summed exactly (both multiples of 2^-42) and log1p(u) its Taylor
 // polynomial to degree 9 (truncation below 1e-20 relative).
 MTG_HD double
-log64(double x)
+log64_wide(double x)
 {
   if (!(x > 0.0))
     return x == 0.0 ? -HUGE_VAL : NAN;
@@ -262,6 +299,50 @@ log64(double x)
   q = fma(q, u, -0.5);                  // -1/2
   q = q * (u * u);
   const double de = double(e);
+  const double hi = fma(de, MTG_LOG_LN2_HI, MTG_TAB(log_hi)[j]);
+  const double lo = fma(de, MTG_LOG_LN2_LO, MTG_TAB(log_lo)[j]);
+  return hi + (u + (lo + q));
+}
+
+// log x with the same arithmetic as log64_wide, hence the same result for every x.
+// For positive normal finite x (judged on the bit pattern) the exponent, the halving
+// of m above sqrt(2) and the interval index come from integer operations on the
+// bits: j = 38 + (f >> 45) for m = 1 + f / 2^52 <= sqrt(2), j = (f >> 46) - 26 for
+// m / 2, the same integer parts of (m - 0.703125) 128 that log64_wide computes in
+// FP64 (exactly: m - 0.703125 is representable).  e becomes a double through the
+// 1.5 * 2^52 trick.
+MTG_HD double
+log64(double x)
+{
+  const uint64_t bits = double_to_bits(x);
+  if (bits - 0x0010000000000000ull >= 0x7fe0000000000000ull) // zero, subnormal, negative, inf, NaN
+    return log64_wide(x);
+  const uint64_t f = bits & 0x000fffffffffffffull;
+  int e = int(bits >> 52) - 1023;
+  double m;
+  int j;
+  if (f > 0x6a09e667f3bcdull) // m = 1 + f / 2^52 > sqrt(2): use m / 2
+  {
+    m = bits_to_double(f | 0x3fe0000000000000ull);
+    e += 1;
+    j = int(f >> 46) - 26;
+  }
+  else
+  {
+    m = bits_to_double(f | 0x3ff0000000000000ull);
+    j = 38 + int(f >> 45);
+  }
+  const double u = fma(m, MTG_TAB(log_invc)[j], -1.0);
+  double q = 0x1.c71c71c71c71cp-4;      // 1/9
+  q = fma(q, u, -0x1.0000000000000p-3); // -1/8
+  q = fma(q, u, 0x1.2492492492492p-3);  // 1/7
+  q = fma(q, u, -0x1.5555555555555p-3); // -1/6
+  q = fma(q, u, 0x1.999999999999ap-3);  // 1/5
+  q = fma(q, u, -0x1.0000000000000p-2); // -1/4
+  q = fma(q, u, 0x1.5555555555555p-2);  // 1/3
+  q = fma(q, u, -0.5);                  // -1/2
+  q = q * (u * u);
+  const double de = bits_to_double(0x4338000000000000ull + uint64_t(int64_t(e))) - 0x1.8p52;
   const double hi = fma(de, MTG_LOG_LN2_HI, MTG_TAB(log_hi)[j]);
   const double lo = fma(de, MTG_LOG_LN2_LO, MTG_TAB(log_lo)[j]);
   return hi + (u + (lo + q));

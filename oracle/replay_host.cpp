@@ -143,6 +143,50 @@ main(int argc, char ** argv)
       printf("%a\n", material_stop64(sc, mc, E));
     return 0;
   }
+  if (argc >= 3 && std::string(argv[2]) == "--mathcheck")
+  {
+    // exp64 / log64 (short routes) against exp64_wide / log64_wide bit for bit on n
+    // inputs: random bit patterns, random values of every magnitude, the edges of
+    // the short routes; prints "checked mismatches"
+    const long long n = argc >= 4 ? atoll(argv[3]) : 1000000;
+    uint64_t st = 0x9e3779b97f4a7c15ull;
+    auto next = [&]() {
+      st += 0x9e3779b97f4a7c15ull;
+      uint64_t z = st;
+      z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+      z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+      return z ^ (z >> 31);
+    };
+    const double edges[] = {0.0, -0.0, 704.0, -704.0, 703.9999999999999, -703.9999999999999, 709.7, -745.2,
+                            1.0, 0x1.6a09e667f3bcdp+0, 0x1.6a09e667f3bcep+0, 0x1p-1022, 0x1p-1023, 0x1.fffffffffffffp+1023,
+                            HUGE_VAL, -HUGE_VAL, NAN, 0.703125, 0.70710678118654757};
+    long long bad = 0, checked = 0;
+    auto check = [&](double x) {
+      const uint64_t a = double_to_bits(exp64(x)), b = double_to_bits(exp64_wide(x));
+      const uint64_t c = double_to_bits(log64(x)), d = double_to_bits(log64_wide(x));
+      const bool nan_ab = exp64(x) != exp64(x) && exp64_wide(x) != exp64_wide(x);
+      const bool nan_cd = log64(x) != log64(x) && log64_wide(x) != log64_wide(x);
+      if ((a != b && !nan_ab) || (c != d && !nan_cd))
+      {
+        if (bad < 5)
+          printf("mismatch x=%a exp %a %a log %a %a\n", x, exp64(x), exp64_wide(x), log64(x), log64_wide(x));
+        ++bad;
+      }
+      ++checked;
+    };
+    for (double x : edges)
+      check(x);
+    for (long long i = 0; i < n; ++i)
+    {
+      const uint64_t r = next();
+      check(bits_to_double(r));                                          // any bit pattern
+      check(double(int64_t(r >> 11) - (1ll << 52)) * 0x1p-43);           // |x| < 512
+      check(ldexp(double(r >> 11) * 0x1p-53, int(next() % 2100) - 1074)); // every magnitude
+      check((double(r >> 11) * 0x1p-53 - 0.5) * 1500.0);                 // around the exp edges
+    }
+    printf("%lld %lld\n", checked, bad);
+    return bad ? 1 : 0;
+  }
   if (argc >= 3 && std::string(argv[2]) == "--scatter")
   {
     // lines "eps b" -> s2; an optional argument after --scatter picks the potential
