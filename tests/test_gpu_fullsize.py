@@ -1,0 +1,138 @@
+"""Size-independent properties of the GPU engine at the full sizes of the five
+measurement configurations (GB300; called through the C ABI):
+
+* C1, Cu 100 keV into Cu, 10^4 primaries, FP64: energy conservation to 1e-12, the
+  range histogram holds every primary that came to rest, FP32 agrees statistically;
+* C2, B 10 keV and As 50 keV at 7 deg into SiO2 / Si, 10^6 primaries each, FP32:
+  energy conservation, the lateral histogram and the range histogram account for
+  every stopped primary inside their extent, two primary shards reproduce the whole
+  run's integer tallies exactly, and FP32 agrees with FP64 (10^6 B, 10^5 As);
+* C3, 4096 independent simulations (about 5.9e7 primaries), FP32: every
+  simulation conserves energy and ran all its primaries;
+* C4, Ag 200 keV into Si, 10^7 primaries, FP32: energy conservation, the mean
+  projected range within 1 % of the FP64 path's (5e4 primaries), and the surrogate
+  path's (2e6 primaries) within 1 % of the FP32 path's;
+* C5, Au 1 MeV into Ag / Cu / Si, 10^6 of the 10^8 primaries (about 5 s), FP32 with
+  256^3 voxels: the voxel total equals the energy deposited inside the box, which
+  is at most the total deposit; sputtered atoms and backscattered ions counted.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from mytrim_gb300 import Engine, summarize
+from mytrim_gb300 import workloads as W
+from mytrim_gb300.engine import SimSpec
+
+pytestmark = pytest.mark.gpu
+
+INT_KEYS = ("members", "collisions", "vacancies", "replacements", "interstitials", "substitutionals", "lost",
+            "range_n")
+
+
+def _conserved(t, E0, n, rel):
+    total = t["Eel"] + t["Enuc"] + t["Elost"] + t["Eunfollowed"]
+    assert abs(total - E0 * n) <= rel * E0 * n, (total, E0 * n)
+
+
+def _run(prec, sims, seed=1):
+    e = Engine(precision=prec, seed=seed)
+    try:
+        return e.run(sims)
+    finally:
+        e.close()
+
+
+def _agree(a, b, key, rel):
+    a, b = summarize(a), summarize(b)
+    z = abs(a[key] - b[key]) / math.hypot(a[key + "_err"], b[key + "_err"])
+    assert z < 3.5 or abs(a[key] - b[key]) <= rel * abs(b[key]), (key, a[key], b[key], z)
+
+
+def test_c1_cu_self_ion_fp64():
+    sim = W.cu_self_ion(n_primaries=10_000)
+    t = _run("fp64", [sim])[0]
+    assert t["primaries"] == 10_000
+    _conserved(t, sim.E, 10_000, 1e-12)
+    beyond = t["range_n"] - int(np.sum(t["hist_range"]))
+    assert 0 <= beyond <= t["range_n"]  # stops past 200 nm fall outside the histogram
+    f = _run("fp32", [sim])[0]
+    _conserved(f, sim.E, 10_000, 2e-6)
+    for key in ("vac_per_ion", "range_mean", "eel_per_ion"):
+        _agree(f, t, key, 0.01)
+
+
+@pytest.mark.parametrize("ion", ["boron", "arsenic"])
+def test_c2_layered_implants(ion):
+    n = 1_000_000
+    sim = W.boron_implant(n) if ion == "boron" else W.arsenic_implant(n)
+    t = _run("fp32", [sim])[0]
+    assert t["primaries"] == n
+    _conserved(t, sim.E, n, 2e-6)
+    # every primary that came to rest inside the lateral window is in the lateral
+    # histogram, every one that stopped within 300 nm in the range histogram
+    assert 0 < int(np.sum(t["hist_lateral"])) <= t["range_n"]
+    assert 0 < int(np.sum(t["hist_range"])) <= t["range_n"]
+    assert t["range_n"] + t["backscattered"] == n  # CUT surface: the rest left through x < 0
+    # two primary shards reproduce the whole run
+    parts = [_run("fp32", [SimSpec(**{**sim.__dict__, "n_primaries": k, "first_primary": f})])[0]
+             for f, k in ((0, n // 2), (n // 2, n - n // 2))]
+    for k in INT_KEYS:
+        assert t[k] == parts[0][k] + parts[1][k], k
+    assert np.array_equal(t["hist_range"], parts[0]["hist_range"] + parts[1]["hist_range"])
+    assert np.array_equal(t["hist_lateral"], parts[0]["hist_lateral"] + parts[1]["hist_lateral"])
+    # FP32 against FP64 (the FP64 run at full size for boron, a tenth for arsenic)
+    n64 = n if ion == "boron" else n // 10
+    d = _run("fp64", [SimSpec(**{**sim.__dict__, "n_primaries": n64})])[0]
+    _conserved(d, sim.E, n64, 1e-12)
+    for key in ("vac_per_ion", "range_mean", "straggle", "lateral"):
+        _agree(t, d, key, 0.01)
+
+
+def test_c3_batched_simulations():
+    sims = W.batched_uneven(n_sims=4096, seed=1)
+    out = _run("fp32", sims)
+    assert len(out) == 4096
+    total = sum(s.n_primaries for s in sims)
+    assert total > 3e7
+    assert sum(t["primaries"] for t in out) == total
+    for s, t in zip(sims, out):
+        assert t["primaries"] == s.n_primaries
+        _conserved(t, s.E, s.n_primaries, 1e-5)
+
+
+def test_c4_silver_into_silicon_range_error():
+    sim = W.silver_into_silicon(n_primaries=10_000_000)
+    f = _run("fp32", [sim])[0]
+    assert f["primaries"] == 10_000_000
+    _conserved(f, sim.E, 10_000_000, 2e-6)
+    d = _run("fp64", [SimSpec(**{**sim.__dict__, "n_primaries": 50_000})])[0]
+    rf, rd = summarize(f)["range_mean"], summarize(d)["range_mean"]
+    assert abs(rf - rd) < 0.01 * rd, (rf, rd)
+    from mytrim_gb300.train_surrogate import PARAMS
+    e = Engine(precision="surrogate", seed=1)
+    e.set_surrogate_params(np.load(PARAMS))
+    g = e.run([SimSpec(**{**sim.__dict__, "n_primaries": 2_000_000})])[0]
+    e.close()
+    _conserved(g, sim.E, 2_000_000, 2e-6)
+    # the surrogate's range against the exact FP32 path (10^7 primaries: statistical
+    # error 0.01 %), whose own agreement with FP64 is checked above
+    rg = summarize(g)["range_mean"]
+    assert abs(rg - rf) < 0.01 * rf, (rg, rf)
+
+
+def test_c5_gold_deposition_voxels():
+    n = 1_000_000
+    sim = W.gold_deposition(n_primaries=n, voxels=256)
+    e = Engine(precision="fp32", seed=1)
+    t = e.run([sim])[0]
+    vox = e.voxels(0)
+    e.close()
+    assert vox.shape == (256, 256, 256)
+    _conserved(t, sim.E, n, 2e-6)
+    inside = float(vox.sum(dtype=np.float64))
+    assert math.isclose(inside, t["Evoxel"], rel_tol=1e-6)
+    assert 0.5 * (t["Eel"] + t["Enuc"]) < t["Evoxel"] <= (t["Eel"] + t["Enuc"]) * (1 + 1e-6)
+    assert t["sputtered"] > 0 and t["backscattered"] > 0
+    assert t["Esputtered"] > 0.0
