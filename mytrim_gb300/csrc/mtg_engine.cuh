@@ -239,6 +239,7 @@ struct LaneSink
   // per-simulation Newton-iteration count (every collision), the rest in `cold`
   unsigned int n_newton;
   bool vox;  // this simulation tallies energy deposition in voxels
+  bool dep_in; // the last deposit's point lies in the voxel box (its cell is pending)
   // events of the current collision, aggregated per warp after it
   int vac_bin, repl_bin;
 
@@ -322,8 +323,10 @@ struct LaneSink
     const int ix = int(floorf(float(x - Real(sim->voxel_origin[0])) * sim->voxel_inv_cell[0]));
     const int iy = int(floorf(float(y - Real(sim->voxel_origin[1])) * sim->voxel_inv_cell[1]));
     const int iz = int(floorf(float(z - Real(sim->voxel_origin[2])) * sim->voxel_inv_cell[2]));
+    dep_in = false;
     if (ix < 0 || iy < 0 || iz < 0 || ix >= sim->voxel_n[0] || iy >= sim->voxel_n[1] || iz >= sim->voxel_n[2])
       return;
+    dep_in = true;
     const long long cell = sim->voxel_base + ((long long)iz * sim->voxel_n[1] + iy) * sim->voxel_n[0] + ix;
     LaneCold<Acc> & c = *cold;
     if (cell == c.vcell)
@@ -359,10 +362,15 @@ struct LaneSink
   __device__ void fallback() { ++cold->n_fallbacks; }
   __device__ void numeric() { atomicOr(prm->error_flags, ERRB_NUMERIC); }
   // nuclear (phonon) deposit e at (x, y, z)
-  __device__ void enuc(Real e, Real x, Real y, Real z)
+  // The collision code deposits a collision's nuclear loss where it deposited the
+  // electronic loss just before (the flight's starting point, which is the recoil's
+  // position, trim.C:306-318), so the pending voxel cell is already the right one:
+  // the same sum as a full deposit, without recomputing the cell.
+  __device__ void enuc(Real e, Real /*x*/, Real /*y*/, Real /*z*/)
   {
     a_enuc.add(e);
-    deposit(x, y, z, e);
+    if (MID && vox && dep_in)
+      cold->vacc += float(e);
   }
   __device__ void unfollowed(Real e) { cold->e_unf.add(e); }
   // the member left the sample carrying `e` (its own energy plus the recoil dropped
@@ -681,6 +689,7 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
   sink.gprim = -1;
   sink.range_mode = 0;
   sink.vox = false;
+  sink.dep_in = false;
   sink.reset_prim();
   sink.reset_sim();
   sink.reset_member();
