@@ -85,6 +85,10 @@ class Totals(C.Structure):
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
+    @classmethod
+    def field_names(cls):
+        return [n for n, _ in cls._fields_]
+
 
 class MemberRecord(C.Structure):
     _fields_ = [("key", C.c_ulonglong), ("sim", C.c_int), ("species", C.c_int), ("gen", C.c_int),

@@ -95,22 +95,10 @@ class SimSpec:
         s = F.Sim()
         s.sample.n_layers = len(self.layers)
         for i, l in enumerate(self.layers):
-            if not 1 <= len(l.elements) <= F.MAX_ELEMENTS:
-                raise ValueError("1 to 4 elements per layer")
             s.sample.thickness[i] = l.thickness
-            mat = s.sample.material[i]
-            mat.rho = l.rho
-            mat.n_elements = len(l.elements)
-            for j, e in enumerate(l.elements):
-                mat.elements[j].Z = e.Z
-                mat.elements[j].m = e.m
-                mat.elements[j].t = e.t
-                mat.elements[j].Edisp = e.Edisp
-                mat.elements[j].Elbind = e.Elbind
-        w = self.box()
-        for i in range(3):
-            s.sample.w[i] = w[i]
-            s.sample.bc[i] = self.bc[i]
+            s.sample.material[i] = _c_material(l)
+        s.sample.w[0:3] = self.box()
+        s.sample.bc[0:3] = self.bc
         if self.geometry == "clusters":
             if len(self.layers) != 2:
                 raise ValueError("a cluster sample needs two materials (matrix, cluster)")
@@ -128,10 +116,8 @@ class SimSpec:
         s.ion.m = self.m
         s.ion.E = self.E
         s.ion.Ef = self.Ef
-        p = self.start()
-        for i in range(3):
-            s.ion.dir[i] = self.dir[i]
-            s.ion.pos[i] = p[i]
+        s.ion.dir[0:3] = self.dir
+        s.ion.pos[0:3] = self.start()
         s.n_primaries = self.n_primaries
         s.first_primary = self.first_primary
         s.tally_mode = {"vaccount": F.TALLY_VACCOUNT, "range": F.TALLY_RANGE,
@@ -147,11 +133,117 @@ class SimSpec:
         s.hist_lateral_n = self.hist_lateral_n
         s.hist_evac_rows = self.hist_evac_rows
         s.potential = POTENTIALS[self.potential]
-        for i in range(3):
-            s.voxel_n[i] = self.voxel_n[i]
-            s.voxel_origin[i] = self.voxel_origin[i]
-            s.voxel_size[i] = self.voxel_size[i]
+        s.voxel_n[0:3] = self.voxel_n
+        s.voxel_origin[0:3] = self.voxel_origin
+        s.voxel_size[0:3] = self.voxel_size
         return s
+
+
+# mtg_material structs by value: batches of many simulations reuse a few materials
+_MATERIALS: dict = {}
+_MAT_BYTES: dict = {}
+
+
+class _SampleRow(C.Structure):
+    # mtg_sample with the cluster pointer as an integer (a numpy dtype needs that)
+    _fields_ = [(n, C.c_uint64 if n == "clusters" else t) for n, t in F.Sample._fields_]
+
+
+class _SimRow(C.Structure):
+    _fields_ = [(n, _SampleRow if n == "sample" else t) for n, t in F.Sim._fields_]
+
+
+_SIM_DTYPE = np.dtype(_SimRow)
+assert _SIM_DTYPE.itemsize == C.sizeof(F.Sim)
+_NO_MATERIAL = bytes(C.sizeof(F.Material))
+_TALLY_MODES = {"vaccount": F.TALLY_VACCOUNT, "range": F.TALLY_RANGE, "primaries": F.TALLY_PRIMARIES}
+
+
+def sims_to_array(sims: Sequence["SimSpec"]):
+    """The mtg_sim array of a run as a numpy structured array with the same bytes
+    as SimSpec.to_c() of each simulation, filled column by column (a batch of
+    thousands of simulations converts in milliseconds).  Returns the array and the
+    objects that must outlive the call reading it (cluster lists)."""
+    n = len(sims)
+    a = np.zeros(n, _SIM_DTYPE)
+    keep = []
+    mats = []
+    thick = np.zeros((n, F.MAX_LAYERS))
+    for k, s in enumerate(sims):
+        nl = len(s.layers)
+        if not 1 <= nl <= F.MAX_LAYERS:
+            raise ValueError("1 to 8 layers")
+        for i, l in enumerate(s.layers):
+            thick[k, i] = l.thickness
+            mats.append(_material_bytes(l))
+        mats.append(_NO_MATERIAL * (F.MAX_LAYERS - nl))
+        if s.geometry == "clusters":
+            if nl != 2:
+                raise ValueError("a cluster sample needs two materials (matrix, cluster)")
+            cl = np.ascontiguousarray(s.clusters if s.clusters is not None else np.zeros((0, 4)),
+                                      dtype=np.float64).reshape(-1, 4)
+            keep.append(cl)
+            a["sample"]["geometry"][k] = F.GEOM_CLUSTERS
+            a["sample"]["cluster_hash"][k] = [int(v) for v in s.cluster_hash]
+            a["sample"]["n_clusters"][k] = len(cl)
+            a["sample"]["clusters"][k] = cl.ctypes.data
+        elif s.geometry != "layers":
+            raise ValueError("geometry is 'layers' or 'clusters'")
+    smp = a["sample"]
+    smp["n_layers"] = [len(s.layers) for s in sims]
+    smp["thickness"] = thick
+    smp["material"] = np.frombuffer(b"".join(mats), dtype=smp.dtype["material"].base).reshape(n, F.MAX_LAYERS)
+    smp["w"] = [s.box() for s in sims]
+    smp["bc"] = [s.bc for s in sims]
+    ion = a["ion"]
+    ion["Z"] = [s.Z for s in sims]
+    ion["m"] = [s.m for s in sims]
+    ion["E"] = [s.E for s in sims]
+    ion["Ef"] = [s.Ef for s in sims]
+    ion["dir"] = [s.dir for s in sims]
+    ion["pos"] = [s.start() for s in sims]
+    a["n_primaries"] = [s.n_primaries for s in sims]
+    a["first_primary"] = [s.first_primary for s in sims]
+    a["tally_mode"] = [_TALLY_MODES[s.mode] for s in sims]
+    a["max_generation"] = [s.max_generation for s in sims]
+    a["primaries_only"] = [int(s.primaries_only) for s in sims]
+    for f in ("hist_range_bin", "hist_range_n", "hist_vac_bin", "hist_vac_n", "surface_binding",
+              "hist_lateral_bin", "hist_lateral_n", "hist_evac_rows", "voxel_n", "voxel_origin", "voxel_size"):
+        a[f] = [getattr(s, f) for s in sims]
+    a["potential"] = [POTENTIALS[s.potential] for s in sims]
+    return a, keep
+
+
+def _material_bytes(l: "LayerSpec") -> bytes:
+    key = (l.rho, tuple((e.Z, e.m, e.t, e.Edisp, e.Elbind) for e in l.elements))
+    b = _MAT_BYTES.get(key)
+    if b is None:
+        b = bytes(_c_material(l))
+        if len(_MAT_BYTES) > 4096:
+            _MAT_BYTES.clear()
+        _MAT_BYTES[key] = b
+    return b
+
+
+def _c_material(l: "LayerSpec") -> F.Material:
+    if not 1 <= len(l.elements) <= F.MAX_ELEMENTS:
+        raise ValueError("1 to 4 elements per layer")
+    key = (l.rho, tuple((e.Z, e.m, e.t, e.Edisp, e.Elbind) for e in l.elements))
+    mat = _MATERIALS.get(key)
+    if mat is None:
+        mat = F.Material()
+        mat.rho = l.rho
+        mat.n_elements = len(l.elements)
+        for j, e in enumerate(l.elements):
+            mat.elements[j].Z = e.Z
+            mat.elements[j].m = e.m
+            mat.elements[j].t = e.t
+            mat.elements[j].Edisp = e.Edisp
+            mat.elements[j].Elbind = e.Elbind
+        if len(_MATERIALS) > 4096:
+            _MATERIALS.clear()
+        _MATERIALS[key] = mat
+    return mat
 
 
 def summarize(t: dict) -> dict:
@@ -237,11 +329,10 @@ class Engine:
 
     # ---- runs
     def prepare(self, sims: Sequence[SimSpec]):
-        cs = [s.to_c() for s in sims]
-        arr = (F.Sim * len(sims))(*cs)
+        arr, keep = sims_to_array(sims)
         self._sims = list(sims)
-        self._check(self.lib.mtg_prepare(self.ctx, arr, len(sims)))
-        del cs  # held until here: cluster arrays are read during mtg_prepare
+        self._check(self.lib.mtg_prepare(self.ctx, arr.ctypes.data_as(C.POINTER(F.Sim)), len(sims)))
+        del keep  # held until here: cluster arrays are read during mtg_prepare
 
     def launch(self, stream: Optional[int] = None):
         self._check(self.lib.mtg_launch_async(self.ctx, C.c_void_p(stream or 0)))
@@ -256,10 +347,12 @@ class Engine:
             self._check(st)
         out = []
         off = 0
+        rows = np.ctypeslib.as_array(tot).tolist()
+        names = F.Totals.field_names()
+        h = np.frombuffer(hist, dtype=np.int64, count=max(nh, 1))
         for i, s in enumerate(self._sims):
-            d = tot[i].as_dict()
+            d = dict(zip(names, rows[i]))
             hr, hv, hp, hl, he = s.hist_sizes()
-            h = np.frombuffer(hist, dtype=np.int64, count=max(nh, 1))
             d["hist_range"] = h[off:off + hr].copy()
             d["hist_vac"] = h[off + hr:off + hr + hv].copy()
             d["hist_repl"] = h[off + hr + hv:off + hr + hv + hp].copy()
