@@ -168,7 +168,7 @@ def run_reference(a):
     from mytrim_gb300 import workloads as W
     oracle_io.build(None)
     reference = have_reference_build()
-    per_core = a.cpu_per_core or 48
+    per_core = a.cpu_per_core or 96
     sim = make_sim(a.workload, 1)
     rates = []
     cores = os.cpu_count() or 1
@@ -415,7 +415,7 @@ def main():
     }
     if not a.no_cpu and world == 1:
         cores = os.cpu_count() or 1
-        per_core = a.cpu_per_core or 100
+        per_core = a.cpu_per_core or 600
         reference = have_reference_build()
         r, wall, cores = cpu_sample(make_sim(a.workload, 1), per_core, seed=7, reference=reference)
         line["cpu_baseline"] = {"value": r["primaries"] / wall, "unit": UNIT, "cores": cores,
