@@ -52,6 +52,8 @@ WORKLOADS = {
     "as50k_sio2_si": ("As 50 keV at 7 deg into 10 nm SiO2 on Si, full cascade", "arsenic_implant"),
     "au1m_agcusi": ("Au 1 MeV into 50 nm Ag / 200 nm Cu / Si, full cascade, sputter counting (E_surf 3 eV), "
                     "256^3 energy-deposition voxels over 300 x 100 x 100 nm", "gold_deposition"),
+    "xe30k_uo2_bubbles": ("Xe 30 keV into UO2 with 200 solid-Xe bubbles of 1.5 nm radius in a periodic 40 nm box "
+                          "(sampleClusters geometry), full cascade", "xenon_bubbles"),
     "batched4096": ("4096 independent simulations in one launch (Z1 1-83, E0 1 keV-1 MeV log-uniform, 0-60 deg, "
                     "1-4 layers of Si/Cu/Ag/Au/SiO2/Al2O3 5-500 nm over Si); primaries per simulation "
                     "log-uniform 1e2-1e5 scaled so that one step holds about the batch size", "batched_uneven"),
@@ -86,6 +88,9 @@ def args_parse():
     p.add_argument("--precision", default="auto", choices=["auto", "fp32", "surrogate", "fp64"])
     p.add_argument("--fp64-batch", type=int, default=8192)
     p.add_argument("--cpu-per-core", type=int, default=0, help="primaries per core in the CPU sample")
+    p.add_argument("--events", default="", help="log these event kinds in every step (comma list of "
+                   "vacancy, replacement, branch, dissipate, rest, lost) and report their rate")
+    p.add_argument("--event-capacity", type=int, default=1 << 26)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--workload", default="ag200k_si", choices=sorted(WORKLOADS),
@@ -240,6 +245,13 @@ def main():
         eng.configure(precision="surrogate", seed=20261203)
     stream = torch.cuda.Stream(device=local)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
+    ev_kinds = [k for k in a.events.split(",") if k]
+    if ev_kinds:
+        from mytrim_gb300 import _ffi as F
+        names = {"vacancy": F.EV_VACANCY, "replacement": F.EV_REPLACEMENT, "branch": F.EV_BRANCH,
+                 "dissipate": F.EV_DISSIPATE, "rest": F.EV_REST, "lost": F.EV_LOST}
+        eng.set_event_log([names[k] for k in ev_kinds], a.event_capacity)
+    n_events = []
 
     def sims_for(step):
         return make_sims(a.workload, a.batch, (step * world + rank) * a.batch)
@@ -276,6 +288,8 @@ def main():
             colls += r["collisions"]
             prims += r["primaries"]
             results.append(r)
+            if ev_kinds:
+                n_events.append(eng.event_count())
     torch.cuda.synchronize()
     clocks = clk.summary()
     total = sum(times)
@@ -387,7 +401,8 @@ def main():
     achieved = per_launch_coll * W_COLL / (kms / 1e3) / 1e12
     traffic = None
     prof = ROOT / "profiles" / "cascade_fp32_agsi.md"
-    if prof.exists():
+    # the captured figure belongs to the FP32 kernel on the default workload
+    if prof.exists() and a.workload == "ag200k_si" and prec == "fp32" and not ev_kinds:
         for line in prof.read_text().splitlines():
             if line.startswith("dram_bytes_per_collision:"):
                 traffic = float(line.split(":")[1]) * per_launch_coll
@@ -413,6 +428,10 @@ def main():
                      "kernel_ms": kms,
                      "hbm": hbm_line(traffic, kms)},
     }
+    if ev_kinds:
+        line["events"] = {"kinds": ev_kinds, "capacity": a.event_capacity,
+                          "per_step": statistics.mean(n_events), "per_s": sum(n_events) / total,
+                          "overflowed": any(n > a.event_capacity for n in n_events)}
     if not a.no_cpu and world == 1:
         cores = os.cpu_count() or 1
         per_core = a.cpu_per_core or 600

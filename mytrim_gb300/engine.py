@@ -410,6 +410,12 @@ class Engine:
         self._check(self.lib.mtg_set_event_log(self.ctx, mask, capacity))
         self._event_cap = capacity if mask else 0
 
+    def event_count(self) -> int:
+        """Events the last run logged (may exceed the log's capacity)."""
+        n, total = C.c_longlong(0), C.c_longlong(0)
+        self._check(self.lib.mtg_get_events(self.ctx, None, 0, C.byref(n), C.byref(total)))
+        return total.value
+
     def events(self) -> np.ndarray:
         """The last run's event records as a structured array (unordered)."""
         cap = getattr(self, "_event_cap", 0)

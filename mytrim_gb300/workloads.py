@@ -3,6 +3,7 @@
 Masses are the SRIM "MAI weight" column of the stopping tables for the ions and
 the natural weights for targets; densities are the ones the workload names.
 """
+import functools
 import math
 
 import numpy as np
@@ -63,6 +64,40 @@ def gold_deposition(n_primaries=100_000_000, voxels=256):
                    hist_range_bin=10.0, hist_range_n=300, hist_vac_bin=10.0, hist_vac_n=300,
                    surface_binding=3.0, voxel_n=(voxels, voxels, voxels), voxel_origin=(0.0, -500.0, -500.0),
                    voxel_size=(3000.0, 1000.0, 1000.0))
+
+
+def xenon_bubbles(n_primaries=1_000_000, n_bubbles=200, radius=15.0, box=400.0, seed=3):
+    """Xe 30 keV into UO2 (10.97 g/cm3; Edisp U 40, O 20 eV) holding n_bubbles solid-Xe
+    bubbles (3.5 g/cm3) of `radius` in a periodic box of edge `box` (sampleClusters,
+    spatial hash of 19^3 cells): the cluster-geometry workload, full cascade.  Bubble
+    centres are placed at random with at least 5 A between surfaces (the placement
+    rule of sampleClusters::addRandomClusters, sample_clusters.C:228-250)."""
+    cl = _bubbles(n_bubbles, radius, box, seed)
+    uo2 = LayerSpec(box, 10.97, [ElementSpec(92, 238.03, 1.0, 40.0, 3.0), ElementSpec(8, O, 2.0, 20.0, 3.0)])
+    xe = LayerSpec(box, 3.5, [ElementSpec(54, 131.29, 1.0, 25.0, 3.0)])
+    return SimSpec(layers=[uo2, xe], Z=54, m=131.29, E=30e3, n_primaries=n_primaries,
+                   pos=(0.0, box / 2, box / 2), size=(box, box, box), geometry="clusters",
+                   clusters=cl, cluster_hash=(19, 19, 19), hist_range_bin=10.0, hist_range_n=200)
+
+
+@functools.lru_cache(maxsize=8)
+def _bubbles(n, radius, box, seed):
+    rng = np.random.default_rng(seed)
+    cl = []
+    while len(cl) < n:
+        q = rng.uniform(0.0, box, 3)
+        ok = True
+        for c in cl:
+            d = q - c[:3]
+            d -= np.round(d / box) * box
+            if d @ d < (2 * radius + 5.0) ** 2:
+                ok = False
+                break
+        if ok:
+            cl.append(np.array([q[0], q[1], q[2], radius]))
+    out = np.array(cl)
+    out.setflags(write=False)
+    return out
 
 
 # targets of the batched workload: (name, rho, [(Z, mass, fraction, Edisp)])
