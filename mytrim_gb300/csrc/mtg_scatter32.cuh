@@ -10,42 +10,49 @@
 // universal and Moliere potentials; for C-Kr the reference writes c_i that are
 // not the derivative's, and they are kept as written.  The Moliere terms
 // exp(-0.3 r)^4 and exp(-0.3 r)^20 are evaluated as exp(-1.2 r) and exp(-6 r).
+// v and v1 are formed once, after the loop, from the last iterate's values.
 #pragma once
 
 namespace mtg
 {
 
+// phi(r) and sum_i c_i exp(-k_i r) with each weighted exponential as one 2^x:
+// w_i exp(-k_i r) = 2^(r (-k_i log2 e) + log2 w_i), and the derivative sum written on
+// the weighted terms (coefficient c_i / w_i).  Constants from the coefficients of
+// trim.C:197-222 in double precision.
 template <int POT>
 __device__ __forceinline__ void
 screening32(float r, float & phi, float & tk)
 {
   if constexpr (POT == 1)
   {
-    // Moliere (trim.C:206-213)
-    const float e1 = __expf(-0.3f * r);
-    const float e2 = __expf(-1.2f * r);
-    const float e3 = __expf(-6.0f * r);
-    phi = 0.35f * e1 + 0.55f * e2 + 0.1f * e3;
-    tk = 0.105f * e1 + 0.66f * e2 + 0.6f * e3;
+    // Moliere (trim.C:206-213): w = 0.35, 0.55, 0.1; k = 0.3, 1.2, 6; c / w = k
+    const float e1 = exp2f(fmaf(r, -0.432808512f, -1.51457317f));
+    const float e2 = exp2f(fmaf(r, -1.73123405f, -0.862496476f));
+    const float e3 = exp2f(fmaf(r, -8.65617025f, -3.32192809f));
+    phi = e1 + e2 + e3;
+    tk = 0.3f * e1 + 1.2f * e2 + 6.0f * e3;
   }
   else if constexpr (POT == 2)
   {
-    // C-Kr (trim.C:215-222)
-    const float e1 = __expf(-0.279f * r);
-    const float e2 = __expf(-0.637f * r);
-    const float e3 = __expf(-1.1919f * r);
-    phi = 0.191f * e1 + 0.474f * e2 + 0.335f * e3;
-    tk = 0.531865f * e1 + 0.30181f * e2 + 0.6437f * e3;
+    // C-Kr (trim.C:215-222): w = 0.191, 0.474, 0.335; k = 0.279, 0.637, 1.1919; the
+    // reference's c = 0.531865, 0.30181, 0.6437 give c / w = 2.7846335, 0.63672996,
+    // 1.9214925
+    const float e1 = exp2f(fmaf(r, -0.402511916f, -2.38835546f));
+    const float e2 = exp2f(fmaf(r, -0.918996741f, -1.07704104f));
+    const float e3 = exp2f(fmaf(r, -1.71954822f, -1.57776700f));
+    phi = e1 + e2 + e3;
+    tk = 2.7846335f * e1 + 0.63672996f * e2 + 1.9214925f * e3;
   }
   else
   {
     // universal (trim.C:197-204)
-    const float ex1 = 0.18175f * __expf(-3.1998f * r);
-    const float ex2 = 0.50986f * __expf(-0.94229f * r);
-    const float ex3 = 0.28022f * __expf(-0.4029f * r);
-    const float ex4 = 0.028171f * __expf(-0.20162f * r);
-    phi = ex1 + ex2 + ex3 + ex4;
-    tk = 3.1998f * ex1 + 0.94229f * ex2 + 0.4029f * ex3 + 0.20162f * ex4;
+    const float e1 = exp2f(fmaf(r, -4.61633559f, -2.45997273f));
+    const float e2 = exp2f(fmaf(r, -1.35943711f, -0.971826936f));
+    const float e3 = exp2f(fmaf(r, -0.581261832f, -1.83536817f));
+    const float e4 = exp2f(fmaf(r, -0.290876174f, -5.14964541f));
+    phi = e1 + e2 + e3 + e4;
+    tk = 3.1998f * e1 + 0.94229f * e2 + 0.4029f * e3 + 0.20162f * e4;
   }
 }
 
@@ -93,15 +100,12 @@ scatter32_pot(float eps, float b, float & s2, float & c2, int & niter)
   }
   float d = r - b;
   const float inv_eps = 1.0f / eps;
-  float v, v1, q;
+  float phi, tk, ir, q;
   do
   {
     r = b + d;
-    float phi, tk;
     screening32<POT>(r, phi, tk);
-    const float ir = 1.0f / r;
-    v = phi * ir;
-    v1 = -(v + tk) * ir;
+    ir = 1.0f / r;
     // f(r) = b^2/r + v r/eps - r and f'(r), written in d = r - b
     const float fr = -d * (2.0f * b + d) * ir + phi * inv_eps;
     const float br = b * ir;
@@ -110,6 +114,9 @@ scatter32_pot(float eps, float b, float & s2, float & c2, int & niter)
     d -= q;
     ++niter;
   } while (fabsf(q) > 0.001f * fabsf(b + d) && niter < 100);
+  // v and v1 at the last iterate's r, as the reference uses them (trim.C:235)
+  const float v = phi * ir;
+  const float v1 = -(v + tk) * ir;
   r = b + d;
   using M = Magic32<POT>;
   const float roc = -2.0f * (eps - v) / v1;
