@@ -326,7 +326,10 @@ typedef struct
   double m;                /* mass [u] of the atom the event describes */
   unsigned long long key;  /* path key of the member that raised the event */
   long long primary;       /* primary index within its simulation (first_primary based) */
-  int sim, kind, Z, gen, state, pad;
+  int sim, kind, Z, gen, state;
+  int tag;                 /* IonBase::_tag of the atom: for a followed recoil created inside a
+                              cluster of a sampleClusters sample, that cluster's index
+                              (trim.C:365, sample_clusters.C:53); -1 otherwise */
 } mtg_event;
 
 /* Log events of the kinds whose bit (1 << kind) is set in kind_mask (0 disables)

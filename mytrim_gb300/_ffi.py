@@ -99,7 +99,7 @@ class MemberRecord(C.Structure):
 class Event(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("x", "y", "z", "E", "aux", "m")] + \
                [("key", C.c_ulonglong), ("primary", C.c_longlong)] + \
-               [(n, C.c_int) for n in ("sim", "kind", "Z", "gen", "state", "pad")]
+               [(n, C.c_int) for n in ("sim", "kind", "Z", "gen", "state", "tag")]
 
 
 # event kinds (mtg_event_kind)

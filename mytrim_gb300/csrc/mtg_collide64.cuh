@@ -38,6 +38,7 @@ struct P64
   int gen;       // 0 for the primary
   int sim;       // simulation index
   uint32_t prim; // global primary index (tally slot)
+  int tag;       // IonBase::_tag: cluster index where a followed recoil was created, else -1
 };
 
 // proton electronic stopping in one element (material.C:134-158)
@@ -238,6 +239,7 @@ collide64(P64 & p, uint32_t ic, double r1, const SimDesc & sim, const SpeciesCon
   // which material: SampleLayers::lookupLayer (sample_layers.C:27-43) or
   // sampleClusters::lookupMaterial (sample_clusters.C:42-53)
   int mat_index;
+  int mat_tag = -1; // the material's _tag (sampleClusters sets material[1]->_tag = l)
   if (EXT && sim.geometry == 1)
   {
     const double pos[3] = {p.x, p.y, p.z};
@@ -246,6 +248,7 @@ collide64(P64 & p, uint32_t ic, double r1, const SimDesc & sim, const SpeciesCon
     if (l == -2)
       return CF_DONE | CF_VOID; // no material: the member is dropped (trim.C:81-83)
     mat_index = l >= 0 ? 1 : 0;
+    mat_tag = l >= 0 ? l : -1;
   }
   else
   {
@@ -322,6 +325,7 @@ collide64(P64 & p, uint32_t ic, double r1, const SimDesc & sim, const SpeciesCon
   rec.dz = p.dz * p1;
   rec.E = den - el.Elbind;
   rec.species = el.rspecies;
+  rec.tag = -1; // a new IonBase (ion.C:26)
 
   // random unit vector perpendicular to dir by unit-ball rejection (trim.C:322-333)
   double px, py, pz, nrm;
@@ -390,6 +394,7 @@ collide64(P64 & p, uint32_t ic, double r1, const SimDesc & sim, const SpeciesCon
       rec.dy *= s;
       rec.dz *= s;
       rec.key = child_key(p.key, ic);
+      rec.tag = mat_tag; // trim.C:365, after followRecoil's output
       flags |= CF_PUSH;
     }
     else

@@ -271,7 +271,7 @@ struct LaneSink
 
   // ---- event log (opt-in): one entry per selected hook call
   __device__ void event(int kind, Real x, Real y, Real z, Real E, int Z, Real m, int gen, int state, Real aux,
-                        uint64_t key)
+                        uint64_t key, int tag)
   {
     if (!(prm->event_mask & (1u << kind)))
       return;
@@ -295,7 +295,7 @@ struct LaneSink
     r.m = double(m);
     r.gen = gen;
     r.state = state;
-    r.pad = 0;
+    r.tag = tag;
   }
   // followRecoil (trim.C:362): a displaced recoil, followed or not
   template <class R, class E>
@@ -303,7 +303,7 @@ struct LaneSink
   {
     if constexpr (EV)
       event(EV_BRANCH, Real(rec.x), Real(rec.y), Real(rec.z), Real(rec.E), el.Z2, Real(el.m2), rec.gen, 0,
-            Real(el.Elbind), key);
+            Real(el.Elbind), key, rec.tag);
   }
   // dissipateRecoilEnergy (trim.C:397-401): a recoil below the displacement energy
   template <class R, class E>
@@ -311,7 +311,7 @@ struct LaneSink
   {
     if constexpr (EV)
       event(EV_DISSIPATE, Real(rec.x), Real(rec.y), Real(rec.z), Erec, el.Z2, Real(el.m2), rec.gen, 0,
-            Real(el.Elbind), key);
+            Real(el.Elbind), key, rec.tag);
   }
 
   // ---- events raised by the collision code (the reference's hooks, trim.h:72-84)
@@ -381,7 +381,7 @@ struct LaneSink
   {
     LaneCold<Acc> & c = *cold;
     if constexpr (EV)
-      event(EV_LOST, Real(p.x), Real(p.y), Real(p.z), Real(p.E), Z1, m1, p.gen, ST_LOST, e - Real(p.E), p.key);
+      event(EV_LOST, Real(p.x), Real(p.y), Real(p.z), Real(p.E), Z1, m1, p.gen, ST_LOST, e - Real(p.E), p.key, p.tag);
     ++c.n_lost;
     c.e_lost.add(e);
     if (MID && prm->records)
@@ -403,7 +403,7 @@ struct LaneSink
   {
     if constexpr (EV)
       event(EV_VACANCY, Real(rec.x), Real(rec.y), Real(rec.z), Erec, el.Z2, Real(el.m2), rec.gen, 0,
-            Real(el.Elbind), key);
+            Real(el.Elbind), key, rec.tag);
     if (MID && range_mode == 2)
     {
       // TrimPrimaries::vacancyCreation (trim.C:446-464): one vacancy per displaced
@@ -474,7 +474,7 @@ struct LaneSink
   {
     if constexpr (EV)
       event(EV_REPLACEMENT, Real(rec.x), Real(rec.y), Real(rec.z), Erec, el.Z2, Real(el.m2), rec.gen, 0,
-            Real(el.Elbind), key);
+            Real(el.Elbind), key, rec.tag);
     ++cold->n_repl;
     const int b = depth_bin(Real(rec.x), inv_vac_bin(), sim->hist_vac_n);
     if (b >= 0)
@@ -486,7 +486,7 @@ struct LaneSink
   __device__ void stop(int state, const P & p, int Z1, Real m1)
   {
     if constexpr (EV)
-      event(EV_REST, Real(p.x), Real(p.y), Real(p.z), Real(p.E), Z1, m1, p.gen, state, Real(0), p.key);
+      event(EV_REST, Real(p.x), Real(p.y), Real(p.z), Real(p.E), Z1, m1, p.gen, state, Real(0), p.key, p.tag);
     if (MID && prm->records)
       cold->m_state = state;
     a_enuc.add(Real(p.E));

@@ -50,6 +50,7 @@ struct P32
   int gen;
   int sim;
   uint32_t prim;
+  int tag; // IonBase::_tag: cluster index where a followed recoil was created, else -1
 };
 
 struct Tables32
@@ -195,6 +196,7 @@ struct Fp32Policy
     p.gen = 0;
     p.sim = si;
     p.prim = uint32_t(g);
+    p.tag = -1;
     return p;
   }
 
@@ -207,6 +209,7 @@ struct Fp32Policy
     float ls, dee; // flight length and electronic loss
     uint32_t azimuth;
     bool gone;     // outside the sample: no collision, the member is dropped
+    int tag;       // the material's _tag: the cluster index inside a cluster, else -1
   };
 
   // flight, target atom and electronic loss (trim.C:80-170)
@@ -220,6 +223,7 @@ struct Fp32Policy
     // (sample_clusters.C:42-53)
     int k;
     a.gone = false;
+    a.tag = -1;
     if (EXT && sim.geometry == 1)
     {
       const float pos[3] = {p.x, p.y, p.z};
@@ -227,6 +231,7 @@ struct Fp32Policy
                                           sim.cl_head, sim.n_clusters);
       a.gone = l == -2; // no material: the member is dropped (trim.C:81-83)
       k = l >= 0 ? 1 : 0;
+      a.tag = l >= 0 ? l : -1; // sampleClusters::lookupMaterial sets material[1]->_tag = l
     }
     else
     {
@@ -363,6 +368,7 @@ struct Fp32Policy
     rec.E = recE;
     rec.El = 0.0f;
     rec.species = el.rspecies;
+    rec.tag = -1; // a new IonBase (ion.C:26)
 
     // azimuth around the flight direction: orthonormal basis by Duff et al.,
     // "Building an Orthonormal Basis, Revisited" (JCGT 2017)
@@ -417,6 +423,7 @@ struct Fp32Policy
         rec.dy *= s;
         rec.dz *= s;
         rec.key = child_key(p.key, ic);
+        rec.tag = a.tag; // trim.C:365, after followRecoil's output
         flags |= CF_PUSH;
       }
       else

@@ -78,6 +78,7 @@ struct Fp64Policy
     p.gen = 0;
     p.sim = si;
     p.prim = uint32_t(g);
+    p.tag = -1;
     return p;
   }
 

@@ -169,7 +169,7 @@ struct EventRec
   double x, y, z, E, aux, m;
   uint64_t key;
   long long primary;
-  int sim, kind, Z, gen, state, pad;
+  int sim, kind, Z, gen, state, tag;
 };
 
 // event kinds (bit k of the log's mask selects kind k)

@@ -421,7 +421,7 @@ class Engine:
         cap = getattr(self, "_event_cap", 0)
         dt = np.dtype([("x", "<f8"), ("y", "<f8"), ("z", "<f8"), ("E", "<f8"), ("aux", "<f8"), ("m", "<f8"), ("key", "<u8"),
                        ("primary", "<i8"), ("sim", "<i4"), ("kind", "<i4"), ("Z", "<i4"), ("gen", "<i4"),
-                       ("state", "<i4"), ("pad", "<i4")])
+                       ("state", "<i4"), ("tag", "<i4")])
         assert dt.itemsize == C.sizeof(F.Event)
         out = np.zeros(max(cap, 1), dtype=dt)
         n, total = C.c_longlong(0), C.c_longlong(0)

@@ -11,9 +11,10 @@ the engine's event log (``Engine.set_event_log`` / ``Engine.events``).
 
 ``<ion>`` is IonBase's stream form (ion.C:74-79): x y z Z m E id gen tag, numbers as
 std::ostream prints them (six significant digits).  The engine has no sequential
-ion ids and no cluster tags: the member's path key stands in for the id (of the
-member that raised the event) and the tag is -1.  The GPU writes events in no
-particular order; the lines are sorted by simulation, primary, path key and kind.
+ion ids: the member's path key stands in for the id (of the member that raised the
+event).  The tag is IonBase::_tag: the index of the cluster a followed recoil was
+created in (sampleClusters), else -1.  The GPU writes events in no particular
+order; the lines are sorted by simulation, primary, path key and kind.
 """
 from typing import Iterable, TextIO
 
@@ -30,7 +31,7 @@ def _g(v: float) -> str:
 
 def _ion(e) -> str:
     return (f"{_g(e['x'])} {_g(e['y'])} {_g(e['z'])} {int(e['Z'])} {_g(e['m'])} {_g(e['E'])} "
-            f"{int(e['key'])} {int(e['gen'])} -1 ")
+            f"{int(e['key'])} {int(e['gen'])} {int(e['tag'])} ")
 
 
 def _sorted(events: np.ndarray) -> np.ndarray:

@@ -283,6 +283,7 @@ main(int argc, char ** argv)
     p.gen = 0;
     p.sim = 0;
     p.prim = uint32_t(n);
+    p.tag = -1;
     stack.push_back(p);
     while (!stack.empty())
     {

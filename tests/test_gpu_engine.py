@@ -528,3 +528,41 @@ def test_event_streams(engine_lib):
     p = list(streams.phonon_log(ev))
     assert all(len(l.split()) == 10 for l in p)
     assert sum(float(l.split()[0]) for l in p) == pytest.approx(t["Enuc"], rel=1e-4)  # 6-digit text
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_event_tags_name_the_cluster_of_birth(engine_lib, prec):
+    """IonBase::_tag in the event log: a followed recoil created inside a cluster of a
+    sampleClusters sample carries that cluster's index (trim.C:365 with
+    sample_clusters.C:53), one created in the matrix -1; in a layered sample every
+    tag is -1."""
+    sim = SimSpec(**{**CASES["xe_uo2_clusters"][0].__dict__, "n_primaries": 300})
+    e = Engine(precision=prec, seed=23)
+    e.set_event_log([F.EV_VACANCY, F.EV_REST], 5_000_000)
+    e.run([sim])
+    ev = e.events()
+    e.close()
+    cl = np.asarray(sim.clusters)
+    box = np.asarray(sim.size)
+    vac = ev[ev["kind"] == F.EV_VACANCY]
+    pos = np.stack([vac["x"], vac["y"], vac["z"]], axis=1)
+    inside = vac["tag"] >= 0
+    assert inside.any() and (~inside).any()
+    # a tagged vacancy lies in its cluster (periodic images), an untagged one in none
+    d = pos[inside] - cl[vac["tag"][inside], :3]
+    d -= np.round(d / box) * box
+    r = cl[vac["tag"][inside], 3]
+    assert np.all(np.sqrt((d * d).sum(axis=1)) <= r * (1 + 1e-5) + 1e-3)
+    for q in pos[~inside][:2000]:
+        dd = q - cl[:, :3]
+        dd -= np.round(dd / box) * box
+        assert np.all(np.sqrt((dd * dd).sum(axis=1)) >= cl[:, 3] * (1 - 1e-5) - 1e-3)
+    rest = ev[ev["kind"] == F.EV_REST]
+    assert (rest["tag"] >= 0).any() and (rest["tag"] < len(cl)).all()
+    # layered sample: no tags
+    e = Engine(precision=prec, seed=23)
+    e.set_event_log([F.EV_VACANCY, F.EV_REST], 5_000_000)
+    e.run([_cu_sim(n=20)])
+    ev = e.events()
+    e.close()
+    assert (ev["tag"] == -1).all()

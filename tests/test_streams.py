@@ -13,22 +13,22 @@ from mytrim_gb300 import streams
 
 DT = np.dtype([("x", "<f8"), ("y", "<f8"), ("z", "<f8"), ("E", "<f8"), ("aux", "<f8"), ("m", "<f8"), ("key", "<u8"),
                ("primary", "<i8"), ("sim", "<i4"), ("kind", "<i4"), ("Z", "<i4"), ("gen", "<i4"), ("state", "<i4"),
-               ("pad", "<i4")])
+               ("tag", "<i4")])
 VALUES = [0.0, 1.0, 123.456789, 1e-7, 2.5e12, -3.25, 63.546, 99999.95, 1234567.0, 0.000123456789]
 
 
 def events():
     e = np.zeros(4, dtype=DT)
-    e[0] = (10.5, 50.0, 49.75, 24.0, 3.0, 63.546, 7, 0, 0, F.EV_VACANCY, 29, 1, 0, 0)
-    e[1] = (11.0, 50.1, 49.8, 2.5, 3.0, 63.546, 7, 0, 0, F.EV_DISSIPATE, 29, 1, 0, 0)
-    e[2] = (12.0, 50.2, 49.9, 1.25, 0.0, 63.546, 9, 0, 0, F.EV_REST, 29, 2, 3, 0)
-    e[3] = (13.0, 50.3, 50.0, 40.0, 3.0, 63.546, 9, 0, 0, F.EV_BRANCH, 29, 3, 0, 0)
+    e[0] = (10.5, 50.0, 49.75, 24.0, 3.0, 63.546, 7, 0, 0, F.EV_VACANCY, 29, 1, 0, 4)  # born in cluster 4
+    e[1] = (11.0, 50.1, 49.8, 2.5, 3.0, 63.546, 7, 0, 0, F.EV_DISSIPATE, 29, 1, 0, -1)
+    e[2] = (12.0, 50.2, 49.9, 1.25, 0.0, 63.546, 9, 0, 0, F.EV_REST, 29, 2, 3, -1)
+    e[3] = (13.0, 50.3, 50.0, 40.0, 3.0, 63.546, 9, 0, 0, F.EV_BRANCH, 29, 3, 0, -1)
     return e
 
 
 def test_defect_and_phonon_lines():
     d = list(streams.defect_log(events()))
-    assert d == ["V 10.5 50 49.75 29 63.546 24 7 1 -1 ", "I 12 50.2 49.9 29 63.546 1.25 9 2 -1 "]
+    assert d == ["V 10.5 50 49.75 29 63.546 24 7 1 4 ", "I 12 50.2 49.9 29 63.546 1.25 9 2 -1 "]
     p = list(streams.phonon_log(events()))
     # sorted by primary, path key, then event kind (branch before rest)
     assert p == ["5.5 11 50.1 49.8 29 63.546 2.5 7 1 -1 ", "3 13 50.3 50 29 63.546 40 9 3 -1 ",
