@@ -4,6 +4,8 @@ the engine's event log (``Engine.set_event_log`` / ``Engine.events``).
 * ``defect_log`` -- TrimDefectLog (trim.C:467-483): "V <ion>" for every vacancy
   (the displaced recoil), "I", "S" or "R" <ion> for every member that came to rest
   as an interstitial, substitutional or replacement;
+* ``vac_map`` -- TrimVacMap (trim.C:484-501): the vacancy map of up to three target
+  species over the sample's (x, y) extent;
 * ``phonon_log`` -- TrimPhononOut (trim.C:504-527): "<E> <ion>" for every energy
   left in the lattice: the binding energy of each displaced recoil, the energy plus
   binding energy of each recoil below the displacement energy, the residual energy
@@ -60,6 +62,31 @@ def phonon_log(events: np.ndarray) -> Iterable[str]:
             yield f"{_g(e['E'] + e['aux'])} " + _ion(e)
         elif k == F.EV_REST:
             yield f"{_g(e['E'])} " + _ion(e)
+
+
+def vac_map(events: np.ndarray, w, z, mx: int = 20, my: int = 20) -> np.ndarray:
+    """TrimVacMap (trim.C:484-501) from events logged with kind EV_VACANCY: counts of
+    vacancies left by atoms of Z = z[0], z[1] (and z[2]) on an mx x my map of the
+    displaced recoil's (x, y) over the sample's extent w[0] x w[1], indices
+    int(x mx / w0) reduced modulo mx as the reference does (x -= int(x / mx) mx).
+    Returns an (mx, my, 3) integer array.  Positions below zero give negative
+    indices, which the reference writes out of its array's bounds; they are not
+    counted here."""
+    out = np.zeros((mx, my, 3), dtype=np.int64)
+    zs = list(z) + [-1] * (3 - len(z))
+    for e in events[events["kind"] == F.EV_VACANCY]:
+        x = int(e["x"] * mx / w[0])
+        y = int(e["y"] * my / w[1])
+        x -= int(x / mx) * mx
+        y -= int(y / my) * my
+        if x < 0 or y < 0:
+            continue
+        Z = int(e["Z"])
+        for k in range(3):
+            if Z == zs[k]:
+                out[x, y, k] += 1
+                break
+    return out
 
 
 def write(lines: Iterable[str], out: TextIO) -> int:

@@ -43,3 +43,17 @@ def test_number_format_is_ostreams(tmp_path):
     out = subprocess.run([str(exe)], input="\n".join(repr(v) for v in VALUES), capture_output=True, text=True,
                          check=True).stdout.split()
     assert out == ["%g" % v for v in VALUES]
+
+
+def test_vac_map_follows_trimvacmap():
+    e = np.zeros(6, dtype=DT)
+    # (x, y) over w = (100, 100) on a 20 x 20 map: cells int(x / 5), int(y / 5)
+    e[0] = (12.0, 3.0, 0.0, 10.0, 3.0, 69.7, 1, 0, 0, F.EV_VACANCY, 31, 1, 0, -1)
+    e[1] = (12.5, 4.9, 0.0, 10.0, 3.0, 69.7, 1, 0, 0, F.EV_VACANCY, 31, 1, 0, -1)
+    e[2] = (103.0, 3.0, 0.0, 10.0, 3.0, 74.9, 1, 0, 0, F.EV_VACANCY, 33, 1, 0, -1)   # x wraps: cell 0
+    e[3] = (-8.0, 3.0, 0.0, 10.0, 3.0, 74.9, 1, 0, 0, F.EV_VACANCY, 33, 1, 0, -1)    # int(-1.6) = -1: dropped
+    e[4] = (12.0, 3.0, 0.0, 10.0, 3.0, 69.7, 1, 0, 0, F.EV_REST, 31, 1, 3, -1)       # not a vacancy
+    e[5] = (-3.0, 3.0, 0.0, 10.0, 3.0, 74.9, 1, 0, 0, F.EV_VACANCY, 33, 1, 0, -1)    # int(-0.6) = 0: cell 0
+    m = streams.vac_map(e, (100.0, 100.0), (31, 33))
+    assert m.shape == (20, 20, 3)
+    assert m[2, 0, 0] == 2 and m[0, 0, 1] == 2 and m.sum() == 4
