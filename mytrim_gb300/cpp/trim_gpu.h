@@ -206,6 +206,26 @@ public:
                           int mode = MTG_TALLY_VACCOUNT, bool primaries_only = false,
                           long long first_primary = 0, int max_generation = 1)
   {
+    Job job{_sample, pka, n, mode, primaries_only, first_primary, max_generation};
+    return runBatch(std::vector<Job>{job}, seed)[0];
+  }
+
+  // One simulation of a batch: its own sample, ion template and primaries.
+  struct Job
+  {
+    SampleBase * sample;
+    IonBase * pka;
+    long long n;
+    int mode = MTG_TALLY_VACCOUNT;
+    bool primaries_only = false;
+    long long first_primary = 0;
+    int max_generation = 1;
+  };
+
+  // Several independent simulations in one launch (a parameter scan, many small
+  // targets); totals in job order, each added to the SimconfType counters.
+  std::vector<mtg_totals> runBatch(const std::vector<Job> & jobs, unsigned long long seed = 1)
+  {
     mtg_config cfg{};
     cfg.tmin = _simconf->tmin;
     cfg.tau = _simconf->tau;
@@ -214,28 +234,37 @@ public:
     cfg.precision = _precision;
     cfg.seed = seed;
     _ctx.check(mtg_configure(_ctx.get(), &cfg));
-    mtg_sim sim{};
-    std::vector<double> cluster_storage;
-    if (auto * layers = dynamic_cast<SampleLayers *>(_sample))
-      sim.sample = mtg::flatten_sample(*layers, &layers->layerThickness);
-    else if (dynamic_cast<SampleSolid *>(_sample))
-      sim.sample = mtg::flatten_sample(*_sample, nullptr);
-    else if (auto * clusters = dynamic_cast<sampleClusters *>(_sample))
-      sim.sample = mtg::flatten_clusters(*clusters, cluster_storage);
-    else
-      throw std::invalid_argument("TrimGPU supports SampleSolid, SampleLayers and sampleClusters");
-    sim.ion = mtg::flatten_ion(*pka);
-    sim.n_primaries = n;
-    sim.first_primary = first_primary;
-    sim.tally_mode = mode;
-    sim.primaries_only = primaries_only ? 1 : 0;
-    sim.max_generation = max_generation;
-    sim.potential = int(_potential); // TrimBase's public member (trim.h:63-69)
-    mtg_totals t{};
-    _ctx.check(mtg_run(_ctx.get(), &sim, 1, &t, nullptr));
-    _simconf->vacancies_created += int(t.vacancies);
-    _simconf->EelTotal += t.Eel;
-    _simconf->EnucTotal += t.Enuc;
+    std::vector<mtg_sim> sims(jobs.size());
+    std::vector<std::vector<double>> cluster_storage(jobs.size()); // read by mtg_run
+    for (size_t i = 0; i < jobs.size(); ++i)
+    {
+      const Job & j = jobs[i];
+      mtg_sim & sim = sims[i];
+      sim = mtg_sim{};
+      if (auto * layers = dynamic_cast<SampleLayers *>(j.sample))
+        sim.sample = mtg::flatten_sample(*layers, &layers->layerThickness);
+      else if (dynamic_cast<SampleSolid *>(j.sample))
+        sim.sample = mtg::flatten_sample(*j.sample, nullptr);
+      else if (auto * clusters = dynamic_cast<sampleClusters *>(j.sample))
+        sim.sample = mtg::flatten_clusters(*clusters, cluster_storage[i]);
+      else
+        throw std::invalid_argument("TrimGPU supports SampleSolid, SampleLayers and sampleClusters");
+      sim.ion = mtg::flatten_ion(*j.pka);
+      sim.n_primaries = j.n;
+      sim.first_primary = j.first_primary;
+      sim.tally_mode = j.mode;
+      sim.primaries_only = j.primaries_only ? 1 : 0;
+      sim.max_generation = j.max_generation;
+      sim.potential = int(_potential); // TrimBase's public member (trim.h:63-69)
+    }
+    std::vector<mtg_totals> t(jobs.size());
+    _ctx.check(mtg_run(_ctx.get(), sims.data(), int(sims.size()), t.data(), nullptr));
+    for (const mtg_totals & x : t)
+    {
+      _simconf->vacancies_created += int(x.vacancies);
+      _simconf->EelTotal += x.Eel;
+      _simconf->EnucTotal += x.Enuc;
+    }
     return t;
   }
 
