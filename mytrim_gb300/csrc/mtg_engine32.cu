@@ -113,7 +113,6 @@ struct Fp32Policy
     const Mat32 * mrow;
     const float * stop;
     float lnE_min, inv_dlnE;
-    float E; // unused
     const SurrogateNet * net;
   };
 
