@@ -85,7 +85,7 @@ struct mtg_ctx
   DevBuf d_species32, d_mats32, d_sims32;
   DevBuf d_sg_params, d_sg_net; // surrogate network
   DevBuf d_vox, d_vox_range, d_vox_sum; // energy-deposition voxels
-  DevBuf d_cl, d_cl32, d_cl_next, d_cl_head; // sampleClusters geometry
+  DevBuf d_cl, d_cl32, d_cl_next, d_cl_head, d_cl_mask; // sampleClusters geometry
   std::vector<SimDesc> sims_dev;             // SimDesc copies with device cluster pointers
   bool sg_ready = false;
   DevBuf p_vac, p_coll, p_eel, p_enuc, p_fx, p_fy, p_fz, p_state;
@@ -448,7 +448,7 @@ mtg_destroy(mtg_ctx * ctx)
                      &ctx->d_out,    &ctx->d_tmp0,     &ctx->d_tmp1,    &ctx->d_tmp2,    &ctx->d_tmp3,
                      &ctx->d_species32, &ctx->d_mats32, &ctx->d_sims32, &ctx->d_sg_params, &ctx->d_sg_net,
                      &ctx->d_vox,    &ctx->d_vox_range, &ctx->d_vox_sum, &ctx->d_cl,     &ctx->d_cl32,
-                     &ctx->d_cl_next, &ctx->d_cl_head};
+                     &ctx->d_cl_next, &ctx->d_cl_head, &ctx->d_cl_mask};
   for (DevBuf * b : bufs)
     if (b->p)
       cudaFree(b->p);
@@ -571,7 +571,11 @@ mtg_prepare(mtg_ctx * ctx, const mtg_sim * sims, int n_sims)
       CK(h2d(ctx, ctx->d_cl_next.p, t.cl_next.data(), sizeof(int) * t.cl_next.size()));
     }
     CK(h2d(ctx, ctx->d_cl_head.p, t.cl_head.data(), sizeof(int) * t.cl_head.size()));
-    patch_cluster_pointers(ctx->sims_dev, ptr<Cl4d>(ctx->d_cl), ptr<int>(ctx->d_cl_next), ptr<int>(ctx->d_cl_head));
+    CK(ensure(ctx->d_cl_mask, sizeof(uint32_t) * std::max<size_t>(t.cl_mask.size(), 1)));
+    if (!t.cl_mask.empty())
+      CK(h2d(ctx, ctx->d_cl_mask.p, t.cl_mask.data(), sizeof(uint32_t) * t.cl_mask.size()));
+    patch_cluster_pointers(ctx->sims_dev, ptr<Cl4d>(ctx->d_cl), ptr<int>(ctx->d_cl_next), ptr<int>(ctx->d_cl_head),
+                           ptr<uint32_t>(ctx->d_cl_mask));
   }
   CK(h2d(ctx, ctx->d_sims.p, ctx->sims_dev.data(), sizeof(SimDesc) * ns));
   CK(h2d(ctx, ctx->d_prim_end.p, t.prim_end.data(), sizeof(long long) * ns));
@@ -632,6 +636,7 @@ mtg_prepare(mtg_ctx * ctx, const mtg_sim * sims, int n_sims)
           sm32[i].cl = ptr<Cl4f>(ctx->d_cl32) + t.sims[i].cl_base;
           sm32[i].cl_next = ptr<int>(ctx->d_cl_next) + t.sims[i].cl_base;
           sm32[i].cl_head = ptr<int>(ctx->d_cl_head) + t.sims[i].cell_base;
+          sm32[i].cl_mask = ptr<uint32_t>(ctx->d_cl_mask) + t.sims[i].mask_base;
         }
     }
     CK(ensure(ctx->d_species32, sizeof(Species32) * sp32.size()));

@@ -244,7 +244,7 @@ collide64(P64 & p, uint32_t ic, double r1, const SimDesc & sim, const SpeciesCon
   {
     const double pos[3] = {p.x, p.y, p.z};
     const int l = cluster_lookup<double>(pos, sim.w, sim.bc, sim.kn, sim.kd, sim.cmr, sim.cl, sim.cl_next,
-                                         sim.cl_head, sim.n_clusters);
+                                         sim.cl_head, sim.n_clusters, sim.cl_mask, sim.mn, sim.inv_mcell);
     if (l == -2)
       return CF_DONE | CF_VOID; // no material: the member is dropped (trim.C:81-83)
     mat_index = l >= 0 ? 1 : 0;

@@ -227,7 +227,7 @@ struct Fp32Policy
     {
       const float pos[3] = {p.x, p.y, p.z};
       const int l = cluster_lookup<float>(pos, sim.w, sim.bc, sim.kn, sim.kd, sim.cmr, sim.cl, sim.cl_next,
-                                          sim.cl_head, sim.n_clusters);
+                                          sim.cl_head, sim.n_clusters, sim.cl_mask, sim.mn, sim.inv_mcell);
       a.gone = l == -2; // no material: the member is dropped (trim.C:81-83)
       k = l >= 0 ? 1 : 0;
       a.tag = l >= 0 ? l : -1; // sampleClusters::lookupMaterial sets material[1]->_tag = l

@@ -35,11 +35,15 @@ geo_round(Real x)
 // of the cluster that contains pos, -1 in the matrix, -2 outside a CUT boundary.
 // The hash cells within ceil(cmr / kd) of pos's cell are searched in the
 // reference's order; periodic axes measure the distance to the nearest image.
-// Every cell list is walked at most n_clusters steps.
+// Every cell list is walked at most n_clusters steps.  Before the search, the
+// occupancy mask (mn cells per axis, bit clear where no cluster reaches) answers
+// "matrix" for most points of a dilute sample; it is consulted only for periodic
+// coordinates within 64 box lengths, where its rounding margin holds.
 template <class Real, class C4>
 MTG_HD int
 cluster_lookup(const Real pos[3], const Real w[3], const int bc[3], const int kn[3], const Real kd[3], Real cmr,
-               const C4 * c, const int * next, const int * head, int n_clusters)
+               const C4 * c, const int * next, const int * head, int n_clusters, const uint32_t * mask,
+               const int mn[3], const Real inv_mcell[3])
 {
   int k[3], k1[3], k2[3];
   for (int i = 0; i < 3; ++i)
@@ -62,6 +66,26 @@ cluster_lookup(const Real pos[3], const Real w[3], const int bc[3], const int kn
       k1[i] = 0;
     if (k2[i] >= kn[i] && bc[i] != 0)
       k2[i] = kn[i] - 1;
+  }
+  if (mask)
+  {
+    bool use = true;
+    long long cell = 0, stride = 1;
+    for (int i = 0; i < 3 && use; ++i)
+    {
+      Real x = pos[i];
+      if (bc[i] == 0)
+      {
+        use = x >= -Real(64) * w[i] && x <= Real(64) * w[i];
+        x -= geo_floor(x / w[i]) * w[i];
+      }
+      int m = int(x * inv_mcell[i]);
+      m = m < 0 ? 0 : (m >= mn[i] ? mn[i] - 1 : m);
+      cell += stride * m;
+      stride *= mn[i];
+    }
+    if (use && !((mask[cell >> 5] >> (cell & 31)) & 1u))
+      return -1;
   }
   for (int j0 = k1[0]; j0 <= k2[0]; ++j0)
     for (int j1 = k1[1]; j1 <= k2[1]; ++j1)

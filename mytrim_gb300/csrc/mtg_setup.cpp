@@ -200,13 +200,15 @@ make_material(const mtg_scoef_row * rows, const SpeciesConst & sc, const mtg_mat
 }
 
 void
-patch_cluster_pointers(std::vector<SimDesc> & sims, const Cl4d * cl, const int * next, const int * head)
+patch_cluster_pointers(std::vector<SimDesc> & sims, const Cl4d * cl, const int * next, const int * head,
+                       const uint32_t * mask)
 {
   for (SimDesc & d : sims)
   {
     d.cl = d.geometry == 1 && cl ? cl + d.cl_base : nullptr;
     d.cl_next = d.geometry == 1 && next ? next + d.cl_base : nullptr;
     d.cl_head = d.geometry == 1 && head ? head + d.cell_base : nullptr;
+    d.cl_mask = d.geometry == 1 && mask ? mask + d.mask_base : nullptr;
   }
 }
 
@@ -289,6 +291,8 @@ build_fp32_tables(const HostTables & t, std::vector<Species32> & species, std::v
     {
       o.kn[k] = d.kn[k];
       o.kd[k] = float(d.kd[k]);
+      o.mn[k] = d.mn[k];
+      o.inv_mcell[k] = float(d.inv_mcell[k]);
     }
     o.cmr = float(d.cmr);
     // cluster pointers: set where the device copies are made
@@ -330,6 +334,81 @@ expected_members(const mtg_sim & s)
   return 1.0 + std::max(0.0, 0.8 * Tdam / (2.0 * Ed));
 }
 
+// Occupancy mask of a cluster sample: a grid of mn cells per axis with edge about
+// max(cmr / 2, w / 1024); a cell's bit is set when some cluster, its radius grown by
+// a margin of max(w) / 1024, reaches into the cell (periodic images on PBC axes).
+// The margin covers the rounding of a position wrapped into the box and of the
+// distance test in single precision (positions within 64 box lengths), so a point
+// in an unset cell lies in no cluster: the lookup returns the matrix there without
+// searching the hash, which would find nothing.
+static void
+build_cluster_mask(SimDesc & d, const mtg_sample & smp, std::vector<uint32_t> & words)
+{
+  const double wmax = std::max(smp.w[0], std::max(smp.w[1], smp.w[2]));
+  const double g = std::max(d.cmr * 0.5, wmax / 1024.0);
+  double cell[3];
+  long long bits = 1;
+  for (int i = 0; i < 3; ++i)
+  {
+    d.mn[i] = int(std::min(512.0, std::max(1.0, std::ceil(smp.w[i] / g))));
+    cell[i] = smp.w[i] / d.mn[i];
+    d.inv_mcell[i] = double(d.mn[i]) / smp.w[i];
+    bits *= d.mn[i];
+  }
+  d.mask_base = (long long)words.size();
+  words.resize(size_t(d.mask_base + (bits + 31) / 32), 0u);
+  const double margin = wmax / 1024.0;
+  for (long long l = 0; l < smp.n_clusters; ++l)
+  {
+    const double * c = smp.clusters + 4 * l;
+    const double R = c[3] + margin;
+    long long lo[3], hi[3];
+    bool full[3] = {false, false, false};
+    bool empty = false;
+    for (int i = 0; i < 3; ++i)
+    {
+      lo[i] = (long long)std::floor((c[i] - R) * d.inv_mcell[i]);
+      hi[i] = (long long)std::floor((c[i] + R) * d.inv_mcell[i]);
+      if (smp.bc[i] == MTG_BC_PBC)
+      {
+        if (hi[i] - lo[i] >= d.mn[i]) // the sphere spans the box: some image reaches every cell
+        {
+          lo[i] = 0;
+          hi[i] = d.mn[i] - 1;
+          full[i] = true;
+        }
+      }
+      else
+      {
+        lo[i] = std::max<long long>(lo[i], 0);
+        hi[i] = std::min<long long>(hi[i], d.mn[i] - 1);
+        empty = empty || lo[i] > hi[i];
+      }
+    }
+    if (empty)
+      continue;
+    for (long long j2 = lo[2]; j2 <= hi[2]; ++j2)
+      for (long long j1 = lo[1]; j1 <= hi[1]; ++j1)
+        for (long long j0 = lo[0]; j0 <= hi[0]; ++j0)
+        {
+          const long long j[3] = {j0, j1, j2};
+          double d2 = 0.0;
+          long long m[3];
+          for (int i = 0; i < 3; ++i)
+          {
+            const double a = double(j[i]) * cell[i], b = double(j[i] + 1) * cell[i];
+            const double e = full[i] ? 0.0 : (c[i] < a ? a - c[i] : (c[i] > b ? c[i] - b : 0.0));
+            d2 += e * e;
+            m[i] = ((j[i] % d.mn[i]) + d.mn[i]) % d.mn[i];
+          }
+          if (d2 > R * R)
+            continue;
+          const long long bit = m[0] + (long long)d.mn[0] * (m[1] + (long long)d.mn[1] * m[2]);
+          words[size_t(d.mask_base + bit / 32)] |= 1u << (bit % 32);
+        }
+  }
+}
+
 int
 build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim * sims, int n_sims,
              HostTables & out, std::string & err)
@@ -344,6 +423,7 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
   out.clusters.clear();
   out.cl_next.clear();
   out.cl_head.clear();
+  out.cl_mask.clear();
   out.total_primaries = out.hist_total = out.voxel_total = 0;
   out.k0 = out.k1 = 0;
   out.emax = 0.0;
@@ -676,6 +756,7 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
         if (c[3] > d.cmr)
           d.cmr = c[3];
       }
+      build_cluster_mask(d, smp, out.cl_mask);
     }
     d.hist_evac_rows = s.hist_vac_n > 0 ? s.hist_evac_rows : 0;
     d.hist_evac_base = hist;

@@ -34,11 +34,13 @@ struct HostTables
   // clusters of all cluster samples of the run (SimDesc::cl_base / cell_base index them)
   std::vector<Cl4d> clusters;
   std::vector<int> cl_next, cl_head;
+  std::vector<uint32_t> cl_mask; // occupancy masks (SimDesc::mask_base indexes them)
 };
 
 // Point the simulations' cluster pointers at arrays holding HostTables::clusters,
-// cl_next and cl_head (host or device copies).
-void patch_cluster_pointers(std::vector<SimDesc> & sims, const Cl4d * cl, const int * next, const int * head);
+// cl_next, cl_head and cl_mask (host or device copies).
+void patch_cluster_pointers(std::vector<SimDesc> & sims, const Cl4d * cl, const int * next, const int * head,
+                            const uint32_t * mask);
 
 // Build the tables; returns MTG_OK or MTG_ERR_BAD_INPUT with `err` set.
 int build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim * sims,

@@ -140,6 +140,13 @@ struct SimDesc
   const struct Cl4d * cl;
   const int * cl_next;
   const int * cl_head;
+  // occupancy mask: one bit per cell of a finer grid (mn cells per axis), set where
+  // some cluster (dilated by a rounding margin) reaches into the cell; a point in an
+  // unset cell is in the matrix without a hash search
+  int mn[3];
+  double inv_mcell[3];
+  long long mask_base; // offset into the run's mask words
+  const uint32_t * cl_mask;
 };
 
 // one cluster: centre and radius
@@ -234,6 +241,9 @@ struct Sim32
   const Cl4f * cl;
   const int * cl_next;
   const int * cl_head;
+  int mn[3];
+  float inv_mcell[3];
+  const uint32_t * cl_mask;
 };
 
 // final state of a cascade member (IonBase::StateType, ion.h:75-84)

@@ -14,6 +14,7 @@
 #include "runspec.h"
 
 #include "mtg_collide64.cuh"
+#include "mtg_geometry.cuh"
 #include "mtg_setup.h"
 
 #include <algorithm>
@@ -265,8 +266,67 @@ main(int argc, char ** argv)
     fprintf(stderr, "replay_host: %s\n", err.c_str());
     return 2;
   }
-  patch_cluster_pointers(t.sims, t.clusters.data(), t.cl_next.data(), t.cl_head.data());
+  patch_cluster_pointers(t.sims, t.clusters.data(), t.cl_next.data(), t.cl_head.data(), t.cl_mask.data());
   const SimDesc & sd = t.sims[0];
+  if (argc >= 4 && std::string(argv[2]) == "--lookupcheck" && sd.geometry == 1)
+  {
+    // the cluster lookup with and without the occupancy mask, in double and in float,
+    // at n random points: inside the box, within 64 box lengths on periodic axes,
+    // and near cluster surfaces; prints "checked mismatches"
+    const long long n = atoll(argv[3]);
+    std::vector<Cl4f> c32(t.clusters.size());
+    for (size_t l = 0; l < c32.size(); ++l)
+      c32[l] = Cl4f{float(t.clusters[l].x), float(t.clusters[l].y), float(t.clusters[l].z), float(t.clusters[l].r)};
+    const float w32[3] = {float(sd.w[0]), float(sd.w[1]), float(sd.w[2])};
+    const float kd32[3] = {float(sd.kd[0]), float(sd.kd[1]), float(sd.kd[2])};
+    const float im32[3] = {float(sd.inv_mcell[0]), float(sd.inv_mcell[1]), float(sd.inv_mcell[2])};
+    uint64_t st = 12345;
+    auto uni = [&]() {
+      st = st * 6364136223846793005ull + 1442695040888963407ull;
+      return double(st >> 11) * 0x1p-53;
+    };
+    long long bad = 0;
+    for (long long i = 0; i < n; ++i)
+    {
+      double q[3];
+      const int kind = int(i % 3);
+      if (kind == 2 && !t.clusters.empty())
+      {
+        // near a cluster surface (and its periodic images)
+        const Cl4d & c = t.clusters[size_t(uni() * double(t.clusters.size())) % t.clusters.size()];
+        double v[3], vv = 0.0;
+        for (int k = 0; k < 3; ++k)
+        {
+          v[k] = uni() - 0.5;
+          vv += v[k] * v[k];
+        }
+        const double rad = c.r * (1.0 + (uni() - 0.5) * 1e-6);
+        const double shift[3] = {(&c.x)[0], (&c.x)[1], (&c.x)[2]};
+        for (int k = 0; k < 3; ++k)
+          q[k] = shift[k] + v[k] / std::sqrt(vv) * rad + (sd.bc[k] == 0 ? sd.w[k] * double(int(uni() * 9.0) - 4) : 0.0);
+      }
+      else
+        for (int k = 0; k < 3; ++k)
+          q[k] = sd.bc[k] == 0 && kind == 1 ? (uni() - 0.5) * 120.0 * sd.w[k] : uni() * sd.w[k];
+      const int a = cluster_lookup<double>(q, sd.w, sd.bc, sd.kn, sd.kd, sd.cmr, sd.cl, sd.cl_next, sd.cl_head,
+                                           sd.n_clusters, sd.cl_mask, sd.mn, sd.inv_mcell);
+      const int b = cluster_lookup<double>(q, sd.w, sd.bc, sd.kn, sd.kd, sd.cmr, sd.cl, sd.cl_next, sd.cl_head,
+                                           sd.n_clusters, nullptr, sd.mn, sd.inv_mcell);
+      const float qf[3] = {float(q[0]), float(q[1]), float(q[2])};
+      const int af = cluster_lookup<float>(qf, w32, sd.bc, sd.kn, kd32, float(sd.cmr), c32.data(), sd.cl_next,
+                                           sd.cl_head, sd.n_clusters, sd.cl_mask, sd.mn, im32);
+      const int bf = cluster_lookup<float>(qf, w32, sd.bc, sd.kn, kd32, float(sd.cmr), c32.data(), sd.cl_next,
+                                           sd.cl_head, sd.n_clusters, nullptr, sd.mn, im32);
+      if (a != b || af != bf)
+      {
+        if (bad < 5)
+          printf("mismatch %.17g %.17g %.17g: %d %d / %d %d\n", q[0], q[1], q[2], a, b, af, bf);
+        ++bad;
+      }
+    }
+    printf("%lld %lld\n", n, bad);
+    return bad ? 1 : 0;
+  }
   std::vector<P64> stack;
   for (long long n = spec.first; n < spec.first + spec.n; ++n)
   {
