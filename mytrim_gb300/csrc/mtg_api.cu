@@ -159,8 +159,10 @@ int
 kernel_level(const mtg_ctx * ctx)
 {
   const HostTables & t = ctx->tables;
-  if ((ctx->event_cap > 0 && ctx->event_mask) || t.any_extended)
+  if (ctx->event_cap > 0 && ctx->event_mask)
     return LVL_FULL;
+  if (t.any_extended)
+    return LVL_GEO;
   if (ctx->record_cap > 0 || t.voxel_total > 0 || t.any_evac || t.any_mode)
     return LVL_MID;
   return LVL_LEAN;

@@ -206,17 +206,19 @@ struct LaneCold
 
 // Kernel feature levels.  Code for a feature a run does not use still costs the
 // collision loop (instruction fetch, registers), so the cascade kernel comes in
-// three variants and each run takes the smallest that has what it needs:
+// four variants and each run takes the smallest that has what it needs:
 //   LVL_LEAN  layered samples, universal potential, TrimVacCount tallies (depth,
 //             range and lateral histograms), CUT boundaries and sputter counting;
 //   LVL_MID   + member records, deposition voxels, the vacancy-energy histogram,
 //             TrimRange / TrimPrimaries tally modes;
-//   LVL_FULL  + the event log, the cluster geometry, the Moliere and C-Kr potentials.
+//   LVL_GEO   + the cluster geometry, the Moliere and C-Kr potentials;
+//   LVL_FULL  + the event log.
 enum KernelLevel : int
 {
   LVL_LEAN = 0,
   LVL_MID = 1,
-  LVL_FULL = 2
+  LVL_GEO = 2,
+  LVL_FULL = 3
 };
 
 // Device tally sink for one lane of a kernel of level LVL.
@@ -627,13 +629,13 @@ struct LaneSink
 };
 
 // LVL: the feature level (KernelLevel); the collision code knows the cluster
-// geometry and the non-universal potentials at LVL_FULL only
+// geometry and the non-universal potentials from LVL_GEO on
 template <class Pol, int LVL>
 __global__ void __launch_bounds__(128, Pol::min_blocks(LVL))
 cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
 {
   constexpr bool MID = LVL >= LVL_MID;
-  constexpr bool EXT = LVL >= LVL_FULL;
+  constexpr bool EXT = LVL >= LVL_GEO;
   using Particle = typename Pol::Particle;
   extern __shared__ __align__(16) unsigned char smem[];
 

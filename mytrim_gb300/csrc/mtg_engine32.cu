@@ -24,14 +24,16 @@
 #include "mtg_surrogate.cuh"
 
 // resident 128-thread blocks per SM the register budget of each feature level is
-// cut for: lean 8 (64 registers), mid 7 (72), full 6 (80), each the most that
-// compiles without spilling in the collision loop (the full level's cluster lookup
-// spills a few words even at 80)
+// cut for: lean 8 (64 registers), mid 7 (72), geometry and full 6 (80), each the
+// most that compiles without spilling much in the collision loop
 #ifndef MTG_FP32_MIN_BLOCKS
 #define MTG_FP32_MIN_BLOCKS 6
 #endif
 #ifndef MTG_FP32_MIN_BLOCKS_MID
 #define MTG_FP32_MIN_BLOCKS_MID 7
+#endif
+#ifndef MTG_FP32_MIN_BLOCKS_GEO
+#define MTG_FP32_MIN_BLOCKS_GEO 6
 #endif
 #ifndef MTG_FP32_MIN_BLOCKS_LEAN
 #define MTG_FP32_MIN_BLOCKS_LEAN 8
@@ -103,7 +105,9 @@ struct Fp32Policy
   {
     return SURROGATE ? 4
                      : (lvl == LVL_LEAN ? MTG_FP32_MIN_BLOCKS_LEAN
-                                        : (lvl == LVL_MID ? MTG_FP32_MIN_BLOCKS_MID : MTG_FP32_MIN_BLOCKS));
+                                        : (lvl == LVL_MID ? MTG_FP32_MIN_BLOCKS_MID
+                                                          : (lvl == LVL_GEO ? MTG_FP32_MIN_BLOCKS_GEO
+                                                                            : MTG_FP32_MIN_BLOCKS)));
   }
 
   struct MemberCtx
@@ -475,6 +479,7 @@ launch_cascade32(const EngineParams & prm, const Fp32Tables & t, int grid, int b
     {
       case LVL_LEAN: cascade_kernel<Fp32Policy<true>, LVL_LEAN><<<grid, block, smem, st>>>(prm, tabs); break;
       case LVL_MID: cascade_kernel<Fp32Policy<true>, LVL_MID><<<grid, block, smem, st>>>(prm, tabs); break;
+      case LVL_GEO: cascade_kernel<Fp32Policy<true>, LVL_GEO><<<grid, block, smem, st>>>(prm, tabs); break;
       default: cascade_kernel<Fp32Policy<true>, LVL_FULL><<<grid, block, smem, st>>>(prm, tabs); break;
     }
   else
@@ -482,6 +487,7 @@ launch_cascade32(const EngineParams & prm, const Fp32Tables & t, int grid, int b
     {
       case LVL_LEAN: cascade_kernel<Fp32Policy<false>, LVL_LEAN><<<grid, block, smem, st>>>(prm, tabs); break;
       case LVL_MID: cascade_kernel<Fp32Policy<false>, LVL_MID><<<grid, block, smem, st>>>(prm, tabs); break;
+      case LVL_GEO: cascade_kernel<Fp32Policy<false>, LVL_GEO><<<grid, block, smem, st>>>(prm, tabs); break;
       default: cascade_kernel<Fp32Policy<false>, LVL_FULL><<<grid, block, smem, st>>>(prm, tabs); break;
     }
   return cudaGetLastError();
@@ -506,9 +512,10 @@ occupancy_variants(int block, size_t smem, int * occ)
 {
   cudaError_t e;
   if ((e = occupancy_of(cascade_kernel<Fp32Policy<SG>, LVL_LEAN>, block, smem, &occ[0])) != cudaSuccess ||
-      (e = occupancy_of(cascade_kernel<Fp32Policy<SG>, LVL_MID>, block, smem, &occ[1])) != cudaSuccess)
+      (e = occupancy_of(cascade_kernel<Fp32Policy<SG>, LVL_MID>, block, smem, &occ[1])) != cudaSuccess ||
+      (e = occupancy_of(cascade_kernel<Fp32Policy<SG>, LVL_GEO>, block, smem, &occ[2])) != cudaSuccess)
     return e;
-  return occupancy_of(cascade_kernel<Fp32Policy<SG>, LVL_FULL>, block, smem, &occ[2]);
+  return occupancy_of(cascade_kernel<Fp32Policy<SG>, LVL_FULL>, block, smem, &occ[3]);
 }
 
 // residency of the variant of feature level `level` (KernelLevel); every variant
@@ -516,11 +523,11 @@ occupancy_variants(int block, size_t smem, int * occ)
 cudaError_t
 occupancy32(int block, size_t smem, int * blocks_per_sm, int surrogate, int level)
 {
-  int occ[3] = {0, 0, 0};
+  int occ[4] = {0, 0, 0, 0};
   cudaError_t e = surrogate ? occupancy_variants<true>(block, smem, occ) : occupancy_variants<false>(block, smem, occ);
   if (e != cudaSuccess)
     return e;
-  *blocks_per_sm = occ[level < 0 ? 0 : (level > 2 ? 2 : level)];
+  *blocks_per_sm = occ[level < 0 ? 0 : (level > 3 ? 3 : level)];
   return cudaSuccess;
 }
 
