@@ -2,9 +2,10 @@
 """Benchmark: primary ions per second, full cascade, on one GB300.
 
 Workload: Ag 200 keV into bulk Si (2.33 g/cm3, Edisp 15 eV, Ebind 3 eV), full
-recoil cascade -- the surrogate workload of the benchmark suite.  One step is
-one batch of fresh primaries through the whole cascade on the fast path
-(FP32, with the learned scattering surrogate when a trained network is present).
+recoil cascade -- the surrogate workload of the benchmark suite.  One step is the
+configuration's 10^7 fresh primaries through the whole cascade on the FP32 path
+(exact scattering); the surrogate path (2^20 primaries per step) and the FP64
+path are timed beside it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -84,7 +85,9 @@ def args_parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--batch", type=int, default=1 << 20, help="primaries per step")
+    p.add_argument("--batch", type=int, default=10_000_000,
+                   help="primaries per step (default: the 10^7 primaries of the Ag 200 keV configuration)")
+    p.add_argument("--surrogate-batch", type=int, default=1 << 20, help="primaries per step of the surrogate leg")
     p.add_argument("--precision", default="auto", choices=["auto", "fp32", "surrogate", "fp64"])
     p.add_argument("--fp64-batch", type=int, default=8192)
     p.add_argument("--cpu-per-core", type=int, default=0, help="primaries per core in the CPU sample")
@@ -253,8 +256,9 @@ def main():
         eng.set_event_log([names[k] for k in ev_kinds], a.event_capacity)
     n_events = []
 
-    def sims_for(step):
-        return make_sims(a.workload, a.batch, (step * world + rank) * a.batch)
+    def sims_for(step, batch=None):
+        b = batch or a.batch
+        return make_sims(a.workload, b, (step * world + rank) * b)
 
     # warm-up steps (untimed)
     for i in range(a.warmup):
@@ -324,7 +328,7 @@ def main():
                                                     "vac_s2", "eel_s2", "enuc_s2", "coll_s2")}
     fast = summarize(agg)
 
-    def time_path(path, steps, base):
+    def time_path(path, steps, base, batch):
         """device-timed steps of another path on fresh primaries (same workload)"""
         e2 = Engine(device=local, precision="fp32", seed=20261203)
         if path == "surrogate":
@@ -334,7 +338,7 @@ def main():
         e2.configure(precision=path, seed=20261203)
         rs, ts = [], []
         for k in range(steps + 1):
-            e2.prepare(sims_for(base + k))
+            e2.prepare(sims_for(base + k, batch))
             with torch.cuda.stream(stream):
                 flush.zero_()
             e0 = torch.cuda.Event(enable_timing=True)
@@ -356,7 +360,7 @@ def main():
     if prec != "surrogate" and not a.no_fp64:
         from mytrim_gb300.train_surrogate import PARAMS
         if PARAMS.exists():
-            sg, sg_rate, sg_agg = time_path("surrogate", 2, 1000)
+            sg, sg_rate, sg_agg = time_path("surrogate", 2, 1000, a.surrogate_batch)
             paths["surrogate"] = {"value": sg_rate, "unit": UNIT, "summary": sg,
                                   "fallback_fraction": sg_agg["surrogate_fallbacks"] / max(sg_agg["collisions"], 1)}
     fp64 = None
