@@ -315,8 +315,11 @@ typedef enum
                              E = its energy, aux = binding energy (E + aux stays there) */
   MTG_EV_REST = 5,        /* checkPKAState: the member came to rest; state = 1 replacement,
                              2 substitutional, 3 interstitial; E = residual energy */
-  MTG_EV_LOST = 6         /* the member left through a CUT boundary; aux = energy of the
+  MTG_EV_LOST = 6,        /* the member left through a CUT boundary; aux = energy of the
                              recoil dropped with it */
+  MTG_EV_HISTORY = 7      /* TrimHistory's followRecoil (trim.h:139-153): the moving atom's
+                             position after its flight at each displaced recoil; E = its
+                             energy after the collision */
 } mtg_event_kind;
 
 typedef struct

@@ -103,7 +103,7 @@ class Event(C.Structure):
 
 
 # event kinds (mtg_event_kind)
-EV_VACANCY, EV_REPLACEMENT, EV_BRANCH, EV_DISSIPATE, EV_REST, EV_LOST = 1, 2, 3, 4, 5, 6
+EV_VACANCY, EV_REPLACEMENT, EV_BRANCH, EV_DISSIPATE, EV_REST, EV_LOST, EV_HISTORY = 1, 2, 3, 4, 5, 6, 7
 
 
 class SurrogateConfig(C.Structure):

@@ -951,8 +951,8 @@ mtg_set_event_log(mtg_ctx * ctx, unsigned int kind_mask, long long capacity)
 {
   if (!ctx)
     return MTG_ERR_BAD_INPUT;
-  if (capacity < 0 || (kind_mask & ~0x7eu))
-    return fail(ctx, MTG_ERR_BAD_INPUT, "event kinds are 1..6 and the capacity must not be negative");
+  if (capacity < 0 || (kind_mask & ~0xfeu))
+    return fail(ctx, MTG_ERR_BAD_INPUT, "event kinds are 1..7 and the capacity must not be negative");
   ctx->event_cap = capacity;
   ctx->event_mask = kind_mask;
   ctx->prepared = false;

@@ -385,6 +385,7 @@ collide64(P64 & p, uint32_t ic, double r1, const SimDesc & sim, const SpeciesCon
   if (rec.E > el.Edisp - el.Elbind)
   {
     sink.enuc(el.Elbind, rec.x, rec.y, rec.z);
+    sink.history(p, sc.Z1, sc.m1);
     sink.branch(rec, el, p.key);
     const bool follow = rec.gen < sim.follow_gen;
     if (follow)

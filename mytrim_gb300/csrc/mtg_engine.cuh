@@ -299,6 +299,14 @@ struct LaneSink
     r.state = state;
     r.tag = tag;
   }
+  // TrimHistory::followRecoil (trim.h:146-150): the moving atom's position (after
+  // its flight, trim.C:310) at each displaced recoil
+  template <class P>
+  __device__ void history(const P & p, int Z1, Real m1)
+  {
+    if constexpr (EV)
+      event(EV_HISTORY, Real(p.x), Real(p.y), Real(p.z), Real(p.E), Z1, m1, p.gen, 0, Real(0), p.key, p.tag);
+  }
   // followRecoil (trim.C:362): a displaced recoil, followed or not
   template <class R, class E>
   __device__ void branch(const R & rec, const E & el, uint64_t key)

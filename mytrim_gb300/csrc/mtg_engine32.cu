@@ -417,6 +417,7 @@ struct Fp32Policy
     if (recE > el.disp_thresh)
     {
       sink.enuc(el.Elbind, rec.x, rec.y, rec.z);
+      sink.history(p, m.sc->Z1, m.sc->m1);
       sink.branch(rec, el, p.key);
       const bool follow = rec.gen < sim.follow_gen;
       if (follow)

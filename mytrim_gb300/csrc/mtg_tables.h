@@ -187,7 +187,8 @@ enum EventKind : int
   EV_BRANCH = 3,
   EV_DISSIPATE = 4,
   EV_REST = 5,
-  EV_LOST = 6
+  EV_LOST = 6,
+  EV_HISTORY = 7
 };
 
 // ---- single-precision copies used by the FP32 engine (built from the tables above)

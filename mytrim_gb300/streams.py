@@ -6,6 +6,8 @@ the engine's event log (``Engine.set_event_log`` / ``Engine.events``).
   as an interstitial, substitutional or replacement;
 * ``vac_map`` -- TrimVacMap (trim.C:484-501): the vacancy map of up to three target
   species over the sample's (x, y) extent;
+* ``history`` -- TrimHistory (trim.h:139-153): the moving atom's positions at its
+  displaced recoils;
 * ``phonon_log`` -- TrimPhononOut (trim.C:504-527): "<E> <ion>" for every energy
   left in the lattice: the binding energy of each displaced recoil, the energy plus
   binding energy of each recoil below the displacement energy, the residual energy
@@ -87,6 +89,14 @@ def vac_map(events: np.ndarray, w, z, mx: int = 20, my: int = 20) -> np.ndarray:
                 out[x, y, k] += 1
                 break
     return out
+
+
+def history(events: np.ndarray) -> np.ndarray:
+    """TrimHistory::getHistory (trim.h:139-153) from events logged with kind
+    EV_HISTORY: the moving atom's position after its flight at each displaced
+    recoil, as an (n, 3) array sorted like the text streams."""
+    h = _sorted(events[events["kind"] == F.EV_HISTORY])
+    return np.stack([h["x"], h["y"], h["z"]], axis=1) if len(h) else np.zeros((0, 3))
 
 
 def write(lines: Iterable[str], out: TextIO) -> int:

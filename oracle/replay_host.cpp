@@ -38,6 +38,10 @@ struct HostSink
   void numeric() {}
   void enuc(double, double, double, double) {}
   void unfollowed(double) {}
+  template <class P>
+  void history(const P &, int, double)
+  {
+  }
   template <class R, class E>
   void branch(const R &, const E &, uint64_t)
   {

@@ -390,7 +390,7 @@ def test_lateral_histogram(engine_lib):
     assert abs(my - t["sy"] / t["range_n"]) < 5.0
 
 
-ALL_EVENTS = [F.EV_VACANCY, F.EV_REPLACEMENT, F.EV_BRANCH, F.EV_DISSIPATE, F.EV_REST, F.EV_LOST]
+ALL_EVENTS = [F.EV_VACANCY, F.EV_REPLACEMENT, F.EV_BRANCH, F.EV_DISSIPATE, F.EV_REST, F.EV_LOST, F.EV_HISTORY]
 
 
 def _cu_sim(n=200, E=5000.0, **kw):
@@ -419,6 +419,12 @@ def test_event_log_matches_tallies(engine_lib, prec):
     assert (rest["state"] == 2).sum() == t["substitutionals"]
     assert len(rest) + (k == F.EV_LOST).sum() == t["members"]
     assert set(np.unique(ev["primary"])) == set(range(sim.n_primaries))
+    # TrimHistory: one position of the moving atom per displaced recoil, raised by
+    # the same atom as the branch event
+    hist, br = ev[k == F.EV_HISTORY], ev[k == F.EV_BRANCH]
+    assert len(hist) == len(br) > 0
+    assert sorted(zip(hist["primary"], hist["key"])) == sorted(zip(br["primary"], br["key"]))
+    assert streams_history(ev).shape == (len(hist), 3)
     # TrimPhononOut's split of the nuclear deposit (trim.C:504-527): binding energy of
     # every displaced recoil, dissipated recoils' energy plus binding, residual
     # energy of the members that came to rest
@@ -430,6 +436,11 @@ def test_event_log_matches_tallies(engine_lib, prec):
         x = ev["x"][k == F.EV_VACANCY]
         x = x[(x > -1.0) & (x < 2000.0)]
         assert np.array_equal(np.bincount(np.trunc(x).astype(np.int64), minlength=2000), t["hist_vac"])
+
+
+def streams_history(ev):
+    from mytrim_gb300 import streams
+    return streams.history(ev)
 
 
 def test_event_log_overflow_keeps_tallies(engine_lib):
