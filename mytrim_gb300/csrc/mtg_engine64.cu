@@ -3,6 +3,11 @@
 // that every multiply and add is rounded separately, exactly as in the host
 // replay build of the same code.
 #include "mtg_collide64.cuh"
+
+// resident 128-thread blocks per SM the register budget is cut for
+#ifndef MTG_FP64_MIN_BLOCKS
+#define MTG_FP64_MIN_BLOCKS 3
+#endif
 #include "mtg_engine.cuh"
 #include "mtg_kernels.h"
 
@@ -16,7 +21,7 @@ struct Fp64Policy
   using Acc = AccF64;
   using AccHot = AccF64;
   static constexpr int FLUSH_EVERY = 0;
-  static constexpr int min_blocks(int) { return 3; } // <= 170 registers: 12 warps per SM
+  static constexpr int min_blocks(int) { return MTG_FP64_MIN_BLOCKS; } // 3: <= 170 registers, 12 warps per SM
 
   struct Tables
   {
