@@ -1,0 +1,67 @@
+"""Edge cases of the cascade path, FP64 engine against the oracle on the same Philox
+streams (integer tallies exactly, energies to 1e-9): a primary below its final
+energy, a fast light ion (electronic stopping dominant), a heavy ion into a light
+target, a three-element four-layer stack, transmission through a thin film with
+CUT on both faces, an empty simulation in a batch."""
+import math
+
+import pytest
+
+from mytrim_gb300 import Engine
+from mytrim_gb300.engine import ElementSpec, LayerSpec, SimSpec
+
+pytestmark = pytest.mark.gpu
+
+SI, O, C, AL = 28.086, 15.999, 12.011, 26.982
+BULK_CU = [LayerSpec(1e7, 8.96, [ElementSpec(29, 63.546, 1.0, 25.0, 3.0)])]
+CASES = {
+    "below_final_energy": SimSpec(layers=BULK_CU, Z=29, m=63.546, E=2.0, n_primaries=50),
+    "fast_proton": SimSpec(layers=[LayerSpec(1e9, 2.33, [ElementSpec(14, SI, 1.0, 15.0, 3.0)])], Z=1, m=1.008,
+                           E=2e6, n_primaries=20, hist_range_bin=1000.0, hist_range_n=1000),
+    "uranium_into_carbon": SimSpec(layers=[LayerSpec(1e7, 2.26, [ElementSpec(6, C, 1.0, 28.0, 3.0)])], Z=92,
+                                   m=238.05, E=5e5, n_primaries=3),
+    "four_layers_three_elements": SimSpec(
+        layers=[LayerSpec(50.0, 3.95, [ElementSpec(13, AL, 2.0, 25.0, 3.0), ElementSpec(8, O, 3.0, 28.0, 3.0)]),
+                LayerSpec(80.0, 2.2, [ElementSpec(14, SI, 1.0, 15.0, 3.0), ElementSpec(8, O, 2.0, 28.0, 3.0)]),
+                LayerSpec(30.0, 5.0, [ElementSpec(13, AL, 1.0, 25.0, 3.0), ElementSpec(14, SI, 1.0, 15.0, 3.0),
+                                      ElementSpec(8, O, 2.0, 28.0, 3.0)]),
+                LayerSpec(1e7, 2.33, [ElementSpec(14, SI, 1.0, 15.0, 3.0)])],
+        Z=18, m=39.948, E=30e3, n_primaries=20, dir=(math.cos(0.3), math.sin(0.3), 0.0), pos=(0.0, 0.0, 0.0),
+        size=(1e9, 1e9, 1e9), bc=(2, 1, 1), hist_range_bin=5.0, hist_range_n=200),
+    "thin_film_transmission": SimSpec(layers=[LayerSpec(200.0, 8.96, [ElementSpec(29, 63.546, 1.0, 25.0, 3.0)])],
+                                      Z=2, m=4.0026, E=50e3, n_primaries=40, pos=(0.0, 0.0, 0.0),
+                                      size=(200.0, 1e9, 1e9), bc=(2, 1, 1)),
+}
+INT_KEYS = ("primaries", "members", "collisions", "vacancies", "replacements", "interstitials", "substitutionals",
+            "lost", "range_n")
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_fp64_equals_oracle(oracle_built, engine_lib, case):
+    sim = CASES[case]
+    e = Engine(precision="fp64", seed=31)
+    g = e.run([sim])[0]
+    e.close()
+    o = oracle_built.run(sim, seed=31, philox=True)
+    for k in INT_KEYS:
+        assert g[k] == o[k], (case, k, g[k], o[k])
+    for k in ("Eel", "Enuc", "Elost"):
+        assert math.isclose(g[k], o[k], rel_tol=1e-9, abs_tol=1e-6), (case, k, g[k], o[k])
+    assert list(g["hist_range"]) == o["hist_range"]
+    total = g["Eel"] + g["Enuc"] + g["Elost"] + g["Eunfollowed"]
+    assert math.isclose(total, sim.E * sim.n_primaries, rel_tol=1e-12)
+    if case == "below_final_energy":
+        assert g["collisions"] == sim.n_primaries and g["interstitials"] == sim.n_primaries
+    if case == "thin_film_transmission":
+        assert g["lost"] > 0 and g["range_n"] + g["lost"] >= sim.n_primaries
+
+
+def test_empty_simulation_in_a_batch(engine_lib):
+    a = CASES["fast_proton"]
+    empty = SimSpec(**{**a.__dict__, "n_primaries": 0})
+    e = Engine(precision="fp32", seed=3)
+    r = e.run([empty, a, empty])
+    e.close()
+    assert r[0]["primaries"] == 0 and r[0]["members"] == 0 and r[0]["Eel"] == 0.0
+    assert r[2]["primaries"] == 0
+    assert r[1]["primaries"] == a.n_primaries
