@@ -32,6 +32,11 @@ struct U4
   uint32_t x, y, z, w;
 };
 
+struct U2
+{
+  uint32_t x, y;
+};
+
 MTG_HD uint32_t
 mulhi32(uint32_t a, uint32_t b)
 {
@@ -53,6 +58,20 @@ philox(U4 c, uint32_t k0, uint32_t k1)
     c = U4{h1 ^ c.y ^ k0, l1, h0 ^ c.w ^ k1, l0};
     k0 += 0x9E3779B9u;
     k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+
+// Philox2x32-10 (same paper): 64-bit counter, 32-bit key, multiplier 0xD256D193
+MTG_HD U2
+philox2(U2 c, uint32_t k)
+{
+#pragma unroll
+  for (int r = 0; r < 10; ++r)
+  {
+    const uint32_t h = mulhi32(0xD256D193u, c.x), l = 0xD256D193u * c.x;
+    c = U2{h ^ k ^ c.y, l};
+    k += 0x9E3779B9u;
   }
   return c;
 }
@@ -94,6 +113,16 @@ MTG_HD U4
 draw_block(uint64_t member, uint32_t ic, uint32_t block, uint32_t k0, uint32_t k1)
 {
   return philox(U4{uint32_t(member), uint32_t(member >> 32), ic, block}, k0, k1);
+}
+
+// Two 32-bit draws of collision ic of a member (the FP32 engine on single-element
+// materials, which needs no target-atom draw): Philox2x32-10 with the member key as
+// counter and the collision index, through a bijection, in the key.  A separate
+// stream family from draw_block's.
+MTG_HD U2
+draw_pair(uint64_t member, uint32_t ic, uint32_t k0, uint32_t k1)
+{
+  return philox2(U2{uint32_t(member), uint32_t(member >> 32)}, (k0 ^ k1) + ic * 0x85EBCA6Bu);
 }
 
 // uniform in (0, 1] with 53 random bits

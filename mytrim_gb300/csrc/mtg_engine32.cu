@@ -264,11 +264,25 @@ struct Fp32Policy
       ls = r1 * fminf(ls, sim.cw);
     a.ls = ls;
 
-    // impact parameter, target atom and azimuth: one Philox block per collision
-    const U4 dr = draw_block(p.key, ic, 0u, k0, k1);
-    const float r2 = u24f(dr.x);
-    float hh = u24f(dr.y);
-    a.azimuth = dr.z;
+    // impact parameter, target atom and azimuth: one Philox4x32-10 block per
+    // collision, or on a single-element material (no target-atom draw) one
+    // Philox2x32-10 block, half the work
+    uint32_t u_imp, u_el = 0u;
+    if (mc.nel == 1)
+    {
+      const U2 d = draw_pair(p.key, ic, k0, k1);
+      u_imp = d.x;
+      a.azimuth = d.y;
+    }
+    else
+    {
+      const U4 dr = draw_block(p.key, ic, 0u, k0, k1);
+      u_imp = dr.x;
+      u_el = dr.y;
+      a.azimuth = dr.z;
+    }
+    const float r2 = u24f(u_imp);
+    float hh = u24f(u_el);
     const float pimp = pmax * sqrtf(r2);
     int nn = 0;
     for (; nn < mc.nel - 1; ++nn)

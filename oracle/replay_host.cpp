@@ -148,6 +148,20 @@ main(int argc, char ** argv)
       printf("%a\n", material_stop64(sc, mc, E));
     return 0;
   }
+  if (argc >= 3 && std::string(argv[2]) == "--philox")
+  {
+    // lines "x y z w k0 k1" -> Philox4x32-10 of (x, y, z, w) under (k0, k1), then
+    // Philox2x32-10 of (x, y) under k0 (hex words)
+    unsigned long long v[6];
+    while (std::cin >> std::hex >> v[0] >> v[1] >> v[2] >> v[3] >> v[4] >> v[5])
+    {
+      const U4 a = philox(U4{uint32_t(v[0]), uint32_t(v[1]), uint32_t(v[2]), uint32_t(v[3])}, uint32_t(v[4]),
+                          uint32_t(v[5]));
+      const U2 b = philox2(U2{uint32_t(v[0]), uint32_t(v[1])}, uint32_t(v[4]));
+      printf("%08x %08x %08x %08x %08x %08x\n", a.x, a.y, a.z, a.w, b.x, b.y);
+    }
+    return 0;
+  }
   if (argc >= 3 && std::string(argv[2]) == "--mathcheck")
   {
     // exp64 / log64 (short routes) against exp64_wide / log64_wide bit for bit on n
