@@ -115,10 +115,9 @@ draw_block(uint64_t member, uint32_t ic, uint32_t block, uint32_t k0, uint32_t k
   return philox(U4{uint32_t(member), uint32_t(member >> 32), ic, block}, k0, k1);
 }
 
-// Two 32-bit draws of collision ic of a member (the FP32 engine on single-element
-// materials, which needs no target-atom draw): Philox2x32-10 with the member key as
-// counter and the collision index, through a bijection, in the key.  A separate
-// stream family from draw_block's.
+// Two 32-bit draws of collision ic of a member (the FP32 engine): Philox2x32-10
+// with the member key as counter and the collision index, through a bijection, in
+// the key.  A separate stream family from draw_block's.
 MTG_HD U2
 draw_pair(uint64_t member, uint32_t ic, uint32_t k0, uint32_t k1)
 {

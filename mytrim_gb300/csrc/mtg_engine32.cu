@@ -264,22 +264,16 @@ struct Fp32Policy
       ls = r1 * fminf(ls, sim.cw);
     a.ls = ls;
 
-    // impact parameter, target atom and azimuth: one Philox4x32-10 block per
-    // collision, or on a single-element material (no target-atom draw) one
-    // Philox2x32-10 block, half the work
+    // impact parameter and azimuth from one Philox2x32-10 block per collision; the
+    // target atom of a multi-element material from a second block whose counter is
+    // the member key with its top bit flipped
     uint32_t u_imp, u_el = 0u;
-    if (mc.nel == 1)
     {
       const U2 d = draw_pair(p.key, ic, k0, k1);
       u_imp = d.x;
       a.azimuth = d.y;
-    }
-    else
-    {
-      const U4 dr = draw_block(p.key, ic, 0u, k0, k1);
-      u_imp = dr.x;
-      u_el = dr.y;
-      a.azimuth = dr.z;
+      if (mc.nel > 1)
+        u_el = draw_pair(p.key ^ 0x8000000000000000ull, ic, k0, k1).x;
     }
     const float r2 = u24f(u_imp);
     float hh = u24f(u_el);
