@@ -10,6 +10,13 @@
 // and collision index.
 //
 // Usage: replay_host <stopping_tables.tsv> < spec     (spec format: runspec.h)
+//
+// Checks of single pieces of the same code, for the tests:
+//   replay_host <tables> --stopping              "Z1 m1 rho n Z m t ...", then energies -> stopping (hex)
+//   replay_host <tables> --scatter [potential]   lines "eps b" -> sin^2(theta/2) (hex)
+//   replay_host <tables> --mathcheck [n]         exp64 / log64 short routes vs full forms
+//   replay_host <tables> --philox                lines of six hex words -> Philox outputs
+//   replay_host <tables> --lookupcheck n < spec  cluster lookup with vs without the mask
 
 #include "runspec.h"
 
