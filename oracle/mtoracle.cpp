@@ -8,19 +8,23 @@
 //   * MaterialBase::prepare / average           material.C:37-110
 //   * MaterialBase::getrstop / rstop / rpstop   material.C:114-281
 //   * SampleLayers::lookupLayer                 sample_layers.C:27-43
-//   * TrimBase::trim (one cascade member)       trim.C:36-425
+//   * sampleClusters::lookupCluster             sample_clusters.C:42-130
+//   * TrimBase::trim (one cascade member)       trim.C:36-425, with the universal,
+//     Moliere and C-Kr potentials of TrimBase::_potential (trim.C:194-258)
 //   * runmytrim's seeding and FIFO cascade loop apps/runmytrim.C:71-93, 287-304
-//   * tallies with TrimVacCount / TrimRange / TrimPhononOut semantics
-//     (apps/src/TrimVacCount.C:32-54, apps/src/TrimRange.C:32-47, trim.C:504-527)
+//   * tallies with TrimVacCount / TrimVacEnergyCount / TrimRange / TrimPrimaries /
+//     TrimRecoils / TrimPhononOut semantics (apps/src/TrimVacCount.C:32-54,
+//     apps/src/TrimVacEnergyCount.C:32-53, apps/src/TrimRange.C:32-47,
+//     trim.C:446-464, trim.C:504-527) and runmytrim's output files (runspec.h)
 // Every floating-point expression is evaluated in the same order as the
 // reference, and the same libm functions are called, so that with mt19937
 // seeding ("seeding compat") the results are bit-identical to the reference
-// library (checked by tests/test_oracle_pin.py against oracle/_ref/ref_driver
-// and against the committed fixtures in tests/golden/).
+// library (checked by tests/test_oracle.py against oracle/_ref/ref_driver and
+// against the committed fixtures in tests/golden/).
 //
 // "seeding philox" replaces the mt19937 stream by the counter-based Philox4x32-10
-// streams the CUDA engine uses (keyed by cascade member and collision index), so
-// that the GPU and this oracle draw the same random numbers.
+// streams the CUDA engine's FP64 path uses (keyed by cascade member and collision
+// index), so that the GPU and this oracle draw the same random numbers.
 //
 // Usage:  mtoracle <tables.tsv> < spec      (spec format: oracle/runspec.h)
 
