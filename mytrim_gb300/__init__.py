@@ -5,7 +5,7 @@ include/mytrim_gpu.h); this package is its Python front.
 """
 from .engine import ElementSpec, Engine, LayerSpec, SimSpec, summarize
 from .api import (Element, IonBase, MaterialBase, SampleBase, SampleLayers, SampleSolid, SimconfType,
-                  TrimGPU)
+                  TrimGPU, sampleClusters)
 
 __all__ = ["Engine", "SimSpec", "LayerSpec", "ElementSpec", "summarize", "SimconfType", "Element",
-           "MaterialBase", "SampleBase", "SampleSolid", "SampleLayers", "IonBase", "TrimGPU"]
+           "MaterialBase", "SampleBase", "SampleSolid", "SampleLayers", "sampleClusters", "IonBase", "TrimGPU"]

@@ -88,6 +88,36 @@ class SampleLayers(SampleBase):
         return [m._layer(t) for m, t in zip(self.material, self.layerThickness)]
 
 
+class sampleClusters(SampleBase):
+    """Spheres of material[1] in a matrix of material[0] (sample_clusters.h:30-57),
+    found through a spatial hash of initSpatialhash(x, y, z) cells."""
+
+    def __init__(self, x: float, y: float, z: float):
+        super().__init__(x, y, z)
+        self.kn = [1, 1, 1]
+        self.c: List[List[float]] = [[], [], [], []]  # x, y, z, r per cluster
+
+    def initSpatialhash(self, x: int, y: int, z: int):
+        self.kn = [int(x), int(y), int(z)]
+
+    def addCluster(self, x: float, y: float, z: float, r: float):
+        for v, lst in zip((x, y, z, r), self.c):
+            lst.append(float(v))
+
+    @property
+    def cn(self) -> int:
+        return len(self.c[0])
+
+    def _layers(self):
+        if len(self.material) != 2:
+            raise ValueError("a cluster sample needs two materials (matrix, cluster)")
+        return [m._layer(self.w[0]) for m in self.material]
+
+    def _cluster_array(self):
+        import numpy as np
+        return np.array(self.c, dtype=np.float64).T.reshape(-1, 4)
+
+
 class IonBase:
     """Ion template (ion.h:30-85)."""
 
@@ -100,34 +130,54 @@ class IonBase:
 
 
 class TrimGPU:
-    """Drop-in for a runmytrim TrimBase subclass (TrimVacCount / TrimRange with
-    TrimPhononOut energy accounting), running every primary's full cascade on the GPU."""
+    """Drop-in for a runmytrim TrimBase subclass (TrimVacCount / TrimRange /
+    TrimPrimaries / TrimRecoils with TrimPhononOut energy accounting), running every
+    primary's full cascade on the GPU.  ``output`` is "vaccount", "range" or
+    "primaries" (with ``max_generation`` 1 for TrimPrimaries, 2 for TrimRecoils)."""
 
     # TrimBase::Potential (trim.h:63-69); assign one to _potential
     UNIVERSAL, MOLIERE, CKR = 0, 1, 2
 
     def __init__(self, simconf: SimconfType, sample: SampleBase, precision: str = "fp64", device: int = 0,
-                 output: str = "vaccount", primaries_only: bool = False):
-        if not isinstance(sample, (SampleSolid, SampleLayers)):
-            raise TypeError("TrimGPU supports SampleSolid and SampleLayers")
+                 output: str = "vaccount", primaries_only: bool = False, max_generation: int = 1):
+        if not isinstance(sample, (SampleSolid, SampleLayers, sampleClusters)):
+            raise TypeError("TrimGPU supports SampleSolid, SampleLayers and sampleClusters")
         self._simconf = simconf
         self._sample = sample
         self._potential = self.UNIVERSAL
         self._output = output
         self._primaries_only = primaries_only
+        self._max_generation = max_generation
         self._engine = Engine(device=device, precision=precision, seed=simconf._seed, tmin=simconf.tmin,
                               tau=simconf.tau, cw=simconf.cw, length_scale=simconf.lengthScale())
 
-    def runPrimaries(self, pka: IonBase, n: int, hist_range=(10.0, 0), hist_vac=(1.0, 0)) -> dict:
-        s = self._sample
-        spec = SimSpec(layers=s._layers(), Z=pka._Z, m=pka._m, E=pka._E, n_primaries=n, Ef=pka._Ef,
-                       dir=tuple(pka._dir), pos=tuple(pka._pos) if pka._pos else None, size=tuple(s.w),
-                       bc=tuple(s.bc), mode=self._output, primaries_only=self._primaries_only,
-                       hist_range_bin=hist_range[0], hist_range_n=hist_range[1], hist_vac_bin=hist_vac[0],
-                       hist_vac_n=hist_vac[1], potential=("universal", "moliere", "ckr")[self._potential])
-        r = self._engine.run([spec])[0]
+    def _spec(self, sample: SampleBase, pka: IonBase, n: int, hist_range, hist_vac) -> SimSpec:
+        extra = {}
+        if isinstance(sample, sampleClusters):
+            extra = dict(geometry="clusters", clusters=sample._cluster_array(), cluster_hash=tuple(sample.kn))
+        return SimSpec(layers=sample._layers(), Z=pka._Z, m=pka._m, E=pka._E, n_primaries=n, Ef=pka._Ef,
+                       dir=tuple(pka._dir), pos=tuple(pka._pos) if pka._pos else None, size=tuple(sample.w),
+                       bc=tuple(sample.bc), mode=self._output, max_generation=self._max_generation,
+                       primaries_only=self._primaries_only, hist_range_bin=hist_range[0],
+                       hist_range_n=hist_range[1], hist_vac_bin=hist_vac[0], hist_vac_n=hist_vac[1],
+                       potential=("universal", "moliere", "ckr")[self._potential], **extra)
+
+    def _account(self, r: dict):
         sc = self._simconf
         sc.EelTotal += r["Eel"]
         sc.EnucTotal += r["Enuc"]
         sc.vacancies_created += r["vacancies"]
+
+    def runPrimaries(self, pka: IonBase, n: int, hist_range=(10.0, 0), hist_vac=(1.0, 0)) -> dict:
+        r = self._engine.run([self._spec(self._sample, pka, n, hist_range, hist_vac)])[0]
+        self._account(r)
         return summarize(r)
+
+    def runBatch(self, jobs, hist_range=(10.0, 0), hist_vac=(1.0, 0)) -> list:
+        """Several independent simulations in one launch: jobs of (sample, pka, n)."""
+        specs = [self._spec(smp, pka, n, hist_range, hist_vac) for smp, pka, n in jobs]
+        out = []
+        for r in self._engine.run(specs):
+            self._account(r)
+            out.append(summarize(r))
+        return out
