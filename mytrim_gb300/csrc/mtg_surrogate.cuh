@@ -20,6 +20,7 @@
 // memory.
 #pragma once
 
+#include <cstddef>
 #include <stdint.h>
 #include <cuda_bf16.h>
 
@@ -36,7 +37,9 @@ constexpr float SG_Y0 = 4.0f;   // output 0 scale (e-folds)
 constexpr float SG_Y1 = 10.0f;  // output 1 scale (reduced length)
 
 // Inference layout of the network (built from the flat FP32 parameter vector).
-struct SurrogateNet
+// 16-byte aligned: the BF16 weight rows (144 bytes apart, from byte offsets 768 and
+// 10240) are read with ldmatrix, which wants 16-byte aligned row addresses.
+struct alignas(16) SurrogateNet
 {
   float w1[SG_H][2];
   float b1[SG_H];
@@ -48,6 +51,9 @@ struct SurrogateNet
   float b4[2];
   float pad[2];
 };
+static_assert(sizeof(SurrogateNet) % 16 == 0 && offsetof(SurrogateNet, w2) % 16 == 0 &&
+                  offsetof(SurrogateNet, w3) % 16 == 0 && (SG_LD * 2) % 16 == 0,
+              "ldmatrix alignment of the weight rows");
 
 __host__ __device__ __forceinline__ bool
 surrogate_in_domain(float eps, float b)
@@ -99,12 +105,27 @@ mma_bf16(float (&c)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
                : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
+// Four 8x8 BF16 tiles of shared memory into the B fragments of two m16n8k16
+// products: lanes 8i..8i+7 give the row addresses of tile i (16-byte aligned rows).
+__device__ __forceinline__ void
+ldsm_x4(uint32_t (&r)[4], const void * p)
+{
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"((uint32_t)__cvta_generic_to_shared(p)));
+}
+
 // One 64x64 hidden layer for one 16-row tile: A fragments in, accumulator
-// fragments of the 8 column tiles out (bias added).
+// fragments of the 8 column tiles out (bias added).  The weights w[out][in] are the
+// B operand in column-major form; each ldmatrix.x4 brings the B fragments of two
+// consecutive 16-wide k chunks of one 8-wide column tile (tile i of the four:
+// k chunk 2 kp + i / 2, its lower or upper 8 columns by i % 2).
 __device__ __forceinline__ void
 hidden_layer(const __nv_bfloat16 (*w)[SG_LD], const float * bias, const uint32_t (&a)[4][4], float (&c)[8][4],
              int g, int t)
 {
+  const int lane = threadIdx.x & 31;
+  const int mrow = lane & 7, msel = lane >> 3;
 #pragma unroll
   for (int nt = 0; nt < 8; ++nt)
   {
@@ -114,12 +135,12 @@ hidden_layer(const __nv_bfloat16 (*w)[SG_LD], const float * bias, const uint32_t
     c[nt][2] = b0;
     c[nt][3] = b1v;
 #pragma unroll
-    for (int kc = 0; kc < 4; ++kc)
+    for (int kp = 0; kp < 2; ++kp)
     {
-      const uint32_t * row = reinterpret_cast<const uint32_t *>(&w[nt * 8 + g][0]);
-      const uint32_t bb0 = lds_u32(row + kc * 8 + t);
-      const uint32_t bb1 = lds_u32(row + kc * 8 + 4 + t);
-      mma_bf16(c[nt], a[kc], bb0, bb1);
+      uint32_t r[4];
+      ldsm_x4(r, &w[nt * 8 + mrow][(2 * kp + (msel >> 1)) * 16 + (msel & 1) * 8]);
+      mma_bf16(c[nt], a[2 * kp], r[0], r[1]);
+      mma_bf16(c[nt], a[2 * kp + 1], r[2], r[3]);
     }
   }
 }
