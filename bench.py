@@ -19,7 +19,8 @@ Printed JSON line (rank 0):
                relative difference of mean projected range fast vs FP64
   roofline     the cascade kernel: 391 algorithmic operations per collision (300 + 91
                per target element) against the FP32 issue rate, SMs x 128 lanes x
-               the measured SM clock
+               the measured SM clock; paths.*.roofline_frac the same for each path
+               against its own unit (FP64: 2 lanes per SM)
   cpu_baseline the CPU oracle (reference algorithm and RNG) on the host cores
 --impl reference times the reference's CPU implementation of the path (the
 reference library itself where it was built from source, else the oracle port
@@ -362,6 +363,7 @@ def main():
         if PARAMS.exists():
             sg, sg_rate, sg_agg = time_path("surrogate", 2, 1000, a.surrogate_batch)
             paths["surrogate"] = {"value": sg_rate, "unit": UNIT, "summary": sg,
+                                  "collisions_per_s": sg_rate * sg_agg["collisions"] / max(sg_agg["primaries"], 1),
                                   "fallback_fraction": sg_agg["surrogate_fallbacks"] / max(sg_agg["collisions"], 1)}
     fp64 = None
     if not a.no_fp64 and prec != "fp64":
@@ -400,6 +402,14 @@ def main():
     props = torch.cuda.get_device_properties(local)
     sm_mhz = clocks.get("sm_mhz") or 1920.0
     peak = props.multi_processor_count * 128 * sm_mhz * 1e6 / 1e12
+    # every path against the issue rate of the unit its arithmetic runs on (FP32
+    # lanes for the FP32 and surrogate paths, the 2 FP64 lanes per SM for the plain
+    # path), with the same algorithmic operations per collision
+    lanes = {"fp32": 128, "surrogate": 128, "fp64": 2}
+    for name, v in paths.items():
+        if v.get("collisions_per_s") and name in lanes:
+            unit_peak = props.multi_processor_count * lanes[name] * sm_mhz * 1e6
+            v["roofline_frac"] = v["collisions_per_s"] * W_COLL / unit_peak
     per_launch_coll = colls / a.steps
     kms = statistics.mean(kernel_ms)
     achieved = per_launch_coll * W_COLL / (kms / 1e3) / 1e12
