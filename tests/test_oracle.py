@@ -18,6 +18,7 @@ import subprocess
 import sys
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
@@ -61,6 +62,18 @@ def test_restatement_matches_reference_live(oracle_built, seed):
                 hist_range_bin=7.0, hist_range_n=80, hist_vac_bin=3.0, hist_vac_n=80),
         SimSpec(layers=[LayerSpec(1e5, 2.33, [ElementSpec(14, 28.086, 1.0, 15.0, 3.0)])], Z=3, m=7.016,
                 E=40e3, n_primaries=20, mode="range", primaries_only=True),
+        SimSpec(layers=[LayerSpec(1e5, 8.96, [ElementSpec(29, 63.546, 1.0, 25.0, 3.0)])], Z=29, m=63.546,
+                E=3e3, n_primaries=10, potential="moliere", hist_range_bin=5.0, hist_range_n=50),
+        SimSpec(layers=[LayerSpec(1e5, 2.26, [ElementSpec(6, 12.011, 1.0, 28.0, 3.0)])], Z=36, m=83.798,
+                E=5e3, n_primaries=10, potential="ckr"),
+        SimSpec(layers=[LayerSpec(1e5, 3.21, [ElementSpec(14, 28.086, 1.0, 35.0, 3.0),
+                                              ElementSpec(6, 12.011, 1.0, 20.0, 3.0)])],
+                Z=54, m=131.29, E=10e3, n_primaries=10, mode="primaries", max_generation=seed % 2 + 1),
+        SimSpec(layers=[LayerSpec(300.0, 10.0, [ElementSpec(92, 235.0, 1.0), ElementSpec(8, 16.0, 2.0)]),
+                        LayerSpec(300.0, 3.5, [ElementSpec(54, 132.0, 1.0)])],
+                Z=54, m=132.0, E=10e3, n_primaries=6, pos=(0.0, 150.0, 150.0), size=(300.0, 300.0, 300.0),
+                geometry="clusters", clusters=np.array([[60.0, 150.0, 150.0, 25.0], [200.0, 100.0, 120.0, 15.0]]),
+                cluster_hash=(10, 10, 10)),
     ]
     for sim in sims:
         a = oracle_built.run(sim, seed=seed, philox=False, records=sim.n_primaries)
