@@ -100,13 +100,14 @@ def parse(text):
     return out
 
 
-def run(sim, seed=1, philox=True, first=0, n=None, records=0, reference=False, timeout=None):
-    """Run one oracle process on primaries [first, first + n)."""
+def run(sim, seed=1, philox=True, first=0, n=None, records=0, reference=False, timeout=None, scale=1.0):
+    """Run one oracle process on primaries [first, first + n); scale is the
+    sample's length unit in Angstrom (SimconfType::setLengthScale)."""
     exe = REF_DRIVER if reference else MTORACLE
     if not exe.exists():
         raise RuntimeError(f"{exe} is not built")
     args = [str(exe)] if reference else [str(exe), str(TABLES)]
-    txt = spec_text(sim, seed=seed, philox=philox, first=first, n=n, records=records)
+    txt = spec_text(sim, seed=seed, philox=philox, first=first, n=n, records=records, scale=scale)
     r = subprocess.run(args, input=txt, capture_output=True, text=True, timeout=timeout)
     if r.returncode != 0:
         raise RuntimeError(f"oracle failed: {r.stderr}")

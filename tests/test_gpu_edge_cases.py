@@ -65,3 +65,25 @@ def test_empty_simulation_in_a_batch(engine_lib):
     assert r[0]["primaries"] == 0 and r[0]["members"] == 0 and r[0]["Eel"] == 0.0
     assert r[2]["primaries"] == 0
     assert r[1]["primaries"] == a.n_primaries
+
+
+def test_length_scale_gives_the_same_cascades(engine_lib):
+    """The reference's length-scale check (tests/json: xe_on_uo2 at scale 1 and 10 give
+    the same vacancy profile), made exact: positions in units of 10 A with a 10-times
+    smaller sample and bin width follow the same cascades (the random streams are
+    keyed by path, the flight lengths are in A either way), so the integer tallies
+    are equal and the depth profile agrees bin for bin up to rounding at bin edges."""
+    uo2 = [ElementSpec(92, 238.03, 1.0, 40.0, 3.0), ElementSpec(8, 15.999, 2.0, 20.0, 3.0)]
+    runs = []
+    for scale in (1.0, 10.0):
+        sim = SimSpec(layers=[LayerSpec(1e6 / scale, 10.97, uo2)], Z=54, m=131.29, E=30e3, n_primaries=300,
+                      hist_vac_bin=10.0 / scale, hist_vac_n=300, hist_range_bin=10.0 / scale, hist_range_n=300)
+        e = Engine(precision="fp64", seed=8, length_scale=scale)
+        runs.append(e.run([sim])[0])
+        e.close()
+    a, b = runs
+    for k in ("members", "collisions", "vacancies", "replacements", "interstitials", "range_n"):
+        assert a[k] == b[k], k
+    assert math.isclose(a["sx"], 10.0 * b["sx"], rel_tol=1e-9)
+    assert abs(a["hist_vac"] - b["hist_vac"]).sum() <= 0.002 * a["vacancies"]
+    assert abs(a["hist_range"] - b["hist_range"]).sum() <= 2

@@ -151,3 +151,23 @@ def test_reference_uo2_golden(oracle_built, tmp_path):
         for a, b in zip(got, ref):
             for x, y in zip(a, b):
                 assert abs(float(x) - float(y)) <= 1e-4
+
+
+def test_length_scale_invariance(oracle_built):
+    """The reference's length-scale check (tests/json: the xe_on_uo2 input at length
+    scale 1 and 10 gives the same vacancy profile), made exact for the restatement: a
+    sample in units of 10 A, ten times thinner with ten times finer bins, follows the
+    same cascades (flight lengths are drawn in A and divided by the scale, trim.C:45-46),
+    so the integer tallies agree and the depth profiles agree up to bin-edge rounding."""
+    uo2 = [ElementSpec(92, 238.03, 1.0, 40.0, 3.0), ElementSpec(8, 15.999, 2.0, 20.0, 3.0)]
+    runs = []
+    for scale in (1.0, 10.0):
+        sim = SimSpec(layers=[LayerSpec(1e6 / scale, 10.97, uo2)], Z=54, m=131.29, E=30e3, n_primaries=100,
+                      hist_vac_bin=10.0 / scale, hist_vac_n=300, hist_range_bin=10.0 / scale, hist_range_n=300)
+        runs.append(oracle_built.run(sim, seed=8, scale=scale))
+    a, b = runs
+    for k in ("members", "collisions", "vacancies", "replacements", "interstitials", "range_n"):
+        assert a[k] == b[k], k
+    assert math.isclose(a["sx"], 10.0 * b["sx"], rel_tol=1e-9)
+    assert np.abs(np.subtract(a["hist_vac"], b["hist_vac"])).sum() <= 0.002 * a["vacancies"]
+    assert np.abs(np.subtract(a["hist_range"], b["hist_range"])).sum() <= 2
