@@ -1,6 +1,7 @@
 """Regenerate the runmytrim fixtures of tests/golden/runmytrim from the reference.
 
-Each case is a runmytrim input (JSON, written here) and the output file the
+Each case is a runmytrim input (JSON, written here or read from the reference's
+tests/json with fewer ions) and the output file the
 reference's own plugin wrote for it: TrimVacCount (_vac.dat), TrimVacEnergyCount
 (_evac.dat) or TrimRange (_ranges.dat), compiled from the reference sources
 with oracle/Makefile ("make ref") and driven by oracle/_ref/ref_runmytrim with
@@ -13,6 +14,7 @@ Usage: python tests/golden/make_runmytrim_golden.py
 """
 import json
 import os
+import re
 import shutil
 import sys
 import tempfile
@@ -72,6 +74,23 @@ CASES = {
 }
 
 
+# the reference's own runmytrim tests (tests/json: 150 keV Cu on a Cu film, 10 MeV Xe
+# into UO2 at length scale 1 and 10), read from the reference checkout with their
+# comments kept, renamed json_<name> and run with a tenth of the ions
+JSON_TESTS = {"cu_on_cu": 100, "xe_on_uo2": 10, "xe_on_uo2_scale10": 10}
+
+
+def reference_json_cases():
+    out = {}
+    for stem, number in JSON_TESTS.items():
+        text = (REF / "tests" / "json" / f"{stem}.json").read_text()
+        text, n_base = re.subn(r'("base"\s*:\s*")' + stem + '"', r'\g<1>json_' + stem + '"', text)
+        text, n_num = re.subn(r'("number"\s*:\s*)\d+', r'\g<1>' + str(number), text)
+        assert n_base == 1 and n_num == 1, stem
+        out[f"json_{stem}"] = text
+    return out
+
+
 def render(name, d):
     d = json.loads(json.dumps(d))
     d["mytrim"]["output"]["base"] = name
@@ -86,8 +105,9 @@ def render(name, d):
 def main():
     oracle_io.build(REF)
     OUT.mkdir(exist_ok=True)
-    for name, d in CASES.items():
-        text = render(name, d)
+    texts = {name: render(name, d) for name, d in CASES.items()}
+    texts.update(reference_json_cases())
+    for name, text in texts.items():
         (OUT / f"{name}.json").write_text(text)
         inp = runmytrim.load(text)
         with tempfile.TemporaryDirectory() as tmp:

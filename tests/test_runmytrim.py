@@ -144,3 +144,20 @@ def test_frontend_rejects_arguments_and_bad_json(frontend):
     r = subprocess.run([str(frontend), "--check-input"], input='{"mytrim": {', capture_output=True, text=True,
                        timeout=60)
     assert r.returncode == 1 and r.stderr.startswith("ERROR: cannot parse")
+
+
+def test_reference_length_scale_profiles():
+    """The reference's length-scale test (tests/json/README.md: the xe_on_uo2 vacancy
+    profile against the xe_on_uo2_scale10 one with depth x 10): in the reference's own
+    output files the 1 A bins of the scale-1 run, summed ten at a time, give the 10 A
+    bins of the scale-10 run exactly, except bin 0, which TrimVacCount's truncating
+    int() also fills from the first sample unit in front of the surface (-1 A at scale
+    1, -10 A at scale 10)."""
+    import numpy as np
+    a = np.loadtxt(GOLD / "json_xe_on_uo2_vac.dat")
+    b = np.loadtxt(GOLD / "json_xe_on_uo2_scale10_vac.dat")
+    rebinned = np.zeros((len(b), 2))
+    np.add.at(rebinned, a[:, 0].astype(int) // 10, a[:, 1:])
+    assert np.array_equal(rebinned[1:], b[1:, 1:])
+    assert (b[0, 1:] >= rebinned[0]).all()
+    assert (GOLD / "json_xe_on_uo2.summary").read_text() == (GOLD / "json_xe_on_uo2_scale10.summary").read_text()
