@@ -160,7 +160,7 @@ kernel_level(const mtg_ctx * ctx)
 {
   const HostTables & t = ctx->tables;
   if (ctx->event_cap > 0 && ctx->event_mask)
-    return LVL_FULL;
+    return t.any_extended ? LVL_FULL : LVL_EVENTS;
   if (t.any_extended)
     return LVL_GEO;
   if (ctx->record_cap > 0 || t.voxel_total > 0 || t.any_evac || t.any_mode)

@@ -206,26 +206,29 @@ struct LaneCold
 
 // Kernel feature levels.  Code for a feature a run does not use still costs the
 // collision loop (instruction fetch, registers), so the cascade kernel comes in
-// four variants and each run takes the smallest that has what it needs:
-//   LVL_LEAN  layered samples, universal potential, TrimVacCount tallies (depth,
-//             range and lateral histograms), CUT boundaries and sputter counting;
-//   LVL_MID   + member records, deposition voxels, the vacancy-energy histogram,
-//             TrimRange / TrimPrimaries tally modes;
-//   LVL_GEO   + the cluster geometry, the Moliere and C-Kr potentials;
-//   LVL_FULL  + the event log.
+// five variants and each run takes the smallest that has what it needs:
+//   LVL_LEAN    layered samples, universal potential, TrimVacCount tallies (depth,
+//               range and lateral histograms), CUT boundaries and sputter counting;
+//   LVL_MID     + member records, deposition voxels, the vacancy-energy histogram,
+//               TrimRange / TrimPrimaries tally modes;
+//   LVL_EVENTS  LVL_MID + the event log (no cluster geometry, universal potential);
+//   LVL_GEO     LVL_MID + the cluster geometry, the Moliere and C-Kr potentials;
+//   LVL_FULL    LVL_GEO + the event log.
 enum KernelLevel : int
 {
   LVL_LEAN = 0,
   LVL_MID = 1,
-  LVL_GEO = 2,
-  LVL_FULL = 3
+  LVL_EVENTS = 2,
+  LVL_GEO = 3,
+  LVL_FULL = 4,
+  LVL_COUNT = 5
 };
 
 // Device tally sink for one lane of a kernel of level LVL.
 template <class Pol, int LVL>
 struct LaneSink
 {
-  static constexpr bool EV = LVL >= LVL_FULL; // feeds the event log
+  static constexpr bool EV = LVL == LVL_EVENTS || LVL == LVL_FULL; // feeds the event log
   static constexpr bool MID = LVL >= LVL_MID;
   using Acc = typename Pol::Acc;       // rare sums (kept in shared memory)
   using AccHot = typename Pol::AccHot; // per-collision sums (registers)

@@ -105,6 +105,7 @@ launch_cascade64(const EngineParams & prm, int grid, int block, size_t smem, cud
   {
     case LVL_LEAN: cascade_kernel<Fp64Policy, LVL_LEAN><<<grid, block, smem, st>>>(prm, tabs); break;
     case LVL_MID: cascade_kernel<Fp64Policy, LVL_MID><<<grid, block, smem, st>>>(prm, tabs); break;
+    case LVL_EVENTS: cascade_kernel<Fp64Policy, LVL_EVENTS><<<grid, block, smem, st>>>(prm, tabs); break;
     case LVL_GEO: cascade_kernel<Fp64Policy, LVL_GEO><<<grid, block, smem, st>>>(prm, tabs); break;
     default: cascade_kernel<Fp64Policy, LVL_FULL><<<grid, block, smem, st>>>(prm, tabs); break;
   }
@@ -129,14 +130,15 @@ occupancy_of(K kernel, int block, size_t smem, int * blocks_per_sm)
 cudaError_t
 occupancy64(int block, size_t smem, int * blocks_per_sm, int level)
 {
-  int occ[4] = {0, 0, 0, 0};
+  int occ[LVL_COUNT] = {};
   cudaError_t e;
-  if ((e = occupancy_of(cascade_kernel<Fp64Policy, LVL_LEAN>, block, smem, &occ[0])) != cudaSuccess ||
-      (e = occupancy_of(cascade_kernel<Fp64Policy, LVL_MID>, block, smem, &occ[1])) != cudaSuccess ||
-      (e = occupancy_of(cascade_kernel<Fp64Policy, LVL_GEO>, block, smem, &occ[2])) != cudaSuccess ||
-      (e = occupancy_of(cascade_kernel<Fp64Policy, LVL_FULL>, block, smem, &occ[3])) != cudaSuccess)
+  if ((e = occupancy_of(cascade_kernel<Fp64Policy, LVL_LEAN>, block, smem, &occ[LVL_LEAN])) != cudaSuccess ||
+      (e = occupancy_of(cascade_kernel<Fp64Policy, LVL_MID>, block, smem, &occ[LVL_MID])) != cudaSuccess ||
+      (e = occupancy_of(cascade_kernel<Fp64Policy, LVL_EVENTS>, block, smem, &occ[LVL_EVENTS])) != cudaSuccess ||
+      (e = occupancy_of(cascade_kernel<Fp64Policy, LVL_GEO>, block, smem, &occ[LVL_GEO])) != cudaSuccess ||
+      (e = occupancy_of(cascade_kernel<Fp64Policy, LVL_FULL>, block, smem, &occ[LVL_FULL])) != cudaSuccess)
     return e;
-  *blocks_per_sm = occ[level < 0 ? 0 : (level > 3 ? 3 : level)];
+  *blocks_per_sm = occ[level < 0 ? 0 : (level >= LVL_COUNT ? LVL_COUNT - 1 : level)];
   return cudaSuccess;
 }
 

@@ -230,16 +230,19 @@ def test_invalid_potential_is_rejected(engine_lib):
 
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
-def test_kernel_levels_agree(engine_lib, prec):
-    """The lean, mid and full kernel variants (chosen by the features a run uses:
-    none, member records, the event log) give the same tallies on the same streams."""
-    sim = SimSpec(**{**CASES["as_sio2_si_cut"][0].__dict__, "n_primaries": 400})
+@pytest.mark.parametrize("potential", ["universal", "moliere"])
+def test_kernel_levels_agree(engine_lib, prec, potential):
+    """The kernel variants (chosen by the features a run uses: none, member records,
+    the event log; the Moliere potential takes the geometry-level variants) give the
+    same tallies on the same streams: lean, mid and events with the universal
+    potential, geometry and full with Moliere."""
+    sim = SimSpec(**{**CASES["as_sio2_si_cut"][0].__dict__, "n_primaries": 400, "potential": potential})
     out = []
-    for level in ("lean", "mid", "full"):
+    for level in ("plain", "records", "events"):
         e = Engine(precision=prec, seed=4)
-        if level == "mid":
+        if level == "records":
             e.set_record_capacity(1 << 20)
-        if level == "full":
+        if level == "events":
             e.set_event_log([F.EV_VACANCY], 1 << 20)
         out.append(e.run([sim])[0])
         e.close()
