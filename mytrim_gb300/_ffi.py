@@ -4,7 +4,6 @@ The library is the product: if it is missing or fails to load, importing the
 engine raises -- there is no CPU fallback.
 """
 import ctypes as C
-import os
 from pathlib import Path
 
 MAX_ELEMENTS = 4

@@ -6,7 +6,7 @@ primary count and the tally options of apps/runmytrim.C:103-285).
 """
 import ctypes as C
 import math
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 from pathlib import Path
 from typing import List, Optional, Sequence, Tuple
 

@@ -6,7 +6,6 @@ writes the same text for the same doubles."""
 import subprocess
 
 import numpy as np
-import pytest
 
 from mytrim_gb300 import _ffi as F
 from mytrim_gb300 import streams
