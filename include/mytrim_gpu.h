@@ -232,6 +232,10 @@ typedef struct
   long long d2h_bytes;     /* device-to-host bytes of the last collect */
   long long warp_steps;    /* collision-loop iterations of all warps in the last run; the
                               lane occupancy is collisions / (32 warp_steps) */
+  int kernel_level;        /* feature level of the last run's cascade kernel: 0 lean, 1 member
+                              records / voxels / tally modes, 2 + event log, 3 cluster geometry
+                              or a non-universal potential, 4 + event log */
+  int pad_stats;
 } mtg_stats;
 
 typedef struct mtg_ctx mtg_ctx;

@@ -121,8 +121,12 @@ class Stats(C.Structure):
     _fields_ = [("kernel_ms", C.c_double), ("reduce_ms", C.c_double), ("launches", C.c_int),
                 ("drains", C.c_int), ("grid", C.c_int), ("block", C.c_int), ("stack_capacity", C.c_int),
                 ("overflowed", C.c_longlong), ("collisions", C.c_longlong), ("device_bytes", C.c_size_t),
-                ("h2d_bytes", C.c_longlong), ("d2h_bytes", C.c_longlong), ("warp_steps", C.c_longlong)]
+                ("h2d_bytes", C.c_longlong), ("d2h_bytes", C.c_longlong), ("warp_steps", C.c_longlong),
+                ("kernel_level", C.c_int), ("pad_stats", C.c_int)]
 
+
+# mtg_stats.kernel_level values
+KERNEL_LEVELS = ("lean", "mid", "events", "geometry", "full")
 
 # symbol -> (restype, argtypes); must match include/mytrim_gpu.h
 _P = C.c_void_p

@@ -319,6 +319,7 @@ fill_params(mtg_ctx * ctx, EngineParams & prm)
   }
   prm.any_evac = t.any_evac;
   prm.level = kernel_level(ctx);
+  ctx->stats.kernel_level = prm.level;
   prm.warp_steps = ptr<unsigned long long>(ctx->d_counters) + C_STEPS;
 }
 

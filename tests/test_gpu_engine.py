@@ -237,14 +237,16 @@ def test_kernel_levels_agree(engine_lib, prec, potential):
     same tallies on the same streams: lean, mid and events with the universal
     potential, geometry and full with Moliere."""
     sim = SimSpec(**{**CASES["as_sio2_si_cut"][0].__dict__, "n_primaries": 400, "potential": potential})
+    want = ("lean", "mid", "events") if potential == "universal" else ("geometry", "geometry", "full")
     out = []
-    for level in ("plain", "records", "events"):
+    for level, name in zip(("plain", "records", "events"), want):
         e = Engine(precision=prec, seed=4)
         if level == "records":
             e.set_record_capacity(1 << 20)
         if level == "events":
             e.set_event_log([F.EV_VACANCY], 1 << 20)
         out.append(e.run([sim])[0])
+        assert F.KERNEL_LEVELS[e.stats()["kernel_level"]] == name, (level, name)
         e.close()
     for r in out[1:]:
         if prec == "fp64":
