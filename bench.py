@@ -161,7 +161,7 @@ def have_reference_build():
         return False
     try:
         subprocess.run([str(ref)], input="ion 1 1.0 1.0 0\nlayer 1 1\nelement 1 1 1\n", capture_output=True,
-                       timeout=30, check=True)
+                       text=True, timeout=30, check=True)
         return True
     except Exception:
         return False
