@@ -388,7 +388,23 @@ typedef struct
   float lr;                /* Adam learning rate (cosine decay to 2 %) */
   unsigned long long seed;
   float w_tau;             /* loss weight of the time-integral output */
+  int target;              /* sin^2(theta/2) target of each sample: MTG_SURROGATE_TARGET_* */
+  int weighting;           /* loss weight of each sample's sin^2(theta/2): MTG_SURROGATE_WEIGHT_* */
 } mtg_surrogate_config;
+
+/* Training targets for sin^2(theta/2); the time-integral output is always the
+ * quadrature's.  QUADRATURE: FP64 Gauss-Mehler quadrature of the scattering integral
+ * (the true integral).  MAGIC: the FP64 magic formula with the reference's Newton
+ * solve (trim.C:180-271) at the same samples, the formula the plain path and the
+ * FP64 oracle evaluate. */
+#define MTG_SURROGATE_TARGET_QUADRATURE 0
+#define MTG_SURROGATE_TARGET_MAGIC 1
+/* Loss weights.  UNIFORM: every sample's error in ln sin^2(theta/2) counts the same.
+ * TRANSFER: weighted by the sample's sin^2(theta/2) (plus 1e-6), the share of the
+ * beam energy and of the angular diffusion theta^2 the collision carries; the
+ * weights are normalised to mean 1 over the training set. */
+#define MTG_SURROGATE_WEIGHT_UNIFORM 0
+#define MTG_SURROGATE_WEIGHT_TRANSFER 1
 
 typedef struct
 {

@@ -107,7 +107,12 @@ EV_VACANCY, EV_REPLACEMENT, EV_BRANCH, EV_DISSIPATE, EV_REST, EV_LOST, EV_HISTOR
 
 class SurrogateConfig(C.Structure):
     _fields_ = [("n_train", C.c_longlong), ("batch", C.c_int), ("epochs", C.c_int), ("qat_epochs", C.c_int),
-                ("lr", C.c_float), ("seed", C.c_ulonglong), ("w_tau", C.c_float)]
+                ("lr", C.c_float), ("seed", C.c_ulonglong), ("w_tau", C.c_float), ("target", C.c_int),
+                ("weighting", C.c_int)]
+
+
+SURROGATE_TARGETS = {"quadrature": 0, "magic": 1}  # MTG_SURROGATE_TARGET_*
+SURROGATE_WEIGHTS = {"uniform": 0, "transfer": 1}  # MTG_SURROGATE_WEIGHT_*
 
 
 class SurrogateReport(C.Structure):

@@ -1085,13 +1085,15 @@ mtg_surrogate_train(mtg_ctx * ctx, const mtg_surrogate_config * cfg, mtg_surroga
   if (st != MTG_OK)
     return st;
   if (!cfg || cfg->n_train < 1024 || cfg->batch < 32 || cfg->batch > cfg->n_train || cfg->epochs < 1 ||
-      cfg->qat_epochs < 0 || cfg->qat_epochs > cfg->epochs || !(cfg->lr > 0.0f))
+      cfg->qat_epochs < 0 || cfg->qat_epochs > cfg->epochs || !(cfg->lr > 0.0f) ||
+      (cfg->target != MTG_SURROGATE_TARGET_QUADRATURE && cfg->target != MTG_SURROGATE_TARGET_MAGIC) ||
+      (cfg->weighting != MTG_SURROGATE_WEIGHT_UNIFORM && cfg->weighting != MTG_SURROGATE_WEIGHT_TRANSFER))
     return fail(ctx, MTG_ERR_BAD_INPUT, "bad surrogate training configuration");
   CK(ensure(ctx->d_sg_params, 4 * MTG_SURROGATE_NPARAM));
   CK(ensure(ctx->d_sg_net, surrogate_net_bytes()));
   double loss = 0.0, secs = 0.0;
   CK(surrogate_train(cfg->n_train, cfg->batch, cfg->epochs, cfg->qat_epochs, cfg->lr, cfg->seed, cfg->w_tau,
-                     ptr<float>(ctx->d_sg_params), ctx->d_sg_net.p, &loss, &secs));
+                     cfg->target, cfg->weighting, ptr<float>(ctx->d_sg_params), ctx->d_sg_net.p, &loss, &secs));
   ctx->sg_ready = true;
   if (rep)
   {

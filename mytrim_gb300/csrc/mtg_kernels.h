@@ -55,7 +55,8 @@ size_t surrogate_net_bytes();
 cudaError_t surrogate_gradients(const float * params_h, const float * x_h, const float * y_h, long long n,
                                 float w_tau, float * loss_h, float * grads_h);
 cudaError_t surrogate_train(long long n_train, int batch, int epochs, int qat_epochs, float lr,
-                            unsigned long long seed, float w_tau, float * params_dev, void * net_dev,
+                            unsigned long long seed, float w_tau, int target, int weighting, float * params_dev,
+                            void * net_dev,
                             double * final_loss, double * train_seconds);
 
 // Tally reduction (mtg_reduce.cu)

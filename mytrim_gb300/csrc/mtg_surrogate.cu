@@ -9,7 +9,9 @@
 //   both with the weight 1/sqrt(1 - u^2) absorbed: the integrands are evaluated as
 //   F(u) = sqrt(1 - u^2) / g(u) at the positive Chebyshev nodes u_j = cos((2j-1) pi / 2N).
 //   Samples are log-uniform in eps over [1e-4, 1e4] and area-weighted in b over
-//   [0, 12] (b = 12 sqrt(U)), drawn from Philox.
+//   [0, 12] (b = 12 sqrt(U)), drawn from Philox.  The sin^2(theta/2) target is the
+//   quadrature's or, on request, the FP64 magic formula's at the same samples
+//   (scatter64: the reference's Newton solve and magic formula, trim.C:180-271).
 // * Training: the project's own FP32 kernels -- dense forward, backward (data and
 //   weight gradients, deterministic two-stage reduction), MSE loss, Adam -- with the
 //   whole step captured in a CUDA graph.  The last epochs are quantisation-aware:
@@ -22,6 +24,8 @@
 #include <cstring>
 #include <vector>
 
+#include "mytrim_gpu.h"
+#include "mtg_collide64.cuh"
 #include "mtg_common.cuh"
 #include "mtg_kernels.h"
 #include "mtg_scatter32.cuh"
@@ -124,7 +128,8 @@ baseline_ln_s2(double eps, double b)
 }
 
 __global__ void
-make_training_data(long long n, uint32_t k0, uint32_t k1, uint32_t offset, float * x, float * y)
+make_training_data(long long n, uint32_t k0, uint32_t k1, uint32_t offset, int target, float * x, float * y,
+                   float * wts)
 {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n)
@@ -135,10 +140,29 @@ make_training_data(long long n, uint32_t k0, uint32_t k1, uint32_t offset, float
   const double eps = exp64(le * 2.302585092994046);
   double s2, tau;
   scatter_quadrature(eps, b, s2, tau);
+  if (target == MTG_SURROGATE_TARGET_MAGIC)
+  {
+    double ct, st;
+    int niter;
+    scatter64(eps, b, s2, ct, st, niter, 0);
+  }
   x[2 * i] = float(le * 0.25);
   x[2 * i + 1] = float(b / 6.0 - 1.0);
   y[2 * i] = float((log(fmax(s2, 1e-300)) - baseline_ln_s2(eps, b)) / SG_Y0);
   y[2 * i + 1] = float(tau / SG_Y1);
+  // energy-transfer weight of the sample's sin^2(theta/2) error: the energy given to
+  // the recoil is proportional to s2, and so is theta^2 at small angles (the angular
+  // diffusion); a floor keeps every sample in the fit
+  if (wts)
+    wts[i] = float(s2 + SG_WEIGHT_FLOOR);
+}
+
+__global__ void
+scale_weights(float * w, long long n, float f)
+{
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+    w[i] *= f;
 }
 
 // ------------------------------------------------------------------ training
@@ -192,15 +216,16 @@ dense_fwd(const float * X, int K, const float * W, const float * bias, int N, lo
     H[idx] = act ? silu_acc(z) : z;
 }
 
-// loss and output gradient: dO = 2 w_c (O - Y) / B
+// loss and output gradient: dO = 2 w_c (O - Y) / B; output 0 weighted per sample
+// by W (NULL: 1), output 1 by w1
 __global__ void
-loss_grad(const float * O, const float * Y, long long B, float w1, float * dO, float * loss_partial)
+loss_grad(const float * O, const float * Y, const float * W, long long B, float w1, float * dO, float * loss_partial)
 {
   __shared__ float red[256];
   float acc = 0.0f;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < B * 2; i += (long long)gridDim.x * blockDim.x)
   {
-    const float wc = (i & 1) ? w1 : 1.0f;
+    const float wc = (i & 1) ? w1 : (W ? W[i >> 1] : 1.0f);
     const float d = O[i] - Y[i];
     dO[i] = 2.0f * wc * d / float(B);
     acc += wc * d * d;
@@ -307,7 +332,8 @@ bump_step(int * step)
 
 // gather batch rows by a device-side step counter (epoch-cyclic)
 __global__ void
-gather_batch(const float * x, const float * y, long long n, long long B, const int * step, float * bx, float * by)
+gather_batch(const float * x, const float * y, const float * w, long long n, long long B, const int * step, float * bx,
+             float * by, float * bw)
 {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= B)
@@ -317,6 +343,8 @@ gather_batch(const float * x, const float * y, long long n, long long B, const i
   bx[2 * i + 1] = x[2 * src + 1];
   by[2 * i] = y[2 * src];
   by[2 * i + 1] = y[2 * src + 1];
+  if (w)
+    bw[i] = w[src];
 }
 
 // flat parameters -> inference layout
@@ -429,6 +457,7 @@ struct TrainBuffers
   long long B;
   int parts;
   float *bx, *by;                // batch inputs/targets [B][2]
+  float * bw;                    // per-sample loss weights of output 0 [B], or NULL
   float *z1, *h1, *z2, *h2, *z3, *h3, *o;
   float *d3, *d2, *d1, *dO;      // gradients of pre-activations
   float * P;                     // partial weight gradients
@@ -445,7 +474,7 @@ fwd_bwd(const float * w, float * g, const TrainBuffers & t, int quant, float w_t
   dense_fwd<<<blocks(B * 64), T, 64 * 64 * 4, st>>>(t.h1, 64, w + OFF.w2, w + OFF.b2, 64, B, t.z2, t.h2, 1, quant);
   dense_fwd<<<blocks(B * 64), T, 64 * 64 * 4, st>>>(t.h2, 64, w + OFF.w3, w + OFF.b3, 64, B, t.z3, t.h3, 1, quant);
   dense_fwd<<<blocks(B * 2), T, 2 * 64 * 4, st>>>(t.h3, 64, w + OFF.w4, w + OFF.b4, 2, B, t.o, nullptr, 0, 0);
-  loss_grad<<<64, 256, 0, st>>>(t.o, t.by, B, w_tau, t.dO, t.lossp);
+  loss_grad<<<64, 256, 0, st>>>(t.o, t.by, t.bw, B, w_tau, t.dO, t.lossp);
   // output layer
   dense_bwd_weight<<<dim3(2, t.parts), 64, 0, st>>>(t.dO, t.h3, 2, 64, B, t.parts, t.P, 0);
   reduce_parts<<<(2 * 64 + 2 + 127) / 128, 128, 0, st>>>(t.P, 2 * 64 + 2, t.parts, g + OFF.w4, g + OFF.b4, 2, 64);
@@ -534,7 +563,8 @@ surrogate_gradients(const float * params_h, const float * x_h, const float * y_h
 // Train from scratch.  params_out: SG_NPARAM floats; net_out: device SurrogateNet.
 cudaError_t
 surrogate_train(long long n_train, int batch, int epochs, int qat_epochs, float lr, unsigned long long seed,
-                float w_tau, float * params_dev, void * net_dev, double * final_loss, double * train_seconds)
+                float w_tau, int target, int weighting, float * params_dev, void * net_dev, double * final_loss,
+                double * train_seconds)
 {
   upload_nodes_once();
   cudaEvent_t e0, e1;
@@ -548,7 +578,7 @@ surrogate_train(long long n_train, int batch, int epochs, int qat_epochs, float 
     return e;
   };
   cudaError_t e = cudaSuccess;
-  float *x = nullptr, *y = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
+  float *x = nullptr, *y = nullptr, *wts = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
   int * step = nullptr;
   TrainBuffers t{};
   t.B = batch;
@@ -556,6 +586,11 @@ surrogate_train(long long n_train, int batch, int epochs, int qat_epochs, float 
   const size_t B = size_t(batch);
   e = e ? e : alloc((void **)&x, 2 * sizeof(float) * n_train);
   e = e ? e : alloc((void **)&y, 2 * sizeof(float) * n_train);
+  if (weighting)
+  {
+    e = e ? e : alloc((void **)&wts, sizeof(float) * n_train);
+    e = e ? e : alloc((void **)&t.bw, 4 * B);
+  }
   e = e ? e : alloc((void **)&g, 4 * SG_NPARAM);
   e = e ? e : alloc((void **)&m, 4 * SG_NPARAM);
   e = e ? e : alloc((void **)&v, 4 * SG_NPARAM);
@@ -576,7 +611,18 @@ surrogate_train(long long n_train, int batch, int epochs, int qat_epochs, float 
     return e;
   }
   uint32_t k0 = uint32_t(seed), k1 = uint32_t(seed >> 32) ^ 0x53474E4Eu;
-  make_training_data<<<(unsigned int)((n_train + 127) / 128), 128>>>(n_train, k0, k1, 0u, x, y);
+  make_training_data<<<(unsigned int)((n_train + 127) / 128), 128>>>(n_train, k0, k1, 0u, target, x, y, wts);
+  if (wts)
+  {
+    // normalise the weights to mean 1 over the training set
+    std::vector<float> hw(n_train);
+    e = cudaMemcpy(hw.data(), wts, sizeof(float) * n_train, cudaMemcpyDeviceToHost);
+    double sum = 0.0;
+    for (float w : hw)
+      sum += double(w);
+    if (!e && sum > 0.0)
+      scale_weights<<<(unsigned int)((n_train + 255) / 256), 256>>>(wts, n_train, float(double(n_train) / sum));
+  }
   // initial weights: uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) from a host LCG
   std::vector<float> w0(SG_NPARAM, 0.0f);
   uint64_t st = seed * 6364136223846793005ull + 1442695040888963407ull;
@@ -607,7 +653,8 @@ surrogate_train(long long n_train, int batch, int epochs, int qat_epochs, float 
     e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
     if (e)
       break;
-    gather_batch<<<(unsigned int)((batch + 255) / 256), 256, 0, s>>>(x, y, n_train, batch, step, t.bx, t.by);
+    gather_batch<<<(unsigned int)((batch + 255) / 256), 256, 0, s>>>(x, y, wts, n_train, batch, step, t.bx, t.by,
+                                                                      t.bw);
     fwd_bwd(params_dev, g, t, q, w_tau, s);
     adam_step<<<(SG_NPARAM + 255) / 256, 256, 0, s>>>(params_dev, g, m, v, SG_NPARAM, step, lr, 0.9f, 0.999f, 1e-8f,
                                                       0.02f, total);

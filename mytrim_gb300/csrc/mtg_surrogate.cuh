@@ -35,6 +35,8 @@ constexpr float SG_B_MAX = 12.0f;
 constexpr float SG_D4 = 0.20162f;
 constexpr float SG_Y0 = 4.0f;   // output 0 scale (e-folds)
 constexpr float SG_Y1 = 10.0f;  // output 1 scale (reduced length)
+constexpr float SG_EPS_NET_MAX = 10.0f; // above: the closed-form Rutherford branch (trim.C:172-179)
+constexpr double SG_WEIGHT_FLOOR = 1e-6; // floor of the energy-transfer loss weight
 
 // Inference layout of the network (built from the flat FP32 parameter vector).
 // 16-byte aligned: the BF16 weight rows (144 bytes apart, from byte offsets 768 and
@@ -55,11 +57,14 @@ static_assert(sizeof(SurrogateNet) % 16 == 0 && offsetof(SurrogateNet, w2) % 16 
                   offsetof(SurrogateNet, w3) % 16 == 0 && (SG_LD * 2) % 16 == 0,
               "ldmatrix alignment of the weight rows");
 
+// Where the network replaces the exact scattering: the trained domain (log10 eps in
+// [-4, 4], b in [0, 12]) cut at eps = 10, above which the exact path is the reference's
+// closed-form Rutherford branch (trim.C:172-179) -- cheaper than the network, and
+// exact.  The network stands in for the Newton solve and magic formula only.
 __host__ __device__ __forceinline__ bool
 surrogate_in_domain(float eps, float b)
 {
-  // log10(1e-4) .. log10(1e4), 0 <= b <= 12
-  return eps >= 1e-4f && eps <= 1e4f && b <= SG_B_MAX;
+  return eps >= 1e-4f && eps <= SG_EPS_NET_MAX && b <= SG_B_MAX;
 }
 
 // Weight reads from shared memory that the compiler may not hoist out of the

@@ -450,8 +450,13 @@ class Engine:
 
     # ---- learned scattering surrogate
     def surrogate_train(self, n_train=20_000_000, batch=16384, epochs=12, qat_epochs=2, lr=2e-3, seed=1,
-                        w_tau=0.1) -> dict:
-        cfg = F.SurrogateConfig(n_train, batch, epochs, qat_epochs, lr, seed, w_tau)
+                        w_tau=0.1, target="quadrature", weighting="uniform") -> dict:
+        """Train the network; target "quadrature" (the true scattering integral) or
+        "magic" (the magic formula the plain path evaluates, at the same samples);
+        weighting "uniform" or "transfer" (each sample's error weighted by its
+        sin^2(theta/2))."""
+        cfg = F.SurrogateConfig(n_train, batch, epochs, qat_epochs, lr, seed, w_tau, F.SURROGATE_TARGETS[target],
+                                F.SURROGATE_WEIGHTS[weighting])
         rep = F.SurrogateReport()
         self._check(self.lib.mtg_surrogate_train(self.ctx, C.byref(cfg), C.byref(rep)))
         return {"final_loss": rep.final_loss, "train_seconds": rep.train_seconds, "steps": rep.steps}

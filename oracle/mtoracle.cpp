@@ -819,6 +819,8 @@ struct Engine
     }
   }
 
+  double seed_sq = 0.0; // compat seeding: sum over distinct seeds of their use count squared
+
   void run()
   {
     std::vector<unsigned int> seeds;
@@ -828,6 +830,15 @@ struct Engine
       seeds.resize(spec.count);
       for (long long i = 0; i < spec.count; ++i)
         seeds[i] = uint16(mt);
+      // primaries that draw the same 16-bit seed repeat one cascade exactly: the
+      // sum over seeds of (primaries with that seed)^2 sets the variance of a
+      // run-wide mean (sum n_s^2 / N^2 times the per-cascade variance)
+      std::vector<long long> uses(65536, 0);
+      for (long long i = 0; i < spec.count; ++i)
+        uses[seeds[i] & 0xFFFFu]++;
+      seed_sq = 0.0;
+      for (long long u : uses)
+        seed_sq += double(u) * double(u);
     }
     std::queue<Ion> fifo;
     for (long long n = spec.first; n < spec.first + spec.n; ++n)
@@ -843,7 +854,7 @@ struct Engine
         pka.dir[i] = spec.dir[i];
         pka.pos[i] = spec.pos[i];
       }
-      pka.key = root_key(0, uint64_t(n));
+      pka.key = root_key(spec.sim_index, uint64_t(n));
       if (!spec.philox)
         reseed(seeds[n]);
       p_vac = 0;
@@ -905,6 +916,8 @@ main(int argc, char ** argv)
   eng.run();
   auto t1 = std::chrono::steady_clock::now();
   eng.t.print(stdout);
+  if (!spec.philox)
+    printf("seed_sq %.17g\n", eng.seed_sq);
   printf("wall_s %.6f\n", std::chrono::duration<double>(t1 - t0).count());
   if (!spec.out_type.empty() && !eng.out.write())
   {

@@ -38,7 +38,8 @@ def build(reference_dir=None):
 POTENTIALS = {"universal": 0, "moliere": 1, "ckr": 2}  # TrimBase::Potential (trim.h:63-69)
 
 
-def spec_text(sim, seed=1, philox=True, first=0, n=None, records=0, tmin=None, output=None, scale=1.0):
+def spec_text(sim, seed=1, philox=True, first=0, n=None, records=0, tmin=None, output=None, scale=1.0,
+              sim_index=0):
     w = sim.box()
     p = sim.start()
     lines = [f"seed {seed}", f"seeding {'philox' if philox else 'compat'}",
@@ -60,6 +61,8 @@ def spec_text(sim, seed=1, philox=True, first=0, n=None, records=0, tmin=None, o
         lines.append(f"subset {first} {n if n is not None else sim.n_primaries - first}")
     if records:
         lines.append(f"records {records}")
+    if sim_index:
+        lines.append(f"sim {int(sim_index)}")
     if output is not None:
         lines.append(f"output {output[0]} {output[1]}")
     if getattr(sim, "geometry", "layers") == "clusters":
@@ -100,14 +103,17 @@ def parse(text):
     return out
 
 
-def run(sim, seed=1, philox=True, first=0, n=None, records=0, reference=False, timeout=None, scale=1.0):
+def run(sim, seed=1, philox=True, first=0, n=None, records=0, reference=False, timeout=None, scale=1.0,
+        sim_index=0):
     """Run one oracle process on primaries [first, first + n); scale is the
-    sample's length unit in Angstrom (SimconfType::setLengthScale)."""
+    sample's length unit in Angstrom (SimconfType::setLengthScale); sim_index
+    selects the member keys of that simulation of a GPU batch (philox seeding)."""
     exe = REF_DRIVER if reference else MTORACLE
     if not exe.exists():
         raise RuntimeError(f"{exe} is not built")
     args = [str(exe)] if reference else [str(exe), str(TABLES)]
-    txt = spec_text(sim, seed=seed, philox=philox, first=first, n=n, records=records, scale=scale)
+    txt = spec_text(sim, seed=seed, philox=philox, first=first, n=n, records=records, scale=scale,
+                    sim_index=sim_index)
     r = subprocess.run(args, input=txt, capture_output=True, text=True, timeout=timeout)
     if r.returncode != 0:
         raise RuntimeError(f"oracle failed: {r.stderr}")
@@ -147,10 +153,13 @@ def merge(parts):
             out[h] = [sum(v) for v in zip(*hs)] if hs[0] else []
     out["records"] = sum((p.get("records", []) for p in parts), [])
     out["wall_s"] = max(p.get("wall_s", 0.0) for p in parts) if parts else 0.0
+    if parts and "seed_sq" in parts[0]:
+        out["seed_sq"] = parts[0]["seed_sq"]  # a property of the whole run, the same in every part
     return out
 
 
-def run_parallel(sim, seed=1, philox=True, procs=None, reference=False, first=0, n=None, timeout=None):
+def run_parallel(sim, seed=1, philox=True, procs=None, reference=False, first=0, n=None, timeout=None,
+                 sim_index=0):
     """Split primaries [first, first + n) over `procs` processes and sum the tallies."""
     total = sim.n_primaries - first if n is None else n
     procs = max(1, min(procs or os.cpu_count() or 1, total))
@@ -158,7 +167,7 @@ def run_parallel(sim, seed=1, philox=True, procs=None, reference=False, first=0,
     jobs = [(bounds[i], bounds[i + 1] - bounds[i]) for i in range(procs) if bounds[i + 1] > bounds[i]]
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         parts = list(ex.map(lambda j: run(sim, seed=seed, philox=philox, first=j[0], n=j[1],
-                                          reference=reference, timeout=timeout), jobs))
+                                          reference=reference, timeout=timeout, sim_index=sim_index), jobs))
     return merge(parts)
 
 

@@ -25,6 +25,8 @@
 //   hist_range <bin_A> <nbins>  histogram of primary stopping depth
 //   hist_vac <bin_A> <nbins>    histogram of vacancy depth (TrimVacCount bins are 1 A)
 //   subset <first> <count>      run primaries [first, first+count)
+//   sim <index>                 simulation index of the member keys (philox seeding):
+//                               the keys the GPU gives simulation <index> of a batch
 //   records <n>                 emit per-primary records for the first n primaries
 //   sputter <Esurf>             count recoils leaving through x < 0 with E cos^2 > Esurf
 //   voxels nx ny nz ox oy oz sx sy sz   energy-deposition voxel box (depth profile reported)
@@ -88,6 +90,7 @@ struct Spec
   double hist_vac_bin = 1.0;
   int hist_vac_n = 0;
   long long first = 0, n = -1;
+  unsigned long long sim_index = 0;
   int records = 0;
   double esurf = 0.0;
   int vox_n[3] = {0, 0, 0};
@@ -217,6 +220,8 @@ parse(std::istream & in, Spec & s, std::string & err)
       ok = bool(ls >> s.first >> s.n);
     else if (key == "records")
       ok = bool(ls >> s.records);
+    else if (key == "sim")
+      ok = bool(ls >> s.sim_index) && s.sim_index < (1ull << 23);
     else if (key == "sputter")
       ok = bool(ls >> s.esurf);
     else if (key == "clusters")

@@ -7,8 +7,12 @@ and the engine path that uses it (GB300).
   gap the surrogate is trained to close, measured;
 * loss and all 8642 gradients of the project's training kernels equal a numpy
   forward/backward of the same network (float64 on the CPU) to 1e-4;
-* a trained network reproduces the quadrature, and improves on the magic formula;
-* the FP32 engine with the surrogate matches the FP64 exact path statistically.
+* the committed default network follows the magic formula it was trained on (the
+  formula of the plain path and of the FP64 oracle), energy-transfer-weighted;
+* the committed quadrature network reproduces the true scattering integral closer
+  than the magic formula does: what the learned part gains over the method
+  without it;
+* the FP32 engine with the surrogate is within 1 % of the FP64 exact path.
 """
 import math
 
@@ -17,6 +21,8 @@ import pytest
 
 from mytrim_gb300 import Engine, summarize
 from mytrim_gb300 import workloads as W
+
+import parity_stats as PS
 
 pytestmark = pytest.mark.gpu
 
@@ -168,23 +174,85 @@ def test_short_training_learns(trained):
     assert np.median(rn[big]) < 0.10
 
 
+def test_magic_target_with_transfer_weights_learns(engine_lib):
+    """A short run on the magic-formula target with energy-transfer-weighted loss fits
+    that formula to a few percent; an unknown target or weighting is rejected."""
+    from mytrim_gb300 import _ffi as F
+    e = Engine(precision="fp32", seed=3)
+    rep = e.surrogate_train(n_train=2_000_000, batch=8192, epochs=6, qat_epochs=1, lr=3e-3, seed=12,
+                            target="magic", weighting="transfer")
+    assert rep["final_loss"] < 1e-3
+    eps, b = _held_out(20000, 5)
+    s2n = e.scatter(eps, b, precision="surrogate")
+    s2m = e.scatter(eps, b, precision="fp64")
+    assert np.sum(np.abs(s2n - s2m)) / np.sum(s2m) < 0.05
+    cfg = F.SurrogateConfig(1 << 20, 8192, 1, 0, 1e-3, 1, 0.1, 2, 0)
+    rep_c = F.SurrogateReport()
+    import ctypes as C
+    assert e.lib.mtg_surrogate_train(e.ctx, C.byref(cfg), C.byref(rep_c)) == 1  # MTG_ERR_BAD_INPUT
+    cfg.target, cfg.weighting = 0, 5
+    assert e.lib.mtg_surrogate_train(e.ctx, C.byref(cfg), C.byref(rep_c)) == 1  # MTG_ERR_BAD_INPUT
+    e.close()
+
+
+def _load(path):
+    e = Engine(precision="fp32", seed=3)
+    e.set_surrogate_params(np.load(path))
+    return e
+
+
 @pytest.fixture(scope="module")
 def committed():
     from mytrim_gb300.train_surrogate import PARAMS
-    e = Engine(precision="fp32", seed=3)
-    e.set_surrogate_params(np.load(PARAMS))
+    e = _load(PARAMS)
     yield e
     e.close()
 
 
-def test_committed_network_reproduces_the_quadrature(committed):
-    """The network trained on 2e7 quadrature samples (mytrim_gb300/data) reproduces the
-    true scattering integral, and closer than the magic formula it replaces: that is
-    what the learned part gains over the method without it."""
-    rn, rm, big, low = _network_errors(committed)
-    assert np.median(rn[big]) < 0.01, np.median(rn[big])
-    assert np.quantile(rn[big], 0.95) < 0.03, np.quantile(rn[big], 0.95)
-    assert np.median(rn[low]) < 0.5 * np.median(rm[low]), (np.median(rn[low]), np.median(rm[low]))
+def _held_out(n=100_000, seed=99):
+    """points where the network runs (eps <= 10), area-weighted in b like the collisions"""
+    rng = np.random.default_rng(seed)
+    eps = 10 ** rng.uniform(-4, 1, n)
+    b = 12 * np.sqrt(rng.uniform(0, 1, n))
+    return eps, b
+
+
+def _transfer_bias(s2, ref, eps):
+    le = np.log10(eps)
+    return np.array([np.sum((s2 - ref)[(le >= lo) & (le < lo + 1)]) / np.sum(ref[(le >= lo) & (le < lo + 1)])
+                     for lo in range(-4, 1)])
+
+
+def test_committed_network_follows_the_magic_formula(committed):
+    """The default network (trained on the magic formula with energy-transfer-weighted
+    loss) reproduces the formula: per decade of eps, the s2-weighted signed error is
+    under 1 %, the s2-weighted absolute error under 0.5 %."""
+    eps, b = _held_out()
+    s2n = committed.scatter(eps, b, precision="surrogate")
+    s2m = committed.scatter(eps, b, precision="fp64")
+    bias = _transfer_bias(s2n, s2m, eps)
+    assert np.all(np.abs(bias) < 0.01), bias
+    assert np.sum(np.abs(s2n - s2m)) / np.sum(s2m) < 0.005
+
+
+def test_quadrature_network_gains_over_the_magic_formula(engine_lib):
+    """The network trained on the quadrature (surrogate_params_quadrature.npy) is closer
+    to the true scattering integral than the magic formula the reference evaluates
+    (trim.C:235-271): median relative error of s2 and s2-weighted absolute error."""
+    from mytrim_gb300.train_surrogate import PARAMS_QUADRATURE
+    e = _load(PARAMS_QUADRATURE)
+    eps, b = _held_out()
+    s2q, _ = e.quadrature(eps, b)
+    s2n = e.scatter(eps, b, precision="surrogate")
+    s2m = e.scatter(eps, b, precision="fp64")
+    e.close()
+    big = s2q > 1e-4
+    rn = np.abs(s2n - s2q) / s2q
+    rm = np.abs(s2m - s2q) / s2q
+    assert np.median(rn[big]) < 0.5 * np.median(rm[big]), (np.median(rn[big]), np.median(rm[big]))
+    wn = np.sum(np.abs(s2n - s2q)) / np.sum(s2q)
+    wm = np.sum(np.abs(s2m - s2q)) / np.sum(s2q)
+    assert wn < wm, (wn, wm)
 
 
 def test_params_roundtrip(trained):
@@ -198,17 +266,14 @@ def test_params_roundtrip(trained):
 
 
 def test_surrogate_engine_matches_fp64(committed):
-    e = committed
-    sim = W.cu_self_ion(n_primaries=2000, E=20e3)
-    e.configure(precision="surrogate", seed=8)
-    g = summarize(e.run([sim])[0])
-    e.configure(precision="fp32", seed=8)
-    f = summarize(e.run([sim])[0])
-    assert g["surrogate_fallbacks"] > 0
-    for key in ("vac_per_ion", "range_mean", "eel_per_ion"):
-        rel = abs(g[key] - f[key]) / abs(f[key])
-        z = abs(g[key] - f[key]) / math.hypot(g[key + "_err"], f[key + "_err"])
-        assert z < 5 or rel < 0.05, (key, g[key], f[key])
+    """Cu 20 keV into Cu: the surrogate path within 1 % of the FP64 exact path, on
+    samples that resolve 1 % at 3 sigma"""
+    sim = W.cu_self_ion(n_primaries=200_000, E=20e3)
+    from mytrim_gb300.train_surrogate import PARAMS
+    t, p = PS.run_primaries("surrogate", sim, seed=8, params=np.load(PARAMS))
+    assert 0 < t["surrogate_fallbacks"] < t["collisions"]
+    _, p64 = PS.run_primaries("fp64", sim, seed=9)
+    PS.assert_within_one_percent(p, p64, "surrogate cu20k")
 
 
 def test_surrogate_path_scatters_other_potentials_exactly(committed):

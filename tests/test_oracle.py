@@ -79,6 +79,7 @@ def test_restatement_matches_reference_live(oracle_built, seed):
         a = oracle_built.run(sim, seed=seed, philox=False, records=sim.n_primaries)
         b = oracle_built.run(sim, seed=seed, philox=False, records=sim.n_primaries, reference=True)
         a.pop("wall_s"), b.pop("wall_s")
+        a.pop("seed_sq")  # the restatement's count of repeated seeds; the driver has none
         assert a == b
 
 
