@@ -15,8 +15,12 @@ Printed JSON line (rank 0):
                write) before every timed step
   e2e          the same metric through the public call (host structs in, host
                totals out, uploads and read-back inside the timed region)
-  fp64         the plain FP64 exact-scattering path on the same workload, and the
-               relative difference of mean projected range fast vs FP64
+  paths        each path on the same workload: fp32 (the headline), surrogate (2^20
+               primaries per step), fp64 -- the plain FP64 exact-scattering path,
+               2^16 primaries per step, timed like the headline (L2 flushed, CUDA
+               events, 3 timed steps) with its own e2e and its ratio over the CPU
+               baseline; the fast paths' relative differences from FP64 in mean
+               range, straggle and vacancies per ion, with their standard errors
   roofline     the cascade kernel: 391 algorithmic operations per collision (300 + 91
                per target element) against the FP32 issue rate, SMs x 128 lanes x
                the measured SM clock; paths.*.roofline_frac the same for each path
@@ -45,6 +49,11 @@ UNIT = "primary ions/s"
 WORKLOAD = "Ag 200 keV into bulk Si (2.33 g/cm3, Edisp 15 eV, Ebind 3 eV), full cascade"
 W_COLL = 300 + 91 * 1  # algorithmic ops per collision (one-element target)
 L2_FLUSH_BYTES = 256 << 20
+# DRAM bytes (read + write) per collision of the FP32 cascade kernel on this workload:
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of 65,536 primaries
+# (1.76e9 collisions), divided by its collisions; the traffic grows with the
+# collisions a launch processes, so the figure scales to the 10^7-primary launch
+DRAM_BYTES_PER_COLLISION_FP32 = 2.03
 
 # name -> (description, builder(n_primaries)); builders from mytrim_gb300.workloads
 WORKLOADS = {
@@ -90,7 +99,8 @@ def args_parse():
                    help="primaries per step (default: the 10^7 primaries of the Ag 200 keV configuration)")
     p.add_argument("--surrogate-batch", type=int, default=1 << 20, help="primaries per step of the surrogate leg")
     p.add_argument("--precision", default="auto", choices=["auto", "fp32", "surrogate", "fp64"])
-    p.add_argument("--fp64-batch", type=int, default=8192)
+    p.add_argument("--fp64-batch", type=int, default=1 << 16, help="primaries per step of the FP64 leg")
+    p.add_argument("--fp64-steps", type=int, default=3, help="timed steps of the FP64 leg")
     p.add_argument("--cpu-per-core", type=int, default=0, help="primaries per core in the CPU sample")
     p.add_argument("--events", default="", help="log these event kinds in every step (comma list of "
                    "vacancy, replacement, branch, dissipate, rest, lost) and report their rate")
@@ -331,7 +341,7 @@ def main():
 
     def time_path(path, steps, base, batch):
         """device-timed steps of another path on fresh primaries (same workload)"""
-        e2 = Engine(device=local, precision="fp32", seed=20261203)
+        e2 = Engine(device=local, precision="fp64" if path == "fp64" else "fp32", seed=20261203)
         if path == "surrogate":
             import numpy as np
             from mytrim_gb300.train_surrogate import PARAMS
@@ -354,7 +364,7 @@ def main():
                 ts.append(e0.elapsed_time(e1) / 1e3)
         e2.close()
         agg2 = {kk: sum(r[kk] for r in rs) for kk in agg}
-        agg2["surrogate_fallbacks"] = sum(r["surrogate_fallbacks"] for r in rs)
+        agg2["surrogate_fallbacks"] = sum(r.get("surrogate_fallbacks", 0) for r in rs)
         return summarize(agg2), agg2["primaries"] / sum(ts), agg2
 
     paths = {prec: {"value": value, "unit": UNIT, "collisions_per_s": coll_rate}}
@@ -367,14 +377,25 @@ def main():
                                   "fallback_fraction": sg_agg["surrogate_fallbacks"] / max(sg_agg["collisions"], 1)}
     fp64 = None
     if not a.no_fp64 and prec != "fp64":
+        # the plain FP64 exact-scattering path, timed like the headline: fresh
+        # primaries each step, L2 flushed, CUDA events on the launching stream, one
+        # untimed warm-up step; then one step end to end through the public call
+        r64, rate64, agg64 = time_path("fp64", a.fp64_steps, 2000, a.fp64_batch)
         e64 = Engine(device=local, precision="fp64", seed=20261203)
-        s = make_sim(a.workload, a.fp64_batch)
-        r64 = summarize(e64.run([s])[0])
-        ms64 = e64.stats()["kernel_ms"]
+        ss = sims_for(3000, a.fp64_batch)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e64.run(ss)
+        torch.cuda.synchronize()
+        e2e64 = sum(x.n_primaries for x in ss) / (time.perf_counter() - t0)
+        st64 = e64.stats()
         e64.close()
-        fp64 = {"value": a.fp64_batch / (ms64 / 1e3), "unit": UNIT, "primaries": a.fp64_batch,
-                "collisions_per_s": r64["collisions"] / (ms64 / 1e3), "range_mean_A": r64["range_mean"],
-                "straggle_A": r64["straggle"], "vac_per_ion": r64["vac_per_ion"]}
+        fp64 = {"value": rate64, "unit": UNIT, "primaries_per_step": a.fp64_batch, "steps": a.fp64_steps,
+                "l2": "flushed before each timed step",
+                "collisions_per_s": rate64 * agg64["collisions"] / max(agg64["primaries"], 1),
+                "e2e": {"value": e2e64, "unit": UNIT, "h2d_bytes_per_step": st64["h2d_bytes"],
+                        "d2h_bytes_per_step": st64["d2h_bytes"]},
+                "range_mean_A": r64["range_mean"], "straggle_A": r64["straggle"], "vac_per_ion": r64["vac_per_ion"]}
 
         def rel_errors(f):
             d = f["range_mean"] - r64["range_mean"]
@@ -414,12 +435,9 @@ def main():
     kms = statistics.mean(kernel_ms)
     achieved = per_launch_coll * W_COLL / (kms / 1e3) / 1e12
     traffic = None
-    prof = ROOT / "profiles" / "cascade_fp32_agsi.md"
     # the captured figure belongs to the FP32 kernel on the default workload
-    if prof.exists() and a.workload == "ag200k_si" and prec == "fp32" and not ev_kinds:
-        for line in prof.read_text().splitlines():
-            if line.startswith("dram_bytes_per_collision:"):
-                traffic = float(line.split(":")[1]) * per_launch_coll
+    if a.workload == "ag200k_si" and prec == "fp32" and not ev_kinds:
+        traffic = DRAM_BYTES_PER_COLLISION_FP32 * per_launch_coll
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": 1e3 * total / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -455,6 +473,12 @@ def main():
                                 "kind": "reference" if reference else "port",
                                 "sample": f"{per_core} primaries per core x {cores} independent processes "
                                           f"({r['primaries']} primaries, {wall:.1f} s)"}
+        # the same-precision comparison: the GPU's FP64 plain path, end to end, over
+        # the CPU's FP64 reference algorithm on all host cores
+        if "fp64" in paths:
+            cpu = line["cpu_baseline"]["value"]
+            paths["fp64"]["e2e_over_cpu_baseline"] = paths["fp64"]["e2e"]["value"] / cpu
+            paths["fp64"]["over_cpu_baseline"] = paths["fp64"]["value"] / cpu
     print(json.dumps(line), flush=True)
     eng.close()
 

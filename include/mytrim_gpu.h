@@ -446,7 +446,10 @@ mtg_status mtg_surrogate_quadrature(mtg_ctx * ctx, const double * eps, const dou
  * message in errbuf (may be NULL).  It works on the current device and queues its
  * kernels on `stream` (a cudaStream_t, NULL = default stream) without waiting.
  * The first call on each device looks up the scratch array's device address,
- * so make that first call before any stream capture.  All calls on a device
+ * so make that first call before any stream capture.  The address belongs to the
+ * device's CUDA context: after cudaDeviceReset, or under another context, the
+ * next call looks it up again (it keeps the context's unique id beside it), and
+ * that call too should come before any stream capture.  All calls on a device
  * share the scratch array: calls whose kernels could overlap on the GPU race,
  * so order them (one stream, or synchronise between them).
  * This entry point has no counterpart in the reference. */

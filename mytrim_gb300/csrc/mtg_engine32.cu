@@ -315,8 +315,10 @@ struct Fp32Policy
         // the network is trained on the universal potential only
         nn = !a.gone && (!EXT || m.sim->potential == 0) && surrogate_in_domain(a.eps, a.b);
       }
-      // every lane of the warp, with or without a member, evaluates the network
-      const float o0 = surrogate_eval_warp(m.net, nn ? surrogate_x1(a.eps) : 0.0f, nn ? surrogate_x2(a.b) : 0.0f);
+      // warp-collective: the lanes whose collision is in the network's domain are
+      // evaluated together, the others (no member, or the exact fallback) only take
+      // part in the shuffles
+      const float o0 = surrogate_eval_warp(m.net, nn, nn ? surrogate_x1(a.eps) : 0.0f, nn ? surrogate_x2(a.b) : 0.0f);
       if (!live)
         return 0;
       if (a.gone)

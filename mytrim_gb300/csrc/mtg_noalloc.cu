@@ -14,6 +14,7 @@
 // primaries reduced with Neumaier-compensated FP64 sums in a fixed order, then
 // the chunks in index order, so the totals are the same bits as the ones
 // mtg_collect reports for a single simulation.
+#include <cuda.h> // CUcontext / CUresult types only: the driver calls are reached through the runtime
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -131,7 +132,52 @@ noalloc_finish_kernel(const double * partials, int nchunks, double * out)
 
 constexpr int MAX_DEVICES = 64;
 std::mutex g_setup_mutex;
-double * g_scratch_addr[MAX_DEVICES] = {nullptr};
+
+// The scratch array's device address is a property of the CUDA context the module
+// was loaded into: after cudaDeviceReset (or under another context on the same
+// device) the array lives elsewhere.  The address is therefore cached per device
+// together with the unique id of the context it was looked up in (cuCtxGetId),
+// and looked up again when the current context's id differs.
+struct ScratchAddr
+{
+  unsigned long long ctx_id; // 0: unknown, look up on every call
+  double * addr;
+};
+ScratchAddr g_scratch[MAX_DEVICES] = {};
+
+using CtxGetCurrent = CUresult (*)(CUcontext *);
+using CtxGetId = CUresult (*)(CUcontext, unsigned long long *);
+CtxGetCurrent g_ctx_get_current = nullptr;
+CtxGetId g_ctx_get_id = nullptr;
+bool g_entry_points_tried = false;
+
+// unique id of the calling thread's current context, 0 if there is none or the
+// driver does not provide the query (caller holds g_setup_mutex)
+unsigned long long
+current_context_id()
+{
+  if (!g_entry_points_tried)
+  {
+    g_entry_points_tried = true;
+    void * f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_ctx_get_current = reinterpret_cast<CtxGetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_ctx_get_id = reinterpret_cast<CtxGetId>(f);
+    cudaGetLastError(); // a failed query leaves no sticky error behind
+  }
+  if (!g_ctx_get_current || !g_ctx_get_id)
+    return 0;
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (g_ctx_get_current(&c) != CUDA_SUCCESS || !c || g_ctx_get_id(c, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
 
 void
 set_error(char * buf, size_t len, const char * msg)
@@ -179,10 +225,12 @@ mtg_reduce_primaries_noalloc(const unsigned long long * vacancies, const unsigne
   }
   double * scratch = nullptr;
   {
-    // once per device, with that device current: the device address of the
-    // scratch array (its host-side name is only a stand-in, not an address)
+    // once per device (and context), with that device current: the device address
+    // of the scratch array (its host-side name is only a stand-in, not an address)
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_addr[dev])
+    unsigned long long id = current_context_id();
+    ScratchAddr & c = g_scratch[dev];
+    if (!c.addr || id == 0 || c.ctx_id != id)
     {
       void * p = nullptr;
       e = cudaGetSymbolAddress(&p, g_noalloc_partials);
@@ -191,9 +239,11 @@ mtg_reduce_primaries_noalloc(const unsigned long long * vacancies, const unsigne
         set_error(errbuf, errbuf_len, e != cudaSuccess ? cudaGetErrorString(e) : "null symbol address");
         return MTG_ERR_CUDA;
       }
-      g_scratch_addr[dev] = static_cast<double *>(p);
+      // the lookup makes the device's primary context current if none was
+      c.addr = static_cast<double *>(p);
+      c.ctx_id = id ? id : current_context_id();
     }
-    scratch = g_scratch_addr[dev];
+    scratch = c.addr;
   }
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   const int nchunks = int((n + NOALLOC_CHUNK - 1) / NOALLOC_CHUNK);

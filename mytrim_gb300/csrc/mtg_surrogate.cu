@@ -385,7 +385,7 @@ surrogate_eval_kernel(const SurrogateNet * gnet, const double * eps, const doubl
   const float e = i < n ? float(eps[i]) : 1.0f;
   const float bb = i < n ? float(b[i]) : 1.0f;
   const bool in = surrogate_in_domain(e, bb);
-  const float o0 = surrogate_eval_warp(&net, surrogate_x1(in ? e : 1.0f), surrogate_x2(in ? bb : 1.0f));
+  const float o0 = surrogate_eval_warp(&net, in && i < n, surrogate_x1(in ? e : 1.0f), surrogate_x2(in ? bb : 1.0f));
   if (i >= n)
     return;
   float s, c;

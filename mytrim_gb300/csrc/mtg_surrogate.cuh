@@ -12,8 +12,9 @@
 // reduced time integral tau / Y1 (not used by the transport: tau = 0 in the
 // reference, trim.C:303, 310).
 //
-// Inference in the FP32 engine is warp-collective: the 32 lanes' inputs form two
-// 16-row tiles; the two 64x64 hidden layers run on the tensor cores
+// Inference in the FP32 engine is warp-collective: the inputs of the lanes whose
+// collision lies in the network's domain are compacted into 16-row tiles (one tile
+// for up to 16 such lanes, none without); the two 64x64 hidden layers run on the tensor cores
 // (mma.sync m16n8k16, BF16 operands, FP32 accumulation) with the accumulator
 // fragments of one layer reused in registers as the A fragments of the next; the
 // 2x64 input and 64x2 output layers stay in FP32.  Weights are staged in shared
@@ -164,22 +165,49 @@ to_a_fragments(const float (&c)[8][4], uint32_t (&a)[4][4])
   }
 }
 
-// Warp-collective evaluation: every lane of the warp calls it (converged) with its
-// own inputs; returns output 0 (the correction) for the lane's sample.  `net` must
-// point to shared memory.
-__device__ __forceinline__ float
-surrogate_eval_warp(const SurrogateNet * net, float x1, float x2)
+// Lane of the (n+1)-th set bit of m (n < popc(m)): binary search on popcounts.
+__device__ __forceinline__ int
+nth_set_lane(unsigned m, int n)
 {
+  int pos = 0;
+#pragma unroll
+  for (int w = 16; w > 0; w >>= 1)
+  {
+    const int c = __popc(m & ((1u << w) - 1u));
+    const bool up = n >= c;
+    n -= up ? c : 0;
+    pos += up ? w : 0;
+    m = up ? (m >> w) : m;
+  }
+  return pos;
+}
+
+// Warp-collective evaluation: every lane of the warp calls it (converged) with its
+// own inputs; lanes with `active` set get output 0 (the correction) for their
+// sample, the others 0.  The active lanes' samples are compacted into the first rows
+// of the 16-row tiles (row r holds the active lane of rank r), so a warp evaluates
+// ceil(active / 16) tiles: none when no lane is active, one for up to 16.  `net`
+// must point to shared memory.
+__device__ __forceinline__ float
+surrogate_eval_warp(const SurrogateNet * net, bool active, float x1, float x2)
+{
+  const unsigned m = __ballot_sync(0xffffffffu, active);
+  const int count = __popc(m);
   const int lane = threadIdx.x & 31;
   const int g = lane >> 2, t = lane & 3;
+  const int rank = __popc(m & ((1u << lane) - 1u));
+  const int tiles = (count + 15) >> 4;
   float out0 = 0.0f;
 #pragma unroll 1
-  for (int mt = 0; mt < 2; ++mt)
+  for (int mt = 0; mt < tiles; ++mt)
   {
-    // rows of this tile owned by the thread: samples mt*16 + g and mt*16 + g + 8
+    // rows of this tile owned by the thread: mt*16 + g and mt*16 + g + 8; a row past
+    // the last active sample reads any lane's input and its result is not used
     const int s0 = mt * 16 + g, s1 = s0 + 8;
-    const float ax1 = __shfl_sync(0xffffffffu, x1, s0), ax2 = __shfl_sync(0xffffffffu, x2, s0);
-    const float bx1 = __shfl_sync(0xffffffffu, x1, s1), bx2 = __shfl_sync(0xffffffffu, x2, s1);
+    const int l0 = s0 < count ? nth_set_lane(m, s0) : lane;
+    const int l1 = s1 < count ? nth_set_lane(m, s1) : lane;
+    const float ax1 = __shfl_sync(0xffffffffu, x1, l0), ax2 = __shfl_sync(0xffffffffu, x2, l0);
+    const float bx1 = __shfl_sync(0xffffffffu, x1, l1), bx2 = __shfl_sync(0xffffffffu, x2, l1);
     // input layer (FP32) directly in A-fragment layout
     uint32_t a[4][4];
 #pragma unroll
@@ -220,12 +248,12 @@ surrogate_eval_warp(const SurrogateNet * net, float x1, float x2)
     p0 += __shfl_xor_sync(0xffffffffu, p0, 2);
     p1 += __shfl_xor_sync(0xffffffffu, p1, 1);
     p1 += __shfl_xor_sync(0xffffffffu, p1, 2);
-    // lane s gets its sample's value from the group owning its row
-    const int r = lane - mt * 16;
+    // the active lane of rank r gets row r's value from the group owning that row
+    const int r = rank - mt * 16;
     const int src = ((r & 7) << 2);
     const float v0 = __shfl_sync(0xffffffffu, p0, src);
     const float v1 = __shfl_sync(0xffffffffu, p1, src);
-    if (r >= 0 && r < 16)
+    if (active && r >= 0 && r < 16)
       out0 = (r < 8 ? v0 : v1) + lds_f32(&net->b4[0]);
   }
   return out0;

@@ -15,6 +15,7 @@ that the parsed doubles are bit-identical to what the reference parses.
 
 Usage:  python make_stopping_tables.py <mytrim data dir>  > stopping_tables.tsv
 """
+import os
 import sys
 from pathlib import Path
 
@@ -48,4 +49,9 @@ def main(datadir):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/data")
+    if len(sys.argv) > 1:
+        main(sys.argv[1])
+    elif os.environ.get("MYTRIM_REFERENCE"):
+        main(os.path.join(os.environ["MYTRIM_REFERENCE"], "data"))
+    else:
+        sys.exit("usage: make_stopping_tables.py <reference data directory> (or set MYTRIM_REFERENCE)")

@@ -18,7 +18,7 @@ std::ostream prints them (six significant digits).  The engine has no sequential
 ion ids: the member's path key stands in for the id (of the member that raised the
 event).  The tag is IonBase::_tag: the index of the cluster a followed recoil was
 created in (sampleClusters), else -1.  The GPU writes events in no particular
-order; the lines are sorted by simulation, primary, path key and kind.
+order; the lines are sorted by simulation, primary, path key, kind and position.
 """
 from typing import Iterable, TextIO
 
@@ -39,7 +39,10 @@ def _ion(e) -> str:
 
 
 def _sorted(events: np.ndarray) -> np.ndarray:
-    order = np.lexsort((events["kind"], events["key"], events["primary"], events["sim"]))
+    """by simulation, primary, path key of the member that raised the event, kind,
+    then position (one member's events of one kind lie a flight path apart)"""
+    order = np.lexsort((events["z"], events["y"], events["x"], events["kind"], events["key"], events["primary"],
+                        events["sim"]))
     return events[order]
 
 

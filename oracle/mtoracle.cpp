@@ -682,6 +682,8 @@ struct Engine
       {
         if (rec.E > el.Edisp - el.Elbind)
         {
+          emit(EV_HISTORY, pka.pos, pka.E, pka.Z, pka.m, pka.gen, 0, 0.0, pka.key);
+          emit(EV_BRANCH, rec.pos, rec.E, el.Z, el.m, rec.gen, 0, el.Elbind, pka.key);
           t.Enuc += el.Elbind;
           p_enuc += el.Elbind;
           t.deposit(rec.pos[0], rec.pos[1], rec.pos[2], el.Elbind);
@@ -700,15 +702,20 @@ struct Engine
           else
             t.Eunfollowed += rec.E;
           if (pka.E > el.Edisp)
+          {
+            emit(EV_VACANCY, rec.pos, rec.E, el.Z, el.m, rec.gen, 0, el.Elbind, pka.key);
             vacancy(rec, el, mat);
+          }
           else
           {
+            emit(EV_REPLACEMENT, rec.pos, rec.E, el.Z, el.m, rec.gen, 0, el.Elbind, pka.key);
             replacement(rec);
             pka.state = (pka.Z == el.Z) ? REPLACEMENT : SUBSTITUTIONAL;
           }
         }
         else
         {
+          emit(EV_DISSIPATE, rec.pos, rec.E, el.Z, el.m, rec.gen, 0, el.Elbind, pka.key);
           const double e = rec.E + el.Elbind;
           out.dissipate(rec.Z, rec.pos[0]);
           t.Enuc += e;
@@ -788,11 +795,13 @@ struct Engine
     last_state = pka.state;
     if (pka.state == LOST)
     {
+      emit(EV_LOST, pka.pos, pka.E, pka.Z, pka.m, pka.gen, LOST, recoil_energy, pka.key);
       t.lost++;
       t.Elost += pka.E + recoil_energy;
       t.exit_surface(pka.pos[0], pka.gen, pka.E, pka.dir[0]);
       return;
     }
+    emit(EV_REST, pka.pos, pka.E, pka.Z, pka.m, pka.gen, pka.state, 0.0, pka.key);
     t.Enuc += pka.E;
     p_enuc += pka.E;
     t.deposit(pka.pos[0], pka.pos[1], pka.pos[2], pka.E);
@@ -820,6 +829,28 @@ struct Engine
   }
 
   double seed_sq = 0.0; // compat seeding: sum over distinct seeds of their use count squared
+  long long cur_primary = 0;
+
+  // Event records with the fields of the GPU event log (mtg_event): the reference's
+  // hook calls that TrimDefectLog, TrimPhononOut and TrimHistory stream
+  // (trim.C:467-527, trim.h:139-153), one line each, floats in hex
+  enum EvKind
+  {
+    EV_VACANCY = 1,
+    EV_REPLACEMENT = 2,
+    EV_BRANCH = 3,
+    EV_DISSIPATE = 4,
+    EV_REST = 5,
+    EV_LOST = 6,
+    EV_HISTORY = 7
+  };
+  void emit(int kind, const double pos[3], double E, int Z, double m, int gen, int state, double aux, uint64_t key)
+  {
+    if (!(spec.event_mask & (1u << kind)))
+      return;
+    printf("ev %d %llu %lld %d %d %d %a %a %a %a %a %a\n", kind, (unsigned long long)key, cur_primary, gen, Z,
+           state, pos[0], pos[1], pos[2], E, aux, m);
+  }
 
   void run()
   {
@@ -855,6 +886,7 @@ struct Engine
         pka.pos[i] = spec.pos[i];
       }
       pka.key = root_key(spec.sim_index, uint64_t(n));
+      cur_primary = n;
       if (!spec.philox)
         reseed(seeds[n]);
       p_vac = 0;

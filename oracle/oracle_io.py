@@ -26,11 +26,24 @@ SUM_KEYS = ("primaries", "members", "collisions", "vacancies", "replacements", "
             "Esputtered", "Evoxel")
 
 
+def reference_dir():
+    """The reference checkout: $MYTRIM_REFERENCE, else the build recipe's default
+    (oracle/Makefile REF); None where it is not present (e.g. on the GPU machine)."""
+    ref = os.environ.get("MYTRIM_REFERENCE")
+    if not ref:
+        r = subprocess.run(["make", "-s", "--no-print-directory", "-C", str(ORACLE_DIR), "print-ref"],
+                           capture_output=True, text=True)
+        ref = r.stdout.strip() if r.returncode == 0 else ""
+    p = Path(ref) if ref else None
+    return p if p is not None and (p / "trim.C").exists() else None
+
+
 def build(reference_dir=None):
-    """Compile the restatement, and the reference driver when the sources exist."""
+    """Compile the restatement, and the reference driver where the reference's
+    sources are present (the argument, else reference_dir())."""
     env = dict(os.environ)
     subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "all"], check=True, env=env)
-    ref = Path(reference_dir) if reference_dir else None
+    ref = Path(reference_dir) if reference_dir else globals()["reference_dir"]()
     if ref is not None and (ref / "trim.C").exists():
         subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "ref", f"REF={ref}"], check=True, env=env)
 
@@ -39,7 +52,7 @@ POTENTIALS = {"universal": 0, "moliere": 1, "ckr": 2}  # TrimBase::Potential (tr
 
 
 def spec_text(sim, seed=1, philox=True, first=0, n=None, records=0, tmin=None, output=None, scale=1.0,
-              sim_index=0):
+              sim_index=0, event_mask=0):
     w = sim.box()
     p = sim.start()
     lines = [f"seed {seed}", f"seeding {'philox' if philox else 'compat'}",
@@ -63,6 +76,8 @@ def spec_text(sim, seed=1, philox=True, first=0, n=None, records=0, tmin=None, o
         lines.append(f"records {records}")
     if sim_index:
         lines.append(f"sim {int(sim_index)}")
+    if event_mask:
+        lines.append(f"events {int(event_mask)}")
     if output is not None:
         lines.append(f"output {output[0]} {output[1]}")
     if getattr(sim, "geometry", "layers") == "clusters":
@@ -81,14 +96,20 @@ def spec_text(sim, seed=1, philox=True, first=0, n=None, records=0, tmin=None, o
     return "\n".join(lines) + "\n"
 
 
+EVENT_FIELDS = ("kind", "key", "primary", "gen", "Z", "state", "x", "y", "z", "E", "aux", "m")
+
+
 def parse(text):
-    out = {"records": []}
+    out = {"records": [], "events": []}
     for line in text.splitlines():
         parts = line.split()
         if not parts:
             continue
         k = parts[0]
-        if k == "rec":
+        if k == "ev":
+            vals = [int(v) for v in parts[1:7]] + [float.fromhex(v) for v in parts[7:13]]
+            out["events"].append(dict(zip(EVENT_FIELDS, vals)))
+        elif k == "rec":
             idx, mem, coll, vac = (int(v) for v in parts[1:5])
             eel, enuc, x, y, z = (float(v) for v in parts[5:10])
             out["records"].append(dict(index=idx, members=mem, collisions=coll, vacancies=vac, eel=eel,
@@ -104,7 +125,7 @@ def parse(text):
 
 
 def run(sim, seed=1, philox=True, first=0, n=None, records=0, reference=False, timeout=None, scale=1.0,
-        sim_index=0):
+        sim_index=0, event_mask=0):
     """Run one oracle process on primaries [first, first + n); scale is the
     sample's length unit in Angstrom (SimconfType::setLengthScale); sim_index
     selects the member keys of that simulation of a GPU batch (philox seeding)."""
@@ -113,7 +134,7 @@ def run(sim, seed=1, philox=True, first=0, n=None, records=0, reference=False, t
         raise RuntimeError(f"{exe} is not built")
     args = [str(exe)] if reference else [str(exe), str(TABLES)]
     txt = spec_text(sim, seed=seed, philox=philox, first=first, n=n, records=records, scale=scale,
-                    sim_index=sim_index)
+                    sim_index=sim_index, event_mask=event_mask)
     r = subprocess.run(args, input=txt, capture_output=True, text=True, timeout=timeout)
     if r.returncode != 0:
         raise RuntimeError(f"oracle failed: {r.stderr}")
@@ -152,6 +173,7 @@ def merge(parts):
         if hs and hs[0] is not None:
             out[h] = [sum(v) for v in zip(*hs)] if hs[0] else []
     out["records"] = sum((p.get("records", []) for p in parts), [])
+    out["events"] = sum((p.get("events", []) for p in parts), [])
     out["wall_s"] = max(p.get("wall_s", 0.0) for p in parts) if parts else 0.0
     if parts and "seed_sq" in parts[0]:
         out["seed_sq"] = parts[0]["seed_sq"]  # a property of the whole run, the same in every part
@@ -159,7 +181,7 @@ def merge(parts):
 
 
 def run_parallel(sim, seed=1, philox=True, procs=None, reference=False, first=0, n=None, timeout=None,
-                 sim_index=0):
+                 sim_index=0, event_mask=0):
     """Split primaries [first, first + n) over `procs` processes and sum the tallies."""
     total = sim.n_primaries - first if n is None else n
     procs = max(1, min(procs or os.cpu_count() or 1, total))
@@ -167,7 +189,8 @@ def run_parallel(sim, seed=1, philox=True, procs=None, reference=False, first=0,
     jobs = [(bounds[i], bounds[i + 1] - bounds[i]) for i in range(procs) if bounds[i + 1] > bounds[i]]
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         parts = list(ex.map(lambda j: run(sim, seed=seed, philox=philox, first=j[0], n=j[1],
-                                          reference=reference, timeout=timeout, sim_index=sim_index), jobs))
+                                          reference=reference, timeout=timeout, sim_index=sim_index,
+                                          event_mask=event_mask), jobs))
     return merge(parts)
 
 

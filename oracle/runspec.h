@@ -25,6 +25,10 @@
 //   hist_range <bin_A> <nbins>  histogram of primary stopping depth
 //   hist_vac <bin_A> <nbins>    histogram of vacancy depth (TrimVacCount bins are 1 A)
 //   subset <first> <count>      run primaries [first, first+count)
+//   events <mask>               print an "ev" line per event of the kinds whose bit
+//                               (1 << kind) is set, with the fields of the GPU event
+//                               log (mtg_event): 1 vacancy, 2 replacement, 3 followRecoil
+//                               branch, 4 dissipated recoil, 5 rest, 6 lost, 7 history
 //   sim <index>                 simulation index of the member keys (philox seeding):
 //                               the keys the GPU gives simulation <index> of a batch
 //   records <n>                 emit per-primary records for the first n primaries
@@ -91,6 +95,7 @@ struct Spec
   int hist_vac_n = 0;
   long long first = 0, n = -1;
   unsigned long long sim_index = 0;
+  unsigned int event_mask = 0;
   int records = 0;
   double esurf = 0.0;
   int vox_n[3] = {0, 0, 0};
@@ -220,6 +225,8 @@ parse(std::istream & in, Spec & s, std::string & err)
       ok = bool(ls >> s.first >> s.n);
     else if (key == "records")
       ok = bool(ls >> s.records);
+    else if (key == "events")
+      ok = bool(ls >> s.event_mask);
     else if (key == "sim")
       ok = bool(ls >> s.sim_index) && s.sim_index < (1ull << 23);
     else if (key == "sputter")

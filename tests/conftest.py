@@ -8,7 +8,10 @@ ROOT = Path(__file__).resolve().parent.parent
 sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "oracle"))
 
-REFERENCE = Path(os.environ.get("MYTRIM_REFERENCE", "/root/reference"))
+import oracle_io  # noqa: E402
+
+# the reference checkout where present (None on machines without it)
+REFERENCE = oracle_io.reference_dir()
 
 
 def pytest_configure(config):
@@ -17,8 +20,7 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session")
 def oracle_built():
-    import oracle_io
-    oracle_io.build(REFERENCE if (REFERENCE / "trim.C").exists() else None)
+    oracle_io.build(REFERENCE)
     return oracle_io
 
 

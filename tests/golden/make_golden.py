@@ -1,6 +1,6 @@
 """Regenerate the golden fixtures of tests/golden from the reference checkout.
 
-Needs the reference sources (default /root/reference, or MYTRIM_REFERENCE): it
+Needs the reference sources ($MYTRIM_REFERENCE, else oracle/Makefile's REF): it
 builds the reference library with oracle/Makefile ("make ref"), runs it through
 oracle/_ref/ref_driver and copies the reference's own validation data.
 
@@ -14,7 +14,6 @@ oracle/_ref/ref_driver and copies the reference's own validation data.
 Usage: python tests/golden/make_golden.py
 """
 import json
-import os
 import sys
 from pathlib import Path
 
@@ -26,7 +25,9 @@ sys.path.insert(0, str(ROOT / "oracle"))
 import oracle_io  # noqa: E402
 from golden_cases import CASES  # noqa: E402
 
-REF = Path(os.environ.get("MYTRIM_REFERENCE", "/root/reference"))
+REF = oracle_io.reference_dir()
+if REF is None:
+    sys.exit("the reference checkout is needed: set MYTRIM_REFERENCE")
 
 
 def main():

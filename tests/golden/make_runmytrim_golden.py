@@ -8,12 +8,11 @@ with oracle/Makefile ("make ref") and driven by oracle/_ref/ref_runmytrim with
 runmytrim's seeding (master seed -> 16-bit per-primary mt19937 seeds).  The
 summary lines runmytrim prints on stderr are kept in <case>.summary.
 
-Needs the reference checkout (default /root/reference, or MYTRIM_REFERENCE).
+Needs the reference checkout ($MYTRIM_REFERENCE, else oracle/Makefile's REF).
 
 Usage: python tests/golden/make_runmytrim_golden.py
 """
 import json
-import os
 import re
 import shutil
 import sys
@@ -29,7 +28,9 @@ sys.path.insert(0, str(ROOT / "oracle"))
 import oracle_io  # noqa: E402
 from mytrim_gb300 import runmytrim  # noqa: E402
 
-REF = Path(os.environ.get("MYTRIM_REFERENCE", "/root/reference"))
+REF = oracle_io.reference_dir()
+if REF is None:
+    sys.exit("the reference checkout is needed: set MYTRIM_REFERENCE")
 
 
 def doc(ion, layers, otype, seed, extra_opts=None, extra_out=None):

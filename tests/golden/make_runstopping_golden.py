@@ -6,12 +6,11 @@ for it ("E S_e" per line), computed by the reference library itself
 oracle/Makefile "make ref").  The ions and targets are the reference's stopping
 validation cases (H and He in Fe, C in W) plus a compound target.
 
-Needs the reference checkout (default /root/reference, or MYTRIM_REFERENCE).
+Needs the reference checkout ($MYTRIM_REFERENCE, else oracle/Makefile's REF).
 
 Usage: python tests/golden/make_runstopping_golden.py
 """
 import json
-import os
 import sys
 from pathlib import Path
 
@@ -24,7 +23,9 @@ sys.path.insert(0, str(ROOT / "oracle"))
 import oracle_io  # noqa: E402
 from mytrim_gb300 import runstopping  # noqa: E402
 
-REF = Path(os.environ.get("MYTRIM_REFERENCE", "/root/reference"))
+REF = oracle_io.reference_dir()
+if REF is None:
+    sys.exit("the reference checkout is needed: set MYTRIM_REFERENCE")
 
 FE = {"rho": 7.8658, "elements": [{"Z": 26, "mass": 55.847, "fraction": 1}]}
 CASES = {

@@ -10,7 +10,13 @@ agree to 1e-9.  The configurations are:
 
 * Cu 100 keV into Cu, the full 10^4 primaries;
 * B 10 keV and As 50 keV at 7 deg into 10 nm SiO2 on Si, 10^5 and 2*10^4 primaries;
-* Ag 200 keV into Si, the benchmark workload, 4000 primaries.
+* Ag 200 keV into Si, the benchmark workload, 4000 primaries;
+* eight simulations of the 4096-simulation batch (largest Z1, highest energy,
+  thickest stack, ...), each against the oracle run on its own;
+* the event log (vacancies, replacements, followed and dissipated recoils, rest
+  states, losses, history) against the oracle's records of the same hook calls,
+  and the TrimDefectLog / TrimPhononOut text streams written from them, line for
+  line.
 
 Per primary, the first 400 primaries of each must match: collisions and vacancies
 exactly; electronic and nuclear loss and the stopping point to 1e-9.
@@ -80,6 +86,88 @@ def test_fp64_equals_oracle_on_same_streams(oracle_built, engine_lib, name):
         for k in keys:
             assert math.isclose(p[k][i], rec[k], rel_tol=1e-9, abs_tol=1e-6), (name, i, k, p[k][i], rec[k])
     assert n_rest > N_RECORDS // 2
+
+
+def _pick_c3(sims):
+    """eight simulations of the batch that stress it differently"""
+    idx = {
+        "largest Z1": max(range(len(sims)), key=lambda i: (sims[i].Z, sims[i].E)),
+        "highest E0": max(range(len(sims)), key=lambda i: sims[i].E),
+        "thickest stack": max(range(len(sims)), key=lambda i: sum(l.thickness for l in sims[i].layers[:-1])),
+        "most layers, steepest": max(range(len(sims)), key=lambda i: (len(sims[i].layers), -sims[i].dir[0])),
+        "lightest ion": min(range(len(sims)), key=lambda i: (sims[i].Z, -sims[i].n_primaries)),
+        "most primaries": max(range(len(sims)), key=lambda i: sims[i].n_primaries),
+        "lowest E0": min(range(len(sims)), key=lambda i: sims[i].E),
+        "last": len(sims) - 1,
+    }
+    return idx
+
+
+def test_c3_simulations_of_the_batch_equal_oracle(oracle_built, engine_lib):
+    """C3: 4096 uneven simulations in one FP64 launch (a thousandth of the
+    configuration's primaries: about 6e4); eight of them, each run by the oracle on
+    its own with that simulation's keys, give the same integer tallies and range
+    histogram exactly and the same energy sums to 1e-9."""
+    sims = W.batched_uneven(n_sims=4096, seed=1, scale_primaries=1e-3)
+    from mytrim_gb300 import Engine
+    e = Engine(precision="fp64", seed=7)
+    out = e.run(sims)
+    e.close()
+    for label, i in _pick_c3(sims).items():
+        o = oracle_built.run_parallel(sims[i], seed=7, philox=True, sim_index=i)
+        g = out[i]
+        for k in INT_KEYS:
+            assert g[k] == o[k], (label, i, k, g[k], o[k])
+        assert list(g["hist_range"]) == list(o["hist_range"]), (label, i)
+        for k in ("Eel", "Enuc", "Elost", "sx", "sxx"):
+            assert math.isclose(g[k], o[k], rel_tol=1e-9, abs_tol=1e-6), (label, i, k, g[k], o[k])
+
+
+ALL_EVENTS = (1, 2, 3, 4, 5, 6, 7)  # vacancy, replacement, branch, dissipate, rest, lost, history
+
+
+def _as_event_array(records, like):
+    """oracle event records as the GPU's structured event array"""
+    out = np.zeros(len(records), dtype=like.dtype)
+    for k in ("kind", "key", "primary", "gen", "Z", "state", "x", "y", "z", "E", "aux", "m"):
+        out[k] = [r[k] for r in records]
+    out["sim"] = 0
+    out["tag"] = -1
+    return out
+
+
+@pytest.mark.parametrize("name", ["cu5k_cu", "as20k_sio2_si_cut"])
+def test_event_streams_equal_oracle(oracle_built, engine_lib, name):
+    """The event log -- the hook calls TrimDefectLog, TrimPhononOut and TrimHistory
+    stream (trim.C:467-527, trim.h:139-153) -- against the oracle's records of the
+    same hook calls on the same streams: the same events, integer fields exactly,
+    positions and energies to 1e-9, and the TrimDefectLog and TrimPhononOut text
+    (mytrim_gb300.streams) line for line."""
+    from mytrim_gb300 import Engine, streams
+    from mytrim_gb300 import _ffi as F
+    if name == "cu5k_cu":
+        sim = W.cu_self_ion(n_primaries=300, E=5e3)
+    else:
+        sim = W.arsenic_implant(n_primaries=300)
+        sim.E = 20e3
+    e = Engine(precision="fp64", seed=31)
+    e.set_event_log(ALL_EVENTS, 10_000_000)
+    t = e.run([sim])[0]
+    ev = e.events()
+    e.close()
+    o = oracle_built.run_parallel(sim, seed=31, philox=True, event_mask=sum(1 << k for k in ALL_EVENTS))
+    oe = _as_event_array(o["events"], ev)
+    assert len(ev) == len(oe) > 1000
+    assert (ev["kind"] == F.EV_VACANCY).sum() == t["vacancies"]
+    if name != "cu5k_cu":
+        assert (ev["kind"] == F.EV_LOST).sum() == t["lost"] > 0
+    a, b = streams._sorted(ev), streams._sorted(oe)
+    for k in ("kind", "key", "primary", "gen", "Z", "state", "tag"):
+        assert np.array_equal(a[k], b[k]), (name, k)
+    for k in ("x", "y", "z", "E", "aux", "m"):
+        assert np.allclose(a[k], b[k], rtol=1e-9, atol=1e-6), (name, k)
+    assert list(streams.defect_log(ev)) == list(streams.defect_log(oe))
+    assert list(streams.phonon_log(ev)) == list(streams.phonon_log(oe))
 
 
 def _copper_10k(n):

@@ -40,10 +40,11 @@ def _reduce_noalloc(lib, prim, stream):
 
 
 def _check(q, t):
+    """the same bits: both reductions add the same numbers in the same order"""
     want = [t["vacancies"], t["vac_s2"], t["collisions"], t["coll_s2"], t["Eel"], t["eel_s2"], t["Enuc"],
             t["enuc_s2"], t["range_n"], t["sx"], t["sxx"], t["sy"], t["syy"], t["sz"], t["szz"]]
     for k, (a, b) in enumerate(zip(q, want)):
-        assert np.isclose(a, float(b), rtol=1e-12, atol=1e-9), (k, a, b)
+        assert float(a) == float(b), (k, a, b)
 
 
 def test_noalloc_reduction_matches_run_totals(engine_lib):
