@@ -288,10 +288,16 @@ mtg_status mtg_get_primaries(mtg_ctx * ctx, long long first, long long n, long l
                              double * y, double * z, int * state);
 
 /* Energy-deposition voxels of simulation `sim` of the last run (voxel_n[0] * voxel_n[1] *
- * voxel_n[2] floats, x fastest): electronic loss at the start of each flight path,
+ * voxel_n[2] cells, x fastest): electronic loss at the start of each flight path,
  * nuclear deposits (binding energy, sub-threshold recoils, stopped members) where
- * they happen, in eV.  No counterpart in the reference. */
+ * they happen, in eV.  Each lane sums its consecutive deposits into one cell in
+ * FP32 and adds the sum to the cell's FP64 total, so a cell that collects ~1e8
+ * deposits keeps them all (an FP32 total would stop growing once it passed 2^24
+ * deposits' worth); mtg_get_voxels rounds each cell's total to FP32 once,
+ * mtg_get_voxels64 returns the FP64 totals.  The run's in-box total (Evoxel) is a
+ * compensated FP64 reduction over the cells.  No counterpart in the reference. */
 mtg_status mtg_get_voxels(mtg_ctx * ctx, int sim, float * out, long long n);
+mtg_status mtg_get_voxels64(mtg_ctx * ctx, int sim, double * out, long long n);
 
 /* Record one summary per cascade member (up to `capacity`) in subsequent runs;
  * 0 disables.  Replaces: the fullTraj trajectory dump (trim.C:370-371, 421-422). */

@@ -151,6 +151,7 @@ SIGNATURES = {
                                     C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                     C.POINTER(C.c_int)]),
     "mtg_get_voxels": (C.c_int, [_P, C.c_int, C.POINTER(C.c_float), C.c_longlong]),
+    "mtg_get_voxels64": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double), C.c_longlong]),
     "mtg_set_record_capacity": (C.c_int, [_P, C.c_longlong]),
     "mtg_get_records": (C.c_int, [_P, C.POINTER(MemberRecord), C.c_longlong, C.POINTER(C.c_longlong)]),
     "mtg_set_event_log": (C.c_int, [_P, C.c_uint, C.c_longlong]),

@@ -284,7 +284,7 @@ fill_params(mtg_ctx * ctx, EngineParams & prm)
   prm.prim.fstate = ptr<int>(ctx->p_state);
   prm.totals = ptr<SimTotals>(ctx->d_totals);
   prm.hist = ptr<unsigned long long>(ctx->d_hist);
-  prm.voxels = t.voxel_total > 0 ? ptr<float>(ctx->d_vox) : nullptr;
+  prm.voxels = t.voxel_total > 0 ? ptr<double>(ctx->d_vox) : nullptr;
   prm.error_flags = ptr<unsigned int>(ctx->d_err);
   prm.k0 = t.k0;
   prm.k1 = t.k1;
@@ -556,7 +556,7 @@ mtg_prepare(mtg_ctx * ctx, const mtg_sim * sims, int n_sims)
       vr[2 * s] = d.voxel_base;
       vr[2 * s + 1] = d.voxel_n[0] > 0 ? (long long)d.voxel_n[0] * d.voxel_n[1] * d.voxel_n[2] : 0;
     }
-    CK(ensure(ctx->d_vox, sizeof(float) * size_t(t.voxel_total)));
+    CK(ensure(ctx->d_vox, sizeof(double) * size_t(t.voxel_total)));
     CK(ensure(ctx->d_vox_range, sizeof(long long) * vr.size()));
     CK(ensure(ctx->d_vox_sum, sizeof(double) * ns));
     CK(h2d(ctx, ctx->d_vox_range.p, vr.data(), sizeof(long long) * vr.size()));
@@ -684,7 +684,7 @@ mtg_launch_async(mtg_ctx * ctx, void * stream)
   CK(cudaMemsetAsync(ctx->d_hist.p, 0, 8 * size_t(std::max<long long>(t.hist_total, 1)), s));
   CK(cudaMemsetAsync(ctx->d_err.p, 0, 16, s));
   if (t.voxel_total > 0)
-    CK(cudaMemsetAsync(ctx->d_vox.p, 0, sizeof(float) * size_t(t.voxel_total), s));
+    CK(cudaMemsetAsync(ctx->d_vox.p, 0, sizeof(double) * size_t(t.voxel_total), s));
   CK(cudaMemsetAsync(ctx->d_counters.p, 0, 8 * C_COUNT, s));
   CK(cudaEventRecord(ctx->ev[0], s));
   st = launch_pass(ctx, 0);
@@ -696,7 +696,7 @@ mtg_launch_async(mtg_ctx * ctx, void * stream)
   CK(cudaEventRecord(ctx->ev[1], s));
   if (t.voxel_total > 0)
   {
-    CK(launch_voxel_sum(ptr<float>(ctx->d_vox), ptr<long long>(ctx->d_vox_range), int(t.sims.size()),
+    CK(launch_voxel_sum(ptr<double>(ctx->d_vox), ptr<long long>(ctx->d_vox_range), int(t.sims.size()),
                         ptr<double>(ctx->d_vox_sum), s));
     ctx->stats.launches += 1;
   }
@@ -770,7 +770,7 @@ mtg_collect(mtg_ctx * ctx, mtg_totals * totals, long long * hist)
   {
     if (extra)
     {
-      CK(launch_voxel_sum(ptr<float>(ctx->d_vox), ptr<long long>(ctx->d_vox_range), int(ns),
+      CK(launch_voxel_sum(ptr<double>(ctx->d_vox), ptr<long long>(ctx->d_vox_range), int(ns),
                           ptr<double>(ctx->d_vox_sum), ctx->stream));
       CK(cudaStreamSynchronize(ctx->stream));
     }
@@ -895,8 +895,9 @@ mtg_get_primaries(mtg_ctx * ctx, long long first, long long n, long long * vacan
   return MTG_OK;
 }
 
-mtg_status
-mtg_get_voxels(mtg_ctx * ctx, int sim, float * out, long long n)
+// the voxel cells of simulation `sim` of the last run (FP64 sums on the device)
+static mtg_status
+voxel_cells(mtg_ctx * ctx, int sim, const void * out, long long n, const double ** src, long long * cells)
 {
   mtg_status st = require_device(ctx);
   if (st != MTG_OK)
@@ -906,11 +907,38 @@ mtg_get_voxels(mtg_ctx * ctx, int sim, float * out, long long n)
   if (sim < 0 || sim >= int(ctx->tables.sims.size()) || !out)
     return fail(ctx, MTG_ERR_BAD_INPUT, "bad simulation index or buffer");
   const SimDesc & d = ctx->tables.sims[sim];
-  const long long cells = d.voxel_n[0] > 0 ? (long long)d.voxel_n[0] * d.voxel_n[1] * d.voxel_n[2] : 0;
-  if (n != cells)
+  *cells = d.voxel_n[0] > 0 ? (long long)d.voxel_n[0] * d.voxel_n[1] * d.voxel_n[2] : 0;
+  if (n != *cells)
     return fail(ctx, MTG_ERR_BAD_INPUT, "buffer size must equal the simulation's voxel count");
-  if (cells > 0)
-    CK(cudaMemcpy(out, ptr<float>(ctx->d_vox) + d.voxel_base, sizeof(float) * cells, cudaMemcpyDeviceToHost));
+  *src = ptr<double>(ctx->d_vox) + d.voxel_base;
+  return MTG_OK;
+}
+
+mtg_status
+mtg_get_voxels(mtg_ctx * ctx, int sim, float * out, long long n)
+{
+  const double * src = nullptr;
+  long long cells = 0;
+  mtg_status st = voxel_cells(ctx, sim, out, n, &src, &cells);
+  if (st != MTG_OK || cells == 0)
+    return st;
+  // FP32 tally: each cell's FP64 sum rounded once
+  std::vector<double> tmp(static_cast<size_t>(cells));
+  CK(cudaMemcpy(tmp.data(), src, sizeof(double) * cells, cudaMemcpyDeviceToHost));
+  for (long long i = 0; i < cells; ++i)
+    out[i] = float(tmp[static_cast<size_t>(i)]);
+  return MTG_OK;
+}
+
+mtg_status
+mtg_get_voxels64(mtg_ctx * ctx, int sim, double * out, long long n)
+{
+  const double * src = nullptr;
+  long long cells = 0;
+  mtg_status st = voxel_cells(ctx, sim, out, n, &src, &cells);
+  if (st != MTG_OK || cells == 0)
+    return st;
+  CK(cudaMemcpy(out, src, sizeof(double) * cells, cudaMemcpyDeviceToHost));
   return MTG_OK;
 }
 

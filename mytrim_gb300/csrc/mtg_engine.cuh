@@ -75,7 +75,9 @@ struct EngineParams
   PrimaryTallies prim;
   SimTotals * totals;
   unsigned long long * hist; // all histograms, per-simulation bases in SimDesc
-  float * voxels;            // energy-deposition voxels of all simulations (may be NULL)
+  double * voxels;           // energy-deposition voxels of all simulations (may be NULL):
+                             // FP64 sums in global memory (L2 atomics), fed by each lane's
+                             // short FP32 run of deposits into one cell
   unsigned int * error_flags;
   uint32_t k0, k1;
   unsigned int max_collisions; // per member
@@ -358,8 +360,12 @@ struct LaneSink
     if constexpr (!MID)
       return;
     LaneCold<Acc> & c = *cold;
+    // the lane's run of deposits into one cell is short (FP32 is exact enough for
+    // it); the cell's sum over the whole run takes up to ~1e8 of them, which FP32
+    // would round away once the sum passes 2^24 deposits' worth, so it is kept in
+    // FP64 (the float is widened on its bit pattern, no FP64 instruction here)
     if (c.vcell >= 0)
-      atomicAdd(prm->voxels + c.vcell, c.vacc);
+      atomicAdd(prm->voxels + c.vcell, widen_f32(c.vacc));
     c.vcell = -1;
     c.vacc = 0.0f;
   }

@@ -66,7 +66,7 @@ struct ReduceJob
   int sim;
   long long begin, end;
 };
-cudaError_t launch_voxel_sum(const float * vox, const long long * range, int nsims, double * out, cudaStream_t st);
+cudaError_t launch_voxel_sum(const double * vox, const long long * range, int nsims, double * out, cudaStream_t st);
 cudaError_t launch_reduce(const ReduceJob * jobs, int njobs, const PrimaryTallies & prim, double * partials,
                           const int * job_first, int nsims, double * out, cudaStream_t st);
 

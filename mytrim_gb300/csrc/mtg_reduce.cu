@@ -107,12 +107,12 @@ reduce_finish_kernel(const int * job_first, int nsims, const double * partials, 
 
 // compensated sum of each simulation's voxel grid (block per simulation, fixed order)
 __global__ void __launch_bounds__(RBLOCK)
-voxel_sum_kernel(const float * vox, const long long * range, double * out)
+voxel_sum_kernel(const double * vox, const long long * range, double * out)
 {
   const long long b = range[2 * blockIdx.x], n = range[2 * blockIdx.x + 1];
   Comp a{0.0, 0.0};
   for (long long i = threadIdx.x; i < n; i += RBLOCK)
-    comp_add(a, double(vox[b + i]));
+    comp_add(a, vox[b + i]);
   __shared__ Comp red[RBLOCK];
   red[threadIdx.x] = a;
   __syncthreads();
@@ -127,7 +127,7 @@ voxel_sum_kernel(const float * vox, const long long * range, double * out)
 }
 
 cudaError_t
-launch_voxel_sum(const float * vox, const long long * range, int nsims, double * out, cudaStream_t st)
+launch_voxel_sum(const double * vox, const long long * range, int nsims, double * out, cudaStream_t st)
 {
   if (nsims > 0)
     voxel_sum_kernel<<<nsims, RBLOCK, 0, st>>>(vox, range, out);

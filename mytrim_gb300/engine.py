@@ -380,11 +380,18 @@ class Engine:
             p(out["y"], C.c_double), p(out["z"], C.c_double), p(out["state"], C.c_int)))
         return out
 
-    def voxels(self, sim: int = 0) -> np.ndarray:
+    def voxels(self, sim: int = 0, fp64: bool = False) -> np.ndarray:
+        """Energy-deposition voxels of simulation `sim` [eV], (nz, ny, nx): the FP32
+        tally, or with fp64 the FP64 cell totals it is rounded from."""
         s = self._sims[sim]
         nx, ny, nz = s.voxel_n
-        out = np.zeros(nx * ny * nz, dtype=np.float32)
-        self._check(self.lib.mtg_get_voxels(self.ctx, sim, out.ctypes.data_as(C.POINTER(C.c_float)), len(out)))
+        if fp64:
+            out = np.zeros(nx * ny * nz, dtype=np.float64)
+            self._check(self.lib.mtg_get_voxels64(self.ctx, sim, out.ctypes.data_as(C.POINTER(C.c_double)),
+                                                  len(out)))
+        else:
+            out = np.zeros(nx * ny * nz, dtype=np.float32)
+            self._check(self.lib.mtg_get_voxels(self.ctx, sim, out.ctypes.data_as(C.POINTER(C.c_float)), len(out)))
         return out.reshape(nz, ny, nx)
 
     def set_record_capacity(self, cap: int):

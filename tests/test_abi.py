@@ -10,7 +10,7 @@ HEADER = ROOT / "include" / "mytrim_gpu.h"
 
 def declared():
     text = HEADER.read_text()
-    return sorted(set(re.findall(r"\b(mtg_[a-z_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(mtg_[a-z0-9_]+)\s*\(", text)))
 
 
 def test_header_declarations_are_exported(engine_lib):

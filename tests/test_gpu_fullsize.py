@@ -13,9 +13,11 @@ measurement configurations (GB300; called through the C ABI):
 * C4, Ag 200 keV into Si, 10^7 primaries, FP32: energy conservation; the FP32
   path's and the surrogate path's (2^21 primaries) range, straggle, lateral spread,
   vacancies and energy split each within 1 % of the FP64 path's (2^18 primaries);
-* C5, Au 1 MeV into Ag / Cu / Si, 10^6 of the 10^8 primaries (about 5 s), FP32 with
-  256^3 voxels: the voxel total equals the energy deposited inside the box, which
-  is at most the total deposit; sputtered atoms and backscattered ions counted.
+* C5, Au 1 MeV into Ag / Cu / Si, 2^20 of the 10^8 primaries (about 7 s), FP32 with
+  256^3 voxels accumulated in FP64: the FP32 tally is the FP64 totals rounded once,
+  the voxel total equals the energy deposited inside the box, which is at most the
+  total deposit; four primary shards add up to the whole run cell by cell;
+  sputtered atoms and backscattered ions counted.
 
 "Within 1 %" means: the relative difference is under 1 % and the combined standard
 error under 1/3 %, so that a 1 % error would show at 3 sigma (parity_stats.py).
@@ -123,16 +125,30 @@ def test_c4_silver_into_silicon_against_fp64():
 
 
 def test_c5_gold_deposition_voxels():
-    n = 1_000_000
+    n = 1 << 20
     sim = W.gold_deposition(n_primaries=n, voxels=256)
     e = Engine(precision="fp32", seed=1)
     t = e.run([sim])[0]
     vox = e.voxels(0)
+    vox64 = e.voxels(0, fp64=True)
     e.close()
     assert vox.shape == (256, 256, 256)
     _conserved(t, sim.E, n, 2e-6)
-    inside = float(vox.sum(dtype=np.float64))
-    assert math.isclose(inside, t["Evoxel"], rel_tol=1e-6)
+    # the FP32 tally is each cell's FP64 total rounded once
+    assert np.array_equal(vox, vox64.astype(np.float32))
+    inside = float(vox64.sum())
+    assert math.isclose(inside, t["Evoxel"], rel_tol=1e-9)
     assert 0.5 * (t["Eel"] + t["Enuc"]) < t["Evoxel"] <= (t["Eel"] + t["Enuc"]) * (1 + 1e-6)
     assert t["sputtered"] > 0 and t["backscattered"] > 0
     assert t["Esputtered"] > 0.0
+    # FP64 cell totals: four primary shards add up to the whole run cell by cell
+    # (an FP32 total would drift by its rounding of every deposit)
+    parts = np.zeros_like(vox64)
+    for k in range(4):
+        e = Engine(precision="fp32", seed=1)
+        e.run([SimSpec(**{**sim.__dict__, "n_primaries": n // 4, "first_primary": k * (n // 4)})])
+        parts += e.voxels(0, fp64=True)
+        e.close()
+    big = vox64 > 1e-6 * vox64.max()
+    assert np.allclose(parts[big], vox64[big], rtol=1e-9)
+    assert float(vox64.max()) > 1e6  # the entrance cells collect millions of deposits' worth
