@@ -171,6 +171,12 @@ typedef struct
   int potential;          /* TrimBase::_potential, an mtg_potential value; 0 = universal.  The
                              learned surrogate covers the universal potential only: the
                              other two scatter exactly on the surrogate path as well */
+  int md_tag_Z;           /* IonMDTag::_md (ion.h:89-100) as the reference's demo programs
+                             set it (apps/mytrim_solid.C:156-159): a member of atomic number
+                             md_tag_Z whose energy at the start of its trajectory lies in
+                             (md_tag_Emin, md_tag_Emax) gets _md = 1; every other member, and
+                             every recoil when it is spawned (ion.C:88-93), 0.  0 = off */
+  double md_tag_Emin, md_tag_Emax; /* the MD energy gap [eV], e.g. 200 and 12000 */
 } mtg_sim;
 
 /* Run-wide settings (SimconfType scalars, simconf.h:66). */
@@ -235,7 +241,7 @@ typedef struct
   int kernel_level;        /* feature level of the last run's cascade kernel: 0 lean, 1 member
                               records / voxels / tally modes, 2 + event log, 3 cluster geometry
                               or a non-universal potential, 4 + event log */
-  int pad_stats;
+  int max_take;            /* fresh primaries one warp took per refill in the last run */
 } mtg_stats;
 
 typedef struct mtg_ctx mtg_ctx;
@@ -343,6 +349,10 @@ typedef struct
   int tag;                 /* IonBase::_tag of the atom: for a followed recoil created inside a
                               cluster of a sampleClusters sample, that cluster's index
                               (trim.C:365, sample_clusters.C:53); -1 otherwise */
+  int md;                  /* IonMDTag::_md of the atom (mtg_sim.md_tag_*): the member's own
+                              for rest, loss and history events, 0 for the recoil of a vacancy,
+                              replacement, branch or dissipation event (a recoil is spawned
+                              with _md = 0, ion.C:88-93) */
 } mtg_event;
 
 /* Log events of the kinds whose bit (1 << kind) is set in kind_mask (0 disables)
@@ -373,6 +383,32 @@ mtg_status mtg_scatter(mtg_ctx * ctx, const double * eps, const double * b, long
  * Replaces: the same block with TrimBase::_potential set (trim.C:194-258). */
 mtg_status mtg_scatter_potential(mtg_ctx * ctx, const double * eps, const double * b, long long n,
                                  int precision, int potential, double * s2);
+
+/* Launch settings chosen by mtg_autotune. */
+typedef struct
+{
+  int block_threads;            /* cascade kernel block shape: 64 or 128 */
+  int max_primaries_per_refill; /* fresh primaries per warp refill, 1..32 */
+  int stack_capacity;           /* recoil stack entries per warp (queue depth); 0 = default */
+  int heuristic_take;           /* the refill size the built-in estimate picks for this run */
+  double default_collisions_per_s; /* trial rate of the built-in settings */
+  double best_collisions_per_s;    /* trial rate of the chosen settings */
+  int trials;                   /* trial launches made */
+  int changed;                  /* 1 if the chosen settings differ from the built-in ones */
+} mtg_tuning;
+
+/* Choose the cascade kernel's launch settings for a run by measurement: the
+ * simulations' primaries are scaled to about `trial_primaries` in total (0 = 65,536)
+ * and launched with the built-in settings, then with each candidate refill size
+ * (1, 2, 4, 8, 16, 32 primaries per warp refill and the built-in estimate), block
+ * shape (64, 128 threads) and recoil stack depth (the default, 2048); the fastest in
+ * collisions per second of kernel time is kept in the context's configuration for
+ * the runs that follow, if it beats the built-in settings by more than 2 %.  The
+ * trials use the context like ordinary runs (their results are discarded).  No
+ * counterpart in the reference, whose threads take primaries one at a time
+ * (apps/runmytrim.C:71-93). */
+mtg_status mtg_autotune(mtg_ctx * ctx, const mtg_sim * sims, int n_sims, long long trial_primaries,
+                        mtg_tuning * out);
 
 /* Counters of the last run. */
 mtg_status mtg_get_stats(const mtg_ctx * ctx, mtg_stats * out);

@@ -60,7 +60,8 @@ class Sim(C.Structure):
                 ("hist_vac_bin", C.c_double), ("hist_vac_n", C.c_int), ("surface_binding", C.c_double),
                 ("voxel_n", C.c_int * 3), ("voxel_origin", C.c_double * 3), ("voxel_size", C.c_double * 3),
                 ("hist_lateral_bin", C.c_double), ("hist_lateral_n", C.c_int), ("max_generation", C.c_int),
-                ("hist_evac_rows", C.c_int), ("potential", C.c_int)]
+                ("hist_evac_rows", C.c_int), ("potential", C.c_int), ("md_tag_Z", C.c_int),
+                ("md_tag_Emin", C.c_double), ("md_tag_Emax", C.c_double)]
 
 
 class Config(C.Structure):
@@ -98,7 +99,7 @@ class MemberRecord(C.Structure):
 class Event(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("x", "y", "z", "E", "aux", "m")] + \
                [("key", C.c_ulonglong), ("primary", C.c_longlong)] + \
-               [(n, C.c_int) for n in ("sim", "kind", "Z", "gen", "state", "tag")]
+               [(n, C.c_int) for n in ("sim", "kind", "Z", "gen", "state", "tag", "md")]
 
 
 # event kinds (mtg_event_kind)
@@ -127,7 +128,13 @@ class Stats(C.Structure):
                 ("drains", C.c_int), ("grid", C.c_int), ("block", C.c_int), ("stack_capacity", C.c_int),
                 ("overflowed", C.c_longlong), ("collisions", C.c_longlong), ("device_bytes", C.c_size_t),
                 ("h2d_bytes", C.c_longlong), ("d2h_bytes", C.c_longlong), ("warp_steps", C.c_longlong),
-                ("kernel_level", C.c_int), ("pad_stats", C.c_int)]
+                ("kernel_level", C.c_int), ("max_take", C.c_int)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("block_threads", C.c_int), ("max_primaries_per_refill", C.c_int), ("stack_capacity", C.c_int),
+                ("heuristic_take", C.c_int), ("default_collisions_per_s", C.c_double),
+                ("best_collisions_per_s", C.c_double), ("trials", C.c_int), ("changed", C.c_int)]
 
 
 # mtg_stats.kernel_level values
@@ -152,6 +159,7 @@ SIGNATURES = {
                                     C.POINTER(C.c_int)]),
     "mtg_get_voxels": (C.c_int, [_P, C.c_int, C.POINTER(C.c_float), C.c_longlong]),
     "mtg_get_voxels64": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double), C.c_longlong]),
+    "mtg_autotune": (C.c_int, [_P, C.c_void_p, C.c_int, C.c_longlong, C.POINTER(Tuning)]),
     "mtg_set_record_capacity": (C.c_int, [_P, C.c_longlong]),
     "mtg_get_records": (C.c_int, [_P, C.POINTER(MemberRecord), C.c_longlong, C.POINTER(C.c_longlong)]),
     "mtg_set_event_log": (C.c_int, [_P, C.c_uint, C.c_longlong]),

@@ -304,6 +304,7 @@ fill_params(mtg_ctx * ctx, EngineParams & prm)
     take = int(std::min<long long>(32, std::min(balance, fill)));
   }
   prm.max_take = take;
+  ctx->stats.max_take = take;
   if (ctx->record_cap > 0)
   {
     prm.records = ptr<MemberRecord>(ctx->d_records);
@@ -858,6 +859,107 @@ mtg_run(mtg_ctx * ctx, const mtg_sim * sims, int n_sims, mtg_totals * totals, lo
   if (st != MTG_OK)
     return st;
   return mtg_collect(ctx, totals, hist);
+}
+
+mtg_status
+mtg_autotune(mtg_ctx * ctx, const mtg_sim * sims, int n_sims, long long trial_primaries, mtg_tuning * out)
+{
+  mtg_status st = require_device(ctx);
+  if (st != MTG_OK)
+    return st;
+  if (!sims || n_sims < 1 || !out || trial_primaries < 0)
+    return fail(ctx, MTG_ERR_BAD_INPUT, "mtg_autotune: simulations, a result and trial_primaries >= 0 are needed");
+  if (trial_primaries == 0)
+    trial_primaries = 65536;
+  long long total = 0;
+  for (int i = 0; i < n_sims; ++i)
+    total += std::max<long long>(0, sims[i].n_primaries);
+  if (total == 0)
+    return fail(ctx, MTG_ERR_BAD_INPUT, "mtg_autotune: no primaries to time");
+  // the trial: the same simulations, primaries scaled to about trial_primaries
+  const double f = total > trial_primaries ? double(trial_primaries) / double(total) : 1.0;
+  std::vector<mtg_sim> trial(sims, sims + n_sims);
+  for (mtg_sim & s : trial)
+    if (s.n_primaries > 0)
+      s.n_primaries = std::max<long long>(1, llround(double(s.n_primaries) * f));
+  const mtg_config base = ctx->cfg;
+  std::vector<mtg_totals> tot(static_cast<size_t>(n_sims));
+  int trials = 0;
+  auto rate = [&](int block, int take, int cap, double & r) -> mtg_status {
+    mtg_config c = base;
+    c.block_threads = block;
+    c.max_primaries_per_refill = take;
+    c.stack_capacity = cap;
+    mtg_status s = mtg_configure(ctx, &c);
+    if (s == MTG_OK)
+      s = mtg_run(ctx, trial.data(), n_sims, tot.data(), nullptr);
+    if (s != MTG_OK)
+      return s;
+    ++trials;
+    r = ctx->stats.kernel_ms > 0.0 ? double(ctx->stats.collisions) / (ctx->stats.kernel_ms * 1e-3) : 0.0;
+    return MTG_OK;
+  };
+  const int block0 = base.block_threads > 0 ? base.block_threads : 128;
+  double r = 0.0, r_def = 0.0;
+  st = rate(block0, 0, base.stack_capacity, r); // warm-up (module load, first allocations)
+  if (st == MTG_OK)
+    st = rate(block0, 0, base.stack_capacity, r_def);
+  const int heuristic = ctx->stats.max_take;
+  int best_block = block0, best_take = 0, best_cap = base.stack_capacity;
+  double best = r_def;
+  const int takes[] = {heuristic, 1, 2, 4, 8, 16, 32};
+  for (int k = 1; k < 7 && st == MTG_OK; ++k)
+  {
+    if (takes[k] == heuristic)
+      continue;
+    st = rate(block0, takes[k], base.stack_capacity, r);
+    if (st == MTG_OK && r > best)
+    {
+      best = r;
+      best_take = takes[k];
+    }
+  }
+  if (st == MTG_OK)
+  {
+    const int other = block0 == 128 ? 64 : 128;
+    st = rate(other, best_take, base.stack_capacity, r);
+    if (st == MTG_OK && r > best)
+    {
+      best = r;
+      best_block = other;
+    }
+  }
+  if (st == MTG_OK && base.stack_capacity != 2048)
+  {
+    st = rate(best_block, best_take, 2048, r);
+    if (st == MTG_OK && r > best)
+    {
+      best = r;
+      best_cap = 2048;
+    }
+  }
+  mtg_config chosen = base;
+  const bool change = st == MTG_OK && best > 1.02 * r_def;
+  if (change)
+  {
+    chosen.block_threads = best_block;
+    chosen.max_primaries_per_refill = best_take;
+    chosen.stack_capacity = best_cap;
+  }
+  mtg_status st2 = mtg_configure(ctx, &chosen);
+  if (st != MTG_OK)
+    return st;
+  if (st2 != MTG_OK)
+    return st2;
+  out->block_threads = change ? best_block : block0;
+  out->max_primaries_per_refill = change ? (best_take > 0 ? best_take : heuristic) : heuristic;
+  out->stack_capacity = change ? best_cap : base.stack_capacity;
+  out->heuristic_take = heuristic;
+  out->default_collisions_per_s = r_def;
+  out->best_collisions_per_s = change ? best : r_def;
+  out->trials = trials;
+  out->changed = change ? 1 : 0;
+  return MTG_OK;
 }
 
 mtg_status

@@ -205,6 +205,7 @@ struct LaneCold
   Acc e_lost, e_unf, e_sput, m_eel;
   long long vcell; // pending voxel deposit: cell and value
   float vacc;
+  int m_md;        // IonMDTag::_md of the lane's member (event-logging levels)
   int evac_bin;    // vacancy-energy bin of the current collision (-1 = none)
 };
 
@@ -280,7 +281,7 @@ struct LaneSink
 
   // ---- event log (opt-in): one entry per selected hook call
   __device__ void event(int kind, Real x, Real y, Real z, Real E, int Z, Real m, int gen, int state, Real aux,
-                        uint64_t key, int tag)
+                        uint64_t key, int tag, int md = 0)
   {
     if (!(prm->event_mask & (1u << kind)))
       return;
@@ -305,6 +306,7 @@ struct LaneSink
     r.gen = gen;
     r.state = state;
     r.tag = tag;
+    r.md = md;
   }
   // TrimHistory::followRecoil (trim.h:146-150): the moving atom's position (after
   // its flight, trim.C:310) at each displaced recoil
@@ -312,7 +314,8 @@ struct LaneSink
   __device__ void history(const P & p, int Z1, Real m1)
   {
     if constexpr (EV)
-      event(EV_HISTORY, Real(p.x), Real(p.y), Real(p.z), Real(p.E), Z1, m1, p.gen, 0, Real(0), p.key, p.tag);
+      event(EV_HISTORY, Real(p.x), Real(p.y), Real(p.z), Real(p.E), Z1, m1, p.gen, 0, Real(0), p.key, p.tag,
+            cold->m_md);
   }
   // followRecoil (trim.C:362): a displaced recoil, followed or not
   template <class R, class E>
@@ -402,7 +405,8 @@ struct LaneSink
   {
     LaneCold<Acc> & c = *cold;
     if constexpr (EV)
-      event(EV_LOST, Real(p.x), Real(p.y), Real(p.z), Real(p.E), Z1, m1, p.gen, ST_LOST, e - Real(p.E), p.key, p.tag);
+      event(EV_LOST, Real(p.x), Real(p.y), Real(p.z), Real(p.E), Z1, m1, p.gen, ST_LOST, e - Real(p.E), p.key, p.tag,
+            cold->m_md);
     ++c.n_lost;
     c.e_lost.add(e);
     if (MID && prm->records)
@@ -507,7 +511,8 @@ struct LaneSink
   __device__ void stop(int state, const P & p, int Z1, Real m1)
   {
     if constexpr (EV)
-      event(EV_REST, Real(p.x), Real(p.y), Real(p.z), Real(p.E), Z1, m1, p.gen, state, Real(0), p.key, p.tag);
+      event(EV_REST, Real(p.x), Real(p.y), Real(p.z), Real(p.E), Z1, m1, p.gen, state, Real(0), p.key, p.tag,
+            cold->m_md);
     if (MID && prm->records)
       cold->m_state = state;
     a_enuc.add(Real(p.E));
@@ -737,6 +742,17 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
         sink.flush_sim(cur_sim);
     }
     Pol::begin_member(mctx, prm, tab, *sim, p);
+    if constexpr (LaneSink<Pol, LVL>::EV)
+    {
+      // IonMDTag: the demo programs' MD-gap mark, taken when the member starts
+      // (apps/mytrim_solid.C:156-159); a spawned recoil's _md is 0 (ion.C:88-93)
+      bool gap;
+      if constexpr (sizeof(typename Pol::Real) == 8)
+        gap = double(p.E) > sim->md_Emin && double(p.E) < sim->md_Emax;
+      else
+        gap = float(p.E) > sim->md_Emin_f && float(p.E) < sim->md_Emax_f; // no FP64 in the FP32 engine
+      sink.cold->m_md = (sim->md_Z != 0 && mctx.sc->Z1 == sim->md_Z && gap) ? 1 : 0;
+    }
     r1 = Pol::first_draw(p.key, prm.k0, prm.k1);
     sink.reset_member();
     ++sink.cold->n_members;

@@ -652,6 +652,17 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
       return MTG_ERR_BAD_INPUT;
     }
     d.potential = s.potential;
+    if (s.md_tag_Z < 0 || s.md_tag_Z > MTG_SCOEF_ROWS ||
+        (s.md_tag_Z > 0 && !(s.md_tag_Emin < s.md_tag_Emax)))
+    {
+      err = "md_tag_Z must be 0..92 with md_tag_Emin < md_tag_Emax";
+      return MTG_ERR_BAD_INPUT;
+    }
+    d.md_Z = s.md_tag_Z;
+    d.md_Emin = s.md_tag_Emin;
+    d.md_Emax = s.md_tag_Emax;
+    d.md_Emin_f = float(s.md_tag_Emin);
+    d.md_Emax_f = float(s.md_tag_Emax);
     if (s.potential != MTG_POT_UNIVERSAL)
       out.any_extended = 1;
     d.prim_begin = prim;

@@ -105,7 +105,9 @@ struct SimDesc
   int follow_gen;       // a displaced recoil is followed iff its generation is below this
   int kp_gen;           // TrimPrimaries: generation whose displaced recoils add a KP count
   int potential;        // TrimBase::Potential: 0 universal, 1 Moliere, 2 C-Kr
-  int pad_potential;
+  int md_Z;             // IonMDTag rule: members of this Z born in (md_Emin, md_Emax) get _md = 1 (0 = off)
+  double md_Emin, md_Emax;
+  float md_Emin_f, md_Emax_f; // single-precision copies (FP32 engine)
   long long prim_begin; // first global primary index of this simulation
   long long n_primaries;
   uint64_t sim_key;     // simulation number used in the member keys
@@ -177,6 +179,7 @@ struct EventRec
   uint64_t key;
   long long primary;
   int sim, kind, Z, gen, state, tag;
+  int md; // IonMDTag::_md of the atom
 };
 
 // event kinds (bit k of the log's mask selects kind k)

@@ -67,6 +67,11 @@ class SimSpec:
     hist_lateral_n: int = 0
     hist_evac_rows: int = 0              # vacancy-energy histogram rows (int(ln E))
     potential: str = "universal"         # TrimBase::_potential: "universal", "moliere" or "ckr"
+    # IonMDTag::_md as the reference's demo programs mark it (apps/mytrim_solid.C:156-159):
+    # members of atomic number md_tag_Z starting with an energy inside md_tag_E get
+    # _md = 1 in the event log; 0 = off
+    md_tag_Z: int = 0
+    md_tag_E: Tuple[float, float] = (200.0, 12000.0)
     # sampleClusters geometry: layers[0] is the matrix, layers[1] the cluster
     # material; clusters is an (n, 4) array of x, y, z, r; cluster_hash the
     # spatial-hash cells per axis (sampleClusters::initSpatialhash)
@@ -133,6 +138,8 @@ class SimSpec:
         s.hist_lateral_n = self.hist_lateral_n
         s.hist_evac_rows = self.hist_evac_rows
         s.potential = POTENTIALS[self.potential]
+        s.md_tag_Z = self.md_tag_Z
+        s.md_tag_Emin, s.md_tag_Emax = self.md_tag_E
         s.voxel_n[0:3] = self.voxel_n
         s.voxel_origin[0:3] = self.voxel_origin
         s.voxel_size[0:3] = self.voxel_size
@@ -211,6 +218,9 @@ def sims_to_array(sims: Sequence["SimSpec"]):
               "hist_lateral_bin", "hist_lateral_n", "hist_evac_rows", "voxel_n", "voxel_origin", "voxel_size"):
         a[f] = [getattr(s, f) for s in sims]
     a["potential"] = [POTENTIALS[s.potential] for s in sims]
+    a["md_tag_Z"] = [s.md_tag_Z for s in sims]
+    a["md_tag_Emin"] = [s.md_tag_E[0] for s in sims]
+    a["md_tag_Emax"] = [s.md_tag_E[1] for s in sims]
     return a, keep
 
 
@@ -428,7 +438,7 @@ class Engine:
         cap = getattr(self, "_event_cap", 0)
         dt = np.dtype([("x", "<f8"), ("y", "<f8"), ("z", "<f8"), ("E", "<f8"), ("aux", "<f8"), ("m", "<f8"), ("key", "<u8"),
                        ("primary", "<i8"), ("sim", "<i4"), ("kind", "<i4"), ("Z", "<i4"), ("gen", "<i4"),
-                       ("state", "<i4"), ("tag", "<i4")])
+                       ("state", "<i4"), ("tag", "<i4"), ("md", "<i4"), ("pad", "<i4")])
         assert dt.itemsize == C.sizeof(F.Event)
         out = np.zeros(max(cap, 1), dtype=dt)
         n, total = C.c_longlong(0), C.c_longlong(0)
@@ -496,6 +506,15 @@ class Engine:
         pd = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
         self._check(self.lib.mtg_surrogate_quadrature(self.ctx, pd(e), pd(bb), len(e), pd(s2), pd(tau)))
         return s2, tau
+
+    def autotune(self, sims: Sequence[SimSpec], trial_primaries: int = 0) -> dict:
+        """Choose the launch settings (refill size, block shape, stack depth) for runs
+        like `sims` by timing trial launches (mtg_autotune); the context keeps them."""
+        arr, keep = sims_to_array(sims)
+        t = F.Tuning()
+        self._check(self.lib.mtg_autotune(self.ctx, arr.ctypes.data, len(sims), trial_primaries, C.byref(t)))
+        del keep
+        return {n: getattr(t, n) for n, _ in t._fields_}
 
     def stats(self) -> dict:
         s = F.Stats()

@@ -8,6 +8,8 @@ the engine's event log (``Engine.set_event_log`` / ``Engine.events``).
   species over the sample's (x, y) extent;
 * ``history`` -- TrimHistory (trim.h:139-153): the moving atom's positions at its
   displaced recoils;
+* ``md_tag_log`` -- IonMDTag's stream form (ion.C:98-104) of the members at rest:
+  "<ion> <_md>";
 * ``phonon_log`` -- TrimPhononOut (trim.C:504-527): "<E> <ion>" for every energy
   left in the lattice: the binding energy of each displaced recoil, the energy plus
   binding energy of each recoil below the displacement energy, the residual energy
@@ -67,6 +69,15 @@ def phonon_log(events: np.ndarray) -> Iterable[str]:
             yield f"{_g(e['E'] + e['aux'])} " + _ion(e)
         elif k == F.EV_REST:
             yield f"{_g(e['E'])} " + _ion(e)
+
+
+def md_tag_log(events: np.ndarray) -> Iterable[str]:
+    """IonMDTag's stream form (ion.C:98-104: the IonBase fields, then _md) of every
+    member that came to rest (events logged with kind EV_REST; SimSpec.md_tag_Z sets
+    the MD-gap rule), as the demo programs print their tagged ions."""
+    for e in _sorted(events):
+        if int(e["kind"]) == F.EV_REST:
+            yield _ion(e) + f"{int(e['md'])} "
 
 
 def vac_map(events: np.ndarray, w, z, mx: int = 20, my: int = 20) -> np.ndarray:

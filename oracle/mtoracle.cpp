@@ -415,6 +415,7 @@ struct Ion
   int gen;
   int state;
   uint64_t key;
+  int md = 0; // IonMDTag::_md: 0 when spawned (ion.C:88-93)
 };
 
 struct Engine
@@ -510,6 +511,9 @@ struct Engine
   void run_member(Ion & pka, Push && push)
   {
     pka.state = MOVING;
+    // the demo programs' MD-gap mark, set when the member is popped (mytrim_solid.C:156-159)
+    if (spec.md_Z != 0 && pka.Z == spec.md_Z && pka.E > spec.md_Emin && pka.E < spec.md_Emax && pka.md == 0)
+      pka.md = 1;
     const double scale = spec.scale;
     const double invscale = 1.0 / scale;
     PhiloxDraw ph{pk0, pk1, pka.key};
@@ -682,7 +686,7 @@ struct Engine
       {
         if (rec.E > el.Edisp - el.Elbind)
         {
-          emit(EV_HISTORY, pka.pos, pka.E, pka.Z, pka.m, pka.gen, 0, 0.0, pka.key);
+          emit(EV_HISTORY, pka.pos, pka.E, pka.Z, pka.m, pka.gen, 0, 0.0, pka.key, pka.md);
           emit(EV_BRANCH, rec.pos, rec.E, el.Z, el.m, rec.gen, 0, el.Elbind, pka.key);
           t.Enuc += el.Elbind;
           p_enuc += el.Elbind;
@@ -795,13 +799,13 @@ struct Engine
     last_state = pka.state;
     if (pka.state == LOST)
     {
-      emit(EV_LOST, pka.pos, pka.E, pka.Z, pka.m, pka.gen, LOST, recoil_energy, pka.key);
+      emit(EV_LOST, pka.pos, pka.E, pka.Z, pka.m, pka.gen, LOST, recoil_energy, pka.key, pka.md);
       t.lost++;
       t.Elost += pka.E + recoil_energy;
       t.exit_surface(pka.pos[0], pka.gen, pka.E, pka.dir[0]);
       return;
     }
-    emit(EV_REST, pka.pos, pka.E, pka.Z, pka.m, pka.gen, pka.state, 0.0, pka.key);
+    emit(EV_REST, pka.pos, pka.E, pka.Z, pka.m, pka.gen, pka.state, 0.0, pka.key, pka.md);
     t.Enuc += pka.E;
     p_enuc += pka.E;
     t.deposit(pka.pos[0], pka.pos[1], pka.pos[2], pka.E);
@@ -844,12 +848,13 @@ struct Engine
     EV_LOST = 6,
     EV_HISTORY = 7
   };
-  void emit(int kind, const double pos[3], double E, int Z, double m, int gen, int state, double aux, uint64_t key)
+  void emit(int kind, const double pos[3], double E, int Z, double m, int gen, int state, double aux, uint64_t key,
+            int md = 0)
   {
     if (!(spec.event_mask & (1u << kind)))
       return;
-    printf("ev %d %llu %lld %d %d %d %a %a %a %a %a %a\n", kind, (unsigned long long)key, cur_primary, gen, Z,
-           state, pos[0], pos[1], pos[2], E, aux, m);
+    printf("ev %d %llu %lld %d %d %d %d %a %a %a %a %a %a\n", kind, (unsigned long long)key, cur_primary, gen, Z,
+           state, md, pos[0], pos[1], pos[2], E, aux, m);
   }
 
   void run()

@@ -78,6 +78,8 @@ def spec_text(sim, seed=1, philox=True, first=0, n=None, records=0, tmin=None, o
         lines.append(f"sim {int(sim_index)}")
     if event_mask:
         lines.append(f"events {int(event_mask)}")
+    if getattr(sim, "md_tag_Z", 0):
+        lines.append(f"mdtag {int(sim.md_tag_Z)} {sim.md_tag_E[0]!r} {sim.md_tag_E[1]!r}")
     if output is not None:
         lines.append(f"output {output[0]} {output[1]}")
     if getattr(sim, "geometry", "layers") == "clusters":
@@ -96,7 +98,7 @@ def spec_text(sim, seed=1, philox=True, first=0, n=None, records=0, tmin=None, o
     return "\n".join(lines) + "\n"
 
 
-EVENT_FIELDS = ("kind", "key", "primary", "gen", "Z", "state", "x", "y", "z", "E", "aux", "m")
+EVENT_FIELDS = ("kind", "key", "primary", "gen", "Z", "state", "md", "x", "y", "z", "E", "aux", "m")
 
 
 def parse(text):
@@ -107,7 +109,7 @@ def parse(text):
             continue
         k = parts[0]
         if k == "ev":
-            vals = [int(v) for v in parts[1:7]] + [float.fromhex(v) for v in parts[7:13]]
+            vals = [int(v) for v in parts[1:8]] + [float.fromhex(v) for v in parts[8:14]]
             out["events"].append(dict(zip(EVENT_FIELDS, vals)))
         elif k == "rec":
             idx, mem, coll, vac = (int(v) for v in parts[1:5])

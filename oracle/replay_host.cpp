@@ -15,6 +15,7 @@
 //   replay_host <tables> --stopping              "Z1 m1 rho n Z m t ...", then energies -> stopping (hex)
 //   replay_host <tables> --scatter [potential]   lines "eps b" -> sin^2(theta/2) (hex)
 //   replay_host <tables> --mathcheck [n]         exp64 / log64 short routes vs full forms
+//   replay_host <tables> --eval exp|log|pow       lines of hex-float arguments -> results (hex)
 //   replay_host <tables> --philox                lines of six hex words -> Philox outputs
 //   replay_host <tables> --lookupcheck n < spec  cluster lookup with vs without the mask
 
@@ -166,6 +167,32 @@ main(int argc, char ** argv)
                           uint32_t(v[5]));
       const U2 b = philox2(U2{uint32_t(v[0]), uint32_t(v[1])}, uint32_t(v[4]));
       printf("%08x %08x %08x %08x %08x %08x\n", a.x, a.y, a.z, a.w, b.x, b.y);
+    }
+    return 0;
+  }
+  if (argc >= 4 && std::string(argv[2]) == "--eval")
+  {
+    // lines of hex-float arguments -> the engine's exp64 / log64 (one argument) or
+    // pow64 (two) of them, in hex
+    const std::string f = argv[3];
+    std::string line;
+    while (std::getline(std::cin, line))
+    {
+      std::istringstream ls(line);
+      std::string a, b;
+      if (!(ls >> a))
+        continue;
+      const double x = std::strtod(a.c_str(), nullptr);
+      double r;
+      if (f == "exp")
+        r = exp64(x);
+      else if (f == "log")
+        r = log64(x);
+      else if (f == "pow" && (ls >> b))
+        r = pow64(x, std::strtod(b.c_str(), nullptr));
+      else
+        return 2;
+      printf("%a\n", r);
     }
     return 0;
   }

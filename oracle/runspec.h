@@ -29,6 +29,9 @@
 //                               (1 << kind) is set, with the fields of the GPU event
 //                               log (mtg_event): 1 vacancy, 2 replacement, 3 followRecoil
 //                               branch, 4 dissipated recoil, 5 rest, 6 lost, 7 history
+//   mdtag <Z> <Emin> <Emax>     IonMDTag::_md as the demo programs set it: a member of
+//                               atomic number Z starting with Emin < E < Emax has _md 1
+//                               (apps/mytrim_solid.C:156-159), reported in the "ev" lines
 //   sim <index>                 simulation index of the member keys (philox seeding):
 //                               the keys the GPU gives simulation <index> of a batch
 //   records <n>                 emit per-primary records for the first n primaries
@@ -96,6 +99,8 @@ struct Spec
   long long first = 0, n = -1;
   unsigned long long sim_index = 0;
   unsigned int event_mask = 0;
+  int md_Z = 0;
+  double md_Emin = 0.0, md_Emax = 0.0;
   int records = 0;
   double esurf = 0.0;
   int vox_n[3] = {0, 0, 0};
@@ -225,6 +230,8 @@ parse(std::istream & in, Spec & s, std::string & err)
       ok = bool(ls >> s.first >> s.n);
     else if (key == "records")
       ok = bool(ls >> s.records);
+    else if (key == "mdtag")
+      ok = bool(ls >> s.md_Z >> s.md_Emin >> s.md_Emax);
     else if (key == "events")
       ok = bool(ls >> s.event_mask);
     else if (key == "sim")

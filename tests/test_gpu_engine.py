@@ -558,3 +558,25 @@ def test_event_tags_name_the_cluster_of_birth(engine_lib, prec):
     ev = e.events()
     e.close()
     assert (ev["tag"] == -1).all()
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_autotune_chooses_settings_that_keep_results(engine_lib, prec):
+    """mtg_autotune times trial launches and keeps the fastest settings in the
+    context; the integer tallies of a run do not depend on the launch settings (the
+    random streams are keyed by member and collision, not by lane)."""
+    sim = W.cu_self_ion(n_primaries=20_000, E=20e3)
+    e = Engine(precision=prec, seed=41)
+    before = e.run([sim])[0]
+    tune = e.autotune([sim], trial_primaries=4096)
+    after = e.run([sim])[0]
+    st = e.stats()
+    e.close()
+    assert tune["trials"] >= 8
+    assert tune["block_threads"] in (64, 128) and 1 <= tune["max_primaries_per_refill"] <= 32
+    assert tune["best_collisions_per_s"] >= tune["default_collisions_per_s"] > 0
+    assert st["block"] == tune["block_threads"]
+    if tune["changed"]:
+        assert st["max_take"] == tune["max_primaries_per_refill"]
+    for k in ("members", "collisions", "vacancies", "replacements", "interstitials", "range_n"):
+        assert before[k] == after[k], k

@@ -141,8 +141,10 @@ def test_c5_gold_deposition_voxels():
     assert 0.5 * (t["Eel"] + t["Enuc"]) < t["Evoxel"] <= (t["Eel"] + t["Enuc"]) * (1 + 1e-6)
     assert t["sputtered"] > 0 and t["backscattered"] > 0
     assert t["Esputtered"] > 0.0
-    # FP64 cell totals: four primary shards add up to the whole run cell by cell
-    # (an FP32 total would drift by its rounding of every deposit)
+    # FP64 cell totals: four primary shards add up to the whole run cell by cell, to
+    # the rounding of the lanes' short FP32 runs of deposits (a few 1e-8 of each,
+    # grouped differently when the primaries are split); an FP32 cell total would
+    # add the rounding of every one of its ~1e5 runs (1e-5 .. 1e-3 here)
     parts = np.zeros_like(vox64)
     for k in range(4):
         e = Engine(precision="fp32", seed=1)
@@ -150,5 +152,5 @@ def test_c5_gold_deposition_voxels():
         parts += e.voxels(0, fp64=True)
         e.close()
     big = vox64 > 1e-6 * vox64.max()
-    assert np.allclose(parts[big], vox64[big], rtol=1e-9)
+    assert np.allclose(parts[big], vox64[big], rtol=1e-6, atol=0.0)
     assert float(vox64.max()) > 1e6  # the entrance cells collect millions of deposits' worth

@@ -14,9 +14,9 @@ agree to 1e-9.  The configurations are:
 * eight simulations of the 4096-simulation batch (largest Z1, highest energy,
   thickest stack, ...), each against the oracle run on its own;
 * the event log (vacancies, replacements, followed and dissipated recoils, rest
-  states, losses, history) against the oracle's records of the same hook calls,
-  and the TrimDefectLog / TrimPhononOut text streams written from them, line for
-  line.
+  states, losses, history, with IonMDTag's _md) against the oracle's records of the
+  same hook calls, and the TrimDefectLog / TrimPhononOut / IonMDTag text streams
+  written from them, line for line.
 
 Per primary, the first 400 primaries of each must match: collisions and vacancies
 exactly; electronic and nuclear loss and the stopping point to 1e-9.
@@ -129,14 +129,14 @@ ALL_EVENTS = (1, 2, 3, 4, 5, 6, 7)  # vacancy, replacement, branch, dissipate, r
 def _as_event_array(records, like):
     """oracle event records as the GPU's structured event array"""
     out = np.zeros(len(records), dtype=like.dtype)
-    for k in ("kind", "key", "primary", "gen", "Z", "state", "x", "y", "z", "E", "aux", "m"):
+    for k in ("kind", "key", "primary", "gen", "Z", "state", "md", "x", "y", "z", "E", "aux", "m"):
         out[k] = [r[k] for r in records]
     out["sim"] = 0
     out["tag"] = -1
     return out
 
 
-@pytest.mark.parametrize("name", ["cu5k_cu", "as20k_sio2_si_cut"])
+@pytest.mark.parametrize("name", ["cu5k_cu", "as20k_sio2_si_cut", "xe20k_xe_mdtag"])
 def test_event_streams_equal_oracle(oracle_built, engine_lib, name):
     """The event log -- the hook calls TrimDefectLog, TrimPhononOut and TrimHistory
     stream (trim.C:467-527, trim.h:139-153) -- against the oracle's records of the
@@ -147,6 +147,10 @@ def test_event_streams_equal_oracle(oracle_built, engine_lib, name):
     from mytrim_gb300 import _ffi as F
     if name == "cu5k_cu":
         sim = W.cu_self_ion(n_primaries=300, E=5e3)
+    elif name == "xe20k_xe_mdtag":
+        # IonMDTag: Xe members that start inside the MD gap (200 eV - 12 keV) carry _md 1
+        sim = SimSpec(layers=[LayerSpec(1e5, 3.5, [ElementSpec(54, 131.29, 1.0, 25.0, 3.0)])], Z=54, m=131.29,
+                      E=20e3, n_primaries=40, md_tag_Z=54, md_tag_E=(200.0, 12000.0))
     else:
         sim = W.arsenic_implant(n_primaries=300)
         sim.E = 20e3
@@ -162,12 +166,19 @@ def test_event_streams_equal_oracle(oracle_built, engine_lib, name):
     if name != "cu5k_cu":
         assert (ev["kind"] == F.EV_LOST).sum() == t["lost"] > 0
     a, b = streams._sorted(ev), streams._sorted(oe)
-    for k in ("kind", "key", "primary", "gen", "Z", "state", "tag"):
+    for k in ("kind", "key", "primary", "gen", "Z", "state", "tag", "md"):
         assert np.array_equal(a[k], b[k]), (name, k)
     for k in ("x", "y", "z", "E", "aux", "m"):
         assert np.allclose(a[k], b[k], rtol=1e-9, atol=1e-6), (name, k)
     assert list(streams.defect_log(ev)) == list(streams.defect_log(oe))
     assert list(streams.phonon_log(ev)) == list(streams.phonon_log(oe))
+    assert list(streams.md_tag_log(ev)) == list(streams.md_tag_log(oe))
+    tagged = ev[ev["md"] == 1]
+    if name == "xe20k_xe_mdtag":
+        assert len(tagged) > 0 and (tagged["gen"] > 0).all()  # recoils born in the gap; the primaries are not
+        assert np.isin(tagged["kind"], (F.EV_REST, F.EV_LOST, F.EV_HISTORY)).all()
+    else:
+        assert len(tagged) == 0
 
 
 def _copper_10k(n):
