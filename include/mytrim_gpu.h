@@ -194,6 +194,10 @@ typedef struct
   int max_primaries_per_refill; /* fresh primaries one warp takes at a time, 1..32;
                                    0 = chosen from the expected cascade size (one for
                                    large cascades), the batch size and the grid */
+  int refill_min_idle;   /* lanes of a warp that must be idle before the warp gives them
+                            new members (recoils from its stack, fresh primaries), 1..32;
+                            waiting lets the member-start code run for several lanes at
+                            once instead of for one or two; 0 = 8 */
 } mtg_config;
 
 /* Results of one simulation. */
@@ -388,8 +392,10 @@ mtg_status mtg_scatter_potential(mtg_ctx * ctx, const double * eps, const double
 typedef struct
 {
   int block_threads;            /* cascade kernel block shape: 64 or 128 */
-  int max_primaries_per_refill; /* fresh primaries per warp refill, 1..32 */
-  int stack_capacity;           /* recoil stack entries per warp (queue depth); 0 = default */
+  int max_primaries_per_refill; /* fresh primaries per warp refill, 1..32; 0 = the built-in
+                                   estimate, which each run makes from its own size */
+  int stack_capacity;           /* recoil stack entries per warp (queue depth) */
+  int refill_min_idle;          /* idle lanes a warp waits for before refilling, 1..32 */
   int heuristic_take;           /* the refill size the built-in estimate picks for this run */
   double default_collisions_per_s; /* trial rate of the built-in settings */
   double best_collisions_per_s;    /* trial rate of the chosen settings */
@@ -399,14 +405,16 @@ typedef struct
 
 /* Choose the cascade kernel's launch settings for a run by measurement: the
  * simulations' primaries are scaled to about `trial_primaries` in total (0 = 65,536)
- * and launched with the built-in settings, then with each candidate refill size
- * (1, 2, 4, 8, 16, 32 primaries per warp refill and the built-in estimate), block
- * shape (64, 128 threads) and recoil stack depth (the default, 2048); the fastest in
+ * and launched with the built-in settings, then, one setting at a time, with each
+ * candidate refill size (1, 2, 4, 8, 16, 32 primaries per warp refill and the
+ * built-in estimate), refill threshold (1, 4, 8, 16 idle lanes), block shape (64,
+ * 128 threads) and recoil stack depth (the default, half of it); the fastest in
  * collisions per second of kernel time is kept in the context's configuration for
- * the runs that follow, if it beats the built-in settings by more than 2 %.  The
- * trials use the context like ordinary runs (their results are discarded).  No
- * counterpart in the reference, whose threads take primaries one at a time
- * (apps/runmytrim.C:71-93). */
+ * the runs that follow, if it beats the built-in settings by more than 2 %.  A
+ * candidate whose trial fails (a stack too shallow for the cascades fills the
+ * overflow list) is skipped.  The trials use the context like ordinary runs (their
+ * results are discarded).  No counterpart in the reference, whose threads take
+ * primaries one at a time (apps/runmytrim.C:71-93). */
 mtg_status mtg_autotune(mtg_ctx * ctx, const mtg_sim * sims, int n_sims, long long trial_primaries,
                         mtg_tuning * out);
 

@@ -67,7 +67,8 @@ class Sim(C.Structure):
 class Config(C.Structure):
     _fields_ = [("tmin", C.c_double), ("tau", C.c_double), ("cw", C.c_double), ("length_scale", C.c_double),
                 ("precision", C.c_int), ("seed", C.c_ulonglong), ("max_collisions_per_member", C.c_longlong),
-                ("stack_capacity", C.c_int), ("block_threads", C.c_int), ("max_primaries_per_refill", C.c_int)]
+                ("stack_capacity", C.c_int), ("block_threads", C.c_int), ("max_primaries_per_refill", C.c_int),
+                ("refill_min_idle", C.c_int)]
 
 
 class Totals(C.Structure):
@@ -133,7 +134,7 @@ class Stats(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("block_threads", C.c_int), ("max_primaries_per_refill", C.c_int), ("stack_capacity", C.c_int),
-                ("heuristic_take", C.c_int), ("default_collisions_per_s", C.c_double),
+                ("refill_min_idle", C.c_int), ("heuristic_take", C.c_int), ("default_collisions_per_s", C.c_double),
                 ("best_collisions_per_s", C.c_double), ("trials", C.c_int), ("changed", C.c_int)]
 
 

@@ -305,6 +305,7 @@ fill_params(mtg_ctx * ctx, EngineParams & prm)
   }
   prm.max_take = take;
   ctx->stats.max_take = take;
+  prm.refill_min = ctx->cfg.refill_min_idle > 0 ? ctx->cfg.refill_min_idle : 8;
   if (ctx->record_cap > 0)
   {
     prm.records = ptr<MemberRecord>(ctx->d_records);
@@ -509,6 +510,8 @@ mtg_configure(mtg_ctx * ctx, const mtg_config * cfg)
     return fail(ctx, MTG_ERR_BAD_INPUT, "block_threads must be 0, 64 or 128");
   if (cfg->max_primaries_per_refill < 0 || cfg->max_primaries_per_refill > 32)
     return fail(ctx, MTG_ERR_BAD_INPUT, "max_primaries_per_refill must be 0..32");
+  if (cfg->refill_min_idle < 0 || cfg->refill_min_idle > 32)
+    return fail(ctx, MTG_ERR_BAD_INPUT, "refill_min_idle must be 0..32");
   ctx->cfg = *cfg;
   ctx->prepared = false;
   return MTG_OK;
@@ -885,78 +888,68 @@ mtg_autotune(mtg_ctx * ctx, const mtg_sim * sims, int n_sims, long long trial_pr
   const mtg_config base = ctx->cfg;
   std::vector<mtg_totals> tot(static_cast<size_t>(n_sims));
   int trials = 0;
-  auto rate = [&](int block, int take, int cap, double & r) -> mtg_status {
-    mtg_config c = base;
-    c.block_threads = block;
-    c.max_primaries_per_refill = take;
-    c.stack_capacity = cap;
-    mtg_status s = mtg_configure(ctx, &c);
-    if (s == MTG_OK)
-      s = mtg_run(ctx, trial.data(), n_sims, tot.data(), nullptr);
-    if (s != MTG_OK)
-      return s;
-    ++trials;
-    r = ctx->stats.kernel_ms > 0.0 ? double(ctx->stats.collisions) / (ctx->stats.kernel_ms * 1e-3) : 0.0;
-    return MTG_OK;
+  struct Setting
+  {
+    int block, take, cap, refill;
   };
-  const int block0 = base.block_threads > 0 ? base.block_threads : 128;
-  double r = 0.0, r_def = 0.0;
-  st = rate(block0, 0, base.stack_capacity, r); // warm-up (module load, first allocations)
-  if (st == MTG_OK)
-    st = rate(block0, 0, base.stack_capacity, r_def);
+  // collisions per second of kernel time of one trial launch; a launch that fails
+  // (an overflow list filled by a stack too shallow for the cascades) rates 0
+  auto rate = [&](const Setting & x) -> double {
+    mtg_config c = base;
+    c.block_threads = x.block;
+    c.max_primaries_per_refill = x.take;
+    c.stack_capacity = x.cap;
+    c.refill_min_idle = x.refill;
+    if (mtg_configure(ctx, &c) != MTG_OK || mtg_run(ctx, trial.data(), n_sims, tot.data(), nullptr) != MTG_OK)
+      return 0.0;
+    ++trials;
+    return ctx->stats.kernel_ms > 0.0 ? double(ctx->stats.collisions) / (ctx->stats.kernel_ms * 1e-3) : 0.0;
+  };
+  const Setting built_in{base.block_threads > 0 ? base.block_threads : 128, base.max_primaries_per_refill,
+                         base.stack_capacity, base.refill_min_idle};
+  rate(built_in); // warm-up (module load, first allocations)
+  const double r_def = rate(built_in);
+  if (!(r_def > 0.0))
+    return fail(ctx, MTG_ERR_BAD_INPUT, std::string("mtg_autotune: the trial run failed: ") + ctx->err);
   const int heuristic = ctx->stats.max_take;
-  int best_block = block0, best_take = 0, best_cap = base.stack_capacity;
-  double best = r_def;
-  const int takes[] = {heuristic, 1, 2, 4, 8, 16, 32};
-  for (int k = 1; k < 7 && st == MTG_OK; ++k)
-  {
-    if (takes[k] == heuristic)
-      continue;
-    st = rate(block0, takes[k], base.stack_capacity, r);
-    if (st == MTG_OK && r > best)
+  const int default_cap = ctx->stats.stack_capacity;
+  Setting best = built_in;
+  double r_best = r_def;
+  // coordinate search, one setting at a time
+  auto consider = [&](Setting x) {
+    const double r = rate(x);
+    if (r > r_best)
     {
-      best = r;
-      best_take = takes[k];
+      r_best = r;
+      best = x;
     }
-  }
-  if (st == MTG_OK)
-  {
-    const int other = block0 == 128 ? 64 : 128;
-    st = rate(other, best_take, base.stack_capacity, r);
-    if (st == MTG_OK && r > best)
-    {
-      best = r;
-      best_block = other;
-    }
-  }
-  if (st == MTG_OK && base.stack_capacity != 2048)
-  {
-    st = rate(best_block, best_take, 2048, r);
-    if (st == MTG_OK && r > best)
-    {
-      best = r;
-      best_cap = 2048;
-    }
-  }
-  mtg_config chosen = base;
-  const bool change = st == MTG_OK && best > 1.02 * r_def;
-  if (change)
-  {
-    chosen.block_threads = best_block;
-    chosen.max_primaries_per_refill = best_take;
-    chosen.stack_capacity = best_cap;
-  }
-  mtg_status st2 = mtg_configure(ctx, &chosen);
+  };
+  for (int take : {1, 2, 4, 8, 16, 32})
+    if (take != heuristic)
+      consider(Setting{best.block, take, best.cap, best.refill});
+  for (int refill : {1, 4, 16})
+    if (refill != (built_in.refill > 0 ? built_in.refill : 8))
+      consider(Setting{best.block, best.take, best.cap, refill});
+  consider(Setting{best.block == 128 ? 64 : 128, best.take, best.cap, best.refill});
+  if (default_cap > 1024)
+    consider(Setting{best.block, best.take, default_cap / 2, best.refill});
+  const bool change = r_best > 1.02 * r_def;
+  const Setting chosen = change ? best : built_in;
+  mtg_config c = base;
+  c.block_threads = chosen.block;
+  c.max_primaries_per_refill = chosen.take;
+  c.stack_capacity = chosen.cap;
+  c.refill_min_idle = chosen.refill;
+  st = mtg_configure(ctx, &c);
   if (st != MTG_OK)
     return st;
-  if (st2 != MTG_OK)
-    return st2;
-  out->block_threads = change ? best_block : block0;
-  out->max_primaries_per_refill = change ? (best_take > 0 ? best_take : heuristic) : heuristic;
-  out->stack_capacity = change ? best_cap : base.stack_capacity;
+  out->block_threads = chosen.block;
+  out->max_primaries_per_refill = chosen.take;
+  out->stack_capacity = chosen.cap > 0 ? chosen.cap : default_cap;
+  out->refill_min_idle = chosen.refill > 0 ? chosen.refill : 8;
   out->heuristic_take = heuristic;
   out->default_collisions_per_s = r_def;
-  out->best_collisions_per_s = change ? best : r_def;
+  out->best_collisions_per_s = change ? r_best : r_def;
   out->trials = trials;
   out->changed = change ? 1 : 0;
   return MTG_OK;

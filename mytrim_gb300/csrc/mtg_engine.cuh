@@ -82,6 +82,7 @@ struct EngineParams
   uint32_t k0, k1;
   unsigned int max_collisions; // per member
   int max_take;                // fresh primaries one warp takes per refill (load balance)
+  int refill_min;              // idle lanes a warp waits for before refilling them
   int cold_offset;             // byte offset of the per-thread LaneCold slots in dynamic shared memory
   // optional per-member records (replay checks)
   MemberRecord * records;
@@ -763,8 +764,11 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
   {
     ++steps;
     // ---- refill idle lanes: recoils from the warp stack first, then new work
+    // idle lanes wait until refill_min (at most 32) of them need a member, so that
+    // the member-start code below runs for several lanes at once: without waiting
+    // it runs in nearly every iteration, for about four lanes of the 32
     const unsigned int idle = __ballot_sync(FULL, !live);
-    if (idle)
+    if (idle && __popc(idle) >= prm.refill_min)
     {
       const int nidle = __popc(idle);
       const int rank = __popc(idle & lt);

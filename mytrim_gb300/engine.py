@@ -315,7 +315,7 @@ class Engine:
         return st
 
     def configure(self, precision="fp64", seed=1, tmin=0.2, tau=0.0, cw=0.001, length_scale=1.0,
-                  max_collisions=0, stack_capacity=0, block_threads=0, max_take=0):
+                  max_collisions=0, stack_capacity=0, block_threads=0, max_take=0, refill_min_idle=0):
         c = self.cfg
         c.tmin, c.tau, c.cw, c.length_scale = tmin, tau, cw, length_scale
         c.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
@@ -324,6 +324,7 @@ class Engine:
         c.stack_capacity = stack_capacity
         c.block_threads = block_threads
         c.max_primaries_per_refill = max_take
+        c.refill_min_idle = refill_min_idle
         self._check(self.lib.mtg_configure(self.ctx, C.byref(c)))
 
     def close(self):
@@ -514,6 +515,11 @@ class Engine:
         t = F.Tuning()
         self._check(self.lib.mtg_autotune(self.ctx, arr.ctypes.data, len(sims), trial_primaries, C.byref(t)))
         del keep
+        if t.changed:  # keep the front end's copy of the configuration in step
+            self.cfg.block_threads = t.block_threads
+            self.cfg.max_primaries_per_refill = t.max_primaries_per_refill
+            self.cfg.stack_capacity = t.stack_capacity
+            self.cfg.refill_min_idle = t.refill_min_idle
         return {n: getattr(t, n) for n, _ in t._fields_}
 
     def stats(self) -> dict:

@@ -572,11 +572,12 @@ def test_autotune_chooses_settings_that_keep_results(engine_lib, prec):
     after = e.run([sim])[0]
     st = e.stats()
     e.close()
-    assert tune["trials"] >= 8
-    assert tune["block_threads"] in (64, 128) and 1 <= tune["max_primaries_per_refill"] <= 32
+    assert tune["trials"] >= 10
+    assert tune["block_threads"] in (64, 128) and 0 <= tune["max_primaries_per_refill"] <= 32
+    assert 1 <= tune["refill_min_idle"] <= 32 and tune["stack_capacity"] > 0
     assert tune["best_collisions_per_s"] >= tune["default_collisions_per_s"] > 0
-    assert st["block"] == tune["block_threads"]
-    if tune["changed"]:
+    assert st["block"] == tune["block_threads"] and st["stack_capacity"] == tune["stack_capacity"]
+    if tune["max_primaries_per_refill"] > 0:
         assert st["max_take"] == tune["max_primaries_per_refill"]
     for k in ("members", "collisions", "vacancies", "replacements", "interstitials", "range_n"):
         assert before[k] == after[k], k
