@@ -197,7 +197,8 @@ typedef struct
   int refill_min_idle;   /* lanes of a warp that must be idle before the warp gives them
                             new members (recoils from its stack, fresh primaries), 1..32;
                             waiting lets the member-start code run for several lanes at
-                            once instead of for one or two; 0 = 8 */
+                            once instead of for one or two; 0 = 8 (FP32, surrogate) or 1
+                            (FP64, whose FP64 pipe an idle lane leaves unused) */
 } mtg_config;
 
 /* Results of one simulation. */

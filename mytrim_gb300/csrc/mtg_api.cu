@@ -305,7 +305,10 @@ fill_params(mtg_ctx * ctx, EngineParams & prm)
   }
   prm.max_take = take;
   ctx->stats.max_take = take;
-  prm.refill_min = ctx->cfg.refill_min_idle > 0 ? ctx->cfg.refill_min_idle : 8;
+  // waiting for idle lanes pays where lanes are cheap (FP32: +3 %); the FP64 kernel is
+  // bound by its FP64 pipe, where an idle lane is lost throughput (-8 % at 8)
+  prm.refill_min = ctx->cfg.refill_min_idle > 0 ? ctx->cfg.refill_min_idle
+                                                : (ctx->cfg.precision == MTG_PREC_FP64 ? 1 : 8);
   if (ctx->record_cap > 0)
   {
     prm.records = ptr<MemberRecord>(ctx->d_records);
@@ -927,8 +930,9 @@ mtg_autotune(mtg_ctx * ctx, const mtg_sim * sims, int n_sims, long long trial_pr
   for (int take : {1, 2, 4, 8, 16, 32})
     if (take != heuristic)
       consider(Setting{best.block, take, best.cap, best.refill});
-  for (int refill : {1, 4, 16})
-    if (refill != (built_in.refill > 0 ? built_in.refill : 8))
+  const int refill0 = built_in.refill > 0 ? built_in.refill : (base.precision == MTG_PREC_FP64 ? 1 : 8);
+  for (int refill : {1, 4, 8, 16})
+    if (refill != refill0)
       consider(Setting{best.block, best.take, best.cap, refill});
   consider(Setting{best.block == 128 ? 64 : 128, best.take, best.cap, best.refill});
   if (default_cap > 1024)
@@ -946,7 +950,7 @@ mtg_autotune(mtg_ctx * ctx, const mtg_sim * sims, int n_sims, long long trial_pr
   out->block_threads = chosen.block;
   out->max_primaries_per_refill = chosen.take;
   out->stack_capacity = chosen.cap > 0 ? chosen.cap : default_cap;
-  out->refill_min_idle = chosen.refill > 0 ? chosen.refill : 8;
+  out->refill_min_idle = chosen.refill > 0 ? chosen.refill : refill0;
   out->heuristic_take = heuristic;
   out->default_collisions_per_s = r_def;
   out->best_collisions_per_s = change ? r_best : r_def;

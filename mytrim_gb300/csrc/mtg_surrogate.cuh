@@ -18,13 +18,12 @@
 // (mma.sync m16n8k16, BF16 operands, FP32 accumulation) with the accumulator
 // fragments of one layer reused in registers as the A fragments of the next; the
 // 2x64 input and 64x2 output layers stay in FP32.  Weights are staged in shared
-// memory; the input, bias and output weights are read pairwise in vector loads.
+// memory.
 #pragma once
 
 #include <cstddef>
 #include <stdint.h>
 #include <cuda_bf16.h>
-#include <cuda_fp16.h>
 
 namespace mtg
 {
@@ -85,41 +84,15 @@ lds_f32(const void * p)
   return __uint_as_float(lds_u32(p));
 }
 
-// two / four consecutive floats (8- / 16-byte aligned) in one shared-memory load
-__device__ __forceinline__ float2
-lds_f32x2(const void * p)
+// SiLU for inference: x sigmoid(x) = x (1 + tanh(x/2)) / 2 with the hardware tanh
+// (one special-function operation instead of an exponential and a reciprocal)
+__device__ __forceinline__ float
+silu(float x)
 {
-  float2 v;
-  asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];"
-               : "=f"(v.x), "=f"(v.y)
-               : "r"((uint32_t)__cvta_generic_to_shared(p)));
-  return v;
-}
-
-__device__ __forceinline__ float4
-lds_f32x4(const void * p)
-{
-  float4 v;
-  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
-               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
-               : "r"((uint32_t)__cvta_generic_to_shared(p)));
-  return v;
-}
-
-// SiLU x sigmoid(x) = h (1 + tanh h), h = x / 2, of two values with one
-// special-function operation: tanh of the pair packed as half2 (tanh.approx.f16x2,
-// about 11 bits like tanh.approx.f32; the results are rounded to BF16 for the next
-// layer anyway), the rest in FP32
-__device__ __forceinline__ void
-silu2(float x0, float x1, float & y0, float & y1)
-{
-  const float h0 = 0.5f * x0, h1 = 0.5f * x1;
-  uint32_t hh, tt;
-  asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(hh) : "f"(h1), "f"(h0)); // h0 in the low half
-  asm("tanh.approx.f16x2 %0, %1;" : "=r"(tt) : "r"(hh));
-  const __half2 t2 = *reinterpret_cast<const __half2 *>(&tt);
-  y0 = fmaf(h0, __low2float(t2), h0);
-  y1 = fmaf(h1, __high2float(t2), h1);
+  const float h = 0.5f * x;
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(h));
+  return fmaf(h, t, h);
 }
 
 __device__ __forceinline__ uint32_t
@@ -162,11 +135,11 @@ hidden_layer(const __nv_bfloat16 (*w)[SG_LD], const float * bias, const uint32_t
 #pragma unroll
   for (int nt = 0; nt < 8; ++nt)
   {
-    const float2 bv = lds_f32x2(bias + nt * 8 + 2 * t);
-    c[nt][0] = bv.x;
-    c[nt][1] = bv.y;
-    c[nt][2] = bv.x;
-    c[nt][3] = bv.y;
+    const float b0 = lds_f32(bias + nt * 8 + 2 * t), b1v = lds_f32(bias + nt * 8 + 2 * t + 1);
+    c[nt][0] = b0;
+    c[nt][1] = b1v;
+    c[nt][2] = b0;
+    c[nt][3] = b1v;
 #pragma unroll
     for (int kp = 0; kp < 2; ++kp)
     {
@@ -185,15 +158,10 @@ to_a_fragments(const float (&c)[8][4], uint32_t (&a)[4][4])
 #pragma unroll
   for (int kc = 0; kc < 4; ++kc)
   {
-    float y[8];
-    silu2(c[2 * kc][0], c[2 * kc][1], y[0], y[1]);
-    silu2(c[2 * kc][2], c[2 * kc][3], y[2], y[3]);
-    silu2(c[2 * kc + 1][0], c[2 * kc + 1][1], y[4], y[5]);
-    silu2(c[2 * kc + 1][2], c[2 * kc + 1][3], y[6], y[7]);
-    a[kc][0] = pack_bf16(y[0], y[1]);
-    a[kc][1] = pack_bf16(y[2], y[3]);
-    a[kc][2] = pack_bf16(y[4], y[5]);
-    a[kc][3] = pack_bf16(y[6], y[7]);
+    a[kc][0] = pack_bf16(silu(c[2 * kc][0]), silu(c[2 * kc][1]));
+    a[kc][1] = pack_bf16(silu(c[2 * kc][2]), silu(c[2 * kc][3]));
+    a[kc][2] = pack_bf16(silu(c[2 * kc + 1][0]), silu(c[2 * kc + 1][1]));
+    a[kc][3] = pack_bf16(silu(c[2 * kc + 1][2]), silu(c[2 * kc + 1][3]));
   }
 }
 
@@ -246,14 +214,16 @@ surrogate_eval_warp(const SurrogateNet * net, bool active, float x1, float x2)
     for (int kc = 0; kc < 4; ++kc)
     {
       const int c0 = kc * 16 + 2 * t, c1 = c0 + 8;
-      // columns c0, c0+1 and c1, c1+1: w1 rows pairwise (16 bytes), biases (8 bytes)
-      const float4 wa = lds_f32x4(&net->w1[c0][0]), wb = lds_f32x4(&net->w1[c1][0]);
-      const float2 ba = lds_f32x2(&net->b1[c0]), bb = lds_f32x2(&net->b1[c1]);
       float h[8];
-      silu2(fmaf(wa.x, ax1, fmaf(wa.y, ax2, ba.x)), fmaf(wa.x, bx1, fmaf(wa.y, bx2, ba.x)), h[0], h[1]);
-      silu2(fmaf(wa.z, ax1, fmaf(wa.w, ax2, ba.y)), fmaf(wa.z, bx1, fmaf(wa.w, bx2, ba.y)), h[2], h[3]);
-      silu2(fmaf(wb.x, ax1, fmaf(wb.y, ax2, bb.x)), fmaf(wb.x, bx1, fmaf(wb.y, bx2, bb.x)), h[4], h[5]);
-      silu2(fmaf(wb.z, ax1, fmaf(wb.w, ax2, bb.y)), fmaf(wb.z, bx1, fmaf(wb.w, bx2, bb.y)), h[6], h[7]);
+      const int cols[4] = {c0, c0 + 1, c1, c1 + 1};
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+      {
+        const int j = cols[q];
+        const float w0 = lds_f32(&net->w1[j][0]), w1v = lds_f32(&net->w1[j][1]), bj = lds_f32(&net->b1[j]);
+        h[2 * q] = silu(fmaf(w0, ax1, fmaf(w1v, ax2, bj)));
+        h[2 * q + 1] = silu(fmaf(w0, bx1, fmaf(w1v, bx2, bj)));
+      }
       a[kc][0] = pack_bf16(h[0], h[2]); // row s0, cols c0, c0+1
       a[kc][1] = pack_bf16(h[1], h[3]); // row s1, cols c0, c0+1
       a[kc][2] = pack_bf16(h[4], h[6]); // row s0, cols c1, c1+1
@@ -269,12 +239,10 @@ surrogate_eval_warp(const SurrogateNet * net, bool active, float x1, float x2)
 #pragma unroll
     for (int nt = 0; nt < 8; ++nt)
     {
-      const float2 w = lds_f32x2(&net->w4[0][nt * 8 + 2 * t]);
-      float y0, y1, y2, y3;
-      silu2(c[nt][0], c[nt][1], y0, y1);
-      silu2(c[nt][2], c[nt][3], y2, y3);
-      p0 = fmaf(y0, w.x, fmaf(y1, w.y, p0));
-      p1 = fmaf(y2, w.x, fmaf(y3, w.y, p1));
+      const int j = nt * 8 + 2 * t;
+      const float wa = lds_f32(&net->w4[0][j]), wb = lds_f32(&net->w4[0][j + 1]);
+      p0 = fmaf(silu(c[nt][0]), wa, fmaf(silu(c[nt][1]), wb, p0));
+      p1 = fmaf(silu(c[nt][2]), wa, fmaf(silu(c[nt][3]), wb, p1));
     }
     p0 += __shfl_xor_sync(0xffffffffu, p0, 1);
     p0 += __shfl_xor_sync(0xffffffffu, p0, 2);
