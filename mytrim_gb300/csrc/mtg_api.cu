@@ -84,7 +84,7 @@ struct mtg_ctx
   DevBuf d_sims, d_prim_end, d_species, d_mats, d_row_species, d_stop;
   DevBuf d_species32, d_mats32, d_sims32;
   DevBuf d_sg_params, d_sg_net; // surrogate network
-  DevBuf d_vox, d_vox_range, d_vox_sum; // energy-deposition voxels
+  DevBuf d_vox, d_vox_range, d_vox_sum, d_vox_part; // energy-deposition voxels
   DevBuf d_cl, d_cl32, d_cl_next, d_cl_head, d_cl_mask; // sampleClusters geometry
   std::vector<SimDesc> sims_dev;             // SimDesc copies with device cluster pointers
   bool sg_ready = false;
@@ -455,7 +455,7 @@ mtg_destroy(mtg_ctx * ctx)
                      &ctx->d_partials,
                      &ctx->d_out,    &ctx->d_tmp0,     &ctx->d_tmp1,    &ctx->d_tmp2,    &ctx->d_tmp3,
                      &ctx->d_species32, &ctx->d_mats32, &ctx->d_sims32, &ctx->d_sg_params, &ctx->d_sg_net,
-                     &ctx->d_vox,    &ctx->d_vox_range, &ctx->d_vox_sum, &ctx->d_cl,     &ctx->d_cl32,
+                     &ctx->d_vox,    &ctx->d_vox_range, &ctx->d_vox_sum, &ctx->d_vox_part, &ctx->d_cl, &ctx->d_cl32,
                      &ctx->d_cl_next, &ctx->d_cl_head, &ctx->d_cl_mask};
   for (DevBuf * b : bufs)
     if (b->p)
@@ -566,6 +566,7 @@ mtg_prepare(mtg_ctx * ctx, const mtg_sim * sims, int n_sims)
     CK(ensure(ctx->d_vox, sizeof(double) * size_t(t.voxel_total)));
     CK(ensure(ctx->d_vox_range, sizeof(long long) * vr.size()));
     CK(ensure(ctx->d_vox_sum, sizeof(double) * ns));
+    CK(ensure(ctx->d_vox_part, voxel_partials_bytes(int(ns))));
     CK(h2d(ctx, ctx->d_vox_range.p, vr.data(), sizeof(long long) * vr.size()));
   }
   // cluster samples: the cluster arrays, and the simulations pointing at them
@@ -704,8 +705,8 @@ mtg_launch_async(mtg_ctx * ctx, void * stream)
   if (t.voxel_total > 0)
   {
     CK(launch_voxel_sum(ptr<double>(ctx->d_vox), ptr<long long>(ctx->d_vox_range), int(t.sims.size()),
-                        ptr<double>(ctx->d_vox_sum), s));
-    ctx->stats.launches += 1;
+                        ptr<double>(ctx->d_vox_part), ptr<double>(ctx->d_vox_sum), s));
+    ctx->stats.launches += 2;
   }
   st = launch_reduction(ctx);
   if (st != MTG_OK)
@@ -778,7 +779,7 @@ mtg_collect(mtg_ctx * ctx, mtg_totals * totals, long long * hist)
     if (extra)
     {
       CK(launch_voxel_sum(ptr<double>(ctx->d_vox), ptr<long long>(ctx->d_vox_range), int(ns),
-                          ptr<double>(ctx->d_vox_sum), ctx->stream));
+                          ptr<double>(ctx->d_vox_part), ptr<double>(ctx->d_vox_sum), ctx->stream));
       CK(cudaStreamSynchronize(ctx->stream));
     }
     CK(cudaMemcpy(vsum.data(), ctx->d_vox_sum.p, sizeof(double) * ns, cudaMemcpyDeviceToHost));
@@ -838,7 +839,7 @@ mtg_collect(mtg_ctx * ctx, mtg_totals * totals, long long * hist)
                      &ctx->d_hist,   &ctx->d_err,      &ctx->d_counters, &ctx->d_stacks, &ctx->d_ovf0,
                      &ctx->d_ovf1,   &ctx->d_records,  &ctx->d_events,  &ctx->d_jobs,    &ctx->d_job_first,
                      &ctx->d_partials,
-                     &ctx->d_out,    &ctx->d_species32, &ctx->d_mats32, &ctx->d_sims32, &ctx->d_vox};
+                     &ctx->d_out,    &ctx->d_species32, &ctx->d_mats32, &ctx->d_sims32, &ctx->d_vox, &ctx->d_vox_part};
   for (DevBuf * b : bufs)
     bytes += b->bytes;
   ctx->stats.device_bytes = bytes;
@@ -876,7 +877,7 @@ mtg_autotune(mtg_ctx * ctx, const mtg_sim * sims, int n_sims, long long trial_pr
   if (!sims || n_sims < 1 || !out || trial_primaries < 0)
     return fail(ctx, MTG_ERR_BAD_INPUT, "mtg_autotune: simulations, a result and trial_primaries >= 0 are needed");
   if (trial_primaries == 0)
-    trial_primaries = 65536;
+    trial_primaries = 262144; // smaller trials are ruled by the end-of-batch tail
   long long total = 0;
   for (int i = 0; i < n_sims; ++i)
     total += std::max<long long>(0, sims[i].n_primaries);

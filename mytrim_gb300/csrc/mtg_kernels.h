@@ -66,7 +66,9 @@ struct ReduceJob
   int sim;
   long long begin, end;
 };
-cudaError_t launch_voxel_sum(const double * vox, const long long * range, int nsims, double * out, cudaStream_t st);
+size_t voxel_partials_bytes(int nsims);
+cudaError_t launch_voxel_sum(const double * vox, const long long * range, int nsims, double * partials, double * out,
+                             cudaStream_t st);
 cudaError_t launch_reduce(const ReduceJob * jobs, int njobs, const PrimaryTallies & prim, double * partials,
                           const int * job_first, int nsims, double * out, cudaStream_t st);
 

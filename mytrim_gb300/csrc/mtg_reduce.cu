@@ -105,14 +105,21 @@ reduce_finish_kernel(const int * job_first, int nsims, const double * partials, 
   }
 }
 
-// compensated sum of each simulation's voxel grid (block per simulation, fixed order)
+// Compensated sum of each simulation's voxel grid in two fixed-order stages: block
+// b of simulation s sums the cells of its stretch [b n / B, (b+1) n / B) into
+// partials[s B + b], then one thread per simulation adds its B partials in order.
+// (One block per grid read a 256^3 grid at 4 GB/s on one SM: 34 ms.)
+constexpr int VOX_BLOCKS = 256; // blocks per simulation
+
 __global__ void __launch_bounds__(RBLOCK)
-voxel_sum_kernel(const double * vox, const long long * range, double * out)
+voxel_partial_kernel(const double * vox, const long long * range, double * partials)
 {
-  const long long b = range[2 * blockIdx.x], n = range[2 * blockIdx.x + 1];
+  const int sim = blockIdx.y, b = blockIdx.x;
+  const long long base = range[2 * sim], n = range[2 * sim + 1];
+  const long long lo = n * b / VOX_BLOCKS, hi = n * (b + 1) / VOX_BLOCKS;
   Comp a{0.0, 0.0};
-  for (long long i = threadIdx.x; i < n; i += RBLOCK)
-    comp_add(a, vox[b + i]);
+  for (long long i = lo + threadIdx.x; i < hi; i += RBLOCK)
+    comp_add(a, vox[base + i]);
   __shared__ Comp red[RBLOCK];
   red[threadIdx.x] = a;
   __syncthreads();
@@ -123,14 +130,36 @@ voxel_sum_kernel(const double * vox, const long long * range, double * out)
     __syncthreads();
   }
   if (threadIdx.x == 0)
-    out[blockIdx.x] = red[0].s + red[0].c;
+    partials[(long long)sim * VOX_BLOCKS + b] = red[0].s + red[0].c;
+}
+
+__global__ void
+voxel_finish_kernel(const double * partials, int nsims, double * out)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsims)
+    return;
+  Comp a{0.0, 0.0};
+  for (int b = 0; b < VOX_BLOCKS; ++b)
+    comp_add(a, partials[(long long)s * VOX_BLOCKS + b]);
+  out[s] = a.s + a.c;
+}
+
+size_t
+voxel_partials_bytes(int nsims)
+{
+  return sizeof(double) * size_t(VOX_BLOCKS) * size_t(nsims > 0 ? nsims : 1);
 }
 
 cudaError_t
-launch_voxel_sum(const double * vox, const long long * range, int nsims, double * out, cudaStream_t st)
+launch_voxel_sum(const double * vox, const long long * range, int nsims, double * partials, double * out,
+                 cudaStream_t st)
 {
   if (nsims > 0)
-    voxel_sum_kernel<<<nsims, RBLOCK, 0, st>>>(vox, range, out);
+  {
+    voxel_partial_kernel<<<dim3(VOX_BLOCKS, nsims), RBLOCK, 0, st>>>(vox, range, partials);
+    voxel_finish_kernel<<<(nsims + 127) / 128, 128, 0, st>>>(partials, nsims, out);
+  }
   return cudaGetLastError();
 }
 
