@@ -10,10 +10,10 @@
 // library's own device memory, NOALLOC_MAX_CHUNKS * NQ doubles (120 KiB), which
 // every GPU that loads the library holds until the process exits.
 //
-// The arithmetic is the one mtg_collect uses (mtg_reduce.cu): chunks of 65536
-// primaries reduced with Neumaier-compensated FP64 sums in a fixed order, then
-// the chunks in index order, so the totals are the same bits as the ones
-// mtg_collect reports for a single simulation.
+// The arithmetic is the one mtg_collect uses (mtg_reduce.cuh, shared with
+// mtg_reduce.cu): chunks of 65536 primaries, each summed by one block in a fixed
+// order, then the chunks in index order with compensated FP64 adds, so the totals
+// are the same bits as the ones mtg_collect reports for a single simulation.
 #include <cuda.h> // CUcontext / CUresult types only: the driver calls are reached through the runtime
 #include <cuda_runtime.h>
 
@@ -24,11 +24,12 @@
 
 #include "mytrim_gpu.h"
 #include "mtg_kernels.h"
+#include "mtg_reduce.cuh"
 
 namespace
 {
 
-constexpr int NOALLOC_BLOCK = 256;
+constexpr int NOALLOC_BLOCK = mtg::RBLOCK;
 constexpr long long NOALLOC_CHUNK = 65536; // primaries per block, as in mtg_collect
 constexpr int NOALLOC_MAX_CHUNKS = 1024;   // at most 67,108,864 primaries per call
 constexpr int NQ = mtg::NQ;
@@ -40,29 +41,6 @@ constexpr int NQ = mtg::NQ;
 // synchronised).
 static __device__ __align__(256) double g_noalloc_partials[NOALLOC_MAX_CHUNKS * NQ];
 
-struct Comp
-{
-  double s, c;
-};
-
-__device__ __forceinline__ void
-comp_add(Comp & a, double x)
-{
-  const double t = a.s + x;
-  if (fabs(a.s) >= fabs(x))
-    a.c += (a.s - t) + x;
-  else
-    a.c += (x - t) + a.s;
-  a.s = t;
-}
-
-__device__ __forceinline__ void
-comp_merge(Comp & a, const Comp & b)
-{
-  comp_add(a, b.s);
-  a.c += b.c;
-}
-
 __global__ void __launch_bounds__(NOALLOC_BLOCK)
 noalloc_chunk_kernel(const unsigned long long * vac, const unsigned long long * coll, const double * eel,
                      const double * enuc, const double * fx, const double * fy, const double * fz,
@@ -70,52 +48,7 @@ noalloc_chunk_kernel(const unsigned long long * vac, const unsigned long long * 
 {
   const long long begin = (long long)blockIdx.x * NOALLOC_CHUNK;
   const long long end = begin + NOALLOC_CHUNK < n ? begin + NOALLOC_CHUNK : n;
-  Comp q[NQ];
-#pragma unroll
-  for (int k = 0; k < NQ; ++k)
-    q[k] = Comp{0.0, 0.0};
-  for (long long i = begin + threadIdx.x; i < end; i += NOALLOC_BLOCK)
-  {
-    const double v = double(vac[i]);
-    const double c = double(coll[i]);
-    const double e = eel[i];
-    const double u = enuc[i];
-    comp_add(q[0], v);
-    comp_add(q[1], v * v);
-    comp_add(q[2], c);
-    comp_add(q[3], c * c);
-    comp_add(q[4], e);
-    comp_add(q[5], e * e);
-    comp_add(q[6], u);
-    comp_add(q[7], u * u);
-    const int st = fstate[i];
-    if (st >= 1 && st <= 3)
-    {
-      const double x = fx[i], y = fy[i], z = fz[i];
-      comp_add(q[8], 1.0);
-      comp_add(q[9], x);
-      comp_add(q[10], x * x);
-      comp_add(q[11], y);
-      comp_add(q[12], y * y);
-      comp_add(q[13], z);
-      comp_add(q[14], z * z);
-    }
-  }
-  __shared__ Comp red[NOALLOC_BLOCK];
-  for (int k = 0; k < NQ; ++k)
-  {
-    red[threadIdx.x] = q[k];
-    __syncthreads();
-    for (int w = NOALLOC_BLOCK / 2; w > 0; w >>= 1)
-    {
-      if (threadIdx.x < w)
-        comp_merge(red[threadIdx.x], red[threadIdx.x + w]);
-      __syncthreads();
-    }
-    if (threadIdx.x == 0)
-      partials[(long long)blockIdx.x * NQ + k] = red[0].s + red[0].c;
-    __syncthreads();
-  }
+  mtg::block_sum_primaries(vac, coll, eel, enuc, fx, fy, fz, fstate, begin, end, partials + (long long)blockIdx.x * NQ);
 }
 
 __global__ void
@@ -124,9 +57,9 @@ noalloc_finish_kernel(const double * partials, int nchunks, double * out)
   const int k = threadIdx.x;
   if (k >= NQ)
     return;
-  Comp a{0.0, 0.0};
+  mtg::Comp a{0.0, 0.0};
   for (int j = 0; j < nchunks; ++j)
-    comp_add(a, partials[(long long)j * NQ + k]);
+    mtg::comp_add(a, partials[(long long)j * NQ + k]);
   out[k] = a.s + a.c;
 }
 

@@ -5,89 +5,24 @@
 // arrays are reduced after the cascade kernel in a fixed order -- a block per job
 // (a contiguous primary range of one simulation), a fixed thread-to-primary map,
 // a fixed tree in shared memory, then the jobs of a simulation in index order --
-// with Neumaier-compensated FP64 sums, so the totals are reproducible bit for bit
-// run to run.  This kernel is HBM-bound: it streams 60 bytes per primary.
+// with plain FP64 sums per thread and Neumaier-compensated FP64 merges
+// (mtg_reduce.cuh), so the totals are reproducible bit for bit run to run.  It
+// streams 60 bytes per primary and does about 20 FP64 operations on them.
 #include "mtg_engine.cuh"
 #include "mtg_kernels.h"
+#include "mtg_reduce.cuh"
 
 namespace mtg
 {
 
-struct Comp
-{
-  double s, c;
-};
-
-__device__ __forceinline__ void
-comp_add(Comp & a, double x)
-{
-  const double t = a.s + x;
-  if (fabs(a.s) >= fabs(x))
-    a.c += (a.s - t) + x;
-  else
-    a.c += (x - t) + a.s;
-  a.s = t;
-}
-
-__device__ __forceinline__ void
-comp_merge(Comp & a, const Comp & b)
-{
-  comp_add(a, b.s);
-  a.c += b.c;
-}
-
-constexpr int RBLOCK = 256;
+static_assert(NQ == NQ_SUM, "the reduction sums the NQ quantities of mtg_kernels.h");
 
 __global__ void __launch_bounds__(RBLOCK)
 reduce_primaries_kernel(const ReduceJob * jobs, PrimaryTallies prim, double * partials)
 {
   const ReduceJob job = jobs[blockIdx.x];
-  Comp q[NQ];
-#pragma unroll
-  for (int k = 0; k < NQ; ++k)
-    q[k] = Comp{0.0, 0.0};
-  for (long long i = job.begin + threadIdx.x; i < job.end; i += RBLOCK)
-  {
-    const double v = double(prim.vac[i]);
-    const double c = double(prim.coll[i]);
-    const double e = prim.eel[i];
-    const double n = prim.enuc[i];
-    comp_add(q[0], v);
-    comp_add(q[1], v * v);
-    comp_add(q[2], c);
-    comp_add(q[3], c * c);
-    comp_add(q[4], e);
-    comp_add(q[5], e * e);
-    comp_add(q[6], n);
-    comp_add(q[7], n * n);
-    const int st = prim.fstate[i];
-    if (st >= 1 && st <= 3)
-    {
-      const double x = prim.fx[i], y = prim.fy[i], z = prim.fz[i];
-      comp_add(q[8], 1.0);
-      comp_add(q[9], x);
-      comp_add(q[10], x * x);
-      comp_add(q[11], y);
-      comp_add(q[12], y * y);
-      comp_add(q[13], z);
-      comp_add(q[14], z * z);
-    }
-  }
-  __shared__ Comp red[RBLOCK];
-  for (int k = 0; k < NQ; ++k)
-  {
-    red[threadIdx.x] = q[k];
-    __syncthreads();
-    for (int w = RBLOCK / 2; w > 0; w >>= 1)
-    {
-      if (threadIdx.x < w)
-        comp_merge(red[threadIdx.x], red[threadIdx.x + w]);
-      __syncthreads();
-    }
-    if (threadIdx.x == 0)
-      partials[(long long)blockIdx.x * NQ + k] = red[0].s + red[0].c;
-    __syncthreads();
-  }
+  block_sum_primaries(prim.vac, prim.coll, prim.eel, prim.enuc, prim.fx, prim.fy, prim.fz, prim.fstate, job.begin,
+                      job.end, partials + (long long)blockIdx.x * NQ);
 }
 
 __global__ void
@@ -117,11 +52,11 @@ voxel_partial_kernel(const double * vox, const long long * range, double * parti
   const int sim = blockIdx.y, b = blockIdx.x;
   const long long base = range[2 * sim], n = range[2 * sim + 1];
   const long long lo = n * b / VOX_BLOCKS, hi = n * (b + 1) / VOX_BLOCKS;
-  Comp a{0.0, 0.0};
+  double a = 0.0; // plain FP64 per thread, compensated merges (mtg_reduce.cuh)
   for (long long i = lo + threadIdx.x; i < hi; i += RBLOCK)
-    comp_add(a, vox[base + i]);
+    a += vox[base + i];
   __shared__ Comp red[RBLOCK];
-  red[threadIdx.x] = a;
+  red[threadIdx.x] = Comp{a, 0.0};
   __syncthreads();
   for (int w = RBLOCK / 2; w > 0; w >>= 1)
   {
