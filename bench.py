@@ -53,7 +53,7 @@ L2_FLUSH_BYTES = 256 << 20
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of 65,536 primaries
 # (1.76e9 collisions), divided by its collisions; the traffic grows with the
 # collisions a launch processes, so the figure scales to the 10^7-primary launch
-DRAM_BYTES_PER_COLLISION_FP32 = 2.03
+DRAM_BYTES_PER_COLLISION_FP32 = 2.08
 
 # name -> (description, builder(n_primaries)); builders from mytrim_gb300.workloads
 WORKLOADS = {
