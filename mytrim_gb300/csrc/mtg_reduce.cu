@@ -25,19 +25,18 @@ reduce_primaries_kernel(const ReduceJob * jobs, PrimaryTallies prim, double * pa
                       job.end, partials + (long long)blockIdx.x * NQ);
 }
 
+// one block per simulation, one thread per quantity: the simulation's job sums in
+// job order (a thread per simulation walking all quantities took 0.6 ms at 153 jobs)
 __global__ void
 reduce_finish_kernel(const int * job_first, int nsims, const double * partials, double * out)
 {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nsims)
+  const int s = blockIdx.x, k = threadIdx.x;
+  if (s >= nsims || k >= NQ)
     return;
-  for (int k = 0; k < NQ; ++k)
-  {
-    Comp a{0.0, 0.0};
-    for (int j = job_first[s]; j < job_first[s + 1]; ++j)
-      comp_add(a, partials[(long long)j * NQ + k]);
-    out[(long long)s * NQ + k] = a.s + a.c;
-  }
+  Comp a{0.0, 0.0};
+  for (int j = job_first[s]; j < job_first[s + 1]; ++j)
+    comp_add(a, partials[(long long)j * NQ + k]);
+  out[(long long)s * NQ + k] = a.s + a.c;
 }
 
 // Compensated sum of each simulation's voxel grid in two fixed-order stages: block
@@ -104,7 +103,8 @@ launch_reduce(const ReduceJob * jobs, int njobs, const PrimaryTallies & prim, do
 {
   if (njobs > 0)
     reduce_primaries_kernel<<<njobs, RBLOCK, 0, st>>>(jobs, prim, partials);
-  reduce_finish_kernel<<<(nsims + 127) / 128, 128, 0, st>>>(job_first, nsims, partials, out);
+  if (nsims > 0)
+    reduce_finish_kernel<<<nsims, 32, 0, st>>>(job_first, nsims, partials, out);
   return cudaGetLastError();
 }
 
