@@ -9,6 +9,10 @@ path are timed beside it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
+Before the warm-up the autotuner (mtg_autotune) picks the launch settings from
+trial launches of 2^18 primaries (untimed; --no-autotune skips it); the line reports
+them in config.launch_settings.
+
 Printed JSON line (rank 0):
   value        primaries/s over the K timed steps, device-timed with CUDA events on
                the launching stream, inputs resident in HBM, L2 flushed (256 MiB
@@ -107,6 +111,8 @@ def args_parse():
     p.add_argument("--event-capacity", type=int, default=1 << 26)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="skip the launch-settings autotuner (mtg_autotune) before the warm-up")
     p.add_argument("--workload", default="ag200k_si", choices=sorted(WORKLOADS),
                    help="ag200k_si is the benchmark; the others are for profiling and checks")
     return p.parse_args()
@@ -270,6 +276,12 @@ def main():
     def sims_for(step, batch=None):
         b = batch or a.batch
         return make_sims(a.workload, b, (step * world + rank) * b)
+
+    # launch settings (refill size and threshold, block shape, stack depth) chosen by
+    # the autotuner from trial launches of this workload, untimed
+    tuning = None
+    if not a.no_autotune:
+        tuning = eng.autotune(sims_for(0), trial_primaries=1 << 18)
 
     # warm-up steps (untimed)
     for i in range(a.warmup):
@@ -443,7 +455,8 @@ def main():
         "ms_per_step": 1e3 * total / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if prec != "fp64" else "f64", "data": "synthetic",
         "config": {"workload": WORKLOADS[a.workload][0], "primaries_per_step": a.batch * world, "path": prec,
-                   "l2": "flushed before each timed step (256 MiB write)", "seeded": True},
+                   "l2": "flushed before each timed step (256 MiB write)", "seeded": True,
+                   "launch_settings": tuning},
         "collisions_per_s": coll_rate,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
