@@ -287,7 +287,7 @@ def main():
     for i in range(a.warmup):
         eng.prepare(sims_for(i))
         eng.launch(stream.cuda_stream)
-        eng.collect()
+        eng.collect(allow_event_overflow=True)
 
     # timed steps: inputs resident, L2 flushed before each step, CUDA events on the
     # launching stream
@@ -306,7 +306,7 @@ def main():
             e0.record(stream)
             eng.launch(stream.cuda_stream)
             e1.record(stream)
-            rr = eng.collect()
+            rr = eng.collect(allow_event_overflow=True)
             r = {kk: sum(x[kk] for x in rr) for kk in rr[0] if not kk.startswith("hist") and kk != "status"}
             times.append(e0.elapsed_time(e1) / 1e3)
             st = eng.stats()

@@ -247,6 +247,8 @@ typedef struct
                               records / voxels / tally modes, 2 + event log, 3 cluster geometry
                               or a non-universal potential, 4 + event log */
   int max_take;            /* fresh primaries one warp took per refill in the last run */
+  int events_overflowed;   /* 1 when the last collect's only error was a full event log (its
+                              status is MTG_ERR_QUEUE_FULL and the tallies are complete) */
 } mtg_stats;
 
 typedef struct mtg_ctx mtg_ctx;

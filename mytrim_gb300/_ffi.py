@@ -16,6 +16,7 @@ STATUS_NAMES = {
     4: "MTG_ERR_QUEUE_FULL", 5: "MTG_ERR_TIMEOUT", 6: "MTG_ERR_NUMERIC", 7: "MTG_ERR_CUDA",
     8: "MTG_ERR_NO_DEVICE", 9: "MTG_ERR_STATE",
 }
+ERR_QUEUE_FULL = 4
 
 PREC_FP64, PREC_FP32, PREC_FP32_SURROGATE = 0, 1, 2
 BC_PBC, BC_INF, BC_CUT = 0, 1, 2
@@ -129,7 +130,7 @@ class Stats(C.Structure):
                 ("drains", C.c_int), ("grid", C.c_int), ("block", C.c_int), ("stack_capacity", C.c_int),
                 ("overflowed", C.c_longlong), ("collisions", C.c_longlong), ("device_bytes", C.c_size_t),
                 ("h2d_bytes", C.c_longlong), ("d2h_bytes", C.c_longlong), ("warp_steps", C.c_longlong),
-                ("kernel_level", C.c_int), ("max_take", C.c_int)]
+                ("kernel_level", C.c_int), ("max_take", C.c_int), ("events_overflowed", C.c_int)]
 
 
 class Tuning(C.Structure):

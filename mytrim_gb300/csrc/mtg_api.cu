@@ -98,7 +98,6 @@ struct mtg_ctx
   size_t smem = 0;
   int cold_offset = 0;
   int hist_smem_bins = 0, hist_smem_offset = 0;
-  bool events_overflowed = false; // the last collect's only error was a full event log
   int stage = 0;
   int stack_cap = 0;
   long long ovf_cap = 0;
@@ -767,7 +766,7 @@ mtg_collect(mtg_ctx * ctx, mtg_totals * totals, long long * hist)
   ctx->stats.stack_capacity = ctx->stack_cap;
   ctx->stats.overflowed = overflowed;
 
-  ctx->events_overflowed = false;
+  ctx->stats.events_overflowed = 0;
   unsigned int errf = 0;
   CK(cudaMemcpy(&errf, ctx->d_err.p, sizeof errf, cudaMemcpyDeviceToHost));
   const size_t ns = t.sims.size();
@@ -846,18 +845,19 @@ mtg_collect(mtg_ctx * ctx, mtg_totals * totals, long long * hist)
     bytes += b->bytes;
   ctx->stats.device_bytes = bytes;
 
+  // a full event log is reported last: any other error of the run takes precedence
   if (unfinished || (errf & ERRB_QUEUE_FULL))
     return fail(ctx, MTG_ERR_QUEUE_FULL, "recoil overflow list exhausted; results incomplete");
-  if (errf & ERRB_EVENTS_FULL)
-  {
-    ctx->events_overflowed = true; // the run itself is complete (the autotuner times it)
-    return fail(ctx, MTG_ERR_QUEUE_FULL,
-                "event log capacity " + std::to_string(ctx->event_cap) + " exceeded; the tallies are complete");
-  }
   if (errf & ERRB_BUDGET)
     return fail(ctx, MTG_ERR_TIMEOUT, "a cascade member exceeded the collision budget");
   if (errf & ERRB_NUMERIC)
     return fail(ctx, MTG_ERR_NUMERIC, "non-finite energy or degenerate direction met");
+  if (errf & ERRB_EVENTS_FULL)
+  {
+    ctx->stats.events_overflowed = 1; // the run itself is complete (the autotuner times it)
+    return fail(ctx, MTG_ERR_QUEUE_FULL,
+                "event log capacity " + std::to_string(ctx->event_cap) + " exceeded; the tallies are complete");
+  }
   return MTG_OK;
 }
 
@@ -912,7 +912,7 @@ mtg_autotune(mtg_ctx * ctx, const mtg_sim * sims, int n_sims, long long trial_pr
     if (mtg_configure(ctx, &c) != MTG_OK)
       return 0.0;
     const mtg_status s = mtg_run(ctx, trial.data(), n_sims, tot.data(), nullptr);
-    if (s != MTG_OK && !(s == MTG_ERR_QUEUE_FULL && ctx->events_overflowed)) // a full event log still times the run
+    if (s != MTG_OK && !(s == MTG_ERR_QUEUE_FULL && ctx->stats.events_overflowed)) // a full event log still times the run
       return 0.0;
     ++trials;
     return ctx->stats.kernel_ms > 0.0 ? double(ctx->stats.collisions) / (ctx->stats.kernel_ms * 1e-3) : 0.0;

@@ -348,13 +348,16 @@ class Engine:
     def launch(self, stream: Optional[int] = None):
         self._check(self.lib.mtg_launch_async(self.ctx, C.c_void_p(stream or 0)))
 
-    def collect(self, check=True):
+    def collect(self, check=True, allow_event_overflow=False):
+        """Wait for the launched run and return one tally dict per sim.  With
+        allow_event_overflow a run whose only error was a full event log returns its
+        (complete) tallies; stats()["events_overflowed"] then reads 1."""
         n = len(self._sims)
         tot = (F.Totals * n)()
         nh = sum(sum(s.hist_sizes()) for s in self._sims)
         hist = (C.c_longlong * max(nh, 1))()
         st = self.lib.mtg_collect(self.ctx, tot, hist)
-        if check:
+        if check and not (allow_event_overflow and st == F.ERR_QUEUE_FULL and self.stats()["events_overflowed"]):
             self._check(st)
         out = []
         off = 0
@@ -375,10 +378,10 @@ class Engine:
             out.append(d)
         return out
 
-    def run(self, sims: Sequence[SimSpec], check=True):
+    def run(self, sims: Sequence[SimSpec], check=True, allow_event_overflow=False):
         self.prepare(sims)
         self.launch()
-        return self.collect(check=check)
+        return self.collect(check=check, allow_event_overflow=allow_event_overflow)
 
     def primaries(self, first: int, n: int) -> dict:
         out = {k: np.zeros(n, dtype=np.int64) for k in ("vacancies", "collisions")}

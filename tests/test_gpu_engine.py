@@ -436,12 +436,17 @@ def test_event_log_overflow_keeps_tallies(engine_lib):
     e.set_event_log([F.EV_DISSIPATE], 50)
     with pytest.raises(F.EngineError) as err:
         e.run([sim])
-    assert err.value.status == 4  # MTG_ERR_QUEUE_FULL
+    assert err.value.status == F.ERR_QUEUE_FULL
+    assert e.stats()["events_overflowed"] == 1
     t = e.run([sim], check=False)[0]
     assert len(e.events()) == 50
+    t2 = e.run([sim], allow_event_overflow=True)[0]
+    e.set_event_log([F.EV_DISSIPATE], 1 << 20)
+    e.run([sim])
+    assert e.stats()["events_overflowed"] == 0
     e.close()
     for key in ("vacancies", "collisions", "Eel"):
-        assert t[key] == t0[key]
+        assert t[key] == t0[key] and t2[key] == t0[key]
 
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
