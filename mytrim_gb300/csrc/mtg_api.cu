@@ -437,6 +437,12 @@ mtg_create(int device, mtg_ctx ** out)
       delete ctx;
       return MTG_ERR_CUDA;
     }
+  if (mtg::upload_newton_guess32() != cudaSuccess ||
+      mtg::upload_newton_guess32_surrogate(mtg::newton_guess_table32()) != cudaSuccess)
+  {
+    mtg_destroy(ctx);
+    return MTG_ERR_CUDA;
+  }
   *out = ctx;
   return MTG_OK;
 }

@@ -8,13 +8,18 @@
 //     d = r - b (the same Newton steps as trim.C:192-233 written in a variable
 //     that does not cancel), and sin^2(theta/2) is formed as (1 - co)(1 + co)
 //     with 1 - co = d (1 - A F / (F + 1)) / (r + roc), algebraically equal to
-//     1 - co^2 of trim.C:266-269 without its cancellation at small angles;
+//     1 - co^2 of trim.C:266-269 without its cancellation at small angles; the
+//     solve starts from a tabulated first guess (mtg_newton_guess.h), so one
+//     step nearly always meets the reference's stopping test;
 //   * the random azimuth is drawn directly (uniform angle around the flight
 //     direction) instead of by unit-ball rejection; the two give the same
 //     distribution, and the direct draw has no data-dependent loop.
 // Energies are kept as a float pair (value + rounding remainder) so that
 // the small per-collision losses are not rounded away, and the lane tallies use
 // Kahan-compensated sums; FP64 instructions stay out of the collision loop.
+#include <mutex>
+#include <vector>
+
 #include "mtg_common.cuh"
 #include "mtg_collide64.cuh"
 #include "mtg_engine.cuh"
@@ -583,6 +588,56 @@ launch_scatter32(const double * eps, const double * b, long long n, double * s2,
   if (n > 0)
     scatter32_kernel<<<(unsigned int)((n + block - 1) / block), block, 0, st>>>(eps, b, n, s2, potential);
   return cudaGetLastError();
+}
+
+// ---- first-guess table of the FP32 Newton solve
+// phi(r) of the universal (pot 0) or Moliere (1) potential in FP64 (trim.C:197-213),
+// with the project's exp64 so that the table has the same bits on every host
+static double
+screening_phi64(int pot, double r)
+{
+  if (pot == 1)
+    return 0.35 * exp64(-0.3 * r) + 0.55 * exp64(-1.2 * r) + 0.1 * exp64(-6.0 * r);
+  return 0.18175 * exp64(-3.1998 * r) + 0.50986 * exp64(-0.94229 * r) + 0.28022 * exp64(-0.4029 * r) +
+         0.028171 * exp64(-0.20162 * r);
+}
+
+const float *
+newton_guess_table32()
+{
+  // f(r) = b^2 / r + phi(r) / eps - r falls strictly with r, f(b) = phi(b) / eps > 0
+  // and f(b + 2 / eps) < 0 because phi <= 1.000001: 72 halvings of that bracket
+  // (at most 2^19 wide) leave the root to 1e-16, far below float resolution of d
+  static std::vector<float> table;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    table.resize(NG_CELLS);
+    for (int pot = 0; pot < NG_POT; ++pot)
+      for (int i = 0; i < NG_U; ++i)
+      {
+        const double eps = exp64((NG_U0 + i * NG_DU) * 0.69314718055994531);
+        for (int j = 0; j < NG_B; ++j)
+        {
+          const double b = j * NG_DB;
+          double lo = b, hi = b + 2.0 / eps;
+          for (int it = 0; it < 72; ++it)
+          {
+            const double m = 0.5 * (lo + hi);
+            const double f = b * b / m + screening_phi64(pot, m) / eps - m;
+            (f > 0.0 ? lo : hi) = m;
+          }
+          const double d = 0.5 * (lo + hi) - b;
+          table[(size_t(pot) * NG_U + i) * NG_B + j] = float(log64(d) * 1.4426950408889634);
+        }
+      }
+  });
+  return table.data();
+}
+
+cudaError_t
+upload_newton_guess32()
+{
+  return upload_newton_guess32_here(newton_guess_table32());
 }
 
 // ---- stopping through the FP32 table (one (species, material) row)

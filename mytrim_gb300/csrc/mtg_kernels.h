@@ -44,6 +44,11 @@ cudaError_t launch_scatter32(const double * eps, const double * b, long long n, 
                              cudaStream_t st);
 cudaError_t launch_stopping32(const float * row, float lnE_min, float inv_d, const double * E, long long n,
                               double * out, cudaStream_t st);
+// the FP32 Newton solve's first-guess table (built once per process) and its
+// upload to the current device, for the engine and for the surrogate's service
+const float * newton_guess_table32();
+cudaError_t upload_newton_guess32();
+cudaError_t upload_newton_guess32_surrogate(const float * table);
 
 // Surrogate (mtg_surrogate.cu)
 cudaError_t launch_quadrature(const double * eps, const double * b, long long n, double * s2, double * tau,

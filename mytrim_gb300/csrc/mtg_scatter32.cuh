@@ -11,10 +11,61 @@
 // not the derivative's, and they are kept as written.  The Moliere terms
 // exp(-0.3 r)^4 and exp(-0.3 r)^20 are evaluated as exp(-1.2 r) and exp(-6 r).
 // v and v1 are formed once, after the loop, from the last iterate's values.
+//
+// The Newton solve starts from a tabulated first guess (mtg_newton_guess.h):
+// inside the table's range one step nearly always meets the stopping test, where
+// the reference's guess needs 2 to 5, so a warp no longer waits on its slowest
+// lane's extra iterations.  The converged root differs from the one reached from
+// the reference's guess by less than the stopping test's tolerance.
 #pragma once
+
+#include <cuda_runtime.h>
+
+#include "mtg_newton_guess.h"
 
 namespace mtg
 {
+
+// log2(r0 - b) per potential, row-major over (log2 eps, b); one copy per
+// translation unit that scatters in FP32, filled by upload_newton_guess32_here
+static __device__ float g_newton_guess32[NG_CELLS];
+
+static inline cudaError_t
+upload_newton_guess32_here(const float * table)
+{
+  return cudaMemcpyToSymbol(g_newton_guess32, table, sizeof(float) * NG_CELLS);
+}
+
+// first guess at d = r0 - b: bilinear in the table inside its range (universal
+// and Moliere potentials), else the reference's guess (trim.C:183-190)
+template <int POT>
+__device__ __forceinline__ float
+newton_start32(float eps, float b)
+{
+  const float fu = (__log2f(eps) - float(NG_U0)) * float(1.0 / NG_DU);
+  const float fb = b * float(1.0 / NG_DB);
+  if (POT < NG_POT && fu >= 0.0f && fb < float(NG_B - 1))
+  {
+    const int i = min(int(fu), NG_U - 2);
+    const int j = int(fb);
+    const float a = fu - float(i), c = fb - float(j);
+    const float * t = g_newton_guess32 + (POT * NG_U + i) * NG_B + j;
+    const float t00 = __ldg(t), t01 = __ldg(t + 1);
+    const float t10 = __ldg(t + NG_B), t11 = __ldg(t + NG_B + 1);
+    const float lo = fmaf(c, t01 - t00, t00);
+    const float hi = fmaf(c, t11 - t10, t10);
+    return exp2f(fmaf(a, hi - lo, lo));
+  }
+  float r = b;
+  float rr = -2.7f * __logf(eps * b);
+  if (rr >= b)
+  {
+    rr = -2.7f * __logf(eps * rr);
+    if (rr >= b)
+      r = rr;
+  }
+  return r - b;
+}
 
 // phi(r) and sum_i c_i exp(-k_i r) with each weighted exponential as one 2^x:
 // w_i exp(-k_i r) = 2^(r (-k_i log2 e) + log2 w_i), and the derivative sum written on
@@ -89,18 +140,9 @@ scatter32_pot(float eps, float b, float & s2, float & c2, int & niter)
     c2 = 1.0f - s2;
     return;
   }
-  // first guess at the distance of closest approach (trim.C:183-190)
-  float r = b;
-  float rr = -2.7f * __logf(eps * b);
-  if (rr >= b)
-  {
-    rr = -2.7f * __logf(eps * rr);
-    if (rr >= b)
-      r = rr;
-  }
-  float d = r - b;
+  float d = newton_start32<POT>(eps, b);
   const float inv_eps = 1.0f / eps;
-  float phi, tk, ir, q;
+  float r, phi, tk, ir, q;
   do
   {
     r = b + d;

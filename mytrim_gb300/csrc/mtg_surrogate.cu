@@ -700,4 +700,10 @@ surrogate_train(long long n_train, int batch, int epochs, int qat_epochs, float 
   return e;
 }
 
+cudaError_t
+upload_newton_guess32_surrogate(const float * table)
+{
+  return upload_newton_guess32_here(table);
+}
+
 } // namespace mtg
