@@ -57,7 +57,7 @@ L2_FLUSH_BYTES = 256 << 20
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of 65,536 primaries
 # (1.76e9 collisions), divided by its collisions; the traffic grows with the
 # collisions a launch processes, so the figure scales to the 10^7-primary launch
-DRAM_BYTES_PER_COLLISION_FP32 = 2.08
+DRAM_BYTES_PER_COLLISION_FP32 = 2.09
 
 # name -> (description, builder(n_primaries)); builders from mytrim_gb300.workloads
 WORKLOADS = {
@@ -337,7 +337,7 @@ def main():
         n_step = sum(x.n_primaries for x in ss)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        eng.run(ss)
+        eng.run(ss, allow_event_overflow=True)
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t0)
         st = eng.stats()
