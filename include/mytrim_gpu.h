@@ -32,7 +32,9 @@ typedef enum
   MTG_ERR_BAD_INPUT = 1,  /* invalid argument or unsupported sample */
   MTG_ERR_DATA = 2,       /* stopping tables missing or unreadable */
   MTG_ERR_OOM = 3,        /* device allocation failed */
-  MTG_ERR_QUEUE_FULL = 4, /* recoil overflow list exhausted; results incomplete */
+  MTG_ERR_QUEUE_FULL = 4, /* recoil overflow list still exhausted after 3 enlargements:
+                             results incomplete; or a full event log: tallies complete
+                             (mtg_set_event_log) */
   MTG_ERR_TIMEOUT = 5,    /* a member exceeded the collision budget */
   MTG_ERR_NUMERIC = 6,    /* NaN energy or degenerate geometry met */
   MTG_ERR_CUDA = 7,       /* CUDA runtime error */
@@ -249,6 +251,9 @@ typedef struct
   int max_take;            /* fresh primaries one warp took per refill in the last run */
   int events_overflowed;   /* 1 when the last collect's only error was a full event log (its
                               status is MTG_ERR_QUEUE_FULL and the tallies are complete) */
+  int overflow_retries;    /* times the last run was made again because its recoil overflow
+                              list filled (each time with lists four times larger, kept for
+                              later runs; at most 3, then MTG_ERR_QUEUE_FULL) */
 } mtg_stats;
 
 typedef struct mtg_ctx mtg_ctx;
@@ -407,7 +412,7 @@ typedef struct
 } mtg_tuning;
 
 /* Choose the cascade kernel's launch settings for a run by measurement: the
- * simulations' primaries are scaled to about `trial_primaries` in total (0 = 65,536)
+ * simulations' primaries are scaled to about `trial_primaries` in total (0 = 262,144)
  * and launched with the built-in settings, then, one setting at a time, with each
  * candidate refill size (1, 2, 4, 8, 16, 32 primaries per warp refill and the
  * built-in estimate), refill threshold (1, 4, 8, 16 idle lanes), block shape (64,
@@ -415,7 +420,9 @@ typedef struct
  * collisions per second of kernel time is kept in the context's configuration for
  * the runs that follow, if it beats the built-in settings by more than 2 %.  A
  * candidate whose trial fails (a stack too shallow for the cascades fills the
- * overflow list) is skipped.  The trials use the context like ordinary runs (their
+ * overflow list) is skipped, and so is one whose trial spilled members to the
+ * overflow list at a rate that, over the run's full primaries, would fill a quarter
+ * of it.  The trials use the context like ordinary runs (their
  * results are discarded).  No counterpart in the reference, whose threads take
  * primaries one at a time (apps/runmytrim.C:71-93). */
 mtg_status mtg_autotune(mtg_ctx * ctx, const mtg_sim * sims, int n_sims, long long trial_primaries,

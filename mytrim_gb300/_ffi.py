@@ -130,7 +130,8 @@ class Stats(C.Structure):
                 ("drains", C.c_int), ("grid", C.c_int), ("block", C.c_int), ("stack_capacity", C.c_int),
                 ("overflowed", C.c_longlong), ("collisions", C.c_longlong), ("device_bytes", C.c_size_t),
                 ("h2d_bytes", C.c_longlong), ("d2h_bytes", C.c_longlong), ("warp_steps", C.c_longlong),
-                ("kernel_level", C.c_int), ("max_take", C.c_int), ("events_overflowed", C.c_int)]
+                ("kernel_level", C.c_int), ("max_take", C.c_int), ("events_overflowed", C.c_int),
+                ("overflow_retries", C.c_int)]
 
 
 class Tuning(C.Structure):

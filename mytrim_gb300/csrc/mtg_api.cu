@@ -62,6 +62,7 @@ enum Counter
   C_COUNT = 72
 };
 constexpr int MAX_PASSES = 64;
+constexpr int MAX_OVF_RETRIES = 3; // runs redone with a larger overflow list
 
 } // namespace
 
@@ -101,6 +102,7 @@ struct mtg_ctx
   int stage = 0;
   int stack_cap = 0;
   long long ovf_cap = 0;
+  long long ovf_floor = 0; // smallest overflow list of later runs, raised when a run exhausted one
   long long record_cap = 0;
   long long event_cap = 0;
   unsigned int event_mask = 0;
@@ -231,7 +233,7 @@ setup_launch_shape(mtg_ctx * ctx)
   if (cap <= 0)
     cap = prec == MTG_PREC_FP64 ? 4096 : 8192;
   ctx->stack_cap = cap;
-  ctx->ovf_cap = std::max<long long>(1 << 20, warps * 64);
+  ctx->ovf_cap = std::max<long long>({1LL << 20, warps * 64, ctx->ovf_floor});
   mtg_status st = MTG_OK;
   auto chk = [&](cudaError_t ce, const char * what) {
     if (ce != cudaSuccess && st == MTG_OK)
@@ -722,6 +724,31 @@ mtg_launch_async(mtg_ctx * ctx, void * stream)
   return MTG_OK;
 }
 
+// Grows both overflow lists to `cap` records; on failure restores the old size (the
+// lists must never be left unallocated under a prepared context).
+static bool
+grow_overflow(mtg_ctx * ctx, long long cap)
+{
+  const size_t rec = record_size(ctx->cfg.precision);
+  if (ensure(ctx->d_ovf0, size_t(cap) * rec) == cudaSuccess && ensure(ctx->d_ovf1, size_t(cap) * rec) == cudaSuccess)
+  {
+    ctx->ovf_cap = cap;
+    ctx->ovf_floor = std::max(ctx->ovf_floor, cap);
+    return true;
+  }
+  cudaGetLastError();
+  if (ensure(ctx->d_ovf0, size_t(ctx->ovf_cap) * rec) != cudaSuccess ||
+      ensure(ctx->d_ovf1, size_t(ctx->ovf_cap) * rec) != cudaSuccess)
+  {
+    cudaGetLastError();
+    ctx->prepared = false; // the next mtg_prepare allocates again (or reports MTG_ERR_OOM)
+  }
+  return false;
+}
+
+static mtg_status
+collect_run(mtg_ctx * ctx, mtg_totals * totals, long long * hist, int retry);
+
 mtg_status
 mtg_collect(mtg_ctx * ctx, mtg_totals * totals, long long * hist)
 {
@@ -730,6 +757,13 @@ mtg_collect(mtg_ctx * ctx, mtg_totals * totals, long long * hist)
     return st;
   if (!ctx->launched)
     return fail(ctx, MTG_ERR_STATE, "nothing launched");
+  return collect_run(ctx, totals, hist, 0);
+}
+
+static mtg_status
+collect_run(mtg_ctx * ctx, mtg_totals * totals, long long * hist, int retry)
+{
+  mtg_status st = MTG_OK;
   CK(cudaStreamSynchronize(ctx->stream));
   const HostTables & t = ctx->tables;
   unsigned long long cnt[C_COUNT];
@@ -750,21 +784,40 @@ mtg_collect(mtg_ctx * ctx, mtg_totals * totals, long long * hist)
     CK(cudaMemcpy(cnt, ctx->d_counters.p, sizeof cnt, cudaMemcpyDeviceToHost));
   }
   const bool unfinished = cnt[ctx->ovf_last ? C_OVF1 : C_OVF0] > 0;
+  // an overflow list that filled dropped members: the run is made again with lists
+  // four times larger, kept for later runs.  The random draws depend on the members'
+  // keys, not on the schedule, so the repeated run is the run the larger lists would
+  // have given in the first place.
+  {
+    unsigned int errq = 0;
+    CK(cudaMemcpy(&errq, ctx->d_err.p, sizeof errq, cudaMemcpyDeviceToHost));
+    if ((errq & ERRB_QUEUE_FULL) && retry < MAX_OVF_RETRIES && grow_overflow(ctx, ctx->ovf_cap * 4))
+    {
+      const int launched_before = ctx->stats.launches; // the count covers every attempt
+      st = mtg_launch_async(ctx, ctx->stream);
+      if (st != MTG_OK)
+        return st;
+      ctx->stats.launches += launched_before;
+      return collect_run(ctx, totals, hist, retry + 1);
+    }
+  }
   if (extra)
   {
+    CK(cudaEventRecord(ctx->ev[3], ctx->stream)); // end of the extra drain passes
     st = launch_reduction(ctx);
     if (st != MTG_OK)
       return st;
+    CK(cudaEventRecord(ctx->ev[2], ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
   }
+  // with extra drain passes the kernel time runs to the end of the last one (it
+  // includes the first reduction and the host's turnaround between the passes)
   float ms = 0.0f;
-  if (!extra)
-  {
-    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
-    ctx->stats.kernel_ms = ms;
-    cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
-    ctx->stats.reduce_ms = ms;
-  }
+  cudaEventElapsedTime(&ms, ctx->ev[0], extra ? ctx->ev[3] : ctx->ev[1]);
+  ctx->stats.kernel_ms = ms;
+  cudaEventElapsedTime(&ms, extra ? ctx->ev[3] : ctx->ev[1], ctx->ev[2]);
+  ctx->stats.reduce_ms = ms;
+  ctx->stats.overflow_retries = retry;
   ctx->stats.drains = ctx->passes - 1;
   ctx->stats.warp_steps = (long long)cnt[C_STEPS];
   ctx->stats.grid = ctx->grid;
@@ -907,9 +960,17 @@ mtg_autotune(mtg_ctx * ctx, const mtg_sim * sims, int n_sims, long long trial_pr
   {
     int block, take, cap, refill;
   };
-  // collisions per second of kernel time of one trial launch; a launch that fails
-  // (an overflow list filled by a stack too shallow for the cascades) rates 0
-  auto rate = [&](const Setting & x) -> double {
+  long long trial_total = 0;
+  for (const mtg_sim & s : trial)
+    trial_total += std::max<long long>(0, s.n_primaries);
+  const double run_scale = double(total) / double(std::max<long long>(1, trial_total));
+  // collisions per second of kernel time of one trial launch.  A launch that fails
+  // (an overflow list filled by a stack too shallow for the cascades) rates 0, and so
+  // does a candidate whose trial spills, scaled from the trial's primaries to the
+  // run's, would fill more than a quarter of the overflow list: spills grow with the
+  // primaries of a pass, and a trial that passes can still exhaust the list at the
+  // run's full size
+  auto rate = [&](const Setting & x, bool guard) -> double {
     mtg_config c = base;
     c.block_threads = x.block;
     c.max_primaries_per_refill = x.take;
@@ -921,12 +982,15 @@ mtg_autotune(mtg_ctx * ctx, const mtg_sim * sims, int n_sims, long long trial_pr
     if (s != MTG_OK && !(s == MTG_ERR_QUEUE_FULL && ctx->stats.events_overflowed)) // a full event log still times the run
       return 0.0;
     ++trials;
+    if (guard && (ctx->stats.overflow_retries > 0 ||
+                  double(ctx->stats.overflowed) * run_scale > 0.25 * double(ctx->ovf_cap)))
+      return 0.0;
     return ctx->stats.kernel_ms > 0.0 ? double(ctx->stats.collisions) / (ctx->stats.kernel_ms * 1e-3) : 0.0;
   };
   const Setting built_in{base.block_threads > 0 ? base.block_threads : 128, base.max_primaries_per_refill,
                          base.stack_capacity, base.refill_min_idle};
-  rate(built_in); // warm-up (module load, first allocations)
-  const double r_def = rate(built_in);
+  rate(built_in, false); // warm-up (module load, first allocations)
+  const double r_def = rate(built_in, false);
   if (!(r_def > 0.0))
     return fail(ctx, MTG_ERR_BAD_INPUT, std::string("mtg_autotune: the trial run failed: ") + ctx->err);
   const int heuristic = ctx->stats.max_take;
@@ -935,7 +999,7 @@ mtg_autotune(mtg_ctx * ctx, const mtg_sim * sims, int n_sims, long long trial_pr
   double r_best = r_def;
   // coordinate search, one setting at a time
   auto consider = [&](Setting x) {
-    const double r = rate(x);
+    const double r = rate(x, true);
     if (r > r_best)
     {
       r_best = r;

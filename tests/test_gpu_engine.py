@@ -297,6 +297,26 @@ def test_overflow_drain_gives_identical_results(engine_lib, prec):
         assert ref[k] == small[k], k
 
 
+def test_exhausted_overflow_list_is_retried(engine_lib):
+    """8192 Cu 100 keV cascades (about 1.5e7 members) on 4-entry recoil stacks spill
+    millions of members in one pass, more than the 2^20-entry overflow list holds:
+    the run is made again with larger lists and gives the tallies of the
+    default-stack run exactly."""
+    sim = W.cu_self_ion(n_primaries=8192)
+    e = Engine(precision="fp32", seed=8)
+    ref = e.run([sim])[0]
+    assert e.stats()["overflow_retries"] == 0
+    e.configure(precision="fp32", seed=8, stack_capacity=4)
+    small = e.run([sim])[0]
+    st = e.stats()
+    again = e.run([sim])[0]  # the enlarged lists are kept for later runs
+    st2 = e.stats()
+    e.close()
+    assert st["overflow_retries"] >= 1 and st2["overflow_retries"] == 0, (st, st2)
+    for k in ("members", "collisions", "vacancies", "replacements", "interstitials"):
+        assert ref[k] == small[k] == again[k], k
+
+
 def test_collision_budget_returns_timeout(engine_lib):
     """A per-member collision budget that is too small ends the run with an
     error status (no hang, context stays usable)."""
