@@ -31,21 +31,42 @@ geo_round(Real x)
     return round(x);
 }
 
+// Whether cluster q contains pos: the distance test of sampleClusters::lookupCluster
+// with dr = 0 (sample_clusters.C:60-130), to the nearest image on periodic axes.
+template <class Real, class C4>
+MTG_HD bool
+cluster_contains(const Real pos[3], const C4 & q, const Real w[3], const int bc[3])
+{
+  Real d0 = pos[0] - Real(q.x), d1 = pos[1] - Real(q.y), d2 = pos[2] - Real(q.z);
+  if (bc[0] == 0)
+    d0 -= geo_round(d0 / w[0]) * w[0];
+  if (bc[1] == 0)
+    d1 -= geo_round(d1 / w[1]) * w[1];
+  if (bc[2] == 0)
+    d2 -= geo_round(d2 / w[2]) * w[2];
+  const Real r2 = d0 * d0 + d1 * d1 + d2 * d2;
+  const Real rr = Real(q.r) + Real(0);
+  return r2 < rr * rr;
+}
+
 // sampleClusters::lookupCluster with dr = 0 (sample_clusters.C:60-130): the index
 // of the cluster that contains pos, -1 in the matrix, -2 outside a CUT boundary.
 // The hash cells within ceil(cmr / kd) of pos's cell are searched in the
 // reference's order; periodic axes measure the distance to the nearest image.
 // Every cell list is walked at most n_clusters steps.  Before the search, the
-// occupancy mask (mn cells per axis, bit clear where no cluster reaches) answers
-// "matrix" for most points of a dilute sample; it is consulted only for periodic
-// coordinates within 64 box lengths, where its rounding margin holds.
+// candidate lists (`cells`, mn cells per axis, built by mtg_setup.cpp) answer for
+// most points: a cell not marked for the search lists every cluster that can
+// contain a point of it, and at most one of them does, the cluster the search
+// would return; no candidate containing pos means the matrix.  They are consulted
+// only for periodic coordinates within 64 box lengths, where their rounding margin
+// holds.
 template <class Real, class C4>
 MTG_HD int
 cluster_lookup(const Real pos[3], const Real w[3], const int bc[3], const int kn[3], const Real kd[3], Real cmr,
-               const C4 * c, const int * next, const int * head, int n_clusters, const uint32_t * mask,
+               const C4 * c, const int * next, const int * head, int n_clusters, const uint32_t * cells,
                const int mn[3], const Real inv_mcell[3])
 {
-  int k[3], k1[3], k2[3];
+  int k[3];
   for (int i = 0; i < 3; ++i)
   {
     k[i] = int(geo_floor((pos[i] * Real(kn[i])) / w[i]));
@@ -59,15 +80,8 @@ cluster_lookup(const Real pos[3], const Real w[3], const int bc[3], const int kn
       if (k[i] < 0)
         k[i] += kn[i];
     }
-    const int ks = int((cmr + Real(0)) / kd[i]) + 1;
-    k1[i] = k[i] - ks;
-    k2[i] = k[i] + ks;
-    if (k1[i] < 0 && bc[i] != 0)
-      k1[i] = 0;
-    if (k2[i] >= kn[i] && bc[i] != 0)
-      k2[i] = kn[i] - 1;
   }
-  if (mask)
+  if (cells)
   {
     bool use = true;
     long long cell = 0, stride = 1;
@@ -84,8 +98,32 @@ cluster_lookup(const Real pos[3], const Real w[3], const int bc[3], const int kn
       cell += stride * m;
       stride *= mn[i];
     }
-    if (use && !((mask[cell >> 5] >> (cell & 31)) & 1u))
-      return -1;
+    if (use)
+    {
+      const uint32_t s0 = cells[cell];
+      if (!(s0 & 0x80000000u))
+      {
+        const uint32_t s1 = cells[cell + 1] & 0x7fffffffu;
+        for (uint32_t j = s0; j < s1; ++j)
+        {
+          const int l = int(cells[j]);
+          if (cluster_contains(pos, c[l], w, bc))
+            return l;
+        }
+        return -1;
+      }
+    }
+  }
+  int k1[3], k2[3];
+  for (int i = 0; i < 3; ++i)
+  {
+    const int ks = int((cmr + Real(0)) / kd[i]) + 1;
+    k1[i] = k[i] - ks;
+    k2[i] = k[i] + ks;
+    if (k1[i] < 0 && bc[i] != 0)
+      k1[i] = 0;
+    if (k2[i] >= kn[i] && bc[i] != 0)
+      k2[i] = kn[i] - 1;
   }
   for (int j0 = k1[0]; j0 <= k2[0]; ++j0)
     for (int j1 = k1[1]; j1 <= k2[1]; ++j1)
@@ -98,17 +136,7 @@ cluster_lookup(const Real pos[3], const Real w[3], const int bc[3], const int kn
         int l = head[m0 + kn[0] * (m1 + kn[1] * m2)];
         for (int guard = 0; l >= 0 && guard < n_clusters; ++guard)
         {
-          const C4 q = c[l];
-          Real d0 = pos[0] - Real(q.x), d1 = pos[1] - Real(q.y), d2 = pos[2] - Real(q.z);
-          if (bc[0] == 0)
-            d0 -= geo_round(d0 / w[0]) * w[0];
-          if (bc[1] == 0)
-            d1 -= geo_round(d1 / w[1]) * w[1];
-          if (bc[2] == 0)
-            d2 -= geo_round(d2 / w[2]) * w[2];
-          const Real r2 = d0 * d0 + d1 * d1 + d2 * d2;
-          const Real rr = Real(q.r) + Real(0);
-          if (r2 < rr * rr)
+          if (cluster_contains(pos, c[l], w, bc))
             return l;
           l = next[l];
         }

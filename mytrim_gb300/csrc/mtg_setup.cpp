@@ -334,37 +334,51 @@ expected_members(const mtg_sim & s)
   return 1.0 + std::max(0.0, 0.8 * Tdam / (2.0 * Ed));
 }
 
-// Occupancy mask of a cluster sample: a grid of mn cells per axis with edge about
-// max(cmr / 2, w / 1024); a cell's bit is set when some cluster, its radius grown by
-// a margin of max(w) / 1024, reaches into the cell (periodic images on PBC axes).
-// The margin covers the rounding of a position wrapped into the box and of the
-// distance test in single precision (positions within 64 box lengths), so a point
-// in an unset cell lies in no cluster: the lookup returns the matrix there without
-// searching the hash, which would find nothing.
+// Candidate lists of a cluster sample.  A grid of mn cells per axis with edge about
+// max(cmr / 2, w / 1024), coarser where it would pass 2^22 cells; for each cell the
+// clusters whose sphere, its radius grown by a margin of max(w) / 1024, reaches into
+// the cell (periodic images on PBC axes).  The margin covers the rounding of a
+// position wrapped into the box and of the distance test in single precision
+// (positions within 64 box lengths), so every cluster containing a point of a cell
+// is among the cell's candidates.  A cell is marked for the hash search when two of
+// its candidates come closer than their radii and two margins (a point could lie in
+// both, and which one the search meets first decides the answer; minimum-image
+// distances on PBC axes), when it has more than 16 candidates, or when a candidate
+// is one the search may not see from every point of its sphere: a cluster centred
+// outside the box on a CUT or INF axis (its hash cell is the wrapped one, outside
+// the clamped window of the points near it) or one whose sphere and two margins
+// span more hash cells than the search window reaches.  Elsewhere at most one
+// candidate contains any point, and the search finds it: the cluster it returns.
+// Layout from mask_base in the run's words: mn0 mn1 mn2 + 1 cell starts (relative
+// to mask_base; bit 31 marks the cell for the search), then the candidates'
+// indexes.  Above 2^26 candidates the lists are left out: a cell then holds none and
+// is marked when any cluster reaches it (an occupancy mask).
 static void
-build_cluster_mask(SimDesc & d, const mtg_sample & smp, std::vector<uint32_t> & words)
+build_cluster_cells(SimDesc & d, const mtg_sample & smp, std::vector<uint32_t> & words)
 {
+  constexpr double MAX_CELLS = double(1 << 22);
+  constexpr long long MAX_ITEMS = 1LL << 26;
+  constexpr uint32_t SEARCH = 0x80000000u;
+  constexpr int MAX_CANDIDATES = 16;
   const double wmax = std::max(smp.w[0], std::max(smp.w[1], smp.w[2]));
-  const double g = std::max(d.cmr * 0.5, wmax / 1024.0);
+  double g = std::max(d.cmr * 0.5, wmax / 1024.0);
+  g = std::max(g, std::cbrt(smp.w[0] * smp.w[1] * smp.w[2] / MAX_CELLS));
   double cell[3];
-  long long bits = 1;
+  long long ncell = 1;
   for (int i = 0; i < 3; ++i)
   {
     d.mn[i] = int(std::min(512.0, std::max(1.0, std::ceil(smp.w[i] / g))));
     cell[i] = smp.w[i] / d.mn[i];
     d.inv_mcell[i] = double(d.mn[i]) / smp.w[i];
-    bits *= d.mn[i];
+    ncell *= d.mn[i];
   }
-  d.mask_base = (long long)words.size();
-  words.resize(size_t(d.mask_base + (bits + 31) / 32), 0u);
   const double margin = wmax / 1024.0;
-  for (long long l = 0; l < smp.n_clusters; ++l)
-  {
+  // the cells cluster l reaches, in the occupancy test of the grown sphere
+  auto for_each_cell = [&](long long l, auto && fn) {
     const double * c = smp.clusters + 4 * l;
     const double R = c[3] + margin;
     long long lo[3], hi[3];
     bool full[3] = {false, false, false};
-    bool empty = false;
     for (int i = 0; i < 3; ++i)
     {
       lo[i] = (long long)std::floor((c[i] - R) * d.inv_mcell[i]);
@@ -382,11 +396,10 @@ build_cluster_mask(SimDesc & d, const mtg_sample & smp, std::vector<uint32_t> & 
       {
         lo[i] = std::max<long long>(lo[i], 0);
         hi[i] = std::min<long long>(hi[i], d.mn[i] - 1);
-        empty = empty || lo[i] > hi[i];
+        if (lo[i] > hi[i])
+          return;
       }
     }
-    if (empty)
-      continue;
     for (long long j2 = lo[2]; j2 <= hi[2]; ++j2)
       for (long long j1 = lo[1]; j1 <= hi[1]; ++j1)
         for (long long j0 = lo[0]; j0 <= hi[0]; ++j0)
@@ -401,11 +414,80 @@ build_cluster_mask(SimDesc & d, const mtg_sample & smp, std::vector<uint32_t> & 
             d2 += e * e;
             m[i] = ((j[i] % d.mn[i]) + d.mn[i]) % d.mn[i];
           }
-          if (d2 > R * R)
-            continue;
-          const long long bit = m[0] + (long long)d.mn[0] * (m[1] + (long long)d.mn[1] * m[2]);
-          words[size_t(d.mask_base + bit / 32)] |= 1u << (bit % 32);
+          if (d2 <= R * R)
+            fn(m[0] + (long long)d.mn[0] * (m[1] + (long long)d.mn[1] * m[2]));
         }
+  };
+  std::vector<uint32_t> count(size_t(ncell), 0u);
+  long long items = 0;
+  for (long long l = 0; l < smp.n_clusters; ++l)
+    for_each_cell(l, [&](long long q) {
+      if (count[size_t(q)] < 0x7fffffffu)
+        ++count[size_t(q)];
+      ++items;
+    });
+  const bool lists = ncell + 1 + items < MAX_ITEMS;
+  d.mask_base = (long long)words.size();
+  words.resize(size_t(d.mask_base + ncell + 1 + (lists ? items : 0)), 0u);
+  uint32_t * w = words.data() + d.mask_base;
+  if (!lists)
+  {
+    for (long long q = 0; q <= ncell; ++q)
+      w[q] = uint32_t(ncell + 1) | (q < ncell && count[size_t(q)] ? SEARCH : 0u);
+    return;
+  }
+  // cell starts, then the candidates in cluster order
+  uint32_t at = uint32_t(ncell + 1);
+  for (long long q = 0; q < ncell; ++q)
+  {
+    w[q] = at;
+    at += count[size_t(q)];
+  }
+  w[ncell] = at;
+  std::vector<uint32_t> fill(w, w + ncell);
+  for (long long l = 0; l < smp.n_clusters; ++l)
+    for_each_cell(l, [&](long long q) { w[fill[size_t(q)]++] = uint32_t(l); });
+  // clusters the search finds from every point they contain
+  std::vector<char> regular(size_t(smp.n_clusters), 1);
+  for (long long l = 0; l < smp.n_clusters; ++l)
+  {
+    const double * c = smp.clusters + 4 * l;
+    for (int i = 0; i < 3; ++i)
+    {
+      const int ks = int(d.cmr / d.kd[i]) + 1; // the window of cluster_lookup
+      if ((smp.bc[i] != MTG_BC_PBC && !(c[i] >= 0.0 && c[i] < smp.w[i])) ||
+          std::ceil((c[3] + 2.0 * margin) / d.kd[i]) > double(ks))
+        regular[size_t(l)] = 0;
+    }
+  }
+  // cells where two candidates could both contain a point, or where the search might
+  // miss one, take the search
+  auto apart = [&](uint32_t a, uint32_t b) {
+    const double * ca = smp.clusters + 4 * size_t(a);
+    const double * cb = smp.clusters + 4 * size_t(b);
+    double d2 = 0.0;
+    for (int i = 0; i < 3; ++i)
+    {
+      double e = ca[i] - cb[i];
+      if (smp.bc[i] == MTG_BC_PBC)
+        e -= std::nearbyint(e / smp.w[i]) * smp.w[i];
+      d2 += e * e;
+    }
+    const double reach = ca[3] + cb[3] + 2.0 * margin;
+    return d2 >= reach * reach;
+  };
+  for (long long q = 0; q < ncell; ++q)
+  {
+    const uint32_t s0 = w[q], s1 = w[q + 1];
+    bool search = s1 - s0 > uint32_t(MAX_CANDIDATES);
+    for (uint32_t x = s0; x < s1 && !search; ++x)
+    {
+      search = !regular[w[x]];
+      for (uint32_t y = x + 1; y < s1 && !search; ++y)
+        search = !apart(w[x], w[y]);
+    }
+    if (search)
+      w[q] |= SEARCH;
   }
 }
 
@@ -767,7 +849,7 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
         if (c[3] > d.cmr)
           d.cmr = c[3];
       }
-      build_cluster_mask(d, smp, out.cl_mask);
+      build_cluster_cells(d, smp, out.cl_mask);
     }
     d.hist_evac_rows = s.hist_vac_n > 0 ? s.hist_evac_rows : 0;
     d.hist_evac_base = hist;

@@ -34,7 +34,7 @@ struct HostTables
   // clusters of all cluster samples of the run (SimDesc::cl_base / cell_base index them)
   std::vector<Cl4d> clusters;
   std::vector<int> cl_next, cl_head;
-  std::vector<uint32_t> cl_mask; // occupancy masks (SimDesc::mask_base indexes them)
+  std::vector<uint32_t> cl_mask; // cluster candidate lists (SimDesc::mask_base indexes them)
 };
 
 // Point the simulations' cluster pointers at arrays holding HostTables::clusters,

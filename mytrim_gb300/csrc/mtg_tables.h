@@ -142,12 +142,12 @@ struct SimDesc
   const struct Cl4d * cl;
   const int * cl_next;
   const int * cl_head;
-  // occupancy mask: one bit per cell of a finer grid (mn cells per axis), set where
-  // some cluster (dilated by a rounding margin) reaches into the cell; a point in an
-  // unset cell is in the matrix without a hash search
+  // candidate lists on a finer grid (mn cells per axis): per cell the clusters that
+  // (dilated by a rounding margin) reach into it, or a mark sending the cell's points
+  // to the hash search (layout in mtg_setup.cpp, build_cluster_cells)
   int mn[3];
   double inv_mcell[3];
-  long long mask_base; // offset into the run's mask words
+  long long mask_base; // offset of this simulation's lists in the run's words
   const uint32_t * cl_mask;
 };
 

@@ -17,7 +17,7 @@
 //   replay_host <tables> --mathcheck [n]         exp64 / log64 short routes vs full forms
 //   replay_host <tables> --eval exp|log|pow       lines of hex-float arguments -> results (hex)
 //   replay_host <tables> --philox                lines of six hex words -> Philox outputs
-//   replay_host <tables> --lookupcheck n < spec  cluster lookup with vs without the mask
+//   replay_host <tables> --lookupcheck n < spec  cluster lookup with vs without the candidate lists
 
 #include "runspec.h"
 
@@ -322,7 +322,7 @@ main(int argc, char ** argv)
   const SimDesc & sd = t.sims[0];
   if (argc >= 4 && std::string(argv[2]) == "--lookupcheck" && sd.geometry == 1)
   {
-    // the cluster lookup with and without the occupancy mask, in double and in float,
+    // the cluster lookup with and without the candidate lists, in double and in float,
     // at n random points: inside the box, within 64 box lengths on periodic axes,
     // and near cluster surfaces; prints "checked mismatches"
     const long long n = atoll(argv[3]);
@@ -376,6 +376,18 @@ main(int argc, char ** argv)
         ++bad;
       }
     }
+    // cells with candidates, and those of them marked for the hash search
+    long long listed = 0, marked = 0;
+    const long long ncell = (long long)sd.mn[0] * sd.mn[1] * sd.mn[2];
+    for (long long q = 0; q < ncell; ++q)
+    {
+      const uint32_t s0 = sd.cl_mask[q], s1 = sd.cl_mask[q + 1] & 0x7fffffffu;
+      if (s0 & 0x80000000u)
+        ++marked;
+      else if (s1 > s0)
+        ++listed;
+    }
+    printf("cells %lld %lld\n", listed, marked);
     printf("%lld %lld\n", n, bad);
     return bad ? 1 : 0;
   }

@@ -1,8 +1,9 @@
-"""The cluster lookup's occupancy mask (mytrim_gb300/csrc/mtg_geometry.cuh, built by
-mtg_setup.cpp): with the mask the lookup answers exactly as the hash search of
-sampleClusters::lookupCluster (sample_clusters.C:60-130) without it, in double and
-in float, at random points inside the box, far out on periodic axes and on cluster
-surfaces (host build of the same code, oracle/_build/replay_host --lookupcheck)."""
+"""The cluster lookup's candidate lists (mytrim_gb300/csrc/mtg_geometry.cuh, built by
+mtg_setup.cpp): with them the lookup answers exactly as the hash search of
+sampleClusters::lookupCluster (sample_clusters.C:60-130) without them, in double
+and in float, at random points inside the box, far out on periodic axes and on
+cluster surfaces (host build of the same code, oracle/_build/replay_host
+--lookupcheck), for separate, overlapping and box-spanning clusters."""
 import subprocess
 from pathlib import Path
 
@@ -36,12 +37,20 @@ CASES = {
                     (8, 12, 5)),
     "spanning_spheres": ((100.0, 100.0, 100.0), (0, 0, 0), _clusters(5, 40, 70, (100, 100, 100), 3), (4, 4, 4)),
     "many_small": ((200.0, 200.0, 200.0), (0, 1, 0), _clusters(1500, 1.0, 3.0, (200, 200, 200), 4), (40, 40, 40)),
+    # most cells hold overlapping candidates and take the search
+    "overlapping": ((200.0, 200.0, 200.0), (0, 0, 2), _clusters(400, 10.0, 30.0, (200, 200, 200), 5), (10, 10, 10)),
+    # separate bubbles, as the xenon workload places them: nearly every cell answers
+    # from its list
+    "separate": ((400.0, 400.0, 400.0), (0, 0, 0), None, (19, 19, 19)),
 }
 
 
 @pytest.mark.parametrize("case", sorted(CASES))
 def test_mask_answers_as_the_search(oracle_built, case):
     box, bc, cl, kn = CASES[case]
+    if cl is None:
+        from mytrim_gb300.workloads import _bubbles
+        cl = _bubbles(200, 15.0, 400.0, 3)
     exe = ROOT / "oracle" / "_build" / "replay_host"
     tables = ROOT / "mytrim_gb300" / "data" / "stopping_tables.tsv"
     r = subprocess.run([str(exe), str(tables), "--lookupcheck", "200000"], input=_spec(box, bc, cl, kn),
@@ -49,3 +58,6 @@ def test_mask_answers_as_the_search(oracle_built, case):
     checked, bad = (int(v) for v in r.stdout.split()[-2:])
     assert checked == 200000
     assert bad == 0, r.stdout
+    listed, marked = (int(v) for v in r.stdout.split("cells")[1].split()[:2])
+    if case == "separate":  # the lists, not the search, answer near separate bubbles
+        assert marked < 0.02 * (listed + marked), (listed, marked)

@@ -66,8 +66,12 @@ def _solid(n, potential="universal"):
 
 
 def _same(got, want):
-    for k in FIELDS + ("Eel", "Enuc"):
+    for k in FIELDS:
         assert got[k] == want[k], (k, got[k], want[k])
+    # the per-primary energy sums take each lane's share through FP64 atomics in the
+    # order the lanes reach them, so two runs agree to rounding, not to the bit
+    for k in ("Eel", "Enuc"):
+        assert math.isclose(got[k], want[k], rel_tol=1e-12), (k, got[k], want[k])
 
 
 def test_run_primaries_equals_engine(runner):

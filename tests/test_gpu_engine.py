@@ -427,8 +427,10 @@ def test_event_log_matches_tallies(engine_lib, prec):
     t = e.run([sim])[0]
     ev = e.events()
     e.close()
-    for key in ("vacancies", "replacements", "collisions", "members", "Eel", "Enuc"):
+    for key in ("vacancies", "replacements", "collisions", "members"):
         assert t[key] == t0[key], key
+    for key in ("Eel", "Enuc"):  # FP64 atomics in lane order: equal to rounding
+        assert math.isclose(t[key], t0[key], rel_tol=1e-12), key
     k = ev["kind"]
     assert (k == F.EV_VACANCY).sum() == t["vacancies"]
     assert (k == F.EV_REPLACEMENT).sum() == t["replacements"]
@@ -477,8 +479,9 @@ def test_event_log_overflow_keeps_tallies(engine_lib):
     e.run([sim])
     assert e.stats()["events_overflowed"] == 0
     e.close()
-    for key in ("vacancies", "collisions", "Eel"):
+    for key in ("vacancies", "collisions"):
         assert t[key] == t0[key] and t2[key] == t0[key]
+    assert math.isclose(t["Eel"], t0["Eel"], rel_tol=1e-12) and math.isclose(t2["Eel"], t0["Eel"], rel_tol=1e-12)
 
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
@@ -526,8 +529,10 @@ def test_cluster_sample_without_clusters_is_the_matrix(engine_lib, prec):
     a = e.run([empty])[0]
     b = e.run([solid])[0]
     e.close()
-    for k in ("members", "collisions", "vacancies", "replacements", "interstitials", "range_n", "Eel", "Enuc"):
+    for k in ("members", "collisions", "vacancies", "replacements", "interstitials", "range_n"):
         assert a[k] == b[k], k
+    for k in ("Eel", "Enuc"):  # FP64 atomics in lane order: equal to rounding
+        assert math.isclose(a[k], b[k], rel_tol=1e-12), k
 
 
 def test_cluster_fp32_matches_fp64(engine_lib):
