@@ -29,17 +29,21 @@
 #include "mtg_surrogate.cuh"
 
 // resident 128-thread blocks per SM the register budget of each feature level is
-// cut for: lean 8 (64 registers), mid and events 7 (72), geometry and full 6 (80),
-// each the most that compiles without spilling much in the collision loop (events
-// at 7 spills 60 bytes and still runs 2 % faster than at 6 without spills)
+// cut for: lean, mid and events 8 (64 registers), full 7 (72), geometry 6 (80).
+// Measured per level: eight blocks beat seven for the mid and events levels in spite
+// of their spills (32 and 80 bytes): +14 % (mid), +7 % (events, full log), +25 %
+// (events, log nearly empty) on B 10 keV into SiO2/Si; the full level gains 7.5 % at
+// seven (Xe into UO2 with bubbles, event log on; 214 bytes of spill), while the
+// geometry level loses 3.5 % at seven and 4 % at eight; the lean level loses 2 to
+// 4 % at nine (56 registers)
 #ifndef MTG_FP32_MIN_BLOCKS
-#define MTG_FP32_MIN_BLOCKS 6
+#define MTG_FP32_MIN_BLOCKS 7
 #endif
 #ifndef MTG_FP32_MIN_BLOCKS_MID
-#define MTG_FP32_MIN_BLOCKS_MID 7
+#define MTG_FP32_MIN_BLOCKS_MID 8
 #endif
 #ifndef MTG_FP32_MIN_BLOCKS_EVENTS
-#define MTG_FP32_MIN_BLOCKS_EVENTS 7
+#define MTG_FP32_MIN_BLOCKS_EVENTS 8
 #endif
 #ifndef MTG_FP32_MIN_BLOCKS_GEO
 #define MTG_FP32_MIN_BLOCKS_GEO 6
