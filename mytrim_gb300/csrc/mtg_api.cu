@@ -57,12 +57,14 @@ enum Counter
   C_OVF0 = 64, // overflow counts of the two ping-pong lists
   C_OVF1 = 65,
   C_NREC = 66,
-  C_NEV = 67,
+  C_NEV = 67,   // event-log slots reserved
   C_STEPS = 68,
+  C_NEV_UNUSED = 69, // reserved event-log slots that no event filled
   C_COUNT = 72
 };
 constexpr int MAX_PASSES = 64;
 constexpr int MAX_OVF_RETRIES = 3; // runs redone with a larger overflow list
+constexpr int EVENT_CHUNK = 8;     // event-log slots a lane reserves at a time in large logs
 
 } // namespace
 
@@ -321,8 +323,14 @@ fill_params(mtg_ctx * ctx, EngineParams & prm)
   {
     prm.events = ptr<EventRec>(ctx->d_events);
     prm.n_events = ptr<unsigned long long>(ctx->d_counters) + C_NEV;
+    prm.n_event_unused = ptr<unsigned long long>(ctx->d_counters) + C_NEV_UNUSED;
     prm.events_cap = ctx->event_cap;
     prm.event_mask = ctx->event_mask;
+    // slots eight at a time per lane where the log holds at least 16 chunks per
+    // resident lane (the slots left unused, at most seven per lane and pass, then
+    // take at most 1/16 of it); one at a time in smaller logs, which fill exactly
+    const long long lanes = (long long)ctx->grid * ctx->block;
+    prm.event_chunk = ctx->event_cap >= 16LL * EVENT_CHUNK * lanes ? EVENT_CHUNK : 1;
   }
   prm.any_evac = t.any_evac;
   prm.level = kernel_level(ctx);
@@ -1179,15 +1187,35 @@ mtg_get_events(mtg_ctx * ctx, mtg_event * out, long long capacity, long long * n
     *n_total = 0;
   if (ctx->event_cap <= 0 || !ctx->event_mask || !ctx->launched)
     return MTG_OK;
-  unsigned long long n = 0;
+  unsigned long long n = 0, unused = 0;
   CK(cudaMemcpy(&n, ptr<unsigned long long>(ctx->d_counters) + C_NEV, 8, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(&unused, ptr<unsigned long long>(ctx->d_counters) + C_NEV_UNUSED, 8, cudaMemcpyDeviceToHost));
   static_assert(sizeof(mtg_event) == sizeof(EventRec), "event layout");
-  const long long m = std::min<long long>((long long)n, std::min(capacity, ctx->event_cap));
-  if (m > 0)
-    CK(cudaMemcpy(out, ctx->d_events.p, sizeof(EventRec) * m, cudaMemcpyDeviceToHost));
-  *n_written = m;
+  const long long filled = (long long)std::min<unsigned long long>(n, (unsigned long long)ctx->event_cap);
   if (n_total)
-    *n_total = (long long)n;
+    *n_total = (long long)(n - unused);
+  if (unused == 0)
+  {
+    // slots taken one at a time: the records are contiguous
+    const long long m = std::min<long long>(filled, capacity);
+    if (m > 0)
+      CK(cudaMemcpy(out, ctx->d_events.p, sizeof(EventRec) * m, cudaMemcpyDeviceToHost));
+    *n_written = m;
+    return MTG_OK;
+  }
+  // slots taken in chunks: copy in blocks and leave out the slots no event filled
+  constexpr long long BLOCK = 1 << 20;
+  std::vector<EventRec> buf(static_cast<size_t>(std::min(BLOCK, std::max(filled, 1LL))));
+  long long m = 0;
+  for (long long at = 0; at < filled && m < capacity; at += BLOCK)
+  {
+    const long long k = std::min(BLOCK, filled - at);
+    CK(cudaMemcpy(buf.data(), ptr<EventRec>(ctx->d_events) + at, sizeof(EventRec) * k, cudaMemcpyDeviceToHost));
+    for (long long i = 0; i < k && m < capacity; ++i)
+      if (buf[size_t(i)].kind != EV_UNUSED)
+        std::memcpy(out + m++, &buf[size_t(i)], sizeof(EventRec));
+  }
+  *n_written = m;
   return MTG_OK;
 }
 

@@ -90,8 +90,10 @@ struct EngineParams
   long long records_cap;
   // optional event log (mask bit k selects EventKind k; 0 = off)
   EventRec * events;
-  unsigned long long * n_events;
+  unsigned long long * n_events;       // slots reserved
+  unsigned long long * n_event_unused; // reserved slots that no event filled
   long long events_cap;
+  int event_chunk;                     // slots a lane reserves at a time (1 or 8)
   unsigned int event_mask;
   int any_evac; // some simulation keeps a vacancy-energy histogram
   int level;    // KernelLevel of the launched variant
@@ -208,6 +210,7 @@ struct LaneCold
   float vacc;
   int m_md;        // IonMDTag::_md of the lane's member (event-logging levels)
   int evac_bin;    // vacancy-energy bin of the current collision (-1 = none)
+  unsigned int ev_next, ev_end; // the lane's reserved event-log slots [ev_next, ev_end)
 };
 
 // Kernel feature levels.  Code for a feature a run does not use still costs the
@@ -264,6 +267,22 @@ struct LaneSink
     c.e_unf.reset();
     c.e_sput.reset();
   }
+  // when the lane leaves the kernel: its reserved slots that no event filled are
+  // marked unused (the host skips them) and counted
+  __device__ void flush_events()
+  {
+    if constexpr (EV)
+    {
+      LaneCold<Acc> & c = *cold;
+      if (c.ev_end > c.ev_next)
+      {
+        atomicAdd(prm->n_event_unused, (unsigned long long)(c.ev_end - c.ev_next));
+        for (unsigned int s = c.ev_next; s < c.ev_end && (long long)s < prm->events_cap; ++s)
+          prm->events[s].kind = EV_UNUSED;
+      }
+      c.ev_next = c.ev_end = 0;
+    }
+  }
   // per-member summaries feed the optional member records only
   __device__ void reset_member()
   {
@@ -286,7 +305,18 @@ struct LaneSink
   {
     if (!(prm->event_mask & (1u << kind)))
       return;
-    const unsigned long long slot = atomicAdd(prm->n_events, 1ull);
+    // a lane takes its slots event_chunk at a time: the atomic that reserves them
+    // returns through L2, and the lane waits for it before writing the record
+    LaneCold<Acc> & c = *cold;
+    if (c.ev_next == c.ev_end)
+    {
+      // slot indexes fit 32 bits: a log of 2^32 88-byte records exceeds the device
+      // memory; the reservation saturates there once a full log keeps reserving
+      const unsigned long long base = atomicAdd(prm->n_events, (unsigned long long)prm->event_chunk);
+      c.ev_next = base < 0xfffffff0ull ? (unsigned int)base : 0xfffffff0u;
+      c.ev_end = c.ev_next + (unsigned int)prm->event_chunk;
+    }
+    const unsigned int slot = c.ev_next++;
     if ((long long)slot >= prm->events_cap)
     {
       atomicOr(prm->error_flags, ERRB_EVENTS_FULL);
@@ -711,6 +741,7 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
   sink.cold->vcell = -1;
   sink.cold->vacc = 0.0f;
   sink.cold->evac_bin = -1;
+  sink.cold->ev_next = sink.cold->ev_end = 0;
   sink.prm = &prm;
   sink.sim = nullptr;
   sink.gprim = -1;
@@ -912,6 +943,7 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
   sink.flush_prim();
   sink.flush_sim(cur_sim);
   sink.flush_voxel();
+  sink.flush_events();
   if (prm.hist_smem_bins)
   {
     // every warp of the block has left its loop: add the block's counts

@@ -191,7 +191,8 @@ enum EventKind : int
   EV_DISSIPATE = 4,
   EV_REST = 5,
   EV_LOST = 6,
-  EV_HISTORY = 7
+  EV_HISTORY = 7,
+  EV_UNUSED = -1 // a reserved slot of the log that no event filled (see LaneSink::event)
 };
 
 // ---- single-precision copies used by the FP32 engine (built from the tables above)

@@ -444,9 +444,10 @@ class Engine:
                        ("primary", "<i8"), ("sim", "<i4"), ("kind", "<i4"), ("Z", "<i4"), ("gen", "<i4"),
                        ("state", "<i4"), ("tag", "<i4"), ("md", "<i4"), ("pad", "<i4")])
         assert dt.itemsize == C.sizeof(F.Event)
-        out = np.zeros(max(cap, 1), dtype=dt)
+        want = min(cap, self.event_count())  # the records logged, at most the capacity
+        out = np.zeros(max(want, 1), dtype=dt)
         n, total = C.c_longlong(0), C.c_longlong(0)
-        self._check(self.lib.mtg_get_events(self.ctx, out.ctypes.data_as(C.POINTER(F.Event)), cap, C.byref(n),
+        self._check(self.lib.mtg_get_events(self.ctx, out.ctypes.data_as(C.POINTER(F.Event)), want, C.byref(n),
                                             C.byref(total)))
         return out[: n.value].copy()
 

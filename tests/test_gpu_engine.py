@@ -463,6 +463,27 @@ def streams_history(ev):
     return streams.history(ev)
 
 
+def test_event_log_in_chunks_equals_exact_log(engine_lib):
+    """A log large enough for slots taken eight at a time per lane returns the same
+    records as one filled a slot at a time, without the slots left unused."""
+    from mytrim_gb300.streams import _sorted
+    sim = _cu_sim(n=400)
+    e = Engine(precision="fp32", seed=9)
+    e.set_event_log(ALL_EVENTS, 2_000_000)
+    e.run([sim])
+    exact, n_exact = e.events(), e.event_count()
+    lanes = e.stats()["grid"] * e.stats()["block"]
+    e.set_event_log(ALL_EVENTS, 16 * 8 * lanes + 1000)
+    e.run([sim])
+    chunked, n_chunked = e.events(), e.event_count()
+    e.close()
+    assert n_exact == n_chunked == len(exact) == len(chunked) > 0
+    assert (chunked["kind"] >= 1).all()
+    a, b = _sorted(exact), _sorted(chunked)
+    for f in exact.dtype.names:
+        assert np.array_equal(a[f], b[f]), f
+
+
 def test_event_log_overflow_keeps_tallies(engine_lib):
     sim = _cu_sim(n=100)
     e = Engine(precision="fp32", seed=6)
