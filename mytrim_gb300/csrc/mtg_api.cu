@@ -634,7 +634,7 @@ mtg_prepare(mtg_ctx * ctx, const mtg_sim * sims, int n_sims)
     // distinct (species, material) of the run
     const size_t nrows = t.stop_row_mat.size();
     CK(ensure(ctx->d_row_species, 2 * sizeof(int) * nrows));
-    CK(ensure(ctx->d_stop, sizeof(float) * STOP_N * nrows));
+    CK(ensure(ctx->d_stop, 2 * sizeof(float) * STOP_N * nrows)); // (S, p_max) pairs
     int * d_row_species = ptr<int>(ctx->d_row_species);
     int * d_row_mat = d_row_species + nrows;
     CK(h2d(ctx, d_row_species, t.stop_row_species.data(), sizeof(int) * nrows));
@@ -1258,9 +1258,9 @@ mtg_stopping(mtg_ctx * ctx, int Z1, double m1, const mtg_material * material, co
       emax = std::max(emax, E[i]);
     const double lo = std::log(STOP_EMIN), hi = std::log(std::max(emax, 1.0) * 1.05);
     const double dl = (hi - lo) / (STOP_N - 1);
-    CK(ensure(ctx->d_tmp3, sizeof(float) * STOP_N + sizeof(int)));
+    CK(ensure(ctx->d_tmp3, 2 * sizeof(float) * STOP_N + sizeof(int)));
     int zero = 0;
-    int * d_rs = reinterpret_cast<int *>(reinterpret_cast<char *>(ctx->d_tmp3.p) + sizeof(float) * STOP_N);
+    int * d_rs = reinterpret_cast<int *>(reinterpret_cast<char *>(ctx->d_tmp3.p) + 2 * sizeof(float) * STOP_N);
     CK(cudaMemcpy(d_rs, &zero, sizeof zero, cudaMemcpyHostToDevice));
     CK(launch_build_stop_tables(d_sc, d_mc, nullptr, 1, d_rs, ptr<float>(ctx->d_tmp3), lo, dl, nullptr));
     CK(launch_stopping32(ptr<float>(ctx->d_tmp3), float(lo), float(1.0 / dl), ptr<double>(ctx->d_tmp1), n,

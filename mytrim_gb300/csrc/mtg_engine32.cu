@@ -1,9 +1,11 @@
 // FP32 cascade path: the same collision loop as the FP64 plain path
 // (TrimBase::trim, trim.C:74-424) in single precision, with three changes of
 // evaluation that keep FP32 accurate and fast:
-//   * electronic stopping is read from a per-(species, material) table of
-//     S(E), uniform in ln E with 2048 points and filled by the FP64 stopping code,
-//     instead of re-evaluating ~11 transcendentals per element per collision;
+//   * electronic stopping and the maximum impact parameter of the free flight are
+//     read from a per-(species, material) table of (S(E), p_max(E)) pairs, uniform
+//     in ln E with 2048 points and filled by the FP64 code, instead of
+//     re-evaluating ~11 transcendentals per element (S) and a chain of two square
+//     roots, a power and two divisions (p_max) per collision;
 //   * the Newton solve for the distance of closest approach iterates on
 //     d = r - b (the same Newton steps as trim.C:192-233 written in a variable
 //     that does not cancel), and sin^2(theta/2) is formed as (1 - co)(1 + co)
@@ -73,7 +75,7 @@ struct Tables32
   const Species32 * species;
   const Mat32 * mats;
   const Sim32 * sims;
-  const float * stop;
+  const float2 * stop; // (S, p_max) pairs, STOP_N per row
   float lnE_min, inv_dlnE;
   const SurrogateNet * net;
 };
@@ -91,16 +93,23 @@ ff_sub(float & hi, float & lo, float d)
   hi = h;
 }
 
-__device__ __forceinline__ float
-stop_lookup(const float * row, float lnE_min, float inv_d, float E)
+// S(E) and p_max(E) from one row of the table; false below its first point, where
+// S scales as sqrt(E) from there and p_max is left to the formula
+__device__ __forceinline__ bool
+stop_lookup(const float2 * row, float lnE_min, float inv_d, float E, float & S, float & pmax)
 {
   const float u = (__logf(E) - lnE_min) * inv_d;
   if (!(u > 0.0f))
-    return row[0] * sqrtf(E * float(1.0 / STOP_EMIN));
+  {
+    S = row[0].x * sqrtf(E * float(1.0 / STOP_EMIN));
+    return false;
+  }
   const int i = min(int(u), STOP_N - 2);
   const float f = u - float(i);
-  const float a = row[i], b = row[i + 1];
-  return fmaf(f, b - a, a);
+  const float2 a = row[i], b = row[i + 1];
+  S = fmaf(f, b.x - a.x, a.x);
+  pmax = fmaf(f, b.y - a.y, a.y);
+  return true;
 }
 
 template <bool SURROGATE>
@@ -129,7 +138,7 @@ struct Fp32Policy
     const Sim32 * sim;
     const Species32 * sc;
     const Mat32 * mrow;
-    const float * stop;
+    const float2 * stop;
     float lnE_min, inv_dlnE;
     const SurrogateNet * net;
   };
@@ -269,10 +278,15 @@ struct Fp32Policy
     }
     const float E = p.E;
 
-    // maximum impact parameter and free flight (trim.C:88-94)
-    const float eps0 = E * mc.f;
-    const float eeg = sqrtf(eps0 * mc.epsdg);
-    const float pmax = mc.a / (eeg + sqrtf(eeg) + 0.125f * __expf(0.1f * __logf(eeg)));
+    // electronic stopping (material.C:114-121) and maximum impact parameter
+    // (trim.C:88-94) from the table; the formula below its first point
+    float S, pmax;
+    if (!stop_lookup(m.stop + (long long)mc.row * STOP_N, m.lnE_min, m.inv_dlnE, E, S, pmax))
+    {
+      const float eeg = sqrtf(E * mc.f * mc.epsdg);
+      pmax = mc.a / (eeg + sqrtf(eeg) + 0.125f * __expf(0.1f * __logf(eeg)));
+    }
+    // free flight (trim.C:88-94)
     float ls = mc.inv_pi_arho / (pmax * pmax);
     if (ic == 1)
       ls = r1 * fminf(ls, sim.cw);
@@ -303,8 +317,8 @@ struct Fp32Policy
     a.eps = mc.el[nn].fi * E;
     a.b = pimp * mc.el[nn].inv_ai;
 
-    // electronic loss from the stopping table (material.C:114-121)
-    a.dee = ls * stop_lookup(m.stop + (long long)mc.row * STOP_N, m.lnE_min, m.inv_dlnE, E);
+    // electronic loss
+    a.dee = ls * S;
     return a;
   }
 
@@ -495,7 +509,7 @@ launch_cascade32(const EngineParams & prm, const Fp32Tables & t, int grid, int b
   tabs.species = reinterpret_cast<const Species32 *>(prm.species);
   tabs.mats = reinterpret_cast<const Mat32 *>(prm.mats);
   tabs.sims = reinterpret_cast<const Sim32 *>(t.sims32);
-  tabs.stop = t.stop;
+  tabs.stop = reinterpret_cast<const float2 *>(t.stop);
   tabs.lnE_min = t.lnE_min;
   tabs.inv_dlnE = t.inv_dlnE;
   tabs.net = reinterpret_cast<const SurrogateNet *>(t.mlp);
@@ -650,7 +664,11 @@ stopping32_kernel(const float * row, float lnE_min, float inv_d, const double * 
 {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n)
-    out[i] = double(stop_lookup(row, lnE_min, inv_d, float(E[i])));
+  {
+    float S = 0.0f, pmax = 0.0f;
+    stop_lookup(reinterpret_cast<const float2 *>(row), lnE_min, inv_d, float(E[i]), S, pmax);
+    out[i] = double(S);
+  }
 }
 
 cudaError_t

@@ -205,8 +205,9 @@ launch_scatter64(const double * eps, const double * b, long long n, double * s2,
 namespace mtg
 {
 
-// FP32-path stopping tables: S(E) of every (species, material) row on a grid
-// uniform in ln E, evaluated with the FP64 stopping above.
+// FP32-path stopping tables: for every (species, material) row, on a grid uniform
+// in ln E, the pair S(E) (the FP64 stopping above) and p_max(E), the maximum impact
+// parameter of the free flight (trim.C:88-94, the FP64 formula of collide64).
 __global__ void
 build_stop_tables_kernel(const SpeciesConst * species, const MatConst * mats, const int * row_mat, int n_rows,
                          const int * row_species, float * out, double lnE_min, double dlnE)
@@ -218,7 +219,10 @@ build_stop_tables_kernel(const SpeciesConst * species, const MatConst * mats, co
   const int j = int(i % STOP_N);
   const double E = exp64(lnE_min + dlnE * double(j));
   const MatConst & mc = mats[row_mat ? row_mat[row] : row];
-  out[i] = float(material_stop64(species[row_species[row]], mc, E));
+  const double eeg = sqrt(E * mc.f * mc.epsdg);
+  const double pmax = mc.a / (eeg + sqrt(eeg) + 0.125 * pow64(eeg, 0.1));
+  out[2 * i] = float(material_stop64(species[row_species[row]], mc, E));
+  out[2 * i + 1] = float(pmax);
 }
 
 cudaError_t

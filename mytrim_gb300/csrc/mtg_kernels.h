@@ -26,7 +26,7 @@ constexpr int STOP_N = 2048;      // points per stopping table (uniform in ln E)
 constexpr double STOP_EMIN = 1e-2; // eV
 struct Fp32Tables
 {
-  const float * stop;   // STOP_N values per MatConst row (same row index as the MatConst table)
+  const float * stop;   // STOP_N pairs (S, p_max) per MatConst row (same row index as the MatConst table)
   float lnE_min;        // ln(STOP_EMIN)
   float inv_dlnE;       // 1 / spacing in ln E
   const void * mlp;     // surrogate weights, NULL without the surrogate
