@@ -208,7 +208,7 @@ def reference_stream_runs(oracle_built, engine_lib):
 
 @pytest.mark.parametrize("name", sorted(STAT_CASES))
 def test_fp64_statistics_vs_reference_streams(reference_stream_runs, name):
-    """spec criterion for the plain method: 3 sigma AND 1 % at 10^6 ions"""
+    """the plain method's criterion: 3 sigma AND 1 % at 10^6 ions"""
     sim, o, p = reference_stream_runs[name]
     res = PS.compare(p, o)
     for q, (rel, sig, a, b) in res.items():
