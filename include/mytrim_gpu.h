@@ -247,7 +247,8 @@ typedef struct
                               lane occupancy is collisions / (32 warp_steps) */
   int kernel_level;        /* feature level of the last run's cascade kernel: 0 lean, 1 member
                               records / voxels / tally modes, 2 + event log, 3 cluster geometry
-                              or a non-universal potential, 4 + event log */
+                              or a non-universal potential, 4 + event log, 5 cluster geometry
+                              with the universal potential only (plain FP32), 6 + event log */
   int max_take;            /* fresh primaries one warp took per refill in the last run */
   int events_overflowed;   /* 1 when the last collect's only error was a full event log (its
                               status is MTG_ERR_QUEUE_FULL and the tallies are complete) */

@@ -141,7 +141,7 @@ class Tuning(C.Structure):
 
 
 # mtg_stats.kernel_level values
-KERNEL_LEVELS = ("lean", "mid", "events", "geometry", "full")
+KERNEL_LEVELS = ("lean", "mid", "events", "geometry", "full", "clusters", "clusters+events")
 
 # symbol -> (restype, argtypes); must match include/mytrim_gpu.h
 _P = C.c_void_p

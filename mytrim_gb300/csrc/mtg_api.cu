@@ -163,10 +163,13 @@ int
 kernel_level(const mtg_ctx * ctx)
 {
   const HostTables & t = ctx->tables;
+  // cluster geometry with the universal potential only: the plain FP32 engine has
+  // variants without the other potentials' code
+  const bool clu_only = t.any_clusters && !t.any_potential && ctx->cfg.precision == MTG_PREC_FP32;
   if (ctx->event_cap > 0 && ctx->event_mask)
-    return t.any_extended ? LVL_FULL : LVL_EVENTS;
+    return clu_only ? LVL_CLU_EV : (t.any_extended ? LVL_FULL : LVL_EVENTS);
   if (t.any_extended)
-    return LVL_GEO;
+    return clu_only ? LVL_CLU : LVL_GEO;
   if (ctx->record_cap > 0 || t.voxel_total > 0 || t.any_evac || t.any_mode)
     return LVL_MID;
   return LVL_LEAN;

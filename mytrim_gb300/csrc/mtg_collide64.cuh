@@ -230,8 +230,8 @@ scatter64(double eps, double b, double & s2, double & ct, double & st, int & nit
 // One collision.  `mats` points at this species' MatConst row of the simulation
 // (n_mat entries), ic is the 1-based collision index, r1 the member's first-flight
 // draw.  Sink receives the tally events (see the engine and the host replay).  EXT
-// enables the cluster geometry and the non-universal potentials.
-template <bool EXT, class Sink>
+// enables the cluster geometry, POT the non-universal potentials.
+template <bool EXT, bool POT = EXT, class Sink>
 MTG_HD int
 collide64(P64 & p, uint32_t ic, double r1, const SimDesc & sim, const SpeciesConst & sc,
           const MatConst * mats, uint32_t k0, uint32_t k1, P64 & rec, Sink & sink)
@@ -296,7 +296,7 @@ collide64(P64 & p, uint32_t ic, double r1, const SimDesc & sim, const SpeciesCon
 
   double s2, ct, st;
   int niter;
-  scatter64(eps, b, s2, ct, st, niter, EXT ? sim.potential : 0);
+  scatter64(eps, b, s2, ct, st, niter, POT ? sim.potential : 0);
   sink.newton(niter);
 
   // energy transfer, electronic loss, momenta (trim.C:275-296)

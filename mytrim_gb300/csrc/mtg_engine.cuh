@@ -215,14 +215,17 @@ struct LaneCold
 
 // Kernel feature levels.  Code for a feature a run does not use still costs the
 // collision loop (instruction fetch, registers), so the cascade kernel comes in
-// five variants and each run takes the smallest that has what it needs:
+// up to seven variants and each run takes the smallest that has what it needs:
 //   LVL_LEAN    layered samples, universal potential, TrimVacCount tallies (depth,
 //               range and lateral histograms), CUT boundaries and sputter counting;
 //   LVL_MID     + member records, deposition voxels, the vacancy-energy histogram,
 //               TrimRange / TrimPrimaries tally modes;
 //   LVL_EVENTS  LVL_MID + the event log (no cluster geometry, universal potential);
 //   LVL_GEO     LVL_MID + the cluster geometry, the Moliere and C-Kr potentials;
-//   LVL_FULL    LVL_GEO + the event log.
+//   LVL_FULL    LVL_GEO + the event log;
+//   LVL_CLU     LVL_MID + the cluster geometry, universal potential only (the plain
+//               FP32 engine; the others run LVL_GEO);
+//   LVL_CLU_EV  LVL_CLU + the event log (the others run LVL_FULL).
 enum KernelLevel : int
 {
   LVL_LEAN = 0,
@@ -230,14 +233,33 @@ enum KernelLevel : int
   LVL_EVENTS = 2,
   LVL_GEO = 3,
   LVL_FULL = 4,
-  LVL_COUNT = 5
+  LVL_CLU = 5,
+  LVL_CLU_EV = 6,
+  LVL_COUNT = 7
 };
+
+// the level's cluster geometry, its non-universal potentials, its event log
+MTG_HD constexpr bool
+level_clusters(int lvl)
+{
+  return lvl == LVL_GEO || lvl == LVL_FULL || lvl == LVL_CLU || lvl == LVL_CLU_EV;
+}
+MTG_HD constexpr bool
+level_potentials(int lvl)
+{
+  return lvl == LVL_GEO || lvl == LVL_FULL;
+}
+MTG_HD constexpr bool
+level_events(int lvl)
+{
+  return lvl == LVL_EVENTS || lvl == LVL_FULL || lvl == LVL_CLU_EV;
+}
 
 // Device tally sink for one lane of a kernel of level LVL.
 template <class Pol, int LVL>
 struct LaneSink
 {
-  static constexpr bool EV = LVL == LVL_EVENTS || LVL == LVL_FULL; // feeds the event log
+  static constexpr bool EV = level_events(LVL); // feeds the event log
   static constexpr bool MID = LVL >= LVL_MID;
   using Acc = typename Pol::Acc;       // rare sums (kept in shared memory)
   using AccHot = typename Pol::AccHot; // per-collision sums (registers)
@@ -684,13 +706,15 @@ struct LaneSink
 };
 
 // LVL: the feature level (KernelLevel); the collision code knows the cluster
-// geometry and the non-universal potentials from LVL_GEO on
+// geometry at LVL_GEO, LVL_FULL, LVL_CLU and LVL_CLU_EV, the non-universal
+// potentials at LVL_GEO and LVL_FULL
 template <class Pol, int LVL>
 __global__ void __launch_bounds__(128, Pol::min_blocks(LVL))
 cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
 {
   constexpr bool MID = LVL >= LVL_MID;
-  constexpr bool EXT = LVL >= LVL_GEO;
+  constexpr bool EXT = level_clusters(LVL);   // the cluster geometry
+  constexpr bool POT = level_potentials(LVL); // the Moliere and C-Kr potentials
   using Particle = typename Pol::Particle;
   extern __shared__ __align__(16) unsigned char smem[];
 
@@ -853,7 +877,7 @@ cascade_kernel(const EngineParams prm, const typename Pol::Tables tabs)
     }
     // every lane takes part (a policy may evaluate warp-collective code); lanes
     // without a member do no work and get no flags
-    flags = Pol::template collide<EXT>(live, p, ic, r1, mctx, prm.k0, prm.k1, rec, sink);
+    flags = Pol::template collide<EXT, POT>(live, p, ic, r1, mctx, prm.k0, prm.k1, rec, sink);
     if (live)
     {
       if (flags & CF_VOID)

@@ -50,6 +50,12 @@
 #ifndef MTG_FP32_MIN_BLOCKS_GEO
 #define MTG_FP32_MIN_BLOCKS_GEO 6
 #endif
+#ifndef MTG_FP32_MIN_BLOCKS_CLU
+#define MTG_FP32_MIN_BLOCKS_CLU 6
+#endif
+#ifndef MTG_FP32_MIN_BLOCKS_CLU_EV
+#define MTG_FP32_MIN_BLOCKS_CLU_EV 7
+#endif
 #ifndef MTG_FP32_MIN_BLOCKS_LEAN
 #define MTG_FP32_MIN_BLOCKS_LEAN 8
 #endif
@@ -130,6 +136,8 @@ struct Fp32Policy
                      : lvl == LVL_MID    ? MTG_FP32_MIN_BLOCKS_MID
                      : lvl == LVL_EVENTS ? MTG_FP32_MIN_BLOCKS_EVENTS
                      : lvl == LVL_GEO    ? MTG_FP32_MIN_BLOCKS_GEO
+                     : lvl == LVL_CLU    ? MTG_FP32_MIN_BLOCKS_CLU
+                     : lvl == LVL_CLU_EV ? MTG_FP32_MIN_BLOCKS_CLU_EV
                                          : MTG_FP32_MIN_BLOCKS;
   }
 
@@ -322,7 +330,8 @@ struct Fp32Policy
     return a;
   }
 
-  template <bool EXT, class Sink>
+  // EXT: the cluster geometry; POT: the Moliere and C-Kr potentials
+  template <bool EXT, bool POT, class Sink>
   static __device__ __forceinline__ int collide(bool live, P32 & p, uint32_t ic, float r1, const MemberCtx & m,
                                                 uint32_t k0, uint32_t k1, P32 & rec, Sink & sink)
   {
@@ -336,7 +345,7 @@ struct Fp32Policy
       {
         a = phase_a<EXT>(p, ic, r1, m, k0, k1);
         // the network is trained on the universal potential only
-        nn = !a.gone && (!EXT || m.sim->potential == 0) && surrogate_in_domain(a.eps, a.b);
+        nn = !a.gone && (!POT || m.sim->potential == 0) && surrogate_in_domain(a.eps, a.b);
       }
       // warp-collective: the lanes whose collision is in the network's domain are
       // evaluated together, the others (no member, or the exact fallback) only take
@@ -351,7 +360,7 @@ struct Fp32Policy
       else
       {
         sink.fallback();
-        scatter32(a.eps, a.b, s2, c2, niter, EXT ? m.sim->potential : 0);
+        scatter32(a.eps, a.b, s2, c2, niter, POT ? m.sim->potential : 0);
       }
     }
     else
@@ -361,7 +370,7 @@ struct Fp32Policy
       a = phase_a<EXT>(p, ic, r1, m, k0, k1);
       if (a.gone)
         return CF_DONE | CF_VOID;
-      scatter32(a.eps, a.b, s2, c2, niter, EXT ? m.sim->potential : 0);
+      scatter32(a.eps, a.b, s2, c2, niter, POT ? m.sim->potential : 0);
     }
     sink.newton(niter);
     const Sim32 & sim = *m.sim;
@@ -519,7 +528,9 @@ launch_cascade32(const EngineParams & prm, const Fp32Tables & t, int grid, int b
       case LVL_LEAN: cascade_kernel<Fp32Policy<true>, LVL_LEAN><<<grid, block, smem, st>>>(prm, tabs); break;
       case LVL_MID: cascade_kernel<Fp32Policy<true>, LVL_MID><<<grid, block, smem, st>>>(prm, tabs); break;
       case LVL_EVENTS: cascade_kernel<Fp32Policy<true>, LVL_EVENTS><<<grid, block, smem, st>>>(prm, tabs); break;
-      case LVL_GEO: cascade_kernel<Fp32Policy<true>, LVL_GEO><<<grid, block, smem, st>>>(prm, tabs); break;
+      // the surrogate engine runs the cluster-only levels in the geometry variants
+      case LVL_GEO:
+      case LVL_CLU: cascade_kernel<Fp32Policy<true>, LVL_GEO><<<grid, block, smem, st>>>(prm, tabs); break;
       default: cascade_kernel<Fp32Policy<true>, LVL_FULL><<<grid, block, smem, st>>>(prm, tabs); break;
     }
   else
@@ -529,6 +540,8 @@ launch_cascade32(const EngineParams & prm, const Fp32Tables & t, int grid, int b
       case LVL_MID: cascade_kernel<Fp32Policy<false>, LVL_MID><<<grid, block, smem, st>>>(prm, tabs); break;
       case LVL_EVENTS: cascade_kernel<Fp32Policy<false>, LVL_EVENTS><<<grid, block, smem, st>>>(prm, tabs); break;
       case LVL_GEO: cascade_kernel<Fp32Policy<false>, LVL_GEO><<<grid, block, smem, st>>>(prm, tabs); break;
+      case LVL_CLU: cascade_kernel<Fp32Policy<false>, LVL_CLU><<<grid, block, smem, st>>>(prm, tabs); break;
+      case LVL_CLU_EV: cascade_kernel<Fp32Policy<false>, LVL_CLU_EV><<<grid, block, smem, st>>>(prm, tabs); break;
       default: cascade_kernel<Fp32Policy<false>, LVL_FULL><<<grid, block, smem, st>>>(prm, tabs); break;
     }
   return cudaGetLastError();
@@ -555,9 +568,21 @@ occupancy_variants(int block, size_t smem, int * occ)
   if ((e = occupancy_of(cascade_kernel<Fp32Policy<SG>, LVL_LEAN>, block, smem, &occ[LVL_LEAN])) != cudaSuccess ||
       (e = occupancy_of(cascade_kernel<Fp32Policy<SG>, LVL_MID>, block, smem, &occ[LVL_MID])) != cudaSuccess ||
       (e = occupancy_of(cascade_kernel<Fp32Policy<SG>, LVL_EVENTS>, block, smem, &occ[LVL_EVENTS])) != cudaSuccess ||
-      (e = occupancy_of(cascade_kernel<Fp32Policy<SG>, LVL_GEO>, block, smem, &occ[LVL_GEO])) != cudaSuccess)
+      (e = occupancy_of(cascade_kernel<Fp32Policy<SG>, LVL_GEO>, block, smem, &occ[LVL_GEO])) != cudaSuccess ||
+      (e = occupancy_of(cascade_kernel<Fp32Policy<SG>, LVL_FULL>, block, smem, &occ[LVL_FULL])) != cudaSuccess)
     return e;
-  return occupancy_of(cascade_kernel<Fp32Policy<SG>, LVL_FULL>, block, smem, &occ[LVL_FULL]);
+  if constexpr (SG)
+  {
+    occ[LVL_CLU] = occ[LVL_GEO];
+    occ[LVL_CLU_EV] = occ[LVL_FULL];
+    return cudaSuccess;
+  }
+  else
+  {
+    if ((e = occupancy_of(cascade_kernel<Fp32Policy<SG>, LVL_CLU>, block, smem, &occ[LVL_CLU])) != cudaSuccess)
+      return e;
+    return occupancy_of(cascade_kernel<Fp32Policy<SG>, LVL_CLU_EV>, block, smem, &occ[LVL_CLU_EV]);
+  }
 }
 
 // residency of the variant of feature level `level` (KernelLevel); every variant

@@ -87,13 +87,13 @@ struct Fp64Policy
     return p;
   }
 
-  template <bool EXT, class Sink>
+  template <bool EXT, bool POT, class Sink>
   static __device__ __forceinline__ int collide(bool live, P64 & p, uint32_t ic, double r1, const MemberCtx & m,
                                                 uint32_t k0, uint32_t k1, P64 & rec, Sink & sink)
   {
     if (!live)
       return 0;
-    return collide64<EXT>(p, ic, r1, *m.sim, *m.sc, m.mrow, k0, k1, rec, sink);
+    return collide64<EXT, POT>(p, ic, r1, *m.sim, *m.sc, m.mrow, k0, k1, rec, sink);
   }
 };
 
@@ -106,7 +106,9 @@ launch_cascade64(const EngineParams & prm, int grid, int block, size_t smem, cud
     case LVL_LEAN: cascade_kernel<Fp64Policy, LVL_LEAN><<<grid, block, smem, st>>>(prm, tabs); break;
     case LVL_MID: cascade_kernel<Fp64Policy, LVL_MID><<<grid, block, smem, st>>>(prm, tabs); break;
     case LVL_EVENTS: cascade_kernel<Fp64Policy, LVL_EVENTS><<<grid, block, smem, st>>>(prm, tabs); break;
-    case LVL_GEO: cascade_kernel<Fp64Policy, LVL_GEO><<<grid, block, smem, st>>>(prm, tabs); break;
+    // the FP64 engine runs the cluster-only levels in the geometry variants
+    case LVL_GEO:
+    case LVL_CLU: cascade_kernel<Fp64Policy, LVL_GEO><<<grid, block, smem, st>>>(prm, tabs); break;
     default: cascade_kernel<Fp64Policy, LVL_FULL><<<grid, block, smem, st>>>(prm, tabs); break;
   }
   return cudaGetLastError();
@@ -138,6 +140,8 @@ occupancy64(int block, size_t smem, int * blocks_per_sm, int level)
       (e = occupancy_of(cascade_kernel<Fp64Policy, LVL_GEO>, block, smem, &occ[LVL_GEO])) != cudaSuccess ||
       (e = occupancy_of(cascade_kernel<Fp64Policy, LVL_FULL>, block, smem, &occ[LVL_FULL])) != cudaSuccess)
     return e;
+  occ[LVL_CLU] = occ[LVL_GEO];
+  occ[LVL_CLU_EV] = occ[LVL_FULL];
   *blocks_per_sm = occ[level < 0 ? 0 : (level >= LVL_COUNT ? LVL_COUNT - 1 : level)];
   return cudaSuccess;
 }

@@ -512,6 +512,8 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
   out.any_evac = 0;
   out.any_mode = 0;
   out.any_extended = 0;
+  out.any_clusters = 0;
+  out.any_potential = 0;
   out.members_est = 1.0;
   if (n_sims < 1 || !sims)
   {
@@ -746,7 +748,7 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
     d.md_Emin_f = float(s.md_tag_Emin);
     d.md_Emax_f = float(s.md_tag_Emax);
     if (s.potential != MTG_POT_UNIVERSAL)
-      out.any_extended = 1;
+      out.any_extended = out.any_potential = 1;
     d.prim_begin = prim;
     d.n_primaries = s.n_primaries;
     d.sim_key = uint64_t(si);
@@ -814,7 +816,7 @@ build_tables(const mtg_scoef_row * rows, const mtg_config & cfg, const mtg_sim *
       // cell of a cluster is floor(c * kn / w) mod kn; each cell lists its clusters
       // in insertion order
       d.geometry = 1;
-      out.any_extended = 1;
+      out.any_extended = out.any_clusters = 1;
       d.n_clusters = int(smp.n_clusters);
       d.cl_base = (long long)out.clusters.size();
       d.cell_base = (long long)out.cl_head.size();

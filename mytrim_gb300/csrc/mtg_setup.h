@@ -27,6 +27,8 @@ struct HostTables
   int any_mode = 0;                       // some simulation tallies in TrimRange / TrimPrimaries mode
   int any_extended = 0;                   // some simulation has the cluster geometry or a
                                           // potential other than the universal one
+  int any_clusters = 0;                   // some simulation has the cluster geometry
+  int any_potential = 0;                  // some simulation has a non-universal potential
   double members_est = 1.0;               // expected cascade members per primary (launch heuristics)
   // stopping-table rows of the FP32 engine, one per distinct (species, material):
   // the MatConst entry and the species each row is built from

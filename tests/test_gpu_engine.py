@@ -281,6 +281,24 @@ def test_sharded_runs_reproduce_the_whole(engine_lib):
     assert list(whole["hist_range"]) == list(parts[0]["hist_range"] + parts[1]["hist_range"])
 
 
+def test_cluster_levels(engine_lib):
+    """A cluster sample with the universal potential runs the FP32 variants without
+    the other potentials' code ("clusters", "clusters+events"), with the tallies of
+    each other; FP64 runs it in the geometry variant."""
+    sim = SimSpec(**{**CASES["xe_uo2_clusters"][0].__dict__, "n_primaries": 300})
+    out = []
+    for prec, events, want in (("fp32", False, "clusters"), ("fp32", True, "clusters+events"),
+                               ("fp64", False, "geometry")):
+        e = Engine(precision=prec, seed=4)
+        if events:
+            e.set_event_log([F.EV_VACANCY], 1 << 20)
+        out.append(e.run([sim])[0])
+        assert F.KERNEL_LEVELS[e.stats()["kernel_level"]] == want, (prec, events)
+        e.close()
+    for k in ("members", "collisions", "vacancies", "replacements", "interstitials"):
+        assert out[0][k] == out[1][k], k
+
+
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
 def test_overflow_drain_gives_identical_results(engine_lib, prec):
     """A recoil stack of 4 entries per warp forces spills to the overflow list and
