@@ -353,11 +353,14 @@ expected_members(const mtg_sim & s)
 // to mask_base; bit 31 marks the cell for the search), then the candidates'
 // indexes.  Above 2^26 candidates the lists are left out: a cell then holds none and
 // is marked when any cluster reaches it (an occupancy mask).
+#ifndef MTG_CELL_MAX_ITEMS
+#define MTG_CELL_MAX_ITEMS (1LL << 26)
+#endif
 static void
 build_cluster_cells(SimDesc & d, const mtg_sample & smp, std::vector<uint32_t> & words)
 {
   constexpr double MAX_CELLS = double(1 << 22);
-  constexpr long long MAX_ITEMS = 1LL << 26;
+  constexpr long long MAX_ITEMS = MTG_CELL_MAX_ITEMS; // cells + candidates; lists are left out above
   constexpr uint32_t SEARCH = 0x80000000u;
   constexpr int MAX_CANDIDATES = 16;
   const double wmax = std::max(smp.w[0], std::max(smp.w[1], smp.w[2]));

@@ -61,3 +61,23 @@ def test_mask_answers_as_the_search(oracle_built, case):
     listed, marked = (int(v) for v in r.stdout.split("cells")[1].split()[:2])
     if case == "separate":  # the lists, not the search, answer near separate bubbles
         assert marked < 0.02 * (listed + marked), (listed, marked)
+
+
+@pytest.mark.parametrize("case", ["periodic", "many_small", "separate"])
+def test_cells_without_lists_answer_as_the_search(oracle_built, case):
+    """Where the candidate lists would pass their size cap (here 4096 entries, in a
+    build for this test), the cells only mark where a cluster reaches: the lookup
+    still answers exactly as the search."""
+    box, bc, cl, kn = CASES[case]
+    if cl is None:
+        from mytrim_gb300.workloads import _bubbles
+        cl = _bubbles(200, 15.0, 400.0, 3)
+    exe = ROOT / "oracle" / "_build" / "replay_host_smallcap"
+    tables = ROOT / "mytrim_gb300" / "data" / "stopping_tables.tsv"
+    r = subprocess.run([str(exe), str(tables), "--lookupcheck", "100000"], input=_spec(box, bc, cl, kn),
+                       capture_output=True, text=True)
+    checked, bad = (int(v) for v in r.stdout.split()[-2:])
+    assert checked == 100000
+    assert bad == 0, r.stdout
+    listed, marked = (int(v) for v in r.stdout.split("cells")[1].split()[:2])
+    assert listed == 0 and marked > 0, (listed, marked)
