@@ -372,10 +372,10 @@ typedef struct
  * in subsequent runs, up to `capacity` records; a run that raises more fails with
  * MTG_ERR_QUEUE_FULL after its tallies are complete.  A log of fewer than 128 slots
  * per resident GPU thread fills slot by slot (one global atomic per event); a larger
- * one is filled eight slots at a time per thread (one atomic per eight events), and
- * the slots a thread leaves unused, at most seven per thread and pass, count toward
- * the capacity: such a log can fill up to 1/16 early.  mtg_get_events returns the
- * records without the unused slots either way. */
+ * one is filled eight slots at a time per thread (sixteen from 256 slots per thread),
+ * and the slots a thread leaves unused, fewer than one such chunk per thread and
+ * pass, count toward the capacity: such a log can fill up to 1/16 early.
+ * mtg_get_events returns the records without the unused slots either way. */
 mtg_status mtg_set_event_log(mtg_ctx * ctx, unsigned int kind_mask, long long capacity);
 /* Copy the last run's records; *n_total receives the number logged (may exceed the
  * capacity when the log overflowed), *n_written the number copied. */

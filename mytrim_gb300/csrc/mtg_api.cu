@@ -64,7 +64,6 @@ enum Counter
 };
 constexpr int MAX_PASSES = 64;
 constexpr int MAX_OVF_RETRIES = 3; // runs redone with a larger overflow list
-constexpr int EVENT_CHUNK = 8;     // event-log slots a lane reserves at a time in large logs
 
 } // namespace
 
@@ -329,11 +328,17 @@ fill_params(mtg_ctx * ctx, EngineParams & prm)
     prm.n_event_unused = ptr<unsigned long long>(ctx->d_counters) + C_NEV_UNUSED;
     prm.events_cap = ctx->event_cap;
     prm.event_mask = ctx->event_mask;
-    // slots eight at a time per lane where the log holds at least 16 chunks per
-    // resident lane (the slots left unused, at most seven per lane and pass, then
+    // slots 16 or 8 at a time per lane where the log holds at least 16 such chunks per
+    // resident lane (the slots left unused, fewer than a chunk per lane and pass, then
     // take at most 1/16 of it); one at a time in smaller logs, which fill exactly
     const long long lanes = (long long)ctx->grid * ctx->block;
-    prm.event_chunk = ctx->event_cap >= 16LL * EVENT_CHUNK * lanes ? EVENT_CHUNK : 1;
+    prm.event_chunk = 1;
+    for (int c : {16, 8})
+      if (ctx->event_cap >= 16LL * c * lanes)
+      {
+        prm.event_chunk = c;
+        break;
+      }
   }
   prm.any_evac = t.any_evac;
   prm.level = kernel_level(ctx);

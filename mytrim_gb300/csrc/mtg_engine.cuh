@@ -93,7 +93,7 @@ struct EngineParams
   unsigned long long * n_events;       // slots reserved
   unsigned long long * n_event_unused; // reserved slots that no event filled
   long long events_cap;
-  int event_chunk;                     // slots a lane reserves at a time (1 or 8)
+  int event_chunk;                     // slots a lane reserves at a time (1, 8 or 16)
   unsigned int event_mask;
   int any_evac; // some simulation keeps a vacancy-energy histogram
   int level;    // KernelLevel of the launched variant

@@ -482,8 +482,8 @@ def streams_history(ev):
 
 
 def test_event_log_in_chunks_equals_exact_log(engine_lib):
-    """A log large enough for slots taken eight at a time per lane returns the same
-    records as one filled a slot at a time, without the slots left unused."""
+    """Logs large enough for slots taken eight or sixteen at a time per lane return
+    the same records as one filled a slot at a time, without the slots left unused."""
     from mytrim_gb300.streams import _sorted
     sim = _cu_sim(n=400)
     e = Engine(precision="fp32", seed=9)
@@ -491,15 +491,17 @@ def test_event_log_in_chunks_equals_exact_log(engine_lib):
     e.run([sim])
     exact, n_exact = e.events(), e.event_count()
     lanes = e.stats()["grid"] * e.stats()["block"]
-    e.set_event_log(ALL_EVENTS, 16 * 8 * lanes + 1000)
-    e.run([sim])
-    chunked, n_chunked = e.events(), e.event_count()
+    a = _sorted(exact)
+    for chunk in (8, 16):
+        e.set_event_log(ALL_EVENTS, 16 * chunk * lanes + 1000)
+        e.run([sim])
+        chunked, n_chunked = e.events(), e.event_count()
+        assert n_exact == n_chunked == len(exact) == len(chunked) > 0, chunk
+        assert (chunked["kind"] >= 1).all()
+        b = _sorted(chunked)
+        for f in exact.dtype.names:
+            assert np.array_equal(a[f], b[f]), (chunk, f)
     e.close()
-    assert n_exact == n_chunked == len(exact) == len(chunked) > 0
-    assert (chunked["kind"] >= 1).all()
-    a, b = _sorted(exact), _sorted(chunked)
-    for f in exact.dtype.names:
-        assert np.array_equal(a[f], b[f]), f
 
 
 def test_event_log_overflow_keeps_tallies(engine_lib):
