@@ -54,8 +54,10 @@ def guess_table(pot):
     return np.log2(0.5 * (lo + hi) - B).astype(np.float32).reshape(NG_U, NG_B)
 
 
-def s2(pot, eps, b, table=None):
-    """sin^2(theta/2) of the FP32 path's algorithm, evaluated in double."""
+def s2(pot, eps, b, table=None, start="table"):
+    """sin^2(theta/2) of the FP32 path's algorithm, evaluated in double; with
+    start="reference" every solve starts from the reference's guess (the FP64 path's
+    iterates)."""
     eps = np.asarray(eps, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
     T = (guess_table(pot) if table is None else table).astype(np.float64)
@@ -67,7 +69,7 @@ def s2(pot, eps, b, table=None):
     fu = (np.log2(e) - NG_U0) / NG_DU
     fb = bb / NG_DB
     # C-Kr keeps the reference's guess everywhere
-    inside = (fu >= 0) & (fb < NG_B - 1) & (pot != "ckr")
+    inside = (fu >= 0) & (fb < NG_B - 1) & (pot != "ckr") & (start == "table")
     i = np.clip(fu, 0, NG_U - 2).astype(int)
     j = np.clip(fb, 0, NG_B - 2).astype(int)
     a, c = fu - i, fb - j
@@ -105,3 +107,27 @@ def s2(pot, eps, b, table=None):
     co = (bb + (r - bb) * aa * ff / (ff + 1.0) + roc) / (r + roc)
     out[~far] = 1.0 - co * co
     return out
+
+
+def converged_s2(pot, eps, b):
+    """The magic formula at the exact root (bisection), v and v1 there: the value the
+    Newton iterates approach."""
+    eps = np.asarray(eps, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    lo, hi = b.copy(), b + 2.0 / eps
+    for _ in range(200):
+        m = 0.5 * (lo + hi)
+        f = b * b / m + _terms(pot, m)[0] / eps - m
+        lo, hi = np.where(f > 0, m, lo), np.where(f > 0, hi, m)
+    r = 0.5 * (lo + hi)
+    phi, tk = _terms(pot, r)
+    v = phi / r
+    v1 = -(v + tk) / r
+    m0, m1, m2, m3, m4 = MAGIC[pot]
+    roc = -2.0 * (eps - v) / v1
+    sqe = np.sqrt(eps)
+    cc = (m0 + sqe) / (m1 + sqe)
+    aa = 2.0 * eps * (1.0 + m2 / sqe) * b ** cc
+    ff = (np.sqrt(aa * aa + 1.0) - aa) * ((m3 + eps) / (m4 + eps))
+    co = (b + (r - b) * aa * ff / (ff + 1.0) + roc) / (r + roc)
+    return 1.0 - co * co
