@@ -31,7 +31,8 @@
 #include "mtg_surrogate.cuh"
 
 // resident 128-thread blocks per SM the register budget of each feature level is
-// cut for: lean, mid and events 8 (64 registers), full 7 (72), geometry 6 (80).
+// cut for: lean, mid and events 8 (64 registers), full and clusters+events 7 (72),
+// geometry and clusters 6 (80).
 // Measured per level: eight blocks beat seven for the mid and events levels in spite
 // of their spills (32 and 80 bytes): +14 % (mid), +7 % (events, full log), +25 %
 // (events, log nearly empty) on B 10 keV into SiO2/Si; the full level gains 7.5 % at
