@@ -16,7 +16,9 @@ them in config.launch_settings.
 Printed JSON line (rank 0):
   value        primaries/s over the K timed steps, device-timed with CUDA events on
                the launching stream, inputs resident in HBM, L2 flushed (256 MiB
-               write) before every timed step
+               write) before every timed step; a step whose collect() launched
+               further drain passes, or made the run again with larger overflow
+               lists, is timed to the end of that work
   e2e          the same metric through the public call (host structs in, host
                totals out, uploads and read-back inside the timed region)
   paths        each path on the same workload: fp32 (the headline), surrogate (2^20
